@@ -1,0 +1,276 @@
+/*
+ * omv.h -- C ABI of the GB300-native OpenMATERIAL BDPT render path.
+ *
+ * The reference renderer is a C++ class facade with no plugin or FFI layer:
+ *   BDPTRenderer::setParameters / setScene / render   (pathtracer/src/renderer/BDPTRenderer.h:147-155)
+ *   RenderScene::allocate / setMesh / setInstance / setMaterial / setLight /
+ *               setBackground / commitScene           (pathtracer/src/scene/RenderScene.h:109-204)
+ *   PinholeCamera (ViewPoint + half sizes + focus)   (pathtracer/src/sensors/PinholeCamera.h,
+ *                                                     pathtracer/src/sensors/RenderSensor.h:36-49)
+ * This header replaces that facade one level above the per-ray Embree call
+ * (rtcIntersect1, BDPTRenderer.cpp:84), which is the only C ABI the reference hot
+ * path itself crosses.  All entry points take plain pointers and sizes; every
+ * pointer argument is a HOST pointer unless the entry point name ends in
+ * `_device`.  The caller owns all buffers it passes; the library owns the
+ * device-side scene behind the opaque `omv_scene` handle.
+ *
+ * Errors: every entry point returns an `omv_status` (0 = OK).  The message of
+ * the last failing call on the calling thread is returned by omv_last_error().
+ * No C++ exception crosses this boundary (the reference reports failures with
+ * C++ exceptions, Exceptions.h:34-104, and a bool from commitScene,
+ * RenderScene.cpp:194).
+ *
+ * Threading: an omv_scene handle is not re-entrant; distinct handles may be
+ * used from different threads.  Each handle owns one CUDA stream.
+ */
+#ifndef OMV_H
+#define OMV_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t omv_status;
+enum {
+    OMV_OK = 0,
+    OMV_ERR_INVALID_ARGUMENT = 1,
+    OMV_ERR_CUDA = 2,
+    OMV_ERR_OUT_OF_MEMORY = 3,
+    OMV_ERR_EMPTY_SCENE = 4,     /* no valid instance: RenderScene::commitScene returns false */
+    OMV_ERR_TIMEOUT = 5,         /* a bounded device-side wait gave up */
+    OMV_ERR_INTERNAL = 6,
+    OMV_ERR_NO_DEVICE = 7
+};
+
+/* ---------------------------------------------------------------- scene --- */
+
+/* One triangle mesh, laid out like RenderScene::setMesh (RenderScene.cpp:82-99).
+ * Strides are in floats.  normals / tangents / texcoord0 may be NULL: the
+ * library then derives them at commit exactly as RenderMesh::commitMesh does
+ * (RenderMesh.cpp:246-264, computeNormals :300, computeTangents :332/:411). */
+typedef struct omv_mesh_desc {
+    int32_t num_vertices;
+    int32_t num_faces;
+    const uint32_t* faces;          /* 3 * num_faces vertex indices */
+    const float* positions;  int32_t position_stride;
+    const float* normals;    int32_t normal_stride;
+    const float* tangents;   int32_t tangent_stride;   /* xyz + handedness w */
+    const float* texcoord0;  int32_t texcoord_stride;
+    int32_t material;               /* <0 or >= num_materials: the missing material */
+} omv_mesh_desc;
+
+/* RenderScene::setInstance (RenderScene.cpp:101-109): row-major 4x4 object-to-world. */
+typedef struct omv_instance_desc {
+    float transform[4][4];
+    int32_t mesh;
+} omv_instance_desc;
+
+enum { OMV_MATERIAL_PBR = 0, OMV_MATERIAL_OPENMATERIAL = 1 };
+enum { OMV_ALPHA_OPAQUE = 0, OMV_ALPHA_MASK = 1, OMV_ALPHA_BLEND = 2 };
+
+/* PBR: PhysicallyBasedMaterial over PbrMaterial factors (PbrMaterial.cpp:100-204).
+ * OpenMaterial: OpenMaterial over AssetMaterialIor (OpenMaterial.cpp, AssetMaterialIor.cpp):
+ * the (wavelength [m], value) tables of the temperature closest to `temperature`,
+ * sorted by wavelength; the library evaluates AssetMaterialIor::getIor at the three
+ * RGB wavelengths (Constants.h:53) once at commit. */
+typedef struct omv_material_desc {
+    int32_t type;
+    float base_color[4];
+    float metallic;
+    float roughness;
+    float ior;                      /* PbrMaterial default 1.5 (PbrMaterial.cpp:119) */
+    int32_t alpha_mode;
+    float alpha_cutoff;
+    int32_t double_sided;
+    float temperature;
+    int32_t ior_n_count;
+    const float* ior_n;             /* ior_n_count (wavelength, n) pairs */
+    int32_t ior_k_count;
+    const float* ior_k;             /* ior_k_count (wavelength, k) pairs */
+} omv_material_desc;
+
+/* RenderLightPoint::set (RenderLightPoint.cpp:20-26).  `intensity` is the
+ * already-flattened RGB intensity (main.cpp:362-363, including its G/B order);
+ * range <= 0 means unlimited (std::numeric_limits<float>::max()). */
+typedef struct omv_light_desc {
+    float position[3];
+    float intensity[3];
+    float range;
+} omv_light_desc;
+
+/* HDRBackground (HdrBackground.cpp:38-97): equirectangular RGB float image,
+ * rotation applied as dir * R (row vector times matrix) and a radiance scale. */
+typedef struct omv_hdri_desc {
+    int32_t width;
+    int32_t height;
+    const float* rgb;               /* width * height * 3 */
+    float rotation[3][3];
+    float scale;
+} omv_hdri_desc;
+
+typedef struct omv_scene_desc {
+    int32_t num_meshes;
+    const omv_mesh_desc* meshes;
+    int32_t num_instances;
+    const omv_instance_desc* instances;
+    int32_t num_materials;
+    const omv_material_desc* materials;
+    int32_t num_lights;
+    const omv_light_desc* lights;
+    const omv_hdri_desc* hdri;      /* NULL: no background */
+} omv_scene_desc;
+
+typedef struct omv_scene omv_scene;
+
+/* RenderScene::allocate + set* + commitScene.  Builds the GPU acceleration
+ * structure (Morton codes -> radix sort -> LBVH -> 8-wide quantized BVH). */
+omv_status omv_scene_create(const omv_scene_desc* desc, int32_t device, omv_scene** out);
+omv_status omv_scene_destroy(omv_scene* scene);
+
+typedef struct omv_scene_info {
+    int64_t num_triangles;
+    int64_t num_blas_nodes;
+    int64_t num_tlas_nodes;
+    int64_t device_bytes;
+    double build_ms;
+} omv_scene_info;
+omv_status omv_scene_get_info(const omv_scene* scene, omv_scene_info* info);
+
+/* --------------------------------------------------------------- camera --- */
+
+/* PinholeCamera (PinholeCamera.cpp:80-95): ray = rotation * normalize(x+.5-half_w+dx,
+ * y+.5-half_h+dy, focus), from `position`.  rotation rows = (left, up, forward)
+ * columns as built by ViewPoint (RenderSensor.cpp:19-26). */
+typedef struct omv_camera {
+    int32_t width;
+    int32_t height;
+    float position[3];
+    float rotation[3][3];
+    float half_width;
+    float half_height;
+    float focus;
+} omv_camera;
+
+/* ----------------------------------------------------------- parameters --- */
+
+enum { OMV_ESTIMATOR_REFERENCE = 0 };
+
+/* RendererParameters (RendererParameters.h:20-96) plus the build's own keys. */
+typedef struct omv_params {
+    int32_t camera_bounces;             /* cameraBouncesN, default 10 */
+    int32_t light_bounces;              /* lightBouncesN,  default 10 */
+    int32_t max_path_length;            /* maxPathLength,  default 8 */
+    int32_t samples_per_pixel;          /* samplesPerPixel, default 20 */
+    int32_t light_distance_attenuation; /* default 1 */
+    float light_scale;                  /* lightScaleValue, default 100 */
+    float light_min_distance;           /* lightMinDistance, default 0.01 */
+    float ray_cut_value;                /* rayCutPixValue, default 0.002 */
+    uint64_t seed;                      /* Philox key */
+    int32_t estimator;                  /* OMV_ESTIMATOR_REFERENCE */
+    int32_t sample_offset;              /* first sample index (progressive rendering) */
+    int32_t accumulate_variance;        /* also accumulate per-pixel sum of squares */
+    int32_t wave_paths;                 /* paths per wavefront wave; 0 = automatic */
+} omv_params;
+
+/* Fills `p` with the reference defaults (RendererParameters.h:56-89). */
+void omv_params_default(omv_params* p);
+
+/* --------------------------------------------------------------- render --- */
+
+typedef struct omv_stats {
+    int64_t paths;
+    int64_t extension_rays;
+    int64_t shadow_rays;
+    int64_t light_rays;
+    double render_ms;
+    int64_t kernel_launches;
+} omv_stats;
+
+/* BDPTRenderer::render (BDPTRenderer.cpp:372-393) for one camera.
+ * Outputs (host, caller-allocated, any may be NULL):
+ *   image_rgba  width*height*4 floats, normalised like PinholeCamera::stop
+ *               (rgb / count, alpha 1; PinholeCamera.cpp:70-78)
+ *   sum_rgb     width*height*3 doubles, per-pixel radiance sums (FP64)
+ *   sumsq_rgb   width*height*3 doubles, per-pixel sums of squares
+ *               (requires params->accumulate_variance)
+ *   count       width*height uint32 sample counts
+ *   stats       counters and device time of the render. */
+omv_status omv_render(omv_scene* scene, const omv_camera* camera, const omv_params* params,
+                      float* image_rgba, double* sum_rgb, double* sumsq_rgb, uint32_t* count,
+                      omv_stats* stats);
+
+/* Same as omv_render, but the film lives in caller-owned DEVICE memory and is
+ * accumulated into (not cleared): d_sum_rgb (3*W*H doubles), d_sumsq_rgb (may
+ * be NULL), d_count (W*H uint32).  `stream` is a cudaStream_t (NULL: the
+ * scene's stream).  Asynchronous: returns after enqueueing all work. */
+omv_status omv_render_device(omv_scene* scene, const omv_camera* camera, const omv_params* params,
+                             double* d_sum_rgb, double* d_sumsq_rgb, uint32_t* d_count,
+                             void* stream, omv_stats* stats);
+
+/* ----------------------------------------------------- rays / ID buffers --- */
+
+/* One closest-hit query (the reference's sceneIntersect, BDPTRenderer.cpp:75-102,
+ * including the alpha-mask retry loop).  geom = mesh index (Embree geomID),
+ * inst = instance index (instID[0]), prim = local face index (primID),
+ * material = mesh material index (the missing material = num_materials).
+ * All ids are 0xFFFFFFFF on a miss. */
+typedef struct omv_hit {
+    uint32_t inst;
+    uint32_t geom;
+    uint32_t prim;
+    uint32_t material;
+    float t;
+    float u;
+    float v;
+    uint32_t pad;
+} omv_hit;
+
+/* Traces `n` rays given as 8 floats each (org xyz, tnear, dir xyz, tfar). */
+omv_status omv_trace_rays(omv_scene* scene, int64_t n, const float* rays, omv_hit* hits);
+
+/* Primary-hit (identification) pass: the validation modes pid/gid/mid
+ * (FCSubject.h:189-240, main.cpp:261-270) as integer buffers.  One primary ray
+ * per pixel; `jitter` = 2*W*H uniforms in [0,1) (dx+0.5, dy+0.5 per pixel) or
+ * NULL for a Philox jitter keyed by `seed`.  Outputs (any may be NULL):
+ * per-pixel omv_hit, and the global primitive id (face id + faces of all lower
+ * meshes, BDPTRenderer.cpp:64). */
+omv_status omv_render_ids(omv_scene* scene, const omv_camera* camera, const float* jitter,
+                          uint64_t seed, omv_hit* hits, uint32_t* global_prim);
+
+/* ------------------------------------------------------ kernel test hooks --- */
+
+/* Device evaluation of the material model on host SoA inputs, for parity tests
+ * against the reference's BSDFModel<ndf::GGX> (BRDFModel.h:211-337) and
+ * OpenMaterial (OpenMaterial.cpp:20-163).
+ *
+ * omv_brdf_eval_direct: BSDFModel::evaluateDirect.  Per case 17 floats in:
+ *   I(3) O(3) N(3) color(4) metallness alpha pad pad; out: brdf(3).
+ * omv_brdf_sample_indirect: BSDFModel::sampleIndirect with the three uniforms
+ *   supplied.  Per case 24 floats in: I(3) N(3) T(3) color(4) metallness alpha
+ *   eta isTransmissive u0 u1 u2 pad pad pad; out 6 floats: O(3) brdf(3).
+ * omv_om_fresnel: OpenMaterial's per-channel brdf = 0.5*(Rp+Rs)/|cos| for complex
+ *   IOR; per case in: n(3) k(3) cos; out 3 floats. */
+omv_status omv_brdf_eval_direct(int64_t n, const float* in, float* out);
+omv_status omv_brdf_sample_indirect(int64_t n, const float* in, float* out);
+omv_status omv_om_fresnel(int64_t n, const float* in, float* out);
+
+/* Camera rays for given jitter uniforms (2 per pixel, row-major), 6 floats per
+ * pixel out (org, dir).  Device evaluation of PinholeCamera::getRay. */
+omv_status omv_camera_rays(const omv_camera* camera, const float* jitter, float* rays);
+
+/* HDRBackground::getRadiance on the device for n directions (3 floats each). */
+omv_status omv_env_radiance(omv_scene* scene, int64_t n, const float* dirs, float* rgb);
+
+/* -------------------------------------------------------------- errors --- */
+
+const char* omv_last_error(void);
+const char* omv_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OMV_H */

@@ -1,0 +1,565 @@
+"""Seeded synthetic scenes of the benchmark shapes, in two forms:
+
+* flattened arrays, exactly as the reference's RenderScene holds them after
+  main.cpp has flattened the glTF asset (main.cpp:285-416) -- what the C ABI
+  (omv_scene_create) takes;
+* glTF 2.0 + OpenMATERIAL files (geometry .gltf/.bin, OpenMATERIAL material and
+  IOR tables, KHR_lights_punctual point lights, a pinhole camera JSON and a
+  Radiance RGBE .hdr environment) that the reference renderer loads itself, so
+  both renderers consume identical inputs.
+
+Scenes (sizes from the benchmark definitions):
+
+* ``c1``: icosphere (4 midpoint subdivisions, 5,120 triangles, radius 1) with an
+  OpenMATERIAL conductor whose IOR table gives n=(0.18,0.42,1.37),
+  k=(3.42,2.35,1.77) at the RGB wavelengths 650/510/440 nm, on a 10x10 diffuse
+  ground quad (PBR, base colour 0.5, metallic 0, roughness 1) at y=-1; one point
+  light at (2,4,2), white, intensity 50; pinhole camera, y-fov 45 deg, 256x256,
+  16 spp, camera/light bounces 6, max path length 6.  The whole asset sits under
+  a root node translated by (0,0,-5) so that the reference's fixed camera (origin,
+  looking down -z, main.cpp:459-476) sees it.  The conductor's GGX roughness 0.3
+  has no counterpart in the reference's OpenMATERIAL model (a perfect mirror,
+  OpenMaterial.cpp:72-93) and is therefore not represented.
+* ``c2``: 64 meshes (32 tori of 12,288 triangles, 32 noise-displaced icospheres
+  of 20,480 triangles: 1,048,576 triangles) under uniform random rotations,
+  scale U[0.5,2] and positions in a 40 m cube in front of the camera; PBR
+  materials baseColor U[0,1]^3, roughness U[0.05,1], metallic Bernoulli(0.5);
+  a 2048x1024 equirectangular HDRI (log-normal sky, mu=0 sigma=1, plus three
+  Gaussian sun lobes of peak 1e4) stored as RGBE; 1920x1080, 64 spp, max path
+  length 10, camera bounces 10, no point lights.
+"""
+from __future__ import annotations
+
+import ctypes
+import ctypes.util
+import dataclasses
+import json
+import math
+import os
+import struct
+from typing import List, Optional
+
+import numpy as np
+
+F32 = np.float32
+
+# Constants.h:53 -- wavelengths of the three base channels [m]
+RGB_WAVELENGTHS = (6.50000004e-07, 5.10000007e-07, 4.40000008e-07)
+
+
+def _libm_tanf():
+    name = ctypes.util.find_library("m") or "libm.so.6"
+    lib = ctypes.CDLL(name)
+    f = lib.tanf
+    f.restype = ctypes.c_float
+    f.argtypes = [ctypes.c_float]
+    return f
+
+
+_TANF = None
+
+
+def tanf(x: float) -> float:
+    """float tangent through the C library, as std::tan(float) evaluates it."""
+    global _TANF
+    if _TANF is None:
+        _TANF = _libm_tanf()
+    return float(_TANF(float(F32(x))))
+
+
+# ----------------------------------------------------------------- geometry --
+
+def icosphere(subdivisions: int):
+    """Unit icosphere by repeated midpoint subdivision of an icosahedron, all
+    vertices projected onto the unit sphere (computed in float64, stored f32)."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    verts = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0),
+             (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+             (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    verts = [np.array(v, dtype=np.float64) / np.linalg.norm(v) for v in verts]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11),
+             (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6), (7, 1, 8),
+             (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9),
+             (4, 9, 5), (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    for _ in range(subdivisions):
+        cache = {}
+        new_faces = []
+
+        def mid(a, b):
+            key = (a, b) if a < b else (b, a)
+            if key not in cache:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                cache[key] = len(verts) - 1
+            return cache[key]
+
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            new_faces += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = new_faces
+    return np.array(verts, dtype=np.float64), np.array(faces, dtype=np.uint32)
+
+
+def torus(R: float, r: float, nu: int, nv: int):
+    u = np.arange(nu) * (2 * np.pi / nu)
+    v = np.arange(nv) * (2 * np.pi / nv)
+    uu, vv = np.meshgrid(u, v, indexing="ij")
+    cx, cz = np.cos(uu), np.sin(uu)
+    pos = np.stack([(R + r * np.cos(vv)) * cx, r * np.sin(vv), (R + r * np.cos(vv)) * cz], -1).reshape(-1, 3)
+    nrm = np.stack([np.cos(vv) * cx, np.sin(vv), np.cos(vv) * cz], -1).reshape(-1, 3)
+    idx = np.arange(nu * nv).reshape(nu, nv)
+    i0 = idx
+    i1 = np.roll(idx, -1, axis=0)
+    i2 = np.roll(idx, -1, axis=1)
+    i3 = np.roll(np.roll(idx, -1, axis=0), -1, axis=1)
+    f = np.concatenate([np.stack([i0, i2, i1], -1).reshape(-1, 3), np.stack([i1, i2, i3], -1).reshape(-1, 3)])
+    return pos, nrm, f.astype(np.uint32)
+
+
+def displaced_icosphere(subdivisions: int, rng: np.random.Generator, amplitude: float = 0.18, modes: int = 6):
+    v, f = icosphere(subdivisions)
+    disp = np.zeros(len(v))
+    for _ in range(modes):
+        k = rng.normal(size=3)
+        k *= rng.uniform(1.5, 5.0) / np.linalg.norm(k)
+        disp += np.sin(v @ k + rng.uniform(0, 2 * np.pi)) / modes ** 0.5
+    return v * (1.0 + amplitude * disp)[:, None], f
+
+
+def random_rotation(rng: np.random.Generator) -> np.ndarray:
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    x, y, z, w = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+# -------------------------------------------------------------- data model --
+
+@dataclasses.dataclass
+class Mesh:
+    positions: np.ndarray                 # (V,3) f32
+    faces: np.ndarray                     # (F,3) u32
+    normals: Optional[np.ndarray] = None  # (V,3) f32 or None (derived at commit)
+    tangents: Optional[np.ndarray] = None  # (V,4) f32 or None (derived at commit)
+    texcoord0: Optional[np.ndarray] = None
+    material: int = -1
+    name: str = "mesh"
+
+
+@dataclasses.dataclass
+class Instance:
+    transform: np.ndarray  # (4,4) f32 object-to-world
+    mesh: int
+
+
+@dataclasses.dataclass
+class Material:
+    type: int                      # 0 PBR, 1 OpenMATERIAL
+    base_color: tuple = (1.0, 1.0, 1.0, 1.0)
+    metallic: float = 1.0
+    roughness: float = 1.0
+    ior: float = 1.5
+    alpha_mode: int = 0
+    alpha_cutoff: float = 0.5
+    double_sided: bool = False
+    temperature: float = 300.0
+    ior_n: Optional[np.ndarray] = None  # (K,2) wavelength[m], n
+    ior_k: Optional[np.ndarray] = None
+    name: str = "material"
+
+
+@dataclasses.dataclass
+class Light:
+    position: tuple
+    intensity: tuple
+    range: float = 0.0  # <= 0: unlimited
+
+
+@dataclasses.dataclass
+class Hdri:
+    rgb: np.ndarray          # (H,W,3) f32, already RGBE-quantised
+    rotation: np.ndarray     # (3,3)
+    scale: float
+
+
+@dataclasses.dataclass
+class CameraSpec:
+    width: int
+    height: int
+    position: tuple
+    rotation: np.ndarray     # (3,3): columns left, up, forward (ViewPoint)
+    half_width: float
+    half_height: float
+    focus: float
+    json_props: Optional[dict] = None
+
+
+@dataclasses.dataclass
+class RenderSpec:
+    samples_per_pixel: int
+    camera_bounces: int
+    light_bounces: int
+    max_path_length: int
+
+
+@dataclasses.dataclass
+class Scene:
+    name: str
+    meshes: List[Mesh]
+    instances: List[Instance]
+    materials: List[Material]
+    lights: List[Light]
+    hdri: Optional[Hdri]
+    camera: CameraSpec
+    render: RenderSpec
+    gltf_nodes: list = dataclasses.field(default_factory=list)  # for the writer
+
+    @property
+    def num_triangles(self) -> int:
+        return int(sum(len(self.meshes[i.mesh].faces) for i in self.instances))
+
+
+# ----------------------------------------------------------------- cameras --
+
+def default_view(position=(0.0, 0.0, 0.0), forward=(0.0, 0.0, -1.0), up=(0.0, 1.0, 0.0)) -> np.ndarray:
+    """ViewPoint as main.cpp:459-476 builds it: left = forward x up,
+    up' = left x forward; rotation columns (left, up', forward)."""
+    f = np.array(forward, dtype=F32)
+    u = np.array(up, dtype=F32)
+
+    def cross(a, b):
+        return np.array([a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]], dtype=F32)
+
+    left = cross(f, u)
+    up2 = cross(left, f)
+    return np.stack([left, up2, f], axis=1).astype(F32)
+
+
+def camera_from_json(width, height, aspect, focus, yfov, position=(0.0, 0.0, 0.0)) -> CameraSpec:
+    """PinholeCamera::loadProperties (PinholeCamera.cpp:115-148)."""
+    focus32 = F32(focus)
+    half_h = F32(focus32 * F32(tanf(F32(F32(F32(0.5) * F32(yfov)) * F32(math.pi)) / F32(180.0))))
+    half_w = F32(F32(aspect) * half_h)
+    return CameraSpec(width, height, tuple(position), default_view(position), float(half_w), float(half_h),
+                      float(focus32), json_props={"pinhole": {"aspect": aspect, "focus": focus, "y-fov": yfov}})
+
+
+def camera_default(width, height, yfov=60.0, position=(0.0, 0.0, 0.0)) -> CameraSpec:
+    """PinholeCamera::adjustToResolution + setYFoV(60) (main.cpp:485-486,
+    PinholeCamera.cpp:156-174)."""
+    half_h = F32(F32(0.5) * F32(height))
+    half_w = F32(F32(0.5) * F32(width))
+    arg = F32(F32(F32(0.5) * F32(yfov)) * F32(math.pi)) / F32(180.0)
+    focus = F32(half_h / F32(tanf(arg)))
+    return CameraSpec(width, height, tuple(position), default_view(position), float(half_w), float(half_h),
+                      float(focus))
+
+
+# ---------------------------------------------------------------- builders --
+
+def _om_conductor(n_rgb, k_rgb, name="om_conductor") -> Material:
+    """IOR tables with points exactly at the three RGB wavelengths (so
+    AssetMaterialIor::getIor returns the given n,k), bracketed by 380 nm and
+    780 nm points so the range check passes (AssetMaterialIor.cpp:140)."""
+    wl = [3.8e-07, RGB_WAVELENGTHS[2], RGB_WAVELENGTHS[1], RGB_WAVELENGTHS[0], 7.8e-07]
+    nv = [n_rgb[2], n_rgb[2], n_rgb[1], n_rgb[0], n_rgb[0]]
+    kv = [k_rgb[2], k_rgb[2], k_rgb[1], k_rgb[0], k_rgb[0]]
+    return Material(type=1, ior_n=np.array(list(zip(wl, nv)), dtype=np.float64),
+                    ior_k=np.array(list(zip(wl, kv)), dtype=np.float64), name=name)
+
+
+def scene_c1(width: int = 256, height: int = 256, spp: int = 16) -> Scene:
+    v, f = icosphere(4)
+    sphere = Mesh(positions=v.astype(F32), normals=(v / np.linalg.norm(v, axis=1, keepdims=True)).astype(F32),
+                  faces=f, material=0, name="icosphere")
+    qv = np.array([[-5, -1, -5], [5, -1, -5], [5, -1, 5], [-5, -1, 5]], dtype=F32)
+    qf = np.array([[0, 2, 1], [0, 3, 2]], dtype=np.uint32)
+    ground = Mesh(positions=qv, normals=np.tile(np.array([0, 1, 0], dtype=F32), (4, 1)), faces=qf, material=1,
+                  name="ground")
+    conductor = _om_conductor((0.18, 0.42, 1.37), (3.42, 2.35, 1.77))
+    diffuse = Material(type=0, base_color=(0.5, 0.5, 0.5, 1.0), metallic=0.0, roughness=1.0, name="ground_diffuse")
+    root_t = np.eye(4, dtype=F32)
+    root_t[2, 3] = -5.0
+    inst = [Instance(root_t.copy(), 0), Instance(root_t.copy(), 1)]
+    light = Light(position=(2.0, 4.0, -3.0), intensity=(50.0, 50.0, 50.0))
+    focus = (height / 2.0) / math.tan(math.radians(22.5))
+    cam = camera_from_json(width, height, width / height, focus, 45.0)
+    nodes = {"root_translation": (0.0, 0.0, -5.0), "light_translation": (2.0, 4.0, 2.0),
+             "light_color": (1.0, 1.0, 1.0), "light_intensity": 50.0}
+    return Scene("c1", [sphere, ground], inst, [conductor, diffuse], [light], None, cam,
+                 RenderSpec(spp, 6, 6, 6), gltf_nodes=[nodes])
+
+
+def make_sky(width: int, height: int, rng: np.random.Generator) -> np.ndarray:
+    """Log-normal sky (mu=0, sigma=1 of the log) from a smooth Gaussian field on
+    the sphere, plus three Gaussian sun lobes of peak 1e4, in the equirect
+    parametrisation HDRBackground::getRadiance reads (row 0 = zenith)."""
+    v = (np.arange(height) + 0.5) / height
+    u = (np.arange(width) + 0.5) / width
+    elev = (0.5 - v) * np.pi
+    phi = u * 2 * np.pi
+    ee, pp = np.meshgrid(elev, phi, indexing="ij")
+    d = np.stack([np.cos(ee) * np.cos(pp), np.cos(ee) * np.sin(pp), np.sin(ee)], -1)
+    g = np.zeros((height, width))
+    modes = 24
+    for _ in range(modes):
+        k = rng.normal(size=3)
+        k *= rng.uniform(0.5, 6.0) / np.linalg.norm(k)
+        g += np.cos(d @ k + rng.uniform(0, 2 * np.pi))
+    g *= (2.0 / modes) ** 0.5  # unit variance
+    sky = np.exp(g)[..., None] * np.array([0.55, 0.7, 1.0])
+    for _ in range(3):
+        e = rng.uniform(0.15, 1.2)
+        a = rng.uniform(0, 2 * np.pi)
+        s = np.array([np.cos(e) * np.cos(a), np.cos(e) * np.sin(a), np.sin(e)])
+        w = math.radians(rng.uniform(1.0, 3.0))
+        ang = np.arccos(np.clip(d @ s, -1, 1))
+        sky += (1e4 * np.exp(-0.5 * (ang / w) ** 2))[..., None] * np.array([1.0, 0.95, 0.85])
+    return rgbe_quantize(sky.astype(F32))
+
+
+def scene_c2(width: int = 1920, height: int = 1080, spp: int = 64, seed: int = 0,
+             tri_scale: float = 1.0) -> Scene:
+    """tri_scale < 1 shrinks the tessellation (for small parity cases)."""
+    rng = np.random.default_rng(seed)
+    meshes, insts, mats = [], [], []
+    sub = 5 if tri_scale >= 1.0 else max(1, int(round(5 + math.log(tri_scale, 4))))
+    nu, nv = max(8, int(round(128 * tri_scale ** 0.5))), max(6, int(round(48 * tri_scale ** 0.5)))
+    for i in range(64):
+        if i % 2 == 0:
+            R = rng.uniform(1.0, 3.0)
+            r = rng.uniform(0.2, 0.8)
+            p, n, f = torus(R, r, nu, nv)
+            m = Mesh(positions=p.astype(F32), normals=n.astype(F32), faces=f, material=i, name=f"torus{i}")
+        else:
+            p, f = displaced_icosphere(sub, rng)
+            m = Mesh(positions=p.astype(F32), normals=None, faces=f, material=i, name=f"blob{i}")
+        meshes.append(m)
+        rot = random_rotation(rng)
+        s = rng.uniform(0.5, 2.0)
+        t = np.array([rng.uniform(-20, 20), rng.uniform(-20, 20), rng.uniform(-60, -20)])
+        M = np.eye(4)
+        M[:3, :3] = rot * s
+        M[:3, 3] = t
+        insts.append(Instance(M.astype(F32), i))
+        mats.append(Material(type=0, base_color=(float(rng.uniform()), float(rng.uniform()), float(rng.uniform()), 1.0),
+                             roughness=float(rng.uniform(0.05, 1.0)), metallic=float(rng.integers(0, 2)),
+                             name=f"pbr{i}"))
+    sky = make_sky(2048, 1024, rng)
+    R = np.array([[1, 0, 0], [0, 0, 1], [0, -1, 0]], dtype=F32)  # main.cpp:401-405 (y-up)
+    hdri = Hdri(sky, R, float(F32(math.pi)))
+    cam = camera_default(width, height)
+    return Scene("c2", meshes, insts, mats, [], hdri, cam, RenderSpec(spp, 10, 10, 10))
+
+
+SCENES = {"c1": scene_c1, "c2": scene_c2}
+
+
+# -------------------------------------------------------------------- RGBE --
+
+def rgbe_encode(rgb: np.ndarray) -> np.ndarray:
+    rgb = np.asarray(rgb, dtype=np.float64)
+    v = rgb.max(axis=-1)
+    out = np.zeros(rgb.shape[:-1] + (4,), dtype=np.uint8)
+    ok = v > 1e-32
+    m, e = np.frexp(v[ok])
+    scale = m * 256.0 / v[ok]
+    out[ok, :3] = np.clip(np.floor(rgb[ok] * scale[:, None]), 0, 255).astype(np.uint8)
+    out[ok, 3] = (e + 128).astype(np.uint8)
+    return out
+
+
+def rgbe_decode(rgbe: np.ndarray) -> np.ndarray:
+    """Radiance RGBE to float, as stb_image's HDR loader converts it:
+    value = byte * 2^(e - 136), zero when e == 0."""
+    e = rgbe[..., 3].astype(np.int32)
+    f = np.ldexp(np.float32(1.0), e - 136).astype(F32)
+    out = rgbe[..., :3].astype(F32) * f[..., None]
+    out[e == 0] = 0.0
+    return out.astype(F32)
+
+
+def rgbe_quantize(rgb: np.ndarray) -> np.ndarray:
+    return rgbe_decode(rgbe_encode(rgb))
+
+
+def write_hdr(path: str, rgb: np.ndarray) -> None:
+    """Flat (uncompressed) RGBE scanlines; the first pixel never starts with
+    the run-length marker bytes 2,2."""
+    h, w, _ = rgb.shape
+    data = rgbe_encode(rgb)
+    if data[0, 0, 0] == 2 and data[0, 0, 1] == 2:
+        raise ValueError("first pixel would read as an RLE marker")
+    with open(path, "wb") as fh:
+        fh.write(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n")
+        fh.write(f"-Y {h} +X {w}\n".encode())
+        fh.write(data.tobytes())
+
+
+def read_hdr(path: str) -> np.ndarray:
+    with open(path, "rb") as fh:
+        raw = fh.read()
+    end = raw.index(b"\n\n") + 2
+    line_end = raw.index(b"\n", end)
+    parts = raw[end:line_end].split()
+    h, w = int(parts[1]), int(parts[3])
+    data = np.frombuffer(raw[line_end + 1:line_end + 1 + 4 * w * h], dtype=np.uint8).reshape(h, w, 4)
+    return rgbe_decode(data)
+
+
+# -------------------------------------------------------------- glTF writer --
+
+def _hexid(tag: str) -> str:
+    h = 0xcbf29ce484222325
+    for ch in tag.encode():
+        h = ((h ^ ch) * 0x100000001b3) & 0xFFFFFFFFFFFFFFFF
+    return f"{h:016x}{(h * 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF:016x}"
+
+
+def _asset_info(asset_type: str, title: str) -> dict:
+    return {"version": "2.0", "generator": "omv synthetic scene generator",
+            "extensions": {"OpenMaterial_asset_info": {
+                "asset_type": asset_type, "id": _hexid(title), "title": title, "asset_version": "1",
+                "asset_variation": "1", "creator": "omv", "description": title}}}
+
+
+def _write_om_material(dirname: str, mat: Material) -> str:
+    ior_file = f"{mat.name}_ior.gltf"
+
+    def table(a):
+        return [[float(w), float(x)] for w, x in a]
+
+    with open(os.path.join(dirname, ior_file), "w") as fh:
+        json.dump({"asset": _asset_info("material_ior", f"IOR {mat.name}"),
+                   "extensions": {"OpenMaterial_ior_data": {"data": [
+                       {"temperature": float(mat.temperature), "n": table(mat.ior_n), "k": table(mat.ior_k)}]}}},
+                  fh, indent=1)
+    mat_file = f"{mat.name}.gltf"
+    params = {
+        "user_preferences": {
+            "geometrical_optics": True, "include_diffraction": False, "include_numerical_simulation": False,
+            "material_scheme": "surface", "material_classification": "solid-metal",
+            "material_type": {"isotropic": True, "homogeneous": True, "magnetic": False},
+            "temperature": float(mat.temperature), "surface_displacement_uri": "",
+            "surface_roughness": {"surface_height_rms": 0.0, "surface_correlation_length": 0.0},
+            "lambert_emission": 0.0, "subsurface": {"subsurface": False, "subsurface_thickness": 0.0},
+            "ingredients": [{"material_ref": "", "order": ""}],
+            "coating_materials": [{"layer_thickness": 0.0, "material_ref": ""}]},
+        "physical_properties": {
+            "refractive_index_uri": ior_file, "mean_free_path": 1e-6, "particle_density": 1.0,
+            "particle_cross_section": 1.0, "emissive_coefficient_uri": "",
+            "detection_wavelength_ranges": [{"min": 3e-07, "max": 8e-07, "typical_sensor": "camera"}],
+            "applicable_sensors": ["camera"], "effective_particle_area": 1.0, "relative_permittivity_uri": "",
+            "relative_permeability_uri": "", "conductivity_uri": "", "acoustic_impedance": 1.0,
+            "shear_velocity": 1.0}}
+    with open(os.path.join(dirname, mat_file), "w") as fh:
+        json.dump({"asset": _asset_info("material", mat.name),
+                   "materials": [{"name": mat.name, "extensions": {"OpenMaterial_material_parameters": params}}],
+                   "extensionsUsed": ["OpenMaterial_asset_info", "OpenMaterial_material_parameters"]}, fh, indent=1)
+    return mat_file
+
+
+def write_gltf(scene: Scene, dirname: str) -> dict:
+    """Writes <name>.gltf/.bin (+ material, IOR, camera and HDR files) and returns
+    the reference command-line flags (main.cpp:161-193) that render it."""
+    os.makedirs(dirname, exist_ok=True)
+    blob = bytearray()
+    accessors, views = [], []
+
+    def add(arr: np.ndarray, comp: int, typ: str, minmax: bool = False) -> int:
+        while len(blob) % 4:
+            blob.append(0)
+        off = len(blob)
+        blob.extend(arr.tobytes())
+        views.append({"buffer": 0, "byteOffset": off, "byteLength": arr.nbytes})
+        acc = {"bufferView": len(views) - 1, "componentType": comp, "count": int(arr.shape[0]), "type": typ}
+        if minmax:
+            acc["min"] = [float(x) for x in arr.min(axis=0)]
+            acc["max"] = [float(x) for x in arr.max(axis=0)]
+        accessors.append(acc)
+        return len(accessors) - 1
+
+    gl_meshes, gl_mats = [], []
+    mat_index = {}
+    for mi, mat in enumerate(scene.materials):
+        if mat.type == 1:
+            uri = _write_om_material(dirname, mat)
+            gl_mats.append({"name": mat.name, "extensions": {"OpenMaterial_reference_link": {
+                "id": _hexid(mat.name), "title": mat.name, "uri": uri}}})
+        else:
+            gm = {"name": mat.name, "pbrMetallicRoughness": {
+                "baseColorFactor": [float(c) for c in mat.base_color], "metallicFactor": float(mat.metallic),
+                "roughnessFactor": float(mat.roughness)}}
+            if mat.double_sided:
+                gm["doubleSided"] = True
+            if mat.alpha_mode:
+                gm["alphaMode"] = ["OPAQUE", "MASK", "BLEND"][mat.alpha_mode]
+                gm["alphaCutoff"] = float(mat.alpha_cutoff)
+            gl_mats.append(gm)
+        mat_index[mi] = mi
+    for m in scene.meshes:
+        attrs = {"POSITION": add(np.ascontiguousarray(m.positions, dtype=F32), 5126, "VEC3", True)}
+        if m.normals is not None:
+            attrs["NORMAL"] = add(np.ascontiguousarray(m.normals, dtype=F32), 5126, "VEC3")
+        if m.tangents is not None:
+            attrs["TANGENT"] = add(np.ascontiguousarray(m.tangents, dtype=F32), 5126, "VEC4")
+        if m.texcoord0 is not None:
+            attrs["TEXCOORD_0"] = add(np.ascontiguousarray(m.texcoord0, dtype=F32), 5126, "VEC2")
+        ind = add(np.ascontiguousarray(m.faces, dtype=np.uint32).reshape(-1), 5125, "SCALAR")
+        prim = {"attributes": attrs, "indices": ind}
+        if 0 <= m.material < len(scene.materials):
+            prim["material"] = mat_index[m.material]
+        gl_meshes.append({"name": m.name, "primitives": [prim]})
+
+    extensions, nodes, scene_nodes = {}, [], []
+    used = ["OpenMaterial_reference_link"] if any(x.type == 1 for x in scene.materials) else []
+    if scene.name == "c1":
+        cfg = scene.gltf_nodes[0]
+        nodes.append({"name": "root", "translation": list(cfg["root_translation"]), "children": [1, 2, 3]})
+        nodes.append({"name": "icosphere", "mesh": 0})
+        nodes.append({"name": "ground", "mesh": 1})
+        nodes.append({"name": "light", "translation": list(cfg["light_translation"]),
+                      "extensions": {"KHR_lights_punctual": {"light": 0}}})
+        extensions["KHR_lights_punctual"] = {"lights": [{"type": "point", "color": list(cfg["light_color"]),
+                                                          "intensity": cfg["light_intensity"]}]}
+        used.append("KHR_lights_punctual")
+        scene_nodes = [0]
+    else:
+        for i, inst in enumerate(scene.instances):
+            M = np.asarray(inst.transform, dtype=F32)
+            nodes.append({"name": f"n{i}", "mesh": inst.mesh,
+                          "matrix": [float(M[r, c]) for c in range(4) for r in range(4)]})
+            scene_nodes.append(i)
+    bin_name = f"{scene.name}.bin"
+    doc = {"asset": {"version": "2.0", "generator": "omv synthetic scene generator"},
+           "scene": 0, "scenes": [{"nodes": scene_nodes}], "nodes": nodes, "meshes": gl_meshes,
+           "materials": gl_mats, "accessors": accessors, "bufferViews": views,
+           "buffers": [{"uri": bin_name, "byteLength": len(blob)}]}
+    if extensions:
+        doc["extensions"] = extensions
+    if used:
+        doc["extensionsUsed"] = used
+    with open(os.path.join(dirname, bin_name), "wb") as fh:
+        fh.write(bytes(blob))
+    gltf = os.path.join(dirname, f"{scene.name}.gltf")
+    with open(gltf, "w") as fh:
+        json.dump(doc, fh)
+    r = scene.render
+    aspect = scene.camera.width / scene.camera.height
+    flags = ["-i", gltf, "-r", str(scene.camera.width), "-a", repr(F32(aspect).item()),
+             "-S", str(r.samples_per_pixel), "-q", str(r.max_path_length), "-B", str(r.camera_bounces),
+             "-b", str(r.light_bounces)]
+    if scene.lights:
+        flags.append("-L")
+    if scene.camera.json_props is not None:
+        cam_path = os.path.join(dirname, f"{scene.name}_camera.json")
+        with open(cam_path, "w") as fh:
+            json.dump(scene.camera.json_props, fh)
+        flags += ["-l", cam_path]
+    if scene.hdri is not None:
+        hdr_path = os.path.join(dirname, f"{scene.name}_sky.hdr")
+        write_hdr(hdr_path, scene.hdri.rgb)
+        flags += ["-H", hdr_path]
+    return {"gltf": gltf, "flags": flags}

@@ -1,0 +1,185 @@
+"""ORACLE -- test infrastructure only.
+
+ctypes wrapper of liboracle.so, the C restatement of the reference renderer's
+hot path (oc_render.c / oc_bvh.c).  Used by the tests as the checker, by
+__graft_entry__.smoke() as the checker and by bench.py as the timed CPU
+reference; never by the product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import importlib
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+capi = importlib.import_module("openmaterial-validation_gb300.capi")
+
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REFERENCE_SEED = 3254638  # RenderScene.cpp:20
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(LIB_PATH) or _stale():
+        subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+    return LIB_PATH
+
+
+def _stale() -> bool:
+    t = os.path.getmtime(LIB_PATH)
+    for f in ("oc_render.c", "oc_bvh.c", "oc_core.h", "oc_bvh.h", "oc_render.h"):
+        if os.path.getmtime(os.path.join(HERE, f)) > t:
+            return True
+    return os.path.getmtime(os.path.join(ROOT, "include", "omv.h")) > t
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        L.oc_scene_create.restype = vp
+        L.oc_scene_create.argtypes = [C.POINTER(capi.SceneDesc)]
+        L.oc_scene_destroy.argtypes = [vp]
+        L.oc_render.argtypes = [vp, C.POINTER(capi.Camera), C.POINTER(capi.Params), C.c_int32, C.c_uint32,
+                                C.c_int32, C.c_int32, C.c_int32, capi.f32p, C.POINTER(C.c_double),
+                                C.POINTER(C.c_uint64)]
+        L.oc_film_stop.argtypes = [capi.f32p, C.c_int64]
+        L.oc_render_ids.argtypes = [vp, C.POINTER(capi.Camera), C.c_uint32, capi.f32p, C.POINTER(capi.Hit)]
+        L.oc_trace_rays.argtypes = [vp, C.c_int64, capi.f32p, C.POINTER(capi.Hit)]
+        for n in ("oc_brdf_eval_direct", "oc_brdf_sample_indirect", "oc_om_fresnel"):
+            getattr(L, n).argtypes = [C.c_int64, capi.f32p, capi.f32p]
+        L.oc_camera_rays.argtypes = [C.POINTER(capi.Camera), capi.f32p, capi.f32p]
+        L.oc_env_radiance.argtypes = [vp, C.c_int64, capi.f32p, capi.f32p]
+        L.oc_mt_uniforms.argtypes = [C.c_uint32, C.c_int64, capi.f32p]
+        L.oc_ior_lookup.restype = C.c_float
+        L.oc_ior_lookup.argtypes = [capi.f32p, C.c_int32, C.c_float]
+        L.oc_scene_mesh_info.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                         C.POINTER(C.c_int32)]
+        L.oc_scene_mesh_vertices.argtypes = [vp, C.c_int32, capi.f32p]
+        L.oc_scene_normal_matrix.argtypes = [vp, C.c_int32, capi.f32p]
+        _lib = L
+    return _lib
+
+
+class OracleScene:
+    def __init__(self, scene) -> None:
+        self.scene = scene
+        self._holder = capi.DescHolder(scene)
+        self.h = lib().oc_scene_create(C.byref(self._holder.desc))
+        if not self.h:
+            raise RuntimeError("oracle: scene has no valid instance")
+
+    def close(self) -> None:
+        if self.h:
+            lib().oc_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def render(self, camera=None, params=None, mode: int = 0, seed: int = REFERENCE_SEED, threads: int = 1,
+               rows=None, variance: bool = False, normalize: bool = True):
+        """Returns (film W*H*4 float32 [normalised like PinholeCamera::stop when
+        normalize], sumsq or None, ray count)."""
+        cam = capi.camera_struct(camera or self.scene.camera)
+        p = params or capi.params_for(self.scene)
+        W, H = cam.width, cam.height
+        r0, r1 = rows if rows is not None else (0, H)
+        film = np.zeros((H, W, 4), dtype=np.float32)
+        sumsq = np.zeros((H, W, 3), dtype=np.float64) if variance else None
+        rays = C.c_uint64(0)
+        rc = lib().oc_render(self.h, C.byref(cam), C.byref(p), mode, seed, threads, r0, r1, capi.fptr(film),
+                             sumsq.ctypes.data_as(C.POINTER(C.c_double)) if variance else None, C.byref(rays))
+        if rc != 0:
+            raise RuntimeError("oracle render failed")
+        if normalize:
+            lib().oc_film_stop(capi.fptr(film), W * H)
+        return film, sumsq, int(rays.value)
+
+    def render_ids(self, camera=None, seed: int = REFERENCE_SEED):
+        cam = capi.camera_struct(camera or self.scene.camera)
+        n = cam.width * cam.height
+        rays = np.zeros((n, 6), dtype=np.float32)
+        hits = np.zeros(n, dtype=capi.HIT_DTYPE)
+        lib().oc_render_ids(self.h, C.byref(cam), seed, capi.fptr(rays), hits.ctypes.data_as(C.POINTER(capi.Hit)))
+        return rays, hits
+
+    def trace(self, rays8: np.ndarray):
+        rays8 = np.ascontiguousarray(rays8, dtype=np.float32)
+        hits = np.zeros(len(rays8), dtype=capi.HIT_DTYPE)
+        lib().oc_trace_rays(self.h, len(rays8), capi.fptr(rays8), hits.ctypes.data_as(C.POINTER(capi.Hit)))
+        return hits
+
+    def env_radiance(self, dirs: np.ndarray) -> np.ndarray:
+        dirs = np.ascontiguousarray(dirs, dtype=np.float32)
+        out = np.zeros((len(dirs), 3), dtype=np.float32)
+        lib().oc_env_radiance(self.h, len(dirs), capi.fptr(dirs), capi.fptr(out))
+        return out
+
+    def mesh_vertices(self, mesh: int) -> np.ndarray:
+        vn, fn, mat = C.c_int32(), C.c_int32(), C.c_int32()
+        lib().oc_scene_mesh_info(self.h, mesh, C.byref(vn), C.byref(fn), C.byref(mat))
+        out = np.zeros((vn.value, 10), dtype=np.float32)
+        lib().oc_scene_mesh_vertices(self.h, mesh, capi.fptr(out))
+        return out
+
+    def mesh_material(self, mesh: int) -> int:
+        vn, fn, mat = C.c_int32(), C.c_int32(), C.c_int32()
+        lib().oc_scene_mesh_info(self.h, mesh, C.byref(vn), C.byref(fn), C.byref(mat))
+        return mat.value
+
+    def normal_matrix(self, inst: int) -> np.ndarray:
+        out = np.zeros(9, dtype=np.float32)
+        lib().oc_scene_normal_matrix(self.h, inst, capi.fptr(out))
+        return out.reshape(3, 3)
+
+
+def _batch(fn, width_in: int, width_out: int, x: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, width_in)
+    out = np.zeros((len(x), width_out), dtype=np.float32)
+    fn(len(x), capi.fptr(x), capi.fptr(out))
+    return out
+
+
+def brdf_eval_direct(x: np.ndarray) -> np.ndarray:
+    return _batch(lib().oc_brdf_eval_direct, 17, 3, x)
+
+
+def brdf_sample_indirect(x: np.ndarray) -> np.ndarray:
+    return _batch(lib().oc_brdf_sample_indirect, 24, 6, x)
+
+
+def om_fresnel(x: np.ndarray) -> np.ndarray:
+    return _batch(lib().oc_om_fresnel, 7, 3, x)
+
+
+def camera_rays(camera, jitter: np.ndarray) -> np.ndarray:
+    cam = capi.camera_struct(camera)
+    jitter = np.ascontiguousarray(jitter, dtype=np.float32)
+    out = np.zeros((cam.width * cam.height, 6), dtype=np.float32)
+    lib().oc_camera_rays(C.byref(cam), capi.fptr(jitter), capi.fptr(out))
+    return out
+
+
+def mt_uniforms(seed: int, n: int) -> np.ndarray:
+    out = np.zeros(n, dtype=np.float32)
+    lib().oc_mt_uniforms(seed, n, capi.fptr(out))
+    return out
+
+
+def ior_lookup(table: np.ndarray, wl: float) -> float:
+    t = np.ascontiguousarray(table, dtype=np.float32)
+    return float(lib().oc_ior_lookup(capi.fptr(t), len(t), wl))
