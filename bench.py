@@ -1,0 +1,321 @@
+"""Benchmark of the GB300 BDPT render path on the large plain-BDPT workload.
+
+Workload (one step = one frame): 64 instanced meshes, 1,048,576 triangles,
+glTF PBR materials, 2048x1024 RGBE HDRI (log-normal sky + three 1e4 sun lobes),
+1920x1080, 64 spp, camera bounces 10, max path length 10, no point lights
+(seeded synthetic scene of that shape; see openmaterial-validation_gb300/scenes.py).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+ours: K frames on cuda:LOCAL_RANK; value = all ranks' paths / max-over-ranks
+device time (CUDA events on the launching stream, L2 flushed between frames,
+flush outside the events).  With N > 1 every rank renders its own sample range
+of the same frame (replicas, no collective in the timed region).
+reference: the CPU reference implementation of the path (the oracle's C port of
+the reference renderer, oracle/oc_render.c, all host threads) on bounded row
+bands of the same frame; rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "BDPT Mpaths/s & Mrays/s at equal RMSE; batched/adjoint vs plain on 1 GB300"
+WORKLOAD = ("plain BDPT, large scene: 64 instances / 1,048,576 triangles, PBR metallic-roughness, "
+            "2048x1024 HDRI, 1920x1080, 64 spp, max path length 10")
+HBM_FALLBACK_GBS = 6800.0
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            j = json.load(fh)
+        return float(j["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+def _traffic_per_launch():
+    """dram bytes per k_extend launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "k_extend_c2_launches.md")
+    try:
+        for line in open(p):
+            if line.strip().startswith("dram_bytes_per_launch:"):
+                return float(line.split(":")[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (200 ms period)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int) -> None:
+        self.index = index
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            out, _ = self.p.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+            out, _ = self.p.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_reference(oracle, scene, spp: int, target_s: float, seed: int = 7, threads: int = None):
+    """Times the oracle port (all host threads) on a centred band of rows sized to
+    about target_s seconds.  Returns (Mpaths/s, Mrays/s, cores, rows, seconds)."""
+    threads = threads or os.cpu_count() or 1
+    os_ = oracle.OracleScene(scene)
+    W, H = scene.camera.width, scene.camera.height
+    p = oracle.capi.params_for(scene, spp=spp)
+    mid = H // 2
+    rows = max(1, min(H, threads))
+    while True:
+        r0 = max(0, mid - rows // 2)
+        t0 = time.perf_counter()
+        _, _, rays = os_.render(params=p, mode=1, threads=threads, rows=(r0, r0 + rows), seed=seed, normalize=False)
+        dt = time.perf_counter() - t0
+        if dt >= 0.5 * target_s or rows >= H:
+            break
+        rows = min(H, max(rows + 1, int(rows * target_s / max(dt, 1e-3))))
+    paths = rows * W * spp
+    os_.close()
+    return paths / dt / 1e6, rays / dt / 1e6, threads, rows, dt
+
+
+def run_reference(args, scene, rank):
+    if rank != 0:
+        return
+    import oracle
+
+    oracle.build()
+    spp = scene.render.samples_per_pixel
+    vals, rvals, rows_used, secs = [], [], 0, []
+    for i in range(args.warmup + args.steps):
+        v, rv, cores, rows, dt = cpu_reference(oracle, scene, spp, target_s=args.ref_step_seconds, seed=100 + i)
+        if i >= args.warmup:
+            vals.append(v)
+            rvals.append(rv)
+            secs.append(dt)
+            rows_used = rows
+    value = statistics.mean(vals)
+    sample = f"rows {scene.camera.height // 2 - rows_used // 2}..+{rows_used} of the 1920x1080 frame at {spp} spp"
+    line = {"metric": METRIC, "value": round(value, 4), "unit": "Mpaths/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * statistics.mean(secs), 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "parallelism": f"{cores} host threads"},
+            "mrays_per_s": round(statistics.mean(rvals), 4),
+            "cpu_baseline": {"value": round(value, 4), "unit": "Mpaths/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 4), "unit": "Mpaths/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, scene, ws, rank, local):
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    omv = importlib.import_module("openmaterial-validation_gb300")
+    if rank == 0:
+        omv.build()
+    if dist:
+        dist.barrier()
+    L = omv.lib()
+    capi = omv.capi
+    rs = omv.RenderScene(scene, device=local)
+    W, H = scene.camera.width, scene.camera.height
+    spp = scene.render.samples_per_pixel
+    npix = W * H
+    cam = capi.camera_struct(scene.camera)
+    params = capi.params_for(scene, spp=spp, seed=1234)
+    params.sample_offset = rank * spp
+    params.time_kernels = 1
+    dev = torch.device("cuda", local)
+    film = torch.zeros(3 * npix, dtype=torch.float64, device=dev)
+    count = torch.zeros(npix, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step(stats):
+        film.zero_()
+        count.zero_()
+        omv.check(L.omv_render_device(rs.handle, C.byref(cam), C.byref(params), C.c_void_p(film.data_ptr()), None,
+                                      C.c_void_p(count.data_ptr()), C.c_void_p(stream.cuda_stream),
+                                      C.byref(stats)))
+
+    for _ in range(args.warmup):
+        step(capi.Stats())
+    torch.cuda.synchronize(dev)
+    if dist:
+        dist.barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    torch.cuda.synchronize(dev)
+    evs = []
+    agg = {k: 0 for k in ("extension_rays", "shadow_rays", "light_rays", "kernel_launches", "nodes_visited",
+                          "triangles_tested", "extend_launches")}
+    ext_ms = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = capi.Stats()
+        step(st)
+        e1.record(stream)
+        evs.append((e0, e1))
+        for k in agg:
+            agg[k] += getattr(st, k)
+        ext_ms += st.extend_ms
+    torch.cuda.synchronize(dev)
+    if dist:
+        dist.barrier()
+    clock = clocks.stop()
+    dev_ms = sum(a.elapsed_time(b) for a, b in evs)
+    t = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    max_ms = float(t.item())
+    cnt_ok = bool((count == spp).all().item())
+    paths = npix * spp * args.steps * ws
+    value = paths / (max_ms / 1e3) / 1e6
+    rays = (agg["extension_rays"] + agg["shadow_rays"] + agg["light_rays"]) * ws
+    # roofline of the closest-hit kernel: algorithmic bytes = nodes x 128 B + triangles x 48 B
+    hbm, peak_kind = _peaks()
+    launches = max(1, agg["extend_launches"])
+    bytes_per_launch = (agg["nodes_visited"] * 128 + agg["triangles_tested"] * 48) / launches
+    ms_per_launch = ext_ms / launches
+    achieved = bytes_per_launch / (ms_per_launch / 1e3) / 1e9 if ms_per_launch > 0 else 0.0
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+            "frac": round(achieved / hbm, 4), "traffic": _traffic_per_launch(), "kernel": "k_extend",
+            "peak_source": peak_kind, "bytes_per_launch": round(bytes_per_launch), "ms_per_launch": round(ms_per_launch, 4),
+            "share_of_step": round(ext_ms / max(dev_ms, 1e-9), 4)}
+    # end to end through the public API: host buffers, H2D of the step's inputs, D2H of the image
+    e2e = None
+    if rank == 0 or ws > 1:
+        img = torch.empty((H, W, 4), dtype=torch.float32, pin_memory=True).numpy()
+        p2 = capi.params_for(scene, spp=spp, seed=99)
+        p2.sample_offset = rank * spp
+        for _ in range(args.warmup):
+            omv.check(L.omv_render(rs.handle, C.byref(cam), C.byref(p2), capi.fptr(img), None, None, None, None))
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            omv.check(L.omv_render(rs.handle, C.byref(cam), C.byref(p2), capi.fptr(img), None, None, None, None))
+            times.append(time.perf_counter() - t0)
+        e2e_t = torch.tensor([sum(times)], dtype=torch.float64, device=dev)
+        if dist:
+            dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
+        e2e = {"value": round(npix * spp * args.steps * ws / float(e2e_t.item()) / 1e6, 4), "unit": "Mpaths/s",
+               "h2d_bytes_per_step": C.sizeof(capi.Camera) + C.sizeof(capi.Params),
+               "d2h_bytes_per_step": int(img.nbytes)}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        import oracle
+
+        oracle.build()
+        v, rv, cores, rows, dt = cpu_reference(oracle, scene, spp, target_s=args.cpu_seconds)
+        cpu = {"value": round(v, 4), "unit": "Mpaths/s", "cores": cores, "kind": "port",
+               "sample": f"rows {H // 2 - rows // 2}..+{rows} of the {W}x{H} frame at {spp} spp ({dt:.1f} s)",
+               "mrays_per_s": round(rv, 4)}
+    if rank == 0:
+        info = rs.info()
+        line = {"metric": METRIC, "value": round(value, 4), "unit": "Mpaths/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(max_ms / args.steps, 3), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": spp,
+                           "max_path_length": scene.render.max_path_length, "triangles": info["triangles"],
+                           "instances": len(scene.instances), "l2": "flushed by a 256 MiB write between timed frames",
+                           "parallelism": f"replicas x{ws} (disjoint sample ranges)", "film": "FP64 sums"},
+                "mrays_per_s": round(rays / (max_ms / 1e3) / 1e6, 4), "film_counts_ok": cnt_ok,
+                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clock,
+                "gpu_launches": agg["kernel_launches"], "scene_build_ms": round(info["build_ms"], 1)}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--spp", type=int, default=64)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=8.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = _dist()
+    if args.impl == "reference" and rank != 0:
+        return
+    S = importlib.import_module("openmaterial-validation_gb300.scenes")
+    scene = S.scene_c2(args.width, args.height, args.spp)
+    if args.impl == "reference":
+        run_reference(args, scene, rank)
+    else:
+        run_ours(args, scene, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -173,6 +173,8 @@ typedef struct omv_params {
     int32_t sample_offset;              /* first sample index (progressive rendering) */
     int32_t accumulate_variance;        /* also accumulate per-pixel sum of squares */
     int32_t wave_paths;                 /* paths per wavefront wave; 0 = automatic */
+    int32_t time_kernels;               /* record CUDA events around every closest-hit
+                                           kernel launch (omv_stats.extend_ms) */
 } omv_params;
 
 /* Fills `p` with the reference defaults (RendererParameters.h:56-89). */
@@ -187,6 +189,12 @@ typedef struct omv_stats {
     int64_t light_rays;
     double render_ms;
     int64_t kernel_launches;
+    int64_t nodes_visited;     /* 8-wide BVH nodes fetched by all closest-hit queries */
+    int64_t triangles_tested;  /* triangle records fetched by all closest-hit queries */
+    double extend_ms;          /* summed device time of the extension-ray kernel (time_kernels) */
+    int64_t extend_launches;
+    double shadow_ms;          /* summed device time of the shadow-ray kernel (time_kernels) */
+    int64_t shadow_launches;
 } omv_stats;
 
 /* BDPTRenderer::render (BDPTRenderer.cpp:372-393) for one camera.
@@ -268,6 +276,13 @@ omv_status omv_env_radiance(omv_scene* scene, int64_t n, const float* dirs, floa
 
 const char* omv_last_error(void);
 const char* omv_version(void);
+
+/* sizeof of the public structs in this order: omv_mesh_desc, omv_instance_desc,
+ * omv_material_desc, omv_light_desc, omv_hdri_desc, omv_scene_desc,
+ * omv_scene_info, omv_camera, omv_params, omv_stats, omv_hit -- for binding
+ * layout checks (no reference counterpart).  With out == NULL returns the
+ * count; otherwise writes min(n, count) sizes and returns that number. */
+int32_t omv_struct_sizes(int64_t* out, int32_t n);
 
 #ifdef __cplusplus
 }

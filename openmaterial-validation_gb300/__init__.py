@@ -1,0 +1,349 @@
+"""GB300-native render path of the OpenMATERIAL validation pathtracer.
+
+Host-side mirror of the reference's renderer facade over the C ABI in
+include/omv.h (libomv.so, hand-written CUDA for sm_103a):
+
+  RenderScene      RenderScene::allocate / set* / commitScene   (RenderScene.h:109-204)
+  PinholeCamera    PinholeCamera + ViewPoint                   (PinholeCamera.h, RenderSensor.h)
+  RendererParameters                                            (RendererParameters.h:20-96)
+  BDPTRenderer     setParameters / setScene / render            (BDPTRenderer.h:147-155)
+
+There is no CPU fallback: every call goes through libomv.so and raises
+OmvError when the library is missing or a call fails.
+"""
+from __future__ import annotations
+
+import concurrent.futures
+import ctypes as C
+import dataclasses
+import json
+import math
+import os
+import subprocess
+from typing import Optional
+
+import numpy as np
+
+from . import capi, scenes
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+REPO_DIR = os.path.dirname(PKG_DIR)
+CSRC = os.path.join(PKG_DIR, "csrc")
+BUILD_DIR = os.path.join(PKG_DIR, "_build")
+LIB_PATH = os.path.join(PKG_DIR, "libomv.so")
+SOURCES = ["bvh_build.cu", "scene.cu", "render.cu", "capi.cu"]
+HEADERS = ["bvh_build.h", "omv_device.cuh", "omv_types.h", "scene.h", "trace.cuh"]
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+NVCC_FLAGS = [ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
+
+
+class OmvError(RuntimeError):
+    pass
+
+
+def _nvcc() -> str:
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if c and (os.path.sep not in c or os.path.exists(c)):
+            return c
+    return "nvcc"
+
+
+def _stale() -> bool:
+    if not os.path.exists(LIB_PATH):
+        return True
+    t = os.path.getmtime(LIB_PATH)
+    deps = [os.path.join(CSRC, f) for f in SOURCES + HEADERS] + [os.path.join(REPO_DIR, "include", "omv.h")]
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compiles libomv.so for sm_103a in-tree (one object per translation unit,
+    compiled in parallel, then linked).  Returns the library path."""
+    if not force and not _stale():
+        return LIB_PATH
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    nvcc = _nvcc()
+
+    def compile_one(src: str) -> str:
+        obj = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
+        cmd = [nvcc, *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise OmvError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+        if verbose:
+            print(r.stderr)
+        return obj
+
+    with concurrent.futures.ThreadPoolExecutor(len(SOURCES)) as ex:
+        objs = list(ex.map(compile_one, SOURCES))
+    tmp = LIB_PATH + ".tmp"
+    r = subprocess.run([nvcc, ARCH, "-shared", "-o", tmp, *objs], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise OmvError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    """The loaded libomv.so (raises OmvError if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise OmvError(f"{LIB_PATH} is missing: run build() first (no CPU fallback exists)")
+    L = C.CDLL(LIB_PATH)
+    vp = C.c_void_p
+    st = C.c_int32
+    L.omv_scene_create.argtypes = [C.POINTER(capi.SceneDesc), C.c_int32, C.POINTER(vp)]
+    L.omv_scene_destroy.argtypes = [vp]
+    L.omv_scene_get_info.argtypes = [vp, C.POINTER(capi.SceneInfo)]
+    L.omv_render.argtypes = [vp, C.POINTER(capi.Camera), C.POINTER(capi.Params), capi.f32p, C.POINTER(C.c_double),
+                             C.POINTER(C.c_double), C.POINTER(C.c_uint32), C.POINTER(capi.Stats)]
+    L.omv_render_device.argtypes = [vp, C.POINTER(capi.Camera), C.POINTER(capi.Params), vp, vp, vp, vp,
+                                    C.POINTER(capi.Stats)]
+    L.omv_trace_rays.argtypes = [vp, C.c_int64, capi.f32p, C.POINTER(capi.Hit)]
+    L.omv_render_ids.argtypes = [vp, C.POINTER(capi.Camera), capi.f32p, C.c_uint64, C.POINTER(capi.Hit),
+                                 C.POINTER(C.c_uint32)]
+    for n in ("omv_brdf_eval_direct", "omv_brdf_sample_indirect", "omv_om_fresnel"):
+        getattr(L, n).argtypes = [C.c_int64, capi.f32p, capi.f32p]
+    L.omv_camera_rays.argtypes = [C.POINTER(capi.Camera), capi.f32p, capi.f32p]
+    L.omv_env_radiance.argtypes = [vp, C.c_int64, capi.f32p, capi.f32p]
+    L.omv_last_error.restype = C.c_char_p
+    L.omv_version.restype = C.c_char_p
+    L.omv_params_default.argtypes = [C.POINTER(capi.Params)]
+    L.omv_params_default.restype = None
+    L.omv_struct_sizes.argtypes = [C.POINTER(C.c_int64), C.c_int32]
+    for n in ("omv_scene_create", "omv_scene_destroy", "omv_scene_get_info", "omv_render", "omv_render_device",
+              "omv_trace_rays", "omv_render_ids", "omv_brdf_eval_direct", "omv_brdf_sample_indirect",
+              "omv_om_fresnel", "omv_camera_rays", "omv_env_radiance", "omv_struct_sizes"):
+        getattr(L, n).restype = st
+    _lib = L
+    return L
+
+
+def check(status: int) -> None:
+    if status != 0:
+        raise OmvError(f"omv status {status}: {lib().omv_last_error().decode(errors='replace')}")
+
+
+# ------------------------------------------------------------ parameters --
+
+@dataclasses.dataclass
+class RendererParameters:
+    """RendererParameters (RendererParameters.h:20-96) plus the build's keys."""
+    cameraBouncesN: int = 10
+    lightBouncesN: int = 10
+    maxPathLength: int = 8
+    samplesPerPixel: int = 20
+    lightDistanceAttenuation: int = 1
+    lightScaleValue: float = 100.0
+    lightMinDistance: float = 0.01
+    rayCutPixValue: float = 0.002
+    seed: int = 0
+    sample_offset: int = 0
+    accumulate_variance: bool = False
+    wave_paths: int = 0
+
+    def to_c(self) -> capi.Params:
+        return capi.Params(camera_bounces=self.cameraBouncesN, light_bounces=self.lightBouncesN, time_kernels=0,
+                           max_path_length=self.maxPathLength, samples_per_pixel=self.samplesPerPixel,
+                           light_distance_attenuation=self.lightDistanceAttenuation,
+                           light_scale=self.lightScaleValue, light_min_distance=self.lightMinDistance,
+                           ray_cut_value=self.rayCutPixValue, seed=self.seed, estimator=0,
+                           sample_offset=self.sample_offset, accumulate_variance=1 if self.accumulate_variance else 0,
+                           wave_paths=self.wave_paths)
+
+    @classmethod
+    def for_scene(cls, scene: scenes.Scene, **kw) -> "RendererParameters":
+        r = scene.render
+        p = cls(cameraBouncesN=r.camera_bounces, lightBouncesN=r.light_bounces, maxPathLength=r.max_path_length,
+                samplesPerPixel=r.samples_per_pixel)
+        for k, v in kw.items():
+            setattr(p, k, v)
+        return p
+
+
+# ---------------------------------------------------------------- camera --
+
+class PinholeCamera:
+    """PinholeCamera (PinholeCamera.cpp): resolution, ViewPoint (position +
+    rotation with columns left/up/forward), half sizes and focus."""
+
+    def __init__(self, width: int, height: int, position=(0.0, 0.0, 0.0), forward=(0.0, 0.0, -1.0),
+                 up=(0.0, 1.0, 0.0)) -> None:
+        self.width, self.height = max(1, int(width)), max(1, int(height))
+        self.position = tuple(float(x) for x in position)
+        self.rotation = scenes.default_view(position, forward, up)
+        self.half_width = 0.0
+        self.half_height = 0.0
+        self.focus = 0.0
+
+    @classmethod
+    def from_spec(cls, spec: scenes.CameraSpec) -> "PinholeCamera":
+        c = cls(spec.width, spec.height, spec.position)
+        c.rotation = np.asarray(spec.rotation, dtype=np.float32)
+        c.half_width, c.half_height, c.focus = spec.half_width, spec.half_height, spec.focus
+        return c
+
+    def adjust_to_resolution(self) -> None:
+        self.half_height = float(np.float32(0.5) * np.float32(self.height))
+        self.half_width = float(np.float32(0.5) * np.float32(self.width))
+
+    def set_y_fov(self, yfov: float) -> None:
+        """PinholeCamera::setYFoV: focus = half_height / tan(fov/2)."""
+        if not (0.0 < yfov < 180.0):
+            raise ValueError("Field-of-view should be greater than zero and smaller than the straight angle.")
+        arg = np.float32(np.float32(np.float32(0.5) * np.float32(yfov)) * np.float32(math.pi)) / np.float32(180.0)
+        self.focus = float(np.float32(self.half_height) / np.float32(scenes.tanf(arg)))
+
+    def load_properties(self, path: str) -> None:
+        """PinholeCamera::loadProperties: pinhole.{aspect, focus, y-fov}."""
+        with open(path) as fh:
+            j = json.load(fh)
+        p = j.get("pinhole", {})
+        spec = scenes.camera_from_json(self.width, self.height, float(p.get("aspect", 0.0)),
+                                       float(p.get("focus", self.focus)), float(p.get("y-fov", 0.0)), self.position)
+        self.half_width, self.half_height, self.focus = spec.half_width, spec.half_height, spec.focus
+
+    def to_c(self) -> capi.Camera:
+        spec = scenes.CameraSpec(self.width, self.height, self.position, np.asarray(self.rotation), self.half_width,
+                                 self.half_height, self.focus)
+        return capi.camera_struct(spec)
+
+
+# ----------------------------------------------------------------- scene --
+
+class RenderScene:
+    """Device scene behind omv_scene_create (RenderScene::commitScene plus the
+    GPU acceleration build)."""
+
+    def __init__(self, scene: scenes.Scene, device: int = 0) -> None:
+        self.spec = scene
+        self._holder = capi.DescHolder(scene)
+        h = C.c_void_p()
+        check(lib().omv_scene_create(C.byref(self._holder.desc), device, C.byref(h)))
+        self.handle = h
+
+    def info(self) -> dict:
+        i = capi.SceneInfo()
+        check(lib().omv_scene_get_info(self.handle, C.byref(i)))
+        return {"triangles": i.num_triangles, "blas_nodes": i.num_blas_nodes, "device_bytes": i.device_bytes,
+                "build_ms": i.build_ms}
+
+    def close(self) -> None:
+        if getattr(self, "handle", None) and self.handle.value:
+            lib().omv_scene_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # closest-hit queries (sceneIntersect) for given rays: (n, 8) org,tnear,dir,tfar
+    def trace(self, rays8: np.ndarray) -> np.ndarray:
+        rays8 = np.ascontiguousarray(rays8, dtype=np.float32)
+        hits = np.zeros(len(rays8), dtype=capi.HIT_DTYPE)
+        check(lib().omv_trace_rays(self.handle, len(rays8), capi.fptr(rays8),
+                                   hits.ctypes.data_as(C.POINTER(capi.Hit))))
+        return hits
+
+    def env_radiance(self, dirs: np.ndarray) -> np.ndarray:
+        dirs = np.ascontiguousarray(dirs, dtype=np.float32)
+        out = np.zeros((len(dirs), 3), dtype=np.float32)
+        check(lib().omv_env_radiance(self.handle, len(dirs), capi.fptr(dirs), capi.fptr(out)))
+        return out
+
+
+class BDPTRenderer:
+    """BDPTRenderer facade (BDPTRenderer.h:147-155) over omv_render."""
+
+    def __init__(self) -> None:
+        self.params: Optional[RendererParameters] = None
+        self.scene: Optional[RenderScene] = None
+        self.last_stats: Optional[dict] = None
+
+    def set_parameters(self, p: RendererParameters) -> None:
+        self.params = p
+
+    def set_scene(self, s: RenderScene) -> None:
+        self.scene = s
+
+    def render(self, camera: PinholeCamera, sums: bool = False):
+        """Renders one frame; returns the normalised RGBA image (H, W, 4) like
+        PinholeCamera::getImpression after stop().  With sums=True returns
+        (image, sum_rgb, sumsq_rgb or None, count)."""
+        if self.params is None or self.scene is None:
+            raise OmvError("set_parameters and set_scene first")
+        cam = camera.to_c()
+        p = self.params.to_c()
+        H, W = cam.height, cam.width
+        img = np.zeros((H, W, 4), dtype=np.float32)
+        s = np.zeros((H, W, 3), dtype=np.float64) if sums else None
+        q = np.zeros((H, W, 3), dtype=np.float64) if (sums and self.params.accumulate_variance) else None
+        cnt = np.zeros((H, W), dtype=np.uint32) if sums else None
+        st = capi.Stats()
+        dp = C.POINTER(C.c_double)
+        check(lib().omv_render(self.scene.handle, C.byref(cam), C.byref(p), capi.fptr(img),
+                               s.ctypes.data_as(dp) if s is not None else None,
+                               q.ctypes.data_as(dp) if q is not None else None,
+                               cnt.ctypes.data_as(C.POINTER(C.c_uint32)) if cnt is not None else None, C.byref(st)))
+        self.last_stats = {"paths": st.paths, "extension_rays": st.extension_rays, "shadow_rays": st.shadow_rays,
+                           "light_rays": st.light_rays, "render_ms": st.render_ms,
+                           "kernel_launches": st.kernel_launches}
+        if sums:
+            return img, s, q, cnt
+        return img
+
+    def render_ids(self, camera: PinholeCamera, jitter: Optional[np.ndarray] = None, seed: int = 0):
+        """Primary-hit identification buffers (pid/gid/mid validation modes):
+        returns (hits structured array (H*W,), global primitive ids (H*W,))."""
+        cam = camera.to_c()
+        n = cam.width * cam.height
+        hits = np.zeros(n, dtype=capi.HIT_DTYPE)
+        gp = np.zeros(n, dtype=np.uint32)
+        j = None
+        if jitter is not None:
+            j = np.ascontiguousarray(jitter, dtype=np.float32).reshape(-1)
+            if len(j) != 2 * n:
+                raise ValueError("jitter must hold 2 uniforms per pixel")
+        check(lib().omv_render_ids(self.scene.handle, C.byref(cam), capi.fptr(j) if j is not None else None, seed,
+                                   hits.ctypes.data_as(C.POINTER(capi.Hit)), gp.ctypes.data_as(C.POINTER(C.c_uint32))))
+        return hits, gp
+
+
+# ------------------------------------------------------ kernel test hooks --
+
+def _hook(name: str, win: int, wout: int, x: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, win)
+    out = np.zeros((len(x), wout), dtype=np.float32)
+    check(getattr(lib(), name)(len(x), capi.fptr(x), capi.fptr(out)))
+    return out
+
+
+def brdf_eval_direct(x: np.ndarray) -> np.ndarray:
+    return _hook("omv_brdf_eval_direct", 17, 3, x)
+
+
+def brdf_sample_indirect(x: np.ndarray) -> np.ndarray:
+    return _hook("omv_brdf_sample_indirect", 24, 6, x)
+
+
+def om_fresnel(x: np.ndarray) -> np.ndarray:
+    return _hook("omv_om_fresnel", 7, 3, x)
+
+
+def camera_rays(camera: PinholeCamera, jitter: np.ndarray) -> np.ndarray:
+    cam = camera.to_c()
+    j = np.ascontiguousarray(jitter, dtype=np.float32)
+    out = np.zeros((cam.width * cam.height, 6), dtype=np.float32)
+    check(lib().omv_camera_rays(C.byref(cam), capi.fptr(j), capi.fptr(out)))
+    return out
+
+
+__all__ = ["build", "lib", "OmvError", "RendererParameters", "PinholeCamera", "RenderScene", "BDPTRenderer",
+           "brdf_eval_direct", "brdf_sample_indirect", "om_fresnel", "camera_rays", "scenes", "capi"]

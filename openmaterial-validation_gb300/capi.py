@@ -72,12 +72,14 @@ class Params(C.Structure):
                 ("samples_per_pixel", C.c_int32), ("light_distance_attenuation", C.c_int32),
                 ("light_scale", C.c_float), ("light_min_distance", C.c_float), ("ray_cut_value", C.c_float),
                 ("seed", C.c_uint64), ("estimator", C.c_int32), ("sample_offset", C.c_int32),
-                ("accumulate_variance", C.c_int32), ("wave_paths", C.c_int32)]
+                ("accumulate_variance", C.c_int32), ("wave_paths", C.c_int32), ("time_kernels", C.c_int32)]
 
 
 class Stats(C.Structure):
     _fields_ = [("paths", C.c_int64), ("extension_rays", C.c_int64), ("shadow_rays", C.c_int64),
-                ("light_rays", C.c_int64), ("render_ms", C.c_double), ("kernel_launches", C.c_int64)]
+                ("light_rays", C.c_int64), ("render_ms", C.c_double), ("kernel_launches", C.c_int64),
+                ("nodes_visited", C.c_int64), ("triangles_tested", C.c_int64), ("extend_ms", C.c_double),
+                ("extend_launches", C.c_int64), ("shadow_ms", C.c_double), ("shadow_launches", C.c_int64)]
 
 
 class Hit(C.Structure):
@@ -98,7 +100,7 @@ def default_params() -> Params:
     return Params(camera_bounces=10, light_bounces=10, max_path_length=8, samples_per_pixel=20,
                   light_distance_attenuation=1, light_scale=100.0, light_min_distance=0.01,
                   ray_cut_value=0.002, seed=0, estimator=0, sample_offset=0, accumulate_variance=0,
-                  wave_paths=0)
+                  wave_paths=0, time_kernels=0)
 
 
 def params_for(scene, spp: int = None, seed: int = 0, variance: bool = False) -> Params:

@@ -1,0 +1,708 @@
+// GPU acceleration-structure build, replacing Embree's BVH build of
+// RenderScene::buildEmbreeScene (RenderScene.cpp:225-272): one bottom-level
+// tree per mesh (Embree: one scene per mesh) and one top-level tree over the
+// instances (Embree: instance geometries in the top scene).
+//
+// Pipeline per tree (all on the device):
+//   1. item boxes + centroid bounds (block reduction, atomics on ordered ints)
+//   2. 30-bit Morton codes of the centroids
+//   3. LSD radix sort of (code, item) pairs, 8-bit digits, stable block ranks
+//      from warp match_any + per-warp digit counts
+//   4. Karras LBVH ("Maximizing parallelism in the construction of BVHs,
+//      octrees, and k-d trees", HPG 2012): one thread per internal node
+//   5. bottom-up boxes with arrival counters
+//   6. top-down collapse into 8-wide nodes (greedy: expand the child of largest
+//      surface area), leaves of at most kLeafMax triangles, child boxes
+//      quantised to 16 bits per bound against the node box, rounded outward and
+//      verified in float so the decoded box always contains the true box.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "bvh_build.h"
+#include "omv_types.h"
+
+namespace omv {
+
+#define OMV_CK(x)                                                                                 \
+    do {                                                                                          \
+        cudaError_t e_ = (x);                                                                     \
+        if (e_ != cudaSuccess)                                                                    \
+            throw std::runtime_error(std::string("CUDA error ") + cudaGetErrorString(e_) + " at " \
+                                     + __FILE__ + ":" + std::to_string(__LINE__));                \
+    } while (0)
+
+namespace {
+
+constexpr int kSortTile = 4096;
+constexpr int kSortThreads = 256;
+
+struct Box {
+    float lo[3], hi[3];
+};
+
+__device__ __forceinline__ uint32_t f2ord(float f)
+{
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(uint32_t u)
+{
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// ---------------------------------------------------------- item boxes ---
+__global__ void k_tri_boxes(int n, const float* __restrict__ pos, const uint32_t* __restrict__ faces, Box* boxes,
+                            uint32_t* cbounds /* 6 ordered: lo xyz, hi xyz */)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float c[3] = {0.f, 0.f, 0.f};
+    bool ok = i < n;
+    if (ok) {
+        Box b;
+        for (int a = 0; a < 3; ++a) {
+            b.lo[a] = 3.0e38f;
+            b.hi[a] = -3.0e38f;
+        }
+        for (int k = 0; k < 3; ++k) {
+            const float* p = pos + 3 * (size_t)faces[3 * (size_t)i + k];
+            for (int a = 0; a < 3; ++a) {
+                b.lo[a] = fminf(b.lo[a], p[a]);
+                b.hi[a] = fmaxf(b.hi[a], p[a]);
+            }
+        }
+        boxes[i] = b;
+        for (int a = 0; a < 3; ++a) c[a] = 0.5f * (b.lo[a] + b.hi[a]);
+    }
+    for (int a = 0; a < 3; ++a) {
+        uint32_t lo = ok ? f2ord(c[a]) : 0xFFFFFFFFu, hi = ok ? f2ord(c[a]) : 0u;
+        for (int o = 16; o; o >>= 1) {
+            lo = min(lo, __shfl_xor_sync(0xFFFFFFFFu, lo, o));
+            hi = max(hi, __shfl_xor_sync(0xFFFFFFFFu, hi, o));
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicMin(&cbounds[a], lo);
+            atomicMax(&cbounds[3 + a], hi);
+        }
+    }
+}
+
+__global__ void k_box_centroid_bounds(int n, const Box* boxes, uint32_t* cbounds)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool ok = i < n;
+    for (int a = 0; a < 3; ++a) {
+        float c = ok ? 0.5f * (boxes[i].lo[a] + boxes[i].hi[a]) : 0.f;
+        uint32_t lo = ok ? f2ord(c) : 0xFFFFFFFFu, hi = ok ? f2ord(c) : 0u;
+        for (int o = 16; o; o >>= 1) {
+            lo = min(lo, __shfl_xor_sync(0xFFFFFFFFu, lo, o));
+            hi = max(hi, __shfl_xor_sync(0xFFFFFFFFu, hi, o));
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicMin(&cbounds[a], lo);
+            atomicMax(&cbounds[3 + a], hi);
+        }
+    }
+}
+
+__device__ __forceinline__ uint32_t expand_bits(uint32_t v)
+{
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+__global__ void k_morton(int n, const Box* boxes, const uint32_t* cbounds, uint32_t* keys, uint32_t* vals)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t q[3];
+    for (int a = 0; a < 3; ++a) {
+        float lo = ord2f(cbounds[a]), hi = ord2f(cbounds[3 + a]);
+        float c = 0.5f * (boxes[i].lo[a] + boxes[i].hi[a]);
+        float ext = hi - lo;
+        float t = ext > 0.f ? (c - lo) / ext : 0.5f;
+        q[a] = (uint32_t)fminf(fmaxf(t * 1024.0f, 0.0f), 1023.0f);
+    }
+    keys[i] = (expand_bits(q[0]) << 2) | (expand_bits(q[1]) << 1) | expand_bits(q[2]);
+    vals[i] = (uint32_t)i;
+}
+
+// ------------------------------------------------------------- sort ---
+__global__ void k_sort_hist(int n, int shift, const uint32_t* __restrict__ keys, uint32_t* hist, int nblocks)
+{
+    __shared__ uint32_t h[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    int base = blockIdx.x * kSortTile;
+    for (int i = base + threadIdx.x; i < min(n, base + kSortTile); i += blockDim.x)
+        atomicAdd(&h[(keys[i] >> shift) & 0xFF], 1u);
+    __syncthreads();
+    for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[d * nblocks + blockIdx.x] = h[d];
+}
+
+// exclusive scan of m entries, one block
+__global__ void k_scan(int m, uint32_t* data)
+{
+    __shared__ uint32_t part[1024];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < m; base += 1024) {
+        int i = base + threadIdx.x;
+        uint32_t v = i < m ? data[i] : 0u;
+        part[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < 1024; o <<= 1) {
+            uint32_t t = threadIdx.x >= o ? part[threadIdx.x - o] : 0u;
+            __syncthreads();
+            part[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (i < m) data[i] = carry + part[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry += part[1023];
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_sort_scatter(int n, int shift, const uint32_t* __restrict__ kin,
+                                                               const uint32_t* __restrict__ vin, uint32_t* kout,
+                                                               uint32_t* vout, const uint32_t* offs, int nblocks)
+{
+    constexpr int W = kSortThreads / 32;
+    __shared__ uint32_t run[256];
+    __shared__ uint32_t cnt[W][256];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int d = threadIdx.x; d < 256; d += blockDim.x) run[d] = offs[d * nblocks + blockIdx.x];
+    const int base = blockIdx.x * kSortTile;
+    const int end = min(n, base + kSortTile);
+    for (int c0 = base; c0 < end; c0 += kSortThreads) {
+        for (int i = threadIdx.x; i < W * 256; i += blockDim.x) (&cnt[0][0])[i] = 0;
+        __syncthreads();
+        int i = c0 + threadIdx.x;
+        bool ok = i < end;
+        uint32_t key = ok ? kin[i] : 0u;
+        uint32_t val = ok ? vin[i] : 0u;
+        uint32_t dig = ok ? (key >> shift) & 0xFF : 256u + lane;  // invalid lanes never match
+        uint32_t peers = __match_any_sync(0xFFFFFFFFu, dig);
+        uint32_t lt = peers & ((1u << lane) - 1u);
+        if (ok && lt == 0) cnt[warp][dig] = __popc(peers);
+        __syncthreads();
+        if (ok) {
+            uint32_t pre = 0;
+            for (int w = 0; w < warp; ++w) pre += cnt[w][dig];
+            uint32_t dst = run[dig] + pre + __popc(lt);
+            kout[dst] = key;
+            vout[dst] = val;
+        }
+        __syncthreads();
+        for (int d = threadIdx.x; d < 256; d += blockDim.x) {
+            uint32_t t = 0;
+            for (int w = 0; w < W; ++w) t += cnt[w][d];
+            run[d] += t;
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------ LBVH ---
+struct Node2 {
+    int left, right;  // >= 0: internal id; < 0: ~leaf position (sorted index)
+    int first, last;  // covered sorted range
+    int parent;
+    Box box;
+};
+
+__device__ __forceinline__ int delta(const uint32_t* k, int n, int i, int j)
+{
+    if (j < 0 || j >= n) return -1;
+    uint32_t a = k[i], b = k[j];
+    return a == b ? 32 + __clz((uint32_t)i ^ (uint32_t)j) : __clz(a ^ b);
+}
+
+__global__ void k_karras(int n, const uint32_t* __restrict__ keys, Node2* nodes, int* leaf_parent)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) > 0 ? 1 : -1;
+    int dmin = delta(keys, n, i, i - d);
+    int lmax = 2;
+    while (delta(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+    int j = i + l * d;
+    int dnode = delta(keys, n, i, j);
+    int s = 0, t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (delta(keys, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    int g = i + s * d + min(d, 0);
+    int lo = min(i, j), hi = max(i, j);
+    Node2& nd = nodes[i];
+    nd.first = lo;
+    nd.last = hi;
+    if (lo == g) {
+        nd.left = ~g;
+        leaf_parent[g] = i;
+    } else {
+        nd.left = g;
+        nodes[g].parent = i;
+    }
+    if (hi == g + 1) {
+        nd.right = ~(g + 1);
+        leaf_parent[g + 1] = i;
+    } else {
+        nd.right = g + 1;
+        nodes[g + 1].parent = i;
+    }
+    if (i == 0) nd.parent = -1;
+}
+
+__device__ __forceinline__ Box box_union(const Box& a, const Box& b)
+{
+    Box r;
+    for (int k = 0; k < 3; ++k) {
+        r.lo[k] = fminf(a.lo[k], b.lo[k]);
+        r.hi[k] = fmaxf(a.hi[k], b.hi[k]);
+    }
+    return r;
+}
+
+__global__ void k_bottom_up(int n, const uint32_t* __restrict__ vals, const Box* __restrict__ item_boxes,
+                            Node2* nodes, const int* leaf_parent, int* arrivals)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int p = leaf_parent[i];
+    for (int guard = 0; p >= 0 && guard < 96; ++guard) {
+        __threadfence();
+        if (atomicAdd(&arrivals[p], 1) == 0) return;
+        __threadfence();
+        Node2& nd = nodes[p];
+        Box bl = nd.left >= 0 ? nodes[nd.left].box : item_boxes[vals[~nd.left]];
+        Box br = nd.right >= 0 ? nodes[nd.right].box : item_boxes[vals[~nd.right]];
+        Box u = box_union(bl, br);
+        volatile float* dst = (volatile float*)&nd.box;
+        for (int k = 0; k < 3; ++k) {
+            dst[k] = u.lo[k];
+            dst[3 + k] = u.hi[k];
+        }
+        p = nd.parent;
+    }
+}
+
+// ---------------------------------------------------------- collapse ---
+struct Work {
+    int node2;  // internal Node2 id, or ~sorted position for a single-item tree
+    uint32_t node8;
+};
+
+__device__ __forceinline__ float half_area(const Box& b)
+{
+    float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+    return dx * dy + dy * dz + dz * dx;
+}
+
+__device__ __forceinline__ void child_info(const Node2* nodes, const uint32_t* vals, const Box* item_boxes, int c,
+                                           Box& b, int& first, int& last)
+{
+    if (c >= 0) {
+        const Node2& nd = nodes[c];
+        volatile const float* src = (volatile const float*)&nd.box;
+        for (int k = 0; k < 3; ++k) {
+            b.lo[k] = src[k];
+            b.hi[k] = src[3 + k];
+        }
+        first = nd.first;
+        last = nd.last;
+    } else {
+        b = item_boxes[vals[~c]];
+        first = last = ~c;
+    }
+}
+
+// exponent byte e such that 2^(e-127) * 65532 >= extent
+__device__ __forceinline__ uint32_t quant_exponent(float ext)
+{
+    if (!(ext > 0.0f)) return 1u;
+    float s = ext / 65532.0f;
+    uint32_t bits = __float_as_uint(s);
+    uint32_t e = (bits >> 23) & 0xFF;
+    if (bits & 0x7FFFFFu) e += 1;  // round up to a power of two
+    if (e < 1) e = 1;
+    if (e > 254) e = 254;
+    return e;
+}
+
+template <bool kTlas>
+__global__ void k_collapse(int nwork, const Work* __restrict__ work, const Node2* nodes, const uint32_t* vals,
+                           const Box* item_boxes, Bvh8Node* out_nodes, uint32_t* node_counter, Work* next_work,
+                           uint32_t* next_count, float4* out_tris, uint32_t* out_items, uint32_t* prim_counter,
+                           const float* pos, const uint32_t* faces, uint32_t node_cap, uint32_t* overflow)
+{
+    int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nwork) return;
+    Work it = work[w];
+    int slot[8];
+    Box sb[8];
+    int sf[8], sl[8];
+    int ns = 0;
+    if (it.node2 < 0) {
+        slot[0] = it.node2;
+        child_info(nodes, vals, item_boxes, slot[0], sb[0], sf[0], sl[0]);
+        ns = 1;
+    } else {
+        const Node2& nd = nodes[it.node2];
+        slot[0] = nd.left;
+        slot[1] = nd.right;
+        child_info(nodes, vals, item_boxes, slot[0], sb[0], sf[0], sl[0]);
+        child_info(nodes, vals, item_boxes, slot[1], sb[1], sf[1], sl[1]);
+        ns = 2;
+        const int leaf_max = kTlas ? 1 : kLeafMax;
+        while (ns < 8) {
+            int best = -1;
+            float ba = -1.0f;
+            bool must = false;
+            for (int s = 0; s < ns; ++s) {
+                if (slot[s] < 0) continue;
+                int cnt = sl[s] - sf[s] + 1;
+                bool m = cnt > leaf_max;
+                float a = half_area(sb[s]);
+                if ((m && !must) || (m == must && a > ba)) {
+                    best = s;
+                    ba = a;
+                    must = m;
+                }
+            }
+            if (best < 0) break;
+            const Node2& e = nodes[slot[best]];
+            int l = e.left, r = e.right;
+            slot[best] = l;
+            child_info(nodes, vals, item_boxes, l, sb[best], sf[best], sl[best]);
+            slot[ns] = r;
+            child_info(nodes, vals, item_boxes, r, sb[ns], sf[ns], sl[ns]);
+            ++ns;
+        }
+    }
+    const int leaf_max = kTlas ? 1 : kLeafMax;
+    Box nb = sb[0];
+    for (int s = 1; s < ns; ++s) nb = box_union(nb, sb[s]);
+    int n_int = 0, n_prim = 0;
+    for (int s = 0; s < ns; ++s) {
+        int cnt = sl[s] - sf[s] + 1;
+        if (cnt > leaf_max)
+            ++n_int;
+        else
+            n_prim += cnt;
+    }
+    uint32_t cbase = n_int ? atomicAdd(node_counter, (uint32_t)n_int) : 0u;
+    uint32_t pbase = n_prim ? atomicAdd(prim_counter, (uint32_t)n_prim) : 0u;
+    if (cbase + n_int > node_cap) {
+        atomicAdd(overflow, 1u);
+        return;
+    }
+    Bvh8Node o;
+    uint32_t e[3];
+    float sc[3];
+    for (int a = 0; a < 3; ++a) {
+        e[a] = quant_exponent(nb.hi[a] - nb.lo[a]);
+        sc[a] = __uint_as_float(e[a] << 23);
+    }
+    o.px = __fsub_rn(nb.lo[0], sc[0]);
+    o.py = __fsub_rn(nb.lo[1], sc[1]);
+    o.pz = __fsub_rn(nb.lo[2], sc[2]);
+    const float p[3] = {o.px, o.py, o.pz};
+    uint32_t imask = 0, meta[8];
+    int rank = 0, off = 0;
+    for (int s = 0; s < 8; ++s) {
+        meta[s] = 0;
+        for (int a = 0; a < 3; ++a) {
+            o.qlo[a][s] = 0xFFFF;
+            o.qhi[a][s] = 0;
+        }
+    }
+    for (int s = 0; s < ns; ++s) {
+        int cnt = sl[s] - sf[s] + 1;
+        for (int a = 0; a < 3; ++a) {
+            float lo = sb[s].lo[a], hi = sb[s].hi[a];
+            int ql = (int)floorf(__fdiv_rn(__fsub_rn(lo, p[a]), sc[a]));
+            int qh = (int)ceilf(__fdiv_rn(__fsub_rn(hi, p[a]), sc[a]));
+            ql = max(0, min(65535, ql));
+            qh = max(0, min(65535, qh));
+            while (ql > 0 && __fadd_rn(p[a], __fmul_rn((float)ql, sc[a])) > lo) --ql;
+            while (qh < 65535 && __fadd_rn(p[a], __fmul_rn((float)qh, sc[a])) < hi) ++qh;
+            ql = ql > 0 ? ql - 1 : 0;          // one quantum of slack each side
+            qh = qh < 65535 ? qh + 1 : 65535;
+            o.qlo[a][s] = (uint16_t)ql;
+            o.qhi[a][s] = (uint16_t)qh;
+        }
+        if (cnt > leaf_max) {
+            imask |= 1u << s;
+            meta[s] = (uint32_t)rank;
+            uint32_t idx = atomicAdd(next_count, 1u);
+            next_work[idx] = Work{slot[s], cbase + (uint32_t)rank};
+            ++rank;
+        } else {
+            meta[s] = ((uint32_t)cnt << 5) | (uint32_t)off;
+            for (int k = 0; k < cnt; ++k) {
+                uint32_t item = vals[sf[s] + k];
+                uint32_t dst = pbase + (uint32_t)(off + k);
+                if (kTlas) {
+                    out_items[dst] = item;
+                } else {
+                    const uint32_t* f = faces + 3 * (size_t)item;
+                    const float* a0 = pos + 3 * (size_t)f[0];
+                    const float* a1 = pos + 3 * (size_t)f[1];
+                    const float* a2 = pos + 3 * (size_t)f[2];
+                    out_tris[3 * (size_t)dst + 0] = make_float4(a0[0], a0[1], a0[2], __uint_as_float(item));
+                    out_tris[3 * (size_t)dst + 1] = make_float4(a1[0], a1[1], a1[2], 0.0f);
+                    out_tris[3 * (size_t)dst + 2] = make_float4(a2[0], a2[1], a2[2], 0.0f);
+                }
+            }
+            off += cnt;
+        }
+    }
+    o.exps = e[0] | (e[1] << 8) | (e[2] << 16) | (imask << 24);
+    o.child_base = cbase;
+    o.prim_base = pbase;
+    o.meta_lo = meta[0] | (meta[1] << 8) | (meta[2] << 16) | (meta[3] << 24);
+    o.meta_hi = meta[4] | (meta[5] << 8) | (meta[6] << 16) | (meta[7] << 24);
+    out_nodes[it.node8] = o;
+}
+
+template <typename T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    explicit DBuf(size_t count) : n(count)
+    {
+        if (count) OMV_CK(cudaMalloc(&p, sizeof(T) * count));
+    }
+    ~DBuf() { cudaFree(p); }
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+};
+
+inline int blocks(size_t n, int t) { return (int)((n + t - 1) / t); }
+
+// sorts (keys, vals) in place; tmp buffers provided
+void radix_sort(int n, uint32_t* keys, uint32_t* vals, uint32_t* k2, uint32_t* v2, cudaStream_t st)
+{
+    int nb = blocks(n, kSortTile);
+    DBuf<uint32_t> hist((size_t)nb * 256);
+    uint32_t *ki = keys, *vi = vals, *ko = k2, *vo = v2;
+    for (int shift = 0; shift < 32; shift += 8) {
+        k_sort_hist<<<nb, 256, 0, st>>>(n, shift, ki, hist.p, nb);
+        k_scan<<<1, 1024, 0, st>>>(nb * 256, hist.p);
+        k_sort_scatter<<<nb, kSortThreads, 0, st>>>(n, shift, ki, vi, ko, vo, hist.p, nb);
+        std::swap(ki, ko);
+        std::swap(vi, vo);
+    }
+    OMV_CK(cudaGetLastError());
+    // four passes: the result is back in (keys, vals)
+}
+
+}  // namespace
+
+// Builds one tree over n items whose boxes are in `item_boxes` (device).
+// Appends nodes at node_base... of `out_nodes`, primitives at prim_base... .
+static uint32_t build_tree(bool tlas, int n, Box* item_boxes, uint32_t* cbounds, const float* pos,
+                           const uint32_t* faces, Bvh8Node* out_nodes, uint32_t* node_counter, uint32_t node_cap,
+                           float4* out_tris, uint32_t* out_items, uint32_t* prim_counter, uint32_t* overflow,
+                           cudaStream_t st)
+{
+    DBuf<uint32_t> keys(n), vals(n), k2(n), v2(n);
+    k_morton<<<blocks(n, 256), 256, 0, st>>>(n, item_boxes, cbounds, keys.p, vals.p);
+    radix_sort(n, keys.p, vals.p, k2.p, v2.p, st);
+    int ni = n > 1 ? n - 1 : 1;
+    DBuf<Node2> nodes(ni);
+    DBuf<int> leaf_parent(n), arrivals(ni);
+    OMV_CK(cudaMemsetAsync(arrivals.p, 0, sizeof(int) * ni, st));
+    Work root{};
+    if (n > 1) {
+        k_karras<<<blocks(n - 1, 256), 256, 0, st>>>(n, keys.p, nodes.p, leaf_parent.p);
+        k_bottom_up<<<blocks(n, 256), 256, 0, st>>>(n, vals.p, item_boxes, nodes.p, leaf_parent.p, arrivals.p);
+        root.node2 = 0;
+    } else {
+        root.node2 = ~0;
+    }
+    uint32_t root_index = 0;
+    OMV_CK(cudaMemcpyAsync(&root_index, node_counter, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    OMV_CK(cudaStreamSynchronize(st));
+    root.node8 = root_index;
+    uint32_t one = root_index + 1;
+    OMV_CK(cudaMemcpyAsync(node_counter, &one, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    DBuf<Work> wa(n + 1), wb(n + 1);
+    DBuf<uint32_t> cnt(1);
+    OMV_CK(cudaMemcpyAsync(wa.p, &root, sizeof(Work), cudaMemcpyHostToDevice, st));
+    int nwork = 1;
+    Work *cur = wa.p, *nxt = wb.p;
+    for (int level = 0; nwork > 0; ++level) {
+        if (level > 200) throw std::runtime_error("BVH collapse did not terminate");
+        OMV_CK(cudaMemsetAsync(cnt.p, 0, sizeof(uint32_t), st));
+        if (tlas)
+            k_collapse<true><<<blocks(nwork, 128), 128, 0, st>>>(nwork, cur, nodes.p, vals.p, item_boxes, out_nodes,
+                                                                 node_counter, nxt, cnt.p, out_tris, out_items,
+                                                                 prim_counter, pos, faces, node_cap, overflow);
+        else
+            k_collapse<false><<<blocks(nwork, 128), 128, 0, st>>>(nwork, cur, nodes.p, vals.p, item_boxes, out_nodes,
+                                                                  node_counter, nxt, cnt.p, out_tris, out_items,
+                                                                  prim_counter, pos, faces, node_cap, overflow);
+        OMV_CK(cudaGetLastError());
+        uint32_t h = 0;
+        OMV_CK(cudaMemcpyAsync(&h, cnt.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        OMV_CK(cudaStreamSynchronize(st));
+        nwork = (int)h;
+        std::swap(cur, nxt);
+    }
+    return root_index;
+}
+
+void validate_accel(const AccelResult& a, const std::vector<MeshGeom>& meshes, cudaStream_t st);
+
+void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<InstanceGeom>& insts, AccelResult& out,
+                 cudaStream_t st)
+{
+    size_t total_tri = 0;
+    for (const auto& m : meshes) total_tri += m.num_faces;
+    const uint32_t node_cap = (uint32_t)(total_tri + 2 * meshes.size() + 2 * insts.size() + 16);
+    OMV_CK(cudaMalloc(&out.nodes, sizeof(Bvh8Node) * node_cap));
+    OMV_CK(cudaMalloc(&out.tris, sizeof(float4) * 3 * (total_tri ? total_tri : 1)));
+    OMV_CK(cudaMalloc(&out.tlas_items, sizeof(uint32_t) * (insts.size() ? insts.size() : 1)));
+    DBuf<uint32_t> counters(3);  // nodes, prims, overflow
+    OMV_CK(cudaMemsetAsync(counters.p, 0, sizeof(uint32_t) * 3, st));
+    DBuf<uint32_t> cb(6);
+    out.blas_root.assign(meshes.size(), 0xFFFFFFFFu);
+    for (size_t mi = 0; mi < meshes.size(); ++mi) {
+        const MeshGeom& m = meshes[mi];
+        if (!m.valid || m.num_faces <= 0) continue;
+        DBuf<Box> boxes(m.num_faces);
+        uint32_t init[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
+        OMV_CK(cudaMemcpyAsync(cb.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
+        k_tri_boxes<<<blocks(m.num_faces, 256), 256, 0, st>>>(m.num_faces, m.d_pos, m.d_faces, boxes.p, cb.p);
+        OMV_CK(cudaGetLastError());
+        out.blas_root[mi] = build_tree(false, m.num_faces, boxes.p, cb.p, m.d_pos, m.d_faces, out.nodes, counters.p,
+                                       node_cap, out.tris, nullptr, counters.p + 1, counters.p + 2, st);
+    }
+    // top level: world boxes of the valid instances, widened so that no
+    // object-space hit is ever culled by world-space rounding
+    std::vector<Box> ib;
+    std::vector<uint32_t> ids;
+    for (size_t i = 0; i < insts.size(); ++i) {
+        const InstanceGeom& g = insts[i];
+        if (!g.valid) continue;
+        const float* lo = meshes[g.mesh].lo;
+        const float* hi = meshes[g.mesh].hi;
+        Box b;
+        for (int a = 0; a < 3; ++a) {
+            b.lo[a] = 3e38f;
+            b.hi[a] = -3e38f;
+        }
+        for (int c = 0; c < 8; ++c) {
+            double p[3] = {(c & 1) ? hi[0] : lo[0], (c & 2) ? hi[1] : lo[1], (c & 4) ? hi[2] : lo[2]};
+            for (int a = 0; a < 3; ++a) {
+                double w = (double)g.xf[a][0] * p[0] + (double)g.xf[a][1] * p[1] + (double)g.xf[a][2] * p[2] +
+                           (double)g.xf[a][3];
+                b.lo[a] = std::min(b.lo[a], (float)w);
+                b.hi[a] = std::max(b.hi[a], (float)w);
+            }
+        }
+        for (int a = 0; a < 3; ++a) {
+            float pad = (b.hi[a] - b.lo[a]) * 1e-5f + (std::fabs(b.lo[a]) + std::fabs(b.hi[a])) * 1e-5f + 1e-20f;
+            b.lo[a] -= pad;
+            b.hi[a] += pad;
+        }
+        ib.push_back(b);
+        ids.push_back((uint32_t)i);
+    }
+    out.num_valid_instances = (uint32_t)ib.size();
+    if (!ib.empty()) {
+        int n = (int)ib.size();
+        DBuf<Box> boxes(n);
+        DBuf<uint32_t> idmap(n);
+        OMV_CK(cudaMemcpyAsync(boxes.p, ib.data(), sizeof(Box) * n, cudaMemcpyHostToDevice, st));
+        uint32_t init[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
+        OMV_CK(cudaMemcpyAsync(cb.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
+        k_box_centroid_bounds<<<blocks(n, 256), 256, 0, st>>>(n, boxes.p, cb.p);
+        OMV_CK(cudaMemsetAsync(counters.p + 1, 0, sizeof(uint32_t), st));
+        out.tlas_root = build_tree(true, n, boxes.p, cb.p, nullptr, nullptr, out.nodes, counters.p, node_cap, nullptr,
+                                   out.tlas_items, counters.p + 1, counters.p + 2, st);
+        // TLAS items are positions in `ids`; translate to instance indices
+        std::vector<uint32_t> items(n);
+        OMV_CK(cudaMemcpyAsync(items.data(), out.tlas_items, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, st));
+        OMV_CK(cudaStreamSynchronize(st));
+        for (auto& x : items) x = ids[x];
+        OMV_CK(cudaMemcpyAsync(out.tlas_items, items.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, st));
+    }
+    uint32_t hc[3];
+    OMV_CK(cudaMemcpyAsync(hc, counters.p, sizeof(hc), cudaMemcpyDeviceToHost, st));
+    OMV_CK(cudaStreamSynchronize(st));
+    if (hc[2]) throw std::runtime_error("BVH node capacity exceeded");
+    out.num_nodes = hc[0];
+    out.num_tris = total_tri;
+    validate_accel(out, meshes, st);
+}
+
+// Host walk of the finished trees before any traversal runs: every child index,
+// primitive range and instance id in bounds, every node reached exactly once.
+void validate_accel(const AccelResult& a, const std::vector<MeshGeom>& meshes, cudaStream_t st)
+{
+    std::vector<Bvh8Node> nodes(a.num_nodes);
+    std::vector<float4> tris(3 * a.num_tris);
+    std::vector<uint32_t> items(a.num_valid_instances);
+    OMV_CK(cudaMemcpyAsync(nodes.data(), a.nodes, sizeof(Bvh8Node) * nodes.size(), cudaMemcpyDeviceToHost, st));
+    if (!tris.empty())
+        OMV_CK(cudaMemcpyAsync(tris.data(), a.tris, sizeof(float4) * tris.size(), cudaMemcpyDeviceToHost, st));
+    if (!items.empty())
+        OMV_CK(cudaMemcpyAsync(items.data(), a.tlas_items, sizeof(uint32_t) * items.size(), cudaMemcpyDeviceToHost, st));
+    OMV_CK(cudaStreamSynchronize(st));
+    std::vector<uint8_t> seen(nodes.size(), 0);
+    auto walk = [&](uint32_t root, bool tlas, uint32_t prim_limit, uint32_t face_limit) {
+        std::vector<std::pair<uint32_t, int>> stack{{root, 0}};
+        while (!stack.empty()) {
+            auto [n, depth] = stack.back();
+            stack.pop_back();
+            if (n >= nodes.size() || seen[n] || depth > 64) throw std::runtime_error("BVH validation: bad node index");
+            seen[n] = 1;
+            const Bvh8Node& nd = nodes[n];
+            const uint32_t imask = nd.exps >> 24;
+            for (int s = 0; s < 8; ++s) {
+                const uint32_t meta = ((s < 4 ? nd.meta_lo : nd.meta_hi) >> (8 * (s & 3))) & 0xFFu;
+                if ((imask >> s) & 1u) {
+                    stack.push_back({nd.child_base + meta, depth + 1});
+                } else if (meta) {
+                    const uint32_t cnt = meta >> 5, off = meta & 31u;
+                    if (cnt == 0 || cnt > (uint32_t)(tlas ? 1 : kLeafMax) ||
+                        (uint64_t)nd.prim_base + off + cnt > prim_limit)
+                        throw std::runtime_error("BVH validation: bad leaf range");
+                    for (uint32_t k = 0; k < cnt; ++k) {
+                        const uint32_t id = nd.prim_base + off + k;
+                        if (tlas) {
+                            if (items[id] >= face_limit) throw std::runtime_error("BVH validation: bad instance id");
+                        } else {
+                            uint32_t prim;
+                            std::memcpy(&prim, &tris[3 * (size_t)id].w, 4);
+                            if (prim >= face_limit) throw std::runtime_error("BVH validation: bad primitive id");
+                        }
+                    }
+                }
+            }
+        }
+    };
+    for (size_t i = 0; i < meshes.size(); ++i)
+        if (a.blas_root[i] != 0xFFFFFFFFu) walk(a.blas_root[i], false, (uint32_t)a.num_tris, (uint32_t)meshes[i].num_faces);
+    if (a.num_valid_instances) walk(a.tlas_root, true, a.num_valid_instances, 0xFFFFFFFFu);
+}
+
+}  // namespace omv

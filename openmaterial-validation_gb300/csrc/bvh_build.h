@@ -1,0 +1,43 @@
+// GPU build of the two-level 8-wide BVH (see bvh_build.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "omv_types.h"
+
+namespace omv {
+
+struct MeshGeom {
+    bool valid = false;
+    int num_faces = 0;
+    const float* d_pos = nullptr;       // device, 3 floats per vertex
+    const uint32_t* d_faces = nullptr;  // device, 3 indices per face
+    float lo[3] = {0, 0, 0};            // exact bounds of the referenced vertices
+    float hi[3] = {0, 0, 0};
+};
+
+struct InstanceGeom {
+    bool valid = false;
+    int mesh = -1;
+    float xf[3][4] = {};
+};
+
+struct AccelResult {
+    Bvh8Node* nodes = nullptr;       // device; owned by the caller after the build
+    float4* tris = nullptr;          // device
+    uint32_t* tlas_items = nullptr;  // device
+    uint32_t num_nodes = 0;
+    size_t num_tris = 0;
+    std::vector<uint32_t> blas_root;  // per mesh, 0xFFFFFFFF when the mesh is invalid
+    uint32_t tlas_root = 0xFFFFFFFFu;
+    uint32_t num_valid_instances = 0;
+};
+
+// Builds every BLAS and the TLAS; throws std::runtime_error on CUDA errors.
+void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<InstanceGeom>& insts, AccelResult& out,
+                 cudaStream_t stream);
+
+}  // namespace omv

@@ -1,0 +1,105 @@
+// Device data layout of a committed scene, shared by host and device code.
+//
+// HBM layout (all arrays 16-byte aligned, read through the read-only path):
+//   nodes   : 8-wide BVH nodes, 128 B each (one L2 line); all per-mesh BLAS
+//             trees and the instance TLAS live in one array
+//   tris    : 48 B per triangle in BLAS-leaf order: 3 x float4 (v0.xyz + primID,
+//             v1.xyz, v2.xyz), object space of its mesh
+//   verts   : 48 B per vertex: (p.xyz, n.x) (n.yz, t.xy) (t.zw, 0, 0)
+//   faces   : 3 x u32 per face, vertex indices local to the mesh
+//   insts   : per instance object<->world transforms, normal matrix and ids
+//   env     : equirectangular RGB as float4 texels
+#pragma once
+
+#include <cstdint>
+
+#include "../../include/omv.h"
+
+namespace omv {
+
+// 8-wide BVH node, 128 bytes = 8 x uint4:
+//   w0 = (px, py, pz, ex | ey<<8 | ez<<16 | imask<<24)
+//   w1 = (child_base, prim_base, meta[0..3], meta[4..7])
+//   w2..w4 = qlo x/y/z as 8 x u16;  w5..w7 = qhi x/y/z as 8 x u16
+// child slot i box: lo = p + qlo[i] * 2^(e-127), hi = p + qhi[i] * 2^(e-127).
+// imask bit i: slot i is an internal node, at child_base + meta[i].
+// leaf slot: meta = (count << 5) | offset, primitives prim_base + offset ...
+// empty slot: imask bit clear and meta = 0.
+struct alignas(16) Bvh8Node {
+    float px, py, pz;
+    uint32_t exps;
+    uint32_t child_base;
+    uint32_t prim_base;
+    uint32_t meta_lo, meta_hi;
+    uint16_t qlo[3][8];
+    uint16_t qhi[3][8];
+};
+static_assert(sizeof(Bvh8Node) == 128, "BVH8 node must be 128 bytes");
+
+constexpr int kLeafMax = 3;  // triangles per leaf slot
+
+struct alignas(16) DevInstance {
+    float inv[12];  // world -> object, 3x4 row-major
+    float xf[12];   // object -> world
+    float nrm[9];   // normal matrix (inverse transpose of the 3x3 part)
+    uint32_t mesh;
+    uint32_t blas_root;
+    uint32_t material;
+    uint32_t face_base;
+    uint32_t vert_base;
+    uint32_t valid;
+    uint32_t pad[1];
+};
+
+enum : int32_t { kMatPbr = 0, kMatOm = 1, kMatMissing = 2 };
+
+// material constants precomputed at commit (PhysicallyBasedMaterial with no
+// textures, OpenMaterial with IOR evaluated at the RGB wavelengths)
+struct alignas(16) DevMaterial {
+    int32_t type;
+    int32_t transmissive;
+    int32_t masked;
+    int32_t om_valid;
+    float color[4];
+    float metal;
+    float alpha;  // roughness^2
+    float eta;    // 1 / ior, or 1 when double sided
+    float pad0;
+    float om_n[4];
+    float om_k[4];
+};
+
+struct DevEnv {
+    const float4* rgb;
+    int32_t width, height;
+    float rot[9];
+    float scale;
+    int32_t present;
+};
+
+struct DevScene {
+    const uint4* nodes;
+    uint32_t tlas_root;
+    uint32_t num_instances;
+    const float4* tris;
+    const DevInstance* insts;
+    const float4* verts;
+    const uint32_t* faces;
+    const DevMaterial* mats;
+    int32_t num_materials;  // including the missing material (last)
+    int32_t num_lights;
+    const float4* light_pos;  // xyz, attenuation distance
+    const float4* light_int;  // xyz intensity, w unused
+    const float* light_cdf;
+    float light_max;
+    DevEnv env;
+};
+
+// hit record of a closest-hit query
+struct alignas(16) HitRec {
+    uint32_t inst;  // kInvalid on a miss
+    uint32_t prim;
+    float u, v;
+};
+
+}  // namespace omv

@@ -1,0 +1,899 @@
+// Wavefront bidirectional render loop: the device form of
+// BDPTRenderer::render -> renderRow -> computePaths (BDPTRenderer.cpp:237-393).
+//
+// A frame of W*H*spp paths is processed in waves of up to `wave_cap` paths.
+// Per wave (all launches on one stream, queue sizes stay on the device):
+//   light stage  (only with point lights)
+//     k_light_gen       light pick + uniformSphere emission (tryComputeLightPath)
+//     k_extend          closest hit of every queued ray
+//     k_light_shade     surface point, BRDF sample, light-vertex store, cut-off
+//   camera stage
+//     k_camera_gen      jittered pinhole rays (PinholeCamera::getRay)
+//     k_extend
+//     k_camera_shade    surface point, BRDF sample, environment on escape,
+//                       light/camera vertex connections -> shadow queue
+//     k_shadow          isConnected (closest hit + end-point test), add
+//   k_film              per-path radiance into the FP64 film (PinholeCamera::hit)
+// Queues are SoA-packed float4 records appended with warp-aggregated atomics
+// (ballot + popc); the tracing kernels are persistent and fetch 32 rays per
+// warp from an atomic work counter.  Random numbers are Philox4x32-10 keyed by
+// (pixel, sample, vertex) so any partition of the work gives the same image.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "omv_device.cuh"
+#include "scene.h"
+#include "trace.cuh"
+
+namespace omv {
+
+namespace {
+
+constexpr int kTraceThreads = 128;
+constexpr int kShadeThreads = 256;
+
+// counter slots within RenderScratch::ctr (reset per wave)
+constexpr int kCtrLight = 0;     // + bounce (0..light_bounces)
+constexpr int kCtrCam = 64;      // + bounce (0..camera_bounces)
+constexpr int kCtrShadow = 128;  // + bounce
+constexpr int kCtrWork = 192;    // + launch index
+enum { kStatExt = 0, kStatShadow = 1, kStatLight = 2, kStatNodes = 3, kStatTris = 4, kStatOverflow = 5 };
+
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want)
+{
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, want);
+    if (!m) return 0;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    return base + __popc(m & ((1u << lane) - 1u));
+}
+
+struct Surf {
+    V3 pos, nrm, tan, bin;
+    float tw;
+    uint32_t mat;
+    uint32_t inst;
+    uint32_t face;
+    uint32_t vert_base;
+    uint32_t face_base;
+};
+
+__device__ __forceinline__ V3 m33(const float* m, V3 v)
+{
+    return v3(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[3] * v.x + m[4] * v.y + m[5] * v.z,
+              m[6] * v.x + m[7] * v.y + m[8] * v.z);
+}
+
+// BDPTRenderer::computeSurfacePoint -> RenderMesh::computeSurfacePoint
+// (RenderMesh.cpp:159-196), then SurfacePoint::applyTextureNormal((0,0,1))
+// (SurfacePoint.cpp:19-34) as every material's modifyFrame without a normal map
+__device__ __forceinline__ Surf surface_point(const DevScene& S, uint32_t inst, uint32_t prim, float u, float v,
+                                              bool frame)
+{
+    const DevInstance* I = S.insts + inst;
+    Surf sp;
+    sp.inst = inst;
+    sp.face = prim;
+    sp.mat = __ldg(&I->material);
+    sp.vert_base = __ldg(&I->vert_base);
+    sp.face_base = __ldg(&I->face_base);
+    const uint32_t* F = S.faces + 3 * (size_t)(sp.face_base + prim);
+    const uint32_t f0 = __ldg(F), f1 = __ldg(F + 1), f2 = __ldg(F + 2);
+    const float b0 = 1.0f - u - v, b1 = u, b2 = v;
+    const float4* V0 = S.verts + 3 * (size_t)(sp.vert_base + f0);
+    const float4* V1 = S.verts + 3 * (size_t)(sp.vert_base + f1);
+    const float4* V2 = S.verts + 3 * (size_t)(sp.vert_base + f2);
+    const float4 a0 = __ldg(V0), a1 = __ldg(V1), a2 = __ldg(V2);
+    V3 pp = v3(b0 * a0.x + b1 * a1.x + b2 * a2.x, b0 * a0.y + b1 * a1.y + b2 * a2.y, b0 * a0.z + b1 * a1.z + b2 * a2.z);
+    float m[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) m[k] = __ldg(&I->xf[k]);
+    sp.pos = v3(m[0] * pp.x + m[1] * pp.y + m[2] * pp.z + m[3], m[4] * pp.x + m[5] * pp.y + m[6] * pp.z + m[7],
+                m[8] * pp.x + m[9] * pp.y + m[10] * pp.z + m[11]);
+    if (!frame) return sp;
+    const float4 c0 = __ldg(V0 + 1), c1 = __ldg(V1 + 1), c2 = __ldg(V2 + 1);
+    const float4 d0 = __ldg(V0 + 2), d1 = __ldg(V1 + 2), d2 = __ldg(V2 + 2);
+    V3 pn = v3(b0 * a0.w + b1 * a1.w + b2 * a2.w, b0 * c0.x + b1 * c1.x + b2 * c2.x, b0 * c0.y + b1 * c1.y + b2 * c2.y);
+    V3 pt = v3(b0 * c0.z + b1 * c1.z + b2 * c2.z, b0 * c0.w + b1 * c1.w + b2 * c2.w, b0 * d0.x + b1 * d1.x + b2 * d2.x);
+    float tw = b0 * d0.y + b1 * d1.y + b2 * d2.y;
+    tw = tw >= 0.0f ? 1.0f : -1.0f;
+    pn = normalize_if_needed(pn);
+    const float tn = dot(pn, pt);
+    pt = normalize_if_needed(pt - pn * tn);
+    V3 pbn = cross(pn, pt) * tw;
+    float nm[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) nm[k] = __ldg(&I->nrm[k]);
+    V3 n = normalize_if_needed(m33(nm, pn));
+    V3 t = normalize_if_needed(m33(nm, pt));
+    V3 b = normalize_if_needed(m33(nm, pbn));
+    // applyTextureNormal((0,0,1)): nn = 0*t + 0*b + 1*n
+    n = normalize_if_needed(t * 0.0f + b * 0.0f + n * 1.0f);
+    t = normalize_if_needed(cross(b, n));
+    b = cross(n, t) * tw;
+    sp.nrm = n;
+    sp.tan = t;
+    sp.bin = b;
+    sp.tw = tw;
+    return sp;
+}
+
+// triangleNormal of the hit face through the normal matrix, normalised
+// (OpenMaterial.cpp:76-86)
+__device__ __forceinline__ V3 face_normal(const DevScene& S, const Surf& sp)
+{
+    const uint32_t* F = S.faces + 3 * (size_t)(sp.face_base + sp.face);
+    const float4 p0 = __ldg(S.verts + 3 * (size_t)(sp.vert_base + __ldg(F)));
+    const float4 p1 = __ldg(S.verts + 3 * (size_t)(sp.vert_base + __ldg(F + 1)));
+    const float4 p2 = __ldg(S.verts + 3 * (size_t)(sp.vert_base + __ldg(F + 2)));
+    V3 e1 = v3(p1.x - p0.x, p1.y - p0.y, p1.z - p0.z);
+    V3 e2 = v3(p2.x - p0.x, p2.y - p0.y, p2.z - p0.z);
+    float nm[9];
+    const DevInstance* I = S.insts + sp.inst;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) nm[k] = __ldg(&I->nrm[k]);
+    return normalize(m33(nm, cross(e1, e2)));
+}
+
+// RenderMaterial::getRayAndBrdf of each material kind; u = the vertex's uniforms
+__device__ __forceinline__ V3 material_sample(const DevScene& S, const DevMaterial& M, const Surf& sp, V3 in, bool inv,
+                                              const Rng4& u, V3& out)
+{
+    if (M.type == kMatPbr) {  // PhysicallyBasedMaterial::getRayAndBrdf (:248-291)
+        BsdfIn d;
+        d.I = in;
+        d.N = sp.nrm;
+        d.T = sp.tan;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) d.color[i] = M.color[i];
+        d.metal = M.metal;
+        d.alpha = M.alpha;
+        d.eta = M.eta;
+        d.transmissive = M.transmissive != 0;
+        return bsdf_sample_indirect(d, u.u[0], u.u[1], u.u[2], out);
+    }
+    if (M.type == kMatOm) {  // OpenMaterial::defineNextDirection + getRayAndBrdf (:72-93, :165-232)
+        out = reflect3(in, sp.nrm);
+        V3 tfn = face_normal(S, sp);
+        float corr = dot(out, tfn);
+        if (corr < 0.1f) out = normalize(tfn * (0.1f - corr) + out);
+        if (!M.om_valid) return v3(0.0f, 0.0f, 0.0f);
+        float c = dot(out, sp.nrm);
+        return v3(om_channel(M.om_n[0], M.om_k[0], c), om_channel(M.om_n[1], M.om_k[1], c),
+                  om_channel(M.om_n[2], M.om_k[2], c));
+    }
+    // missing material: DiffuseColorMaterial (uniform hemisphere, brdf = albedo)
+    out = to_basis(sp.tan, sp.bin, sp.nrm, uniform_hemisphere(u.u[0], u.u[1]));
+    (void)inv;
+    return v3(M.color[0], M.color[1], M.color[2]);
+}
+
+// RenderMaterial::getBrdf (impSmpScale = false) for a connection
+__device__ __forceinline__ V3 material_eval(const DevMaterial& M, const Surf& sp, V3 in, V3 out)
+{
+    if (M.type == kMatPbr) {  // PhysicallyBasedMaterial::getBrdf (:178-245)
+        V3 N = sp.nrm;
+        if (dot(in, N) > 0.0f && M.transmissive) N = -N;
+        return bsdf_eval_direct(in, out, N, M.color, M.metal, M.alpha);
+    }
+    if (M.type == kMatOm) {  // OpenMaterial::getBrdf (:95-163): mirror directions only
+        if (!M.om_valid) return v3(0.0f, 0.0f, 0.0f);
+        float c = -dot(in, sp.nrm);
+        if (fabsf(dot(out, sp.nrm) - c) > 1e-6f) return v3(0.0f, 0.0f, 0.0f);
+        return v3(om_channel(M.om_n[0], M.om_k[0], c), om_channel(M.om_n[1], M.om_k[1], c),
+                  om_channel(M.om_n[2], M.om_k[2], c));
+    }
+    return v3(M.color[0], M.color[1], M.color[2]);
+}
+
+// BDPTRenderer::sceneIntersect (BDPTRenderer.cpp:75-102): closest hit, skipping
+// alpha-masked materials up to 10 times; tnear persists like the reference's
+// RTCRayHit does across the bounces of one path
+__device__ __forceinline__ bool scene_intersect(const DevScene& S, const uint32_t* items, V3 o, V3 d, float& tnear,
+                                                float tfar, RayHit& h, TraceStack& st, TraceCounters& tc)
+{
+    const float t1 = tfar;
+    for (int itr = 0; itr < 10; ++itr) {
+        if (!trace_closest(S, items, o, d, tnear, tfar, h, st, tc)) return false;
+        const uint32_t mat = __ldg(&S.insts[h.inst].material);
+        if (!S.mats[mat].masked) return true;
+        V3 org = v3(o.x + h.t * d.x, o.y + h.t * d.y, o.z + h.t * d.z);
+        float vv = max_abs(org, 1.0f);
+        vv = vv > h.t ? vv : h.t;
+        const float delta = kEpsAcc * kEps * vv;
+        tnear = h.t + delta;
+        tfar = t1;
+        if (tfar <= tnear) return false;
+    }
+    return false;
+}
+
+struct WaveArgs {
+    DevScene S;
+    const uint32_t* items;
+    omv_camera cam;
+    uint64_t seed;
+    int64_t wave_base;
+    int32_t wave_n;
+    int32_t wave_cap;
+    int32_t npix;
+    int32_t sample_offset;
+    int32_t cam_bounces, light_bounces, max_len;
+    int32_t atten_mode;
+    float light_scale, min_dist, cut;
+    RenderScratch R;
+};
+
+__device__ __forceinline__ void path_ids(const WaveArgs& A, int k, uint32_t& pixel, uint32_t& sample)
+{
+    const int64_t g = A.wave_base + k;
+    pixel = (uint32_t)(g % A.npix);
+    sample = (uint32_t)(A.sample_offset + g / A.npix);
+}
+
+// ------------------------------------------------------------ raygen ---
+__global__ void __launch_bounds__(kShadeThreads) k_camera_gen(WaveArgs A)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool ok = k < A.wave_n;
+    uint32_t pixel = 0, sample = 0;
+    V3 O = v3(0, 0, 0), R = v3(0, 0, 1);
+    if (ok) {
+        path_ids(A, k, pixel, sample);
+        Rng4 r = rng4(A.seed, pixel, sample, 0u, kStreamCamera);
+        camera_ray(A.cam, (int)(pixel % A.cam.width), (int)(pixel / A.cam.width), r.u[0], r.u[1], O, R);
+        A.R.tp[k] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        A.R.rad[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    const uint32_t slot = warp_append(&A.R.ctr[kCtrCam + 1], ok);
+    if (ok) {
+        V3 so = shifted_origin(O, R, 1.0f);
+        A.R.rq[0][2 * (size_t)slot] = make_float4(so.x, so.y, so.z, 0.0f);
+        A.R.rq[0][2 * (size_t)slot + 1] = make_float4(R.x, R.y, R.z, __int_as_float(k));
+    }
+}
+
+// tryComputeLightPath (BDPTRenderer.cpp:194-206): sampleLight + getRandomRay
+__global__ void __launch_bounds__(kShadeThreads) k_light_gen(WaveArgs A)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool ok = k < A.wave_n;
+    V3 O = v3(0, 0, 0), R = v3(0, 0, 1);
+    if (ok) {
+        uint32_t pixel, sample;
+        path_ids(A, k, pixel, sample);
+        const DevScene& S = A.S;
+        // DistanceRandom::getValue (DistanceRandom.h:98-115)
+        const float d = rng4(A.seed, pixel, sample, 0u, kStreamLight).u[0] * S.light_max;
+        int li = 0;
+        const int N = S.num_lights;
+        if (N > 1) {
+            if (d <= S.light_cdf[0])
+                li = 0;
+            else if (d >= S.light_cdf[N - 2])
+                li = N - 1;
+            else {
+                int L = 0, Rr = N - 1;
+                while (L < Rr) {
+                    int C = (L + Rr) / 2;
+                    if (d <= S.light_cdf[C])
+                        Rr = C;
+                    else
+                        L = C + 1;
+                }
+                li = (L + Rr) / 2;
+            }
+        }
+        // RandomSampler::uniformSphere: rejection in the [0,1)^3 cube
+        V3 v = v3(1.0f, 0.0f, 0.0f);
+        float sl = 1.0f;
+        for (uint32_t t = 0; t < 64; ++t) {
+            Rng4 r = rng4(A.seed, pixel, sample, 1u + t, kStreamLight);
+            v = v3(r.u[0], r.u[1], r.u[2]);
+            sl = dot(v, v);
+            if (!(sl > 1.0f || sl < kEps)) break;
+        }
+        R = v * (1.0f / sqrtf(sl));
+        const float4 lp = __ldg(S.light_pos + li);
+        const float4 I = __ldg(S.light_int + li);
+        O = v3(lp.x, lp.y, lp.z);
+        const V3 rad = v3(I.x * A.light_scale, I.y * A.light_scale, I.z * A.light_scale);
+        A.R.ltp[k] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        A.R.lrad[k] = make_float4(rad.x, rad.y, rad.z, 1.0f);
+        A.R.lmeta[k] = (uint32_t)li | (1u << 16);
+        A.R.lv_pos[k] = make_float4(O.x, O.y, O.z, 0.0f);
+        A.R.lv_rad[k] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+    }
+    const bool push = ok && A.light_bounces >= 1;
+    const uint32_t slot = warp_append(&A.R.ctr[kCtrLight + 1], push);
+    if (push) {
+        V3 so = shifted_origin(O, R, 1.0f);
+        A.R.rq[1][2 * (size_t)slot] = make_float4(so.x, so.y, so.z, 0.0f);
+        A.R.rq[1][2 * (size_t)slot + 1] = make_float4(R.x, R.y, R.z, __int_as_float(k));
+    }
+}
+
+// ------------------------------------------------------------ extend ---
+// persistent closest-hit over one ray queue (count at *count)
+__global__ void __launch_bounds__(kTraceThreads) k_extend(DevScene S, const uint32_t* items, float4* rq, uint4* hits,
+                                                          const uint32_t* count, uint32_t* work,
+                                                          unsigned long long* stats, int stat_kind)
+{
+    __shared__ uint2 sstack[kStackShared * kTraceThreads];
+    TraceStack st;
+    st.sh = sstack + threadIdx.x;
+    st.stride = kTraceThreads;
+    st.overflow = 0;
+    TraceCounters tc{0u, 0u};
+    const uint32_t n = *count;
+    const int lane = threadIdx.x & 31;
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(work, 32u);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= n) break;
+        const uint32_t i = base + lane;
+        if (i < n) {
+            float4 a = rq[2 * (size_t)i], b = rq[2 * (size_t)i + 1];
+            V3 o = v3(a.x, a.y, a.z), d = v3(b.x, b.y, b.z);
+            float tnear = a.w;
+            RayHit h;
+            uint4 out;
+            if (scene_intersect(S, items, o, d, tnear, kFltMax, h, st, tc))
+                out = make_uint4(h.inst, h.prim, __float_as_uint(h.u), __float_as_uint(h.v));
+            else
+                out = make_uint4(kInvalid, kInvalid, 0u, 0u);
+            hits[i] = out;
+            if (tnear != a.w) rq[2 * (size_t)i].w = tnear;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&stats[stat_kind], (unsigned long long)n);
+    uint32_t nodes = tc.nodes, tris = tc.tris;
+    for (int o = 16; o; o >>= 1) {
+        nodes += __shfl_xor_sync(0xFFFFFFFFu, nodes, o);
+        tris += __shfl_xor_sync(0xFFFFFFFFu, tris, o);
+    }
+    const bool ov = __any_sync(0xFFFFFFFFu, st.overflow);
+    if (lane == 0) {
+        atomicAdd(&stats[kStatNodes], (unsigned long long)nodes);
+        atomicAdd(&stats[kStatTris], (unsigned long long)tris);
+        if (ov) atomicAdd(&stats[kStatOverflow], 1ull);
+    }
+}
+
+// ------------------------------------------------------- light shade ---
+// BDPTRenderer::computePath for the light subpath (inv = false), vertex b
+__global__ void __launch_bounds__(kShadeThreads) k_light_shade(WaveArgs A, int b, const float4* rq_in,
+                                                                float4* rq_out)
+{
+    const uint32_t n = A.R.ctr[kCtrLight + b];
+    const DevScene& S = A.S;
+    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+        const uint32_t i = i0 + threadIdx.x;
+        bool push = false;
+        V3 so = v3(0, 0, 0), O = v3(0, 0, 1);
+        float tnear = 0.0f;
+        int k = 0;
+        if (i < n) {
+            const float4 ra = rq_in[2 * (size_t)i], rb = rq_in[2 * (size_t)i + 1];
+            const uint4 h = A.R.hits[i];
+            k = __float_as_int(rb.w);
+            tnear = ra.w;
+            if (h.x != kInvalid) {
+                uint32_t pixel, sample;
+                path_ids(A, k, pixel, sample);
+                const Surf sp = surface_point(S, h.x, h.y, __uint_as_float(h.z), __uint_as_float(h.w), true);
+                const DevMaterial M = S.mats[sp.mat];
+                const V3 in = v3(rb.x, rb.y, rb.z);
+                const Rng4 u = rng4(A.seed, pixel, sample, kDimLightBounce + (uint32_t)b, kStreamLight);
+                const V3 brdf = material_sample(S, M, sp, in, false, u, O);
+                const float ct = fabsf(dot(in, sp.nrm));
+                const float4 tp0 = A.R.ltp[k];
+                float4 lr = A.R.lrad[k];
+                const V3 tp = v3(tp0.x * brdf.x * ct, tp0.y * brdf.y * ct, tp0.z * brdf.z * ct);
+                const uint32_t meta = A.R.lmeta[k];
+                const uint32_t li = meta & 0xFFFFu;
+                if (b == 1) {
+                    const float4 lp = __ldg(S.light_pos + li);
+                    const V3 d = sp.pos - v3(lp.x, lp.y, lp.z);
+                    lr.w = light_attenuation(A.atten_mode, A.min_dist, sqrtf(dot(d, d)), lp.w);
+                    A.R.lrad[k] = lr;
+                }
+                const V3 orad = v3(tp.x * lr.x * lr.w, tp.y * lr.y * lr.w, tp.z * lr.z * lr.w);
+                if (!(intensity(orad) < A.cut)) {
+                    const size_t slot = (size_t)b * A.wave_cap + k;
+                    A.R.lv_pos[slot] = make_float4(sp.pos.x, sp.pos.y, sp.pos.z, 0.0f);
+                    A.R.lv_rad[slot] = make_float4(orad.x, orad.y, orad.z, 0.0f);
+                    A.R.lmeta[k] = li | ((uint32_t)(b + 1) << 16);
+                    A.R.ltp[k] = make_float4(tp.x, tp.y, tp.z, 0.0f);
+                    if (b < A.light_bounces && (tp.x != 0.0f || tp.y != 0.0f || tp.z != 0.0f)) {
+                        push = true;
+                        so = shifted_origin(sp.pos, O, 1.0f);
+                    }
+                }
+            }
+        }
+        const uint32_t slot = warp_append(&A.R.ctr[kCtrLight + b + 1], push);
+        if (push) {
+            rq_out[2 * (size_t)slot] = make_float4(so.x, so.y, so.z, tnear);
+            rq_out[2 * (size_t)slot + 1] = make_float4(O.x, O.y, O.z, __int_as_float(k));
+        }
+    }
+}
+
+// ------------------------------------------------------ camera shade ---
+// BDPTRenderer::computePath for the camera subpath (inv = true), vertex b, plus
+// the escape term and the connections of computePaths (:251-298) at vertex b
+__global__ void __launch_bounds__(kShadeThreads) k_camera_shade(WaveArgs A, int b, const float4* rq_in,
+                                                                 float4* rq_out)
+{
+    const uint32_t n = A.R.ctr[kCtrCam + b];
+    const DevScene& S = A.S;
+    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+        const uint32_t i = i0 + threadIdx.x;
+        bool push = false;
+        V3 so = v3(0, 0, 0), O = v3(0, 0, 1);
+        float tnear = 0.0f;
+        int k = 0;
+        if (i < n) {
+            const float4 ra = rq_in[2 * (size_t)i], rb = rq_in[2 * (size_t)i + 1];
+            const uint4 h = A.R.hits[i];
+            k = __float_as_int(rb.w);
+            tnear = ra.w;
+            const V3 in = v3(rb.x, rb.y, rb.z);
+            const float4 tp4 = A.R.tp[k];
+            const V3 tp = v3(tp4.x, tp4.y, tp4.z);
+            if (h.x == kInvalid) {
+                // escape: background x throughput when cp_len <= maxPathLength (:251-258)
+                if (S.env.present && b <= A.max_len) {
+                    const V3 bg = env_radiance(S.env, in);
+                    float4 r = A.R.rad[k];
+                    r.x += bg.x * tp.x;
+                    r.y += bg.y * tp.y;
+                    r.z += bg.z * tp.z;
+                    A.R.rad[k] = r;
+                }
+            } else {
+                uint32_t pixel, sample;
+                path_ids(A, k, pixel, sample);
+                const Surf sp = surface_point(S, h.x, h.y, __uint_as_float(h.z), __uint_as_float(h.w), true);
+                const DevMaterial M = S.mats[sp.mat];
+                const Rng4 u = rng4(A.seed, pixel, sample, (uint32_t)b, kStreamCamera);
+                const V3 brdf = material_sample(S, M, sp, in, true, u, O);
+                const float ct = fabsf(dot(O, sp.nrm));
+                const V3 tpn = v3(tp.x * brdf.x * ct, tp.y * brdf.y * ct, tp.z * brdf.z * ct);
+                if (S.num_lights > 0) {
+                    const uint32_t meta = A.R.lmeta[k];
+                    const int lp_len = (int)(meta >> 16);
+                    const uint32_t li = meta & 0xFFFFu;
+                    const V3 outV = -in;
+                    for (int li_v = 0; li_v < lp_len && li_v + b <= A.max_len; ++li_v) {
+                        const size_t slot = (size_t)li_v * A.wave_cap + k;
+                        const float4 lp = A.R.lv_pos[slot];
+                        const V3 lPos = v3(lp.x, lp.y, lp.z);
+                        V3 lRad;
+                        const V3 LC = normalize(sp.pos - lPos);
+                        if (li_v == 0) {
+                            const float4 I = __ldg(S.light_int + li);
+                            const float4 L = __ldg(S.light_pos + li);
+                            const V3 dd = sp.pos - lPos;
+                            const float lsc = light_attenuation(A.atten_mode, A.min_dist, sqrtf(dot(dd, dd)), L.w);
+                            const float f = A.light_scale * lsc;
+                            lRad = v3(I.x * f, I.y * f, I.z * f);
+                        } else {
+                            const float4 lr = A.R.lv_rad[slot];
+                            lRad = v3(lr.x, lr.y, lr.z);
+                        }
+                        const float c = fabsf(dot(LC, sp.nrm));
+                        V3 lc = v3(lRad.x * c * tp.x, lRad.y * c * tp.y, lRad.z * c * tp.z);
+                        if (intensity(lc) < A.cut) continue;
+                        V3 f = material_eval(M, sp, LC, outV) * c;
+                        lc = v3(f.x * tp.x * lRad.x, f.y * tp.y * lRad.y, f.z * tp.z * lRad.z);
+                        if (intensity(lc) < A.cut) continue;
+                        const uint32_t sl = atomicAdd(&A.R.ctr[kCtrShadow + b], 1u);
+                        float4* q = A.R.sq + 3 * (size_t)sl;
+                        q[0] = make_float4(lPos.x, lPos.y, lPos.z, __int_as_float(k));
+                        q[1] = make_float4(sp.pos.x, sp.pos.y, sp.pos.z, 0.0f);
+                        q[2] = make_float4(lc.x, lc.y, lc.z, 0.0f);
+                    }
+                }
+                A.R.tp[k] = make_float4(tpn.x, tpn.y, tpn.z, 0.0f);
+                if (b < A.cam_bounces && (tpn.x != 0.0f || tpn.y != 0.0f || tpn.z != 0.0f)) {
+                    push = true;
+                    so = shifted_origin(sp.pos, O, 1.0f);
+                }
+            }
+        }
+        const uint32_t slot = warp_append(&A.R.ctr[kCtrCam + b + 1], push);
+        if (push) {
+            rq_out[2 * (size_t)slot] = make_float4(so.x, so.y, so.z, tnear);
+            rq_out[2 * (size_t)slot + 1] = make_float4(O.x, O.y, O.z, __int_as_float(k));
+        }
+    }
+}
+
+// ------------------------------------------------------------ shadow ---
+// BDPTRenderer::isConnected (BDPTRenderer.cpp:208-235)
+__global__ void __launch_bounds__(kTraceThreads) k_shadow(DevScene S, const uint32_t* items, const float4* sq,
+                                                          const uint32_t* count, uint32_t* work, float4* rad,
+                                                          unsigned long long* stats)
+{
+    __shared__ uint2 sstack[kStackShared * kTraceThreads];
+    TraceStack st;
+    st.sh = sstack + threadIdx.x;
+    st.stride = kTraceThreads;
+    st.overflow = 0;
+    TraceCounters tc{0u, 0u};
+    const uint32_t n = *count;
+    const int lane = threadIdx.x & 31;
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(work, 32u);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= n) break;
+        const uint32_t i = base + lane;
+        if (i < n) {
+        const float4 q0 = sq[3 * (size_t)i], q1 = sq[3 * (size_t)i + 1], q2 = sq[3 * (size_t)i + 2];
+        const V3 A = v3(q0.x, q0.y, q0.z), B = v3(q1.x, q1.y, q1.z);
+        const int k = __float_as_int(q0.w);
+        V3 dir = B - A;
+        const float len = sqrtf(dot(dir, dir));
+        float maxsz = max_abs(A, 1.0f);
+        float safeD = 2.0f * kEpsAcc * kEps * maxsz;
+        bool connected = true;
+        if (!(len <= safeD)) {
+            dir = v3(dir.x / len, dir.y / len, dir.z / len);
+            float tnear = safeD;
+            const float tfar = len + (0.1f * len > safeD ? 0.1f * len : safeD);
+            RayHit h;
+            if (scene_intersect(S, items, A, dir, tnear, tfar, h, st, tc)) {
+                const Surf sp = surface_point(S, h.inst, h.prim, h.u, h.v, false);
+                const V3 dd = sp.pos - B;
+                const float sd = dot(dd, dd);
+                const float sb = 10.0f * kEps * max_abs(B, 1.0f);
+                connected = sd <= sb * sb;
+            }
+        }
+        if (connected) {
+            atomicAdd(&rad[k].x, q2.x);
+            atomicAdd(&rad[k].y, q2.y);
+            atomicAdd(&rad[k].z, q2.z);
+        }
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&stats[kStatShadow], (unsigned long long)n);
+    uint32_t nodes = tc.nodes, tris = tc.tris;
+    for (int o = 16; o; o >>= 1) {
+        nodes += __shfl_xor_sync(0xFFFFFFFFu, nodes, o);
+        tris += __shfl_xor_sync(0xFFFFFFFFu, tris, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&stats[kStatNodes], (unsigned long long)nodes);
+        atomicAdd(&stats[kStatTris], (unsigned long long)tris);
+    }
+}
+
+// -------------------------------------------------------------- film ---
+// PinholeCamera::hit (PinholeCamera.cpp:97-108), FP64 accumulation
+__global__ void __launch_bounds__(kShadeThreads) k_film(WaveArgs A, double* sum, double* sumsq, uint32_t* count)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= A.wave_n) return;
+    uint32_t pixel, sample;
+    path_ids(A, k, pixel, sample);
+    const float4 r = A.R.rad[k];
+    atomicAdd(sum + 3 * (size_t)pixel, (double)r.x);
+    atomicAdd(sum + 3 * (size_t)pixel + 1, (double)r.y);
+    atomicAdd(sum + 3 * (size_t)pixel + 2, (double)r.z);
+    if (sumsq) {
+        atomicAdd(sumsq + 3 * (size_t)pixel, (double)r.x * r.x);
+        atomicAdd(sumsq + 3 * (size_t)pixel + 1, (double)r.y * r.y);
+        atomicAdd(sumsq + 3 * (size_t)pixel + 2, (double)r.z * r.z);
+    }
+    atomicAdd(count + pixel, 1u);
+}
+
+// ------------------------------------------------------------ ID pass ---
+__global__ void k_ids(DevScene S, const uint32_t* items, omv_camera cam, const float* jitter, uint64_t seed,
+                      omv_hit* out, uint32_t* gprim, const uint32_t* face_prefix)
+{
+    __shared__ uint2 sstack[kStackShared * kTraceThreads];
+    TraceStack st;
+    st.sh = sstack + threadIdx.x;
+    st.stride = kTraceThreads;
+    st.overflow = 0;
+    TraceCounters tc{0u, 0u};
+    const int npix = cam.width * cam.height;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    float ux, uy;
+    if (jitter) {
+        ux = jitter[2 * (size_t)p];
+        uy = jitter[2 * (size_t)p + 1];
+    } else {
+        Rng4 r = rng4(seed, (uint32_t)p, 0u, 0u, kStreamCamera);
+        ux = r.u[0];
+        uy = r.u[1];
+    }
+    V3 O, R;
+    camera_ray(cam, p % cam.width, p / cam.width, ux, uy, O, R);
+    const V3 so = shifted_origin(O, R, 1.0f);
+    float tnear = 0.0f;
+    RayHit h;
+    omv_hit o;
+    if (scene_intersect(S, items, so, R, tnear, kFltMax, h, st, tc)) {
+        const DevInstance* I = S.insts + h.inst;
+        o.inst = h.inst;
+        o.geom = I->mesh;
+        o.prim = h.prim;
+        o.material = I->material;
+        o.t = h.t;
+        o.u = h.u;
+        o.v = h.v;
+        if (gprim) gprim[p] = face_prefix[I->mesh] + h.prim;
+    } else {
+        o.inst = o.geom = o.prim = o.material = kInvalid;
+        o.t = o.u = o.v = 0.0f;
+        if (gprim) gprim[p] = kInvalid;
+    }
+    o.pad = 0;
+    out[p] = o;
+}
+
+__global__ void k_trace_rays(DevScene S, const uint32_t* items, int64_t n, const float* rays, omv_hit* out)
+{
+    __shared__ uint2 sstack[kStackShared * kTraceThreads];
+    TraceStack st;
+    st.sh = sstack + threadIdx.x;
+    st.stride = kTraceThreads;
+    st.overflow = 0;
+    TraceCounters tc{0u, 0u};
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* r = rays + 8 * i;
+    float tnear = r[3];
+    RayHit h;
+    omv_hit o;
+    if (scene_intersect(S, items, v3(r[0], r[1], r[2]), v3(r[4], r[5], r[6]), tnear, r[7], h, st, tc)) {
+        const DevInstance* I = S.insts + h.inst;
+        o.inst = h.inst;
+        o.geom = I->mesh;
+        o.prim = h.prim;
+        o.material = I->material;
+        o.t = h.t;
+        o.u = h.u;
+        o.v = h.v;
+    } else {
+        o.inst = o.geom = o.prim = o.material = kInvalid;
+        o.t = o.u = o.v = 0.0f;
+    }
+    o.pad = 0;
+    out[i] = o;
+}
+
+__global__ void k_env(DevEnv env, int64_t n, const float* dirs, float* rgb)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    V3 v = env.present ? env_radiance(env, v3(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2])) : v3(0, 0, 0);
+    rgb[3 * i] = v.x;
+    rgb[3 * i + 1] = v.y;
+    rgb[3 * i + 2] = v.z;
+}
+
+inline int grid_for(int64_t n, int t) { return (int)std::max<int64_t>(1, (n + t - 1) / t); }
+
+}  // namespace
+
+// -------------------------------------------------------------- host ---
+
+static void ensure_scratch(SceneHost& s, int64_t wave_cap, int light_slots, int shadow_slots)
+{
+    RenderScratch& R = s.scratch;
+    if (R.base && R.wave_cap >= wave_cap && R.light_slots >= light_slots && R.shadow_slots >= shadow_slots) return;
+    if (R.base) {
+        OMV_CUDA(cudaStreamSynchronize(s.stream));
+        cudaFree(R.base);
+        R = RenderScratch{};
+    }
+    const size_t W = (size_t)wave_cap;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off += (bytes + 255) & ~(size_t)255;
+        return o;
+    };
+    size_t o_tp = take(W * 16), o_rad = take(W * 16), o_ltp = take(W * 16), o_lrad = take(W * 16),
+           o_lmeta = take(W * 4), o_lvp = take((size_t)light_slots * W * 16), o_lvr = take((size_t)light_slots * W * 16),
+           o_rq0 = take(W * 32), o_rq1 = take(W * 32), o_hits = take(W * 16),
+           o_sq = take((size_t)shadow_slots * W * 48 + 48), o_ctr = take(kMaxCounters * 4), o_stats = take(16 * 8),
+           o_err = take(16 * 4);
+    OMV_CUDA(cudaMalloc(&R.base, off));
+    char* b = static_cast<char*>(R.base);
+    R.bytes = off;
+    R.wave_cap = wave_cap;
+    R.light_slots = light_slots;
+    R.shadow_slots = shadow_slots;
+    R.tp = (float4*)(b + o_tp);
+    R.rad = (float4*)(b + o_rad);
+    R.ltp = (float4*)(b + o_ltp);
+    R.lrad = (float4*)(b + o_lrad);
+    R.lmeta = (uint32_t*)(b + o_lmeta);
+    R.lv_pos = (float4*)(b + o_lvp);
+    R.lv_rad = (float4*)(b + o_lvr);
+    R.rq[0] = (float4*)(b + o_rq0);
+    R.rq[1] = (float4*)(b + o_rq1);
+    R.hits = (uint4*)(b + o_hits);
+    R.sq = (float4*)(b + o_sq);
+    R.ctr = (uint32_t*)(b + o_ctr);
+    R.stats = (unsigned long long*)(b + o_stats);
+    R.err = (uint32_t*)(b + o_err);
+}
+
+void render_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, double* d_sum, double* d_sumsq,
+                  uint32_t* d_count, cudaStream_t st, omv_stats* stats)
+{
+    if (cam.width <= 0 || cam.height <= 0) throw ArgError("camera resolution must be positive");
+    if (p.samples_per_pixel < 0 || p.camera_bounces < 0 || p.light_bounces < 0)
+        throw ArgError("negative sample or bounce count");
+    if (p.camera_bounces > 60 || p.light_bounces > 60) throw ArgError("at most 60 bounces are supported");
+    const int64_t npix = (int64_t)cam.width * cam.height;
+    const int64_t total = npix * p.samples_per_pixel;
+    if (npix > (int64_t)0x7FFFFFFF) throw ArgError("image too large");
+    int64_t cap = p.wave_paths > 0 ? p.wave_paths : (int64_t)1 << 22;
+    cap = std::min<int64_t>(cap, std::max<int64_t>(total, 1));
+    const bool lights = s.num_lights > 0;
+    const int light_slots = lights ? p.light_bounces + 1 : 1;
+    const int shadow_slots = lights ? light_slots : 1;
+    ensure_scratch(s, cap, light_slots, shadow_slots);
+    RenderScratch& R = s.scratch;
+    OMV_CUDA(cudaMemsetAsync(R.stats, 0, 16 * 8, st));
+    WaveArgs A;
+    A.S = s.dev;
+    A.items = s.tlas_items;
+    A.cam = cam;
+    A.seed = p.seed;
+    A.wave_cap = (int32_t)cap;
+    A.npix = (int32_t)npix;
+    A.sample_offset = p.sample_offset;
+    A.cam_bounces = p.camera_bounces;
+    A.light_bounces = p.light_bounces;
+    A.max_len = p.max_path_length;
+    A.atten_mode = p.light_distance_attenuation;
+    A.light_scale = p.light_scale;
+    A.min_dist = p.light_min_distance;
+    A.cut = p.ray_cut_value;
+    A.R = R;
+    int occ_t = 0, occ_s = 0;
+    OMV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, k_extend, kTraceThreads, 0));
+    OMV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_camera_shade, kShadeThreads, 0));
+    const int trace_grid = std::max(1, occ_t) * s.num_sms;
+    const int shade_grid = std::max(1, occ_s) * s.num_sms;
+    int64_t launches = 0;
+    // optional per-launch events around the closest-hit kernels
+    std::vector<cudaEvent_t> ext_ev, sh_ev;
+    auto timed = [&](std::vector<cudaEvent_t>& pool) -> cudaEvent_t {
+        cudaEvent_t e;
+        OMV_CUDA(cudaEventCreate(&e));
+        OMV_CUDA(cudaEventRecord(e, st));
+        pool.push_back(e);
+        return e;
+    };
+    cudaEvent_t e0, e1;
+    OMV_CUDA(cudaEventCreate(&e0));
+    OMV_CUDA(cudaEventCreate(&e1));
+    OMV_CUDA(cudaEventRecord(e0, st));
+    for (int64_t wb = 0; wb < total; wb += cap) {
+        A.wave_base = wb;
+        A.wave_n = (int32_t)std::min<int64_t>(cap, total - wb);
+        OMV_CUDA(cudaMemsetAsync(R.ctr, 0, kMaxCounters * 4, st));
+        int work = 0;
+        if (lights) {
+            k_light_gen<<<grid_for(A.wave_n, kShadeThreads), kShadeThreads, 0, st>>>(A);
+            ++launches;
+            for (int b = 1; b <= p.light_bounces; ++b) {
+                float4* in = R.rq[1];
+                float4* out = R.rq[0];
+                if (b % 2 == 0) std::swap(in, out);
+                if (p.time_kernels) timed(ext_ev);
+                k_extend<<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, in, R.hits,
+                                                               R.ctr + kCtrLight + b, R.ctr + kCtrWork + work++,
+                                                               R.stats, kStatLight);
+                if (p.time_kernels) timed(ext_ev);
+                k_light_shade<<<shade_grid, kShadeThreads, 0, st>>>(A, b, in, out);
+                launches += 2;
+            }
+        }
+        k_camera_gen<<<grid_for(A.wave_n, kShadeThreads), kShadeThreads, 0, st>>>(A);
+        ++launches;
+        for (int b = 1; b <= p.camera_bounces; ++b) {
+            float4* in = R.rq[(b + 1) % 2];
+            float4* out = R.rq[b % 2];
+            if (p.time_kernels) timed(ext_ev);
+            k_extend<<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, in, R.hits, R.ctr + kCtrCam + b,
+                                                           R.ctr + kCtrWork + work++, R.stats, kStatExt);
+            if (p.time_kernels) timed(ext_ev);
+            k_camera_shade<<<shade_grid, kShadeThreads, 0, st>>>(A, b, in, out);
+            launches += 2;
+            if (lights) {
+                if (p.time_kernels) timed(sh_ev);
+                k_shadow<<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, R.sq, R.ctr + kCtrShadow + b,
+                                                               R.ctr + kCtrWork + work++, R.rad, R.stats);
+                if (p.time_kernels) timed(sh_ev);
+                ++launches;
+            }
+        }
+        k_film<<<grid_for(A.wave_n, kShadeThreads), kShadeThreads, 0, st>>>(A, d_sum, d_sumsq, d_count);
+        ++launches;
+        OMV_CUDA(cudaGetLastError());
+    }
+    OMV_CUDA(cudaEventRecord(e1, st));
+    if (stats) {
+        unsigned long long h[16];
+        OMV_CUDA(cudaMemcpyAsync(h, R.stats, sizeof(h), cudaMemcpyDeviceToHost, st));
+        OMV_CUDA(cudaEventSynchronize(e1));
+        OMV_CUDA(cudaStreamSynchronize(st));
+        float ms = 0.0f;
+        OMV_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        stats->paths = total;
+        stats->extension_rays = (int64_t)h[kStatExt];
+        stats->shadow_rays = (int64_t)h[kStatShadow];
+        stats->light_rays = (int64_t)h[kStatLight];
+        stats->render_ms = ms;
+        stats->kernel_launches = launches;
+        stats->nodes_visited = (int64_t)h[kStatNodes];
+        stats->triangles_tested = (int64_t)h[kStatTris];
+        auto sum_pairs = [](std::vector<cudaEvent_t>& ev) {
+            double t = 0.0;
+            for (size_t i = 0; i + 1 < ev.size(); i += 2) {
+                float x = 0.0f;
+                cudaEventElapsedTime(&x, ev[i], ev[i + 1]);
+                t += x;
+            }
+            return t;
+        };
+        stats->extend_ms = sum_pairs(ext_ev);
+        stats->extend_launches = (int64_t)ext_ev.size() / 2;
+        stats->shadow_ms = sum_pairs(sh_ev);
+        stats->shadow_launches = (int64_t)sh_ev.size() / 2;
+    } else if (!ext_ev.empty() || !sh_ev.empty()) {
+        OMV_CUDA(cudaStreamSynchronize(st));
+    }
+    for (auto e : ext_ev) cudaEventDestroy(e);
+    for (auto e : sh_ev) cudaEventDestroy(e);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+}
+
+void render_ids(SceneHost& s, const omv_camera& cam, const float* d_jitter, uint64_t seed, omv_hit* d_hits,
+                uint32_t* d_gprim, cudaStream_t st)
+{
+    const int64_t npix = (int64_t)cam.width * cam.height;
+    k_ids<<<grid_for(npix, kTraceThreads), kTraceThreads, 0, st>>>(s.dev, s.tlas_items, cam, d_jitter, seed, d_hits,
+                                                                    d_gprim, s.d_face_prefix);
+    OMV_CUDA(cudaGetLastError());
+}
+
+void trace_rays(SceneHost& s, int64_t n, const float* d_rays, omv_hit* d_hits, cudaStream_t st)
+{
+    if (n <= 0) return;
+    k_trace_rays<<<grid_for(n, kTraceThreads), kTraceThreads, 0, st>>>(s.dev, s.tlas_items, n, d_rays, d_hits);
+    OMV_CUDA(cudaGetLastError());
+}
+
+void env_radiance(SceneHost& s, int64_t n, const float* d_dirs, float* d_rgb, cudaStream_t st)
+{
+    if (n <= 0) return;
+    k_env<<<grid_for(n, 256), 256, 0, st>>>(s.dev.env, n, d_dirs, d_rgb);
+    OMV_CUDA(cudaGetLastError());
+}
+
+}  // namespace omv

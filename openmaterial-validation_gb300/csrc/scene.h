@@ -1,0 +1,101 @@
+// Host-side scene handle (the object behind the opaque omv_scene*) and the
+// entry points of the render path used by the C ABI layer (capi.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/omv.h"
+#include "omv_types.h"
+
+#define OMV_CUDA(x)                                                                               \
+    do {                                                                                          \
+        cudaError_t e_ = (x);                                                                     \
+        if (e_ != cudaSuccess)                                                                    \
+            throw omv::CudaError(std::string(#x) + ": " + cudaGetErrorString(e_));                \
+    } while (0)
+
+namespace omv {
+
+struct CudaError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+struct ArgError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+// reusable per-scene device work space of the wavefront renderer
+struct RenderScratch {
+    int64_t wave_cap = 0;
+    int light_slots = 0;
+    int shadow_slots = 0;
+    void* base = nullptr;  // one allocation, carved into the arrays below
+    size_t bytes = 0;
+    float4* tp = nullptr;        // camera throughput (outFactor of the last vertex)
+    float4* rad = nullptr;       // per-path radiance
+    float4* ltp = nullptr;       // light throughput
+    float4* lrad = nullptr;      // light Rad (xyz) and distance term (w)
+    uint32_t* lmeta = nullptr;   // light index | (light vertex count << 16)
+    float4* lv_pos = nullptr;    // [light_slots][wave_cap]
+    float4* lv_rad = nullptr;    // [light_slots][wave_cap]
+    float4* rq[2] = {nullptr, nullptr};  // ray queues: 2 float4 per entry
+    uint4* hits = nullptr;       // per queue entry
+    float4* sq = nullptr;        // shadow queue: 3 float4 per entry
+    uint32_t* ctr = nullptr;     // per-wave queue and work counters
+    unsigned long long* stats = nullptr;  // cumulative ray counters
+    uint32_t* err = nullptr;     // device error flags
+};
+
+constexpr int kMaxCounters = 512;
+
+struct SceneHost {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int num_sms = 0;
+    DevScene dev{};
+    std::vector<void*> allocs;
+    uint32_t* tlas_items = nullptr;
+    int num_meshes = 0;
+    int num_instances = 0;
+    int num_materials = 0;  // including the missing material
+    int num_lights = 0;
+    int64_t num_triangles = 0;
+    int64_t blas_nodes = 0;
+    int64_t tlas_nodes = 0;
+    int64_t device_bytes = 0;
+    double build_ms = 0.0;
+    std::vector<uint32_t> mesh_face_prefix;  // global primitive id base per mesh
+    uint32_t* d_face_prefix = nullptr;
+    RenderScratch scratch;
+
+    ~SceneHost();
+    void* alloc(size_t bytes);
+    template <typename T>
+    T* upload(const std::vector<T>& v)
+    {
+        T* p = static_cast<T*>(alloc(sizeof(T) * (v.empty() ? 1 : v.size())));
+        if (!v.empty()) OMV_CUDA(cudaMemcpyAsync(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, stream));
+        return p;
+    }
+};
+
+SceneHost* scene_create(const omv_scene_desc& desc, int device);
+
+void render_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, double* d_sum, double* d_sumsq,
+                  uint32_t* d_count, cudaStream_t st, omv_stats* stats);
+void render_ids(SceneHost& s, const omv_camera& cam, const float* d_jitter, uint64_t seed, omv_hit* d_hits,
+                uint32_t* d_gprim, cudaStream_t st);
+void trace_rays(SceneHost& s, int64_t n, const float* d_rays, omv_hit* d_hits, cudaStream_t st);
+void env_radiance(SceneHost& s, int64_t n, const float* d_dirs, float* d_rgb, cudaStream_t st);
+
+// kernel-level hooks (no scene)
+void hook_eval_direct(int64_t n, const float* d_in, float* d_out, cudaStream_t st);
+void hook_sample_indirect(int64_t n, const float* d_in, float* d_out, cudaStream_t st);
+void hook_om_fresnel(int64_t n, const float* d_in, float* d_out, cudaStream_t st);
+void hook_camera_rays(const omv_camera& cam, const float* d_jitter, float* d_rays, cudaStream_t st);
+
+}  // namespace omv

@@ -1,0 +1,320 @@
+// Closest-hit traversal of the two-level 8-wide BVH: the device replacement of
+// Embree's rtcIntersect1 as the reference calls it (BDPTRenderer.cpp:84).
+//
+// Hit contract (identical to the CPU oracle, oracle/oc_bvh.c):
+//   * the ray is moved into instance object space with the float inverse of the
+//     3x4 instance matrix, in a fixed operation order (t is preserved);
+//   * Woop/Benthin/Wald watertight triangle test, fixed order, double-precision
+//     retry of the edge functions when one is exactly zero;
+//   * accept tnear <= t <= tfar; equal t -> lowest (instance, primitive).
+// Every box test is conservative (quantised boxes rounded outward plus a
+// relative margin on t), so the result does not depend on the tree layout.
+#pragma once
+
+#include "omv_device.cuh"
+#include "omv_types.h"
+
+namespace omv {
+
+constexpr int kStackShared = 16;  // entries per thread kept in shared memory
+constexpr int kStackTotal = 64;   // further entries spill to local memory
+constexpr uint32_t kInstTag = 0x80000000u;
+
+struct TraceStack {
+    uint2* sh;  // this thread's first shared entry; entry i at sh[i * stride]
+    int stride;
+    int sp;
+    int overflow;
+    uint2 spill[kStackTotal - kStackShared];
+
+    __device__ __forceinline__ void push(uint32_t id, float t)
+    {
+        uint2 e = make_uint2(id, __float_as_uint(t));
+        if (sp < kStackShared)
+            sh[sp * stride] = e;
+        else if (sp < kStackTotal)
+            spill[sp - kStackShared] = e;
+        else {
+            overflow = 1;
+            return;
+        }
+        ++sp;
+    }
+    __device__ __forceinline__ uint2 pop()
+    {
+        --sp;
+        return sp < kStackShared ? sh[sp * stride] : spill[sp - kStackShared];
+    }
+};
+
+struct RayHit {
+    uint32_t inst, prim;
+    float t, u, v;
+};
+
+struct Shear {
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+};
+
+__device__ __forceinline__ float pick3(V3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
+__device__ __forceinline__ float pick4(float4 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
+
+// oc_bvh.c wt_setup: false for a zero or non-finite direction
+__device__ __forceinline__ bool shear_setup(V3 d, Shear& w)
+{
+    const float F = kFltMax;
+    if (!(fabsf(d.x) <= F && fabsf(d.y) <= F && fabsf(d.z) <= F)) return false;
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    int kz = 0;
+    float m = ax;
+    if (ay > m) {
+        kz = 1;
+        m = ay;
+    }
+    if (az > m) {
+        kz = 2;
+        m = az;
+    }
+    if (!(m > 0.0f)) return false;
+    int kx = kz + 1;
+    if (kx == 3) kx = 0;
+    int ky = kx + 1;
+    if (ky == 3) ky = 0;
+    float dz = pick3(d, kz);
+    if (dz < 0.0f) {
+        int t = kx;
+        kx = ky;
+        ky = t;
+    }
+    w.kx = kx;
+    w.ky = ky;
+    w.kz = kz;
+    w.Sx = __fdiv_rn(pick3(d, kx), dz);
+    w.Sy = __fdiv_rn(pick3(d, ky), dz);
+    w.Sz = __fdiv_rn(1.0f, dz);
+    return true;
+}
+
+// oc_bvh.c wt_triangle, same operation order
+__device__ __forceinline__ bool tri_hit(const Shear& w, V3 o, float4 p0, float4 p1, float4 p2, float tnear, float tfar,
+                                        float& t, float& u, float& v)
+{
+    const float okx = pick3(o, w.kx), oky = pick3(o, w.ky), okz = pick3(o, w.kz);
+    const float Akx = __fsub_rn(pick4(p0, w.kx), okx), Aky = __fsub_rn(pick4(p0, w.ky), oky),
+                Akz = __fsub_rn(pick4(p0, w.kz), okz);
+    const float Bkx = __fsub_rn(pick4(p1, w.kx), okx), Bky = __fsub_rn(pick4(p1, w.ky), oky),
+                Bkz = __fsub_rn(pick4(p1, w.kz), okz);
+    const float Ckx = __fsub_rn(pick4(p2, w.kx), okx), Cky = __fsub_rn(pick4(p2, w.ky), oky),
+                Ckz = __fsub_rn(pick4(p2, w.kz), okz);
+    const float Ax = __fsub_rn(Akx, __fmul_rn(w.Sx, Akz));
+    const float Ay = __fsub_rn(Aky, __fmul_rn(w.Sy, Akz));
+    const float Bx = __fsub_rn(Bkx, __fmul_rn(w.Sx, Bkz));
+    const float By = __fsub_rn(Bky, __fmul_rn(w.Sy, Bkz));
+    const float Cx = __fsub_rn(Ckx, __fmul_rn(w.Sx, Ckz));
+    const float Cy = __fsub_rn(Cky, __fmul_rn(w.Sy, Ckz));
+    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = (float)__dsub_rn(__dmul_rn((double)Cx, (double)By), __dmul_rn((double)Cy, (double)Bx));
+        V = (float)__dsub_rn(__dmul_rn((double)Ax, (double)Cy), __dmul_rn((double)Ay, (double)Cx));
+        W = (float)__dsub_rn(__dmul_rn((double)Bx, (double)Ay), __dmul_rn((double)By, (double)Ax));
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = __fadd_rn(__fadd_rn(U, V), W);
+    if (det == 0.0f) return false;
+    const float Az = __fmul_rn(w.Sz, Akz);
+    const float Bz = __fmul_rn(w.Sz, Bkz);
+    const float Cz = __fmul_rn(w.Sz, Ckz);
+    const float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
+    const float rcp = __fdiv_rn(1.0f, det);
+    const float tt = __fmul_rn(T, rcp);
+    if (!(tt >= tnear && tt <= tfar)) return false;
+    t = tt;
+    u = __fmul_rn(V, rcp);
+    v = __fmul_rn(W, rcp);
+    return true;
+}
+
+// reciprocal for box tests only: zero components become +-1e-20 so that no
+// 0 * inf NaN can appear (the triangle test uses the true direction)
+__device__ __forceinline__ float box_rcp(float d) { return 1.0f / (fabsf(d) < 1e-20f ? copysignf(1e-20f, d) : d); }
+
+__device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b)
+{
+    uint32_t lo = min(a, b), hi = max(a, b);
+    a = lo;
+    b = hi;
+}
+
+// world -> object space, 3x4 row-major inverse, fixed order
+__device__ __forceinline__ void to_object(const float* m, V3 o, V3 d, V3& ro, V3& rd)
+{
+    ro = v3(__fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[0], o.x), __fmul_rn(m[1], o.y)), __fmul_rn(m[2], o.z)), m[3]),
+            __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[4], o.x), __fmul_rn(m[5], o.y)), __fmul_rn(m[6], o.z)), m[7]),
+            __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[8], o.x), __fmul_rn(m[9], o.y)), __fmul_rn(m[10], o.z)), m[11]));
+    rd = v3(__fadd_rn(__fadd_rn(__fmul_rn(m[0], d.x), __fmul_rn(m[1], d.y)), __fmul_rn(m[2], d.z)),
+            __fadd_rn(__fadd_rn(__fmul_rn(m[4], d.x), __fmul_rn(m[5], d.y)), __fmul_rn(m[6], d.z)),
+            __fadd_rn(__fadd_rn(__fmul_rn(m[8], d.x), __fmul_rn(m[9], d.y)), __fmul_rn(m[10], d.z)));
+}
+
+struct TraceCounters {
+    uint32_t nodes;
+    uint32_t tris;
+};
+
+// Closest hit; returns true and fills `hit` when a triangle is found.
+__device__ __noinline__ bool trace_closest(const DevScene& S, const uint32_t* __restrict__ tlas_items, V3 o, V3 d,
+                                           float tnear, float tfar, RayHit& hit, TraceStack& st, TraceCounters& tc)
+{
+    Shear sw;
+    if (!(tnear <= tfar) || S.num_instances == 0) return false;
+    if (!shear_setup(d, sw)) return false;
+    const V3 idw = v3(box_rcp(d.x), box_rcp(d.y), box_rcp(d.z));
+    float best_t = tfar, bu = 0.0f, bv = 0.0f;
+    uint32_t best_inst = kInvalid, best_prim = kInvalid;
+    bool found = false;
+    V3 ro = o, rid = idw;
+    Shear rs = sw;
+    bool in_blas = false;
+    int blas_base = 0;
+    uint32_t cur_inst = 0;
+    st.sp = 0;
+    st.push(S.tlas_root, tnear);
+    for (uint32_t guard = 0;; ++guard) {
+        if (guard > (1u << 22)) {  // a malformed tree can never spin a warp forever
+            st.overflow = 1;
+            break;
+        }
+        if (in_blas && st.sp == blas_base) {
+            in_blas = false;
+            ro = o;
+            rid = idw;
+        }
+        if (st.sp == 0) break;
+        uint2 e = st.pop();
+        if (__uint_as_float(e.y) > best_t) continue;
+        if (e.x & kInstTag) {
+            const uint32_t ii = e.x & ~kInstTag;
+            const DevInstance* I = S.insts + ii;
+            float m[12];
+#pragma unroll
+            for (int k = 0; k < 12; ++k) m[k] = __ldg(&I->inv[k]);
+            V3 rd;
+            to_object(m, o, d, ro, rd);
+            if (!shear_setup(rd, rs)) {
+                ro = o;
+                continue;
+            }
+            rid = v3(box_rcp(rd.x), box_rcp(rd.y), box_rcp(rd.z));
+            in_blas = true;
+            blas_base = st.sp;
+            cur_inst = ii;
+            st.push(__ldg(&I->blas_root), __uint_as_float(e.y));
+            continue;
+        }
+        ++tc.nodes;
+        const uint4* N = S.nodes + 8 * (size_t)e.x;
+        const uint4 w0 = __ldg(N + 0), w1 = __ldg(N + 1);
+        const uint4 qlx = __ldg(N + 2), qly = __ldg(N + 3), qlz = __ldg(N + 4);
+        const uint4 qhx = __ldg(N + 5), qhy = __ldg(N + 6), qhz = __ldg(N + 7);
+        const float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
+        const uint32_t exps = w0.w;
+        const uint32_t imask = exps >> 24;
+        const uint32_t child_base = w1.x, prim_base = w1.y, meta_lo = w1.z, meta_hi = w1.w;
+        const float sx = __uint_as_float((exps & 0xFFu) << 23);
+        const float sy = __uint_as_float(((exps >> 8) & 0xFFu) << 23);
+        const float sz = __uint_as_float(((exps >> 16) & 0xFFu) << 23);
+        const float ax = sx * rid.x, ay = sy * rid.y, az = sz * rid.z;
+        const float bx = (px - ro.x) * rid.x, by = (py - ro.y) * rid.y, bz = (pz - ro.z) * rid.z;
+        const float lim = best_t;
+        uint32_t key[8];
+        uint32_t leafmask = 0;
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> (8 * (s & 3))) & 0xFFu;
+            const bool internal = (imask >> s) & 1u;
+            const bool valid = internal || meta != 0u;
+            const int sh = 16 * (s & 1);
+            const uint32_t wlx = s < 2 ? qlx.x : s < 4 ? qlx.y : s < 6 ? qlx.z : qlx.w;
+            const uint32_t wly = s < 2 ? qly.x : s < 4 ? qly.y : s < 6 ? qly.z : qly.w;
+            const uint32_t wlz = s < 2 ? qlz.x : s < 4 ? qlz.y : s < 6 ? qlz.z : qlz.w;
+            const uint32_t whx = s < 2 ? qhx.x : s < 4 ? qhx.y : s < 6 ? qhx.z : qhx.w;
+            const uint32_t why = s < 2 ? qhy.x : s < 4 ? qhy.y : s < 6 ? qhy.z : qhy.w;
+            const uint32_t whz = s < 2 ? qhz.x : s < 4 ? qhz.y : s < 6 ? qhz.z : qhz.w;
+            const float tlx = fmaf((float)((wlx >> sh) & 0xFFFFu), ax, bx);
+            const float thx = fmaf((float)((whx >> sh) & 0xFFFFu), ax, bx);
+            const float tly = fmaf((float)((wly >> sh) & 0xFFFFu), ay, by);
+            const float thy = fmaf((float)((why >> sh) & 0xFFFFu), ay, by);
+            const float tlz = fmaf((float)((wlz >> sh) & 0xFFFFu), az, bz);
+            const float thz = fmaf((float)((whz >> sh) & 0xFFFFu), az, bz);
+            float tin = fmaxf(fmaxf(fminf(tlx, thx), fminf(tly, thy)), fminf(tlz, thz));
+            float tout = fminf(fminf(fmaxf(tlx, thx), fmaxf(tly, thy)), fmaxf(tlz, thz));
+            tin = fmaxf(tin * 0.99999952f, tnear);
+            tout = fminf(tout * 1.00000048f, lim);
+            const bool hit = valid && tin <= tout;
+            key[s] = 0xFFFFFFFFu;
+            if (hit) {
+                if (!internal && in_blas)
+                    leafmask |= 1u << s;
+                else
+                    key[s] = (__float_as_uint(fmaxf(tin, 0.0f)) & ~7u) | (uint32_t)s;
+            }
+        }
+        // leaf triangles first: they can shrink best_t before children are pushed
+        for (uint32_t m = leafmask; m; m &= m - 1u) {
+            const int s = __ffs(m) - 1;
+            const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> (8 * (s & 3))) & 0xFFu;
+            const uint32_t cnt = meta >> 5, off = meta & 31u;
+            for (uint32_t k = 0; k < cnt; ++k) {
+                const float4* T = S.tris + 3 * (size_t)(prim_base + off + k);
+                const float4 a = __ldg(T), b = __ldg(T + 1), c = __ldg(T + 2);
+                ++tc.tris;
+                float t, u, v;
+                if (tri_hit(rs, ro, a, b, c, tnear, best_t, t, u, v)) {
+                    const uint32_t prim = __float_as_uint(a.w);
+                    bool take = !found || t < best_t ||
+                                (t == best_t && (cur_inst < best_inst || (cur_inst == best_inst && prim < best_prim)));
+                    if (take) {
+                        found = true;
+                        best_t = t;
+                        bu = u;
+                        bv = v;
+                        best_inst = cur_inst;
+                        best_prim = prim;
+                    }
+                }
+            }
+        }
+        // 19-comparator sorting network (Knuth, TAOCP vol. 3, 5.3.4), ascending entry t
+        cswap(key[0], key[2]); cswap(key[1], key[3]); cswap(key[4], key[6]); cswap(key[5], key[7]);
+        cswap(key[0], key[4]); cswap(key[1], key[5]); cswap(key[2], key[6]); cswap(key[3], key[7]);
+        cswap(key[0], key[1]); cswap(key[2], key[3]); cswap(key[4], key[5]); cswap(key[6], key[7]);
+        cswap(key[2], key[4]); cswap(key[3], key[5]);
+        cswap(key[1], key[4]); cswap(key[3], key[6]);
+        cswap(key[1], key[2]); cswap(key[3], key[4]); cswap(key[5], key[6]);
+#pragma unroll
+        for (int j = 7; j >= 0; --j) {
+            const uint32_t k = key[j];
+            if (k == 0xFFFFFFFFu) continue;
+            const float te = __uint_as_float(k & ~7u);
+            if (te > best_t) continue;
+            const uint32_t s = k & 7u;
+            const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> (8 * (s & 3))) & 0xFFu;
+            if ((imask >> s) & 1u)
+                st.push(child_base + meta, te);
+            else
+                st.push(kInstTag | __ldg(tlas_items + prim_base + (meta & 31u)), te);
+        }
+    }
+    if (!found) return false;
+    hit.inst = best_inst;
+    hit.prim = best_prim;
+    hit.t = best_t;
+    hit.u = bu;
+    hit.v = bv;
+    return true;
+}
+
+}  // namespace omv

@@ -33,6 +33,7 @@ from __future__ import annotations
 import ctypes
 import ctypes.util
 import dataclasses
+import functools
 import json
 import math
 import os
@@ -69,7 +70,20 @@ def tanf(x: float) -> float:
 
 # ----------------------------------------------------------------- geometry --
 
+@functools.lru_cache(maxsize=8)
+def _icosphere_cached(subdivisions: int):
+    v, f = _icosphere(subdivisions)
+    v.setflags(write=False)
+    f.setflags(write=False)
+    return v, f
+
+
 def icosphere(subdivisions: int):
+    v, f = _icosphere_cached(subdivisions)
+    return v.copy(), f.copy()
+
+
+def _icosphere(subdivisions: int):
     """Unit icosphere by repeated midpoint subdivision of an icosahedron, all
     vertices projected onto the unit sphere (computed in float64, stored f32)."""
     t = (1.0 + 5.0 ** 0.5) / 2.0
@@ -292,7 +306,7 @@ def scene_c1(width: int = 256, height: int = 256, spp: int = 16) -> Scene:
                  RenderSpec(spp, 6, 6, 6), gltf_nodes=[nodes])
 
 
-def make_sky(width: int, height: int, rng: np.random.Generator) -> np.ndarray:
+def make_sky(width: int, height: int, rng: np.random.Generator, suns: bool = True) -> np.ndarray:
     """Log-normal sky (mu=0, sigma=1 of the log) from a smooth Gaussian field on
     the sphere, plus three Gaussian sun lobes of peak 1e4, in the equirect
     parametrisation HDRBackground::getRadiance reads (row 0 = zenith)."""
@@ -310,7 +324,7 @@ def make_sky(width: int, height: int, rng: np.random.Generator) -> np.ndarray:
         g += np.cos(d @ k + rng.uniform(0, 2 * np.pi))
     g *= (2.0 / modes) ** 0.5  # unit variance
     sky = np.exp(g)[..., None] * np.array([0.55, 0.7, 1.0])
-    for _ in range(3):
+    for _ in range(3 if suns else 0):
         e = rng.uniform(0.15, 1.2)
         a = rng.uniform(0, 2 * np.pi)
         s = np.array([np.cos(e) * np.cos(a), np.cos(e) * np.sin(a), np.sin(e)])
@@ -321,8 +335,9 @@ def make_sky(width: int, height: int, rng: np.random.Generator) -> np.ndarray:
 
 
 def scene_c2(width: int = 1920, height: int = 1080, spp: int = 64, seed: int = 0,
-             tri_scale: float = 1.0) -> Scene:
-    """tri_scale < 1 shrinks the tessellation (for small parity cases)."""
+             tri_scale: float = 1.0, suns: bool = True, sky_size=(2048, 1024)) -> Scene:
+    """tri_scale < 1 shrinks the tessellation and suns=False drops the three
+    1e4 sun lobes (low-variance variants for parity tests)."""
     rng = np.random.default_rng(seed)
     meshes, insts, mats = [], [], []
     sub = 5 if tri_scale >= 1.0 else max(1, int(round(5 + math.log(tri_scale, 4))))
@@ -347,14 +362,51 @@ def scene_c2(width: int = 1920, height: int = 1080, spp: int = 64, seed: int = 0
         mats.append(Material(type=0, base_color=(float(rng.uniform()), float(rng.uniform()), float(rng.uniform()), 1.0),
                              roughness=float(rng.uniform(0.05, 1.0)), metallic=float(rng.integers(0, 2)),
                              name=f"pbr{i}"))
-    sky = make_sky(2048, 1024, rng)
+    sky = make_sky(sky_size[0], sky_size[1], rng, suns)
     R = np.array([[1, 0, 0], [0, 0, 1], [0, -1, 0]], dtype=F32)  # main.cpp:401-405 (y-up)
     hdri = Hdri(sky, R, float(F32(math.pi)))
     cam = camera_default(width, height)
     return Scene("c2", meshes, insts, mats, [], hdri, cam, RenderSpec(spp, 10, 10, 10))
 
 
-SCENES = {"c1": scene_c1, "c2": scene_c2}
+def scene_mixed(width: int = 32, height: int = 32, spp: int = 8) -> Scene:
+    """Parity scene covering every material branch of the reference: the
+    OpenMATERIAL conductor, a rough PBR metal (specular GGX branch), a
+    double-sided PBR dielectric (transmission branch, BRDFModel.h:291-310), a
+    BLEND PBR with alpha 0.5, a mesh without material (the missing-material
+    diffuse, DiffuseColorMaterial.cpp) and the diffuse ground; C1's light and
+    camera model, bounces 4, max path length 5."""
+    v, f = icosphere(2)
+    v32 = v.astype(F32)
+    n32 = (v / np.linalg.norm(v, axis=1, keepdims=True)).astype(F32)
+    meshes = []
+    centers = [(-1.6, -0.3, 0.0), (0.0, -0.3, -0.8), (1.6, -0.3, 0.0), (-0.8, 0.9, -1.2), (0.9, 0.9, -1.5)]
+    scale = F32(0.7)
+    for i, c in enumerate(centers):
+        p = (v32 * scale + np.array(c, dtype=F32)).astype(F32)
+        meshes.append(Mesh(positions=p, normals=n32.copy(), faces=f, material=[0, 1, 2, 3, -1][i], name=f"ball{i}"))
+    qv = np.array([[-5, -1, -5], [5, -1, -5], [5, -1, 5], [-5, -1, 5]], dtype=F32)
+    qf = np.array([[0, 2, 1], [0, 3, 2]], dtype=np.uint32)
+    meshes.append(Mesh(positions=qv, normals=None, faces=qf, material=4, name="ground"))
+    mats = [_om_conductor((0.18, 0.42, 1.37), (3.42, 2.35, 1.77)),
+            Material(type=0, base_color=(0.9, 0.6, 0.3, 1.0), metallic=1.0, roughness=0.3, name="rough_metal"),
+            Material(type=0, base_color=(0.8, 0.9, 1.0, 1.0), metallic=0.0, roughness=0.15, double_sided=True,
+                     name="dielectric"),
+            Material(type=0, base_color=(0.2, 0.8, 0.3, 0.5), metallic=0.2, roughness=0.5, alpha_mode=2,
+                     name="blend"),
+            Material(type=0, base_color=(0.5, 0.5, 0.5, 1.0), metallic=0.0, roughness=1.0, name="ground_diffuse")]
+    root_t = np.eye(4, dtype=F32)
+    root_t[2, 3] = -5.0
+    inst = [Instance(root_t.copy(), i) for i in range(len(meshes))]
+    light = Light(position=(2.0, 4.0, -3.0), intensity=(50.0, 50.0, 50.0))
+    focus = (height / 2.0) / math.tan(math.radians(22.5))
+    cam = camera_from_json(width, height, width / height, focus, 45.0)
+    nodes = {"root_translation": (0.0, 0.0, -5.0), "light_translation": (2.0, 4.0, 2.0),
+             "light_color": (1.0, 1.0, 1.0), "light_intensity": 50.0}
+    return Scene("mixed", meshes, inst, mats, [light], None, cam, RenderSpec(spp, 4, 4, 5), gltf_nodes=[nodes])
+
+
+SCENES = {"c1": scene_c1, "c2": scene_c2, "mixed": scene_mixed}
 
 
 # -------------------------------------------------------------------- RGBE --
@@ -515,11 +567,14 @@ def write_gltf(scene: Scene, dirname: str) -> dict:
 
     extensions, nodes, scene_nodes = {}, [], []
     used = ["OpenMaterial_reference_link"] if any(x.type == 1 for x in scene.materials) else []
-    if scene.name == "c1":
+    if scene.gltf_nodes:
+        # one root node (translated) holding a node per mesh and the light node
         cfg = scene.gltf_nodes[0]
-        nodes.append({"name": "root", "translation": list(cfg["root_translation"]), "children": [1, 2, 3]})
-        nodes.append({"name": "icosphere", "mesh": 0})
-        nodes.append({"name": "ground", "mesh": 1})
+        nm = len(scene.meshes)
+        nodes.append({"name": "root", "translation": list(cfg["root_translation"]),
+                      "children": list(range(1, nm + 2))})
+        for i, m in enumerate(scene.meshes):
+            nodes.append({"name": m.name, "mesh": i})
         nodes.append({"name": "light", "translation": list(cfg["light_translation"]),
                       "extensions": {"KHR_lights_punctual": {"light": 0}}})
         extensions["KHR_lights_punctual"] = {"lights": [{"type": "point", "color": list(cfg["light_color"]),

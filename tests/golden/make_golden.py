@@ -1,0 +1,293 @@
+"""Generates the golden fixtures in this directory by running the reference
+renderer's own code (built from its unmodified sources by oracle/Makefile
+`make ref` against the Embree-API shim).  Needs the reference tree
+(REF=... or /root/reference) and runs on the development host only; the
+fixtures it writes are committed and are all the tests need elsewhere.
+
+    python tests/golden/make_golden.py [--only name,...] [--big]
+
+Fixtures (numpy .npz):
+  mt.npz            RandomSampler draws (std::mt19937 + uniform_real_distribution<float>)
+  brdf_eval.npz     BSDFModel<GGX>::evaluateDirect on seeded inputs
+  brdf_sample.npz   BSDFModel<GGX>::sampleIndirect with RandomSampler(seed) per case
+  om.npz            OpenMaterial::getBrdf (Fresnel of a complex IOR) for the C1 conductor
+  ior.npz           AssetMaterialIor::getIor on a synthetic IOR table
+  env.npz           HDRBackground::getRadiance on a synthetic RGBE image
+  camera.npz        PinholeCamera::loadProperties + getRay (one RandomSampler)
+  scene_<s>.npz     the committed RenderScene of scene <s> (vertex block, normal
+                    matrices, material ids, lights) dumped after commitScene
+  film_<s>.npz      linear film (PinholeCamera after stop) of a -C 1 render + ray count
+  ids_c1_64.npz     primary rays and hits of the false-colour (-F mid) pass
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+S = importlib.import_module("openmaterial-validation_gb300.scenes")
+REF = os.environ.get("REF", "/root/reference")
+BIN = os.path.join(ROOT, "oracle", "_ref")
+
+
+def run(cmd, env=None):
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env)
+    if r.returncode != 0:
+        raise RuntimeError(f"{cmd[0]} failed ({r.returncode}):\n{r.stdout[-3000:]}\n{r.stderr[-3000:]}")
+    return r
+
+
+def harness(*args):
+    return run([os.path.join(BIN, "golden_harness"), *map(str, args)])
+
+
+def f32file(d, name, arr):
+    p = os.path.join(d, name)
+    np.ascontiguousarray(arr, dtype=np.float32).tofile(p)
+    return p
+
+
+def unit(rng, n):
+    v = rng.normal(size=(n, 3))
+    return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+def gen_mt(tmp):
+    out = os.path.join(tmp, "mt.bin")
+    harness("mt", 3254638, 20000, out)
+    np.savez_compressed(os.path.join(HERE, "mt.npz"), seed=3254638, u=np.fromfile(out, dtype=np.float32))
+
+
+def gen_brdf(tmp):
+    rng = np.random.default_rng(1)
+    n = 4000
+    N = unit(rng, n)
+    V = unit(rng, n)
+    V[: n * 3 // 4] = np.where((np.sum(V * N, 1) < 0)[:, None], -V, V)[: n * 3 // 4]
+    L = unit(rng, n)
+    L[: n * 3 // 4] = np.where((np.sum(L * N, 1) < 0)[:, None], -L, L)[: n * 3 // 4]
+    I = -V
+    color = np.concatenate([rng.uniform(0, 1, (n, 3)), np.ones((n, 1))], 1)
+    metal = rng.uniform(0, 1, n)
+    metal[::5] = 0.0
+    metal[1::5] = 1.0
+    rough = rng.uniform(0.02, 1.0, n)
+    alpha = rough ** 2
+    x = np.zeros((n, 17), dtype=np.float32)
+    x[:, 0:3], x[:, 3:6], x[:, 6:9], x[:, 9:13], x[:, 13], x[:, 14] = I, L, N, color, metal, alpha
+    out = os.path.join(tmp, "eval.out")
+    harness("eval", f32file(tmp, "eval.in", x), out)
+    np.savez_compressed(os.path.join(HERE, "brdf_eval.npz"), x=x, y=np.fromfile(out, dtype=np.float32).reshape(n, 3))
+    # sampleIndirect: random frames, both facing sides, transmissive cases
+    N = unit(rng, n)
+    T = unit(rng, n)
+    T = T - N * np.sum(T * N, 1, keepdims=True)
+    T /= np.linalg.norm(T, axis=1, keepdims=True)
+    V = unit(rng, n)
+    I = -V
+    color = np.concatenate([rng.uniform(0, 1, (n, 3)), np.where(rng.uniform(0, 1, (n, 1)) < 0.3,
+                                                                 rng.uniform(0.1, 1, (n, 1)), 1.0)], 1)
+    x = np.zeros((n, 24), dtype=np.float32)
+    x[:, 0:3], x[:, 3:6], x[:, 6:9], x[:, 9:13] = I, N, T, color
+    x[:, 13] = rng.uniform(0, 1, n)
+    x[:, 14] = rng.uniform(0.02, 1.0, n) ** 2
+    x[:, 15] = np.where(rng.uniform(0, 1, n) < 0.5, 1.0 / 1.5, 1.0)
+    x[:, 16] = (rng.uniform(0, 1, n) < 0.4).astype(np.float32)
+    seeds = np.arange(1000, 1000 + n, dtype=np.uint32)
+    x[:, 17] = seeds.view(np.float32)
+    out = os.path.join(tmp, "sample.out")
+    harness("sample", f32file(tmp, "sample.in", x), out)
+    np.savez_compressed(os.path.join(HERE, "brdf_sample.npz"), x=x, seeds=seeds,
+                        y=np.fromfile(out, dtype=np.float32).reshape(n, 6))
+
+
+def gen_om(tmp):
+    sc = S.scene_c1(8, 8, 1)
+    d = os.path.join(tmp, "om")
+    S.write_gltf(sc, d)
+    mat = sc.materials[0]
+    c = np.concatenate([np.linspace(1e-3, 1.0, 400), np.random.default_rng(2).uniform(0, 1, 600)]).astype(np.float32)
+    out = os.path.join(tmp, "om.out")
+    harness("om", os.path.join(d, f"{mat.name}.gltf"), f32file(tmp, "om.in", c), out)
+    np.savez_compressed(os.path.join(HERE, "om.npz"), cos=c, y=np.fromfile(out, dtype=np.float32).reshape(-1, 3),
+                        n=np.array([0.18, 0.42, 1.37], dtype=np.float32),
+                        k=np.array([3.42, 2.35, 1.77], dtype=np.float32))
+
+
+def gen_ior(tmp):
+    rng = np.random.default_rng(3)
+    wl = np.sort(rng.uniform(2.0e-7, 1.2e-6, 60))
+    nv = 1.0 + np.cumsum(rng.uniform(-0.05, 0.08, 60)).clip(-0.5, 3)
+    kv = np.abs(2.0 + np.cumsum(rng.uniform(-0.1, 0.1, 60)))
+    mat = S.Material(type=1, ior_n=np.stack([wl, nv], 1), ior_k=np.stack([wl, kv], 1), name="synthetic")
+    d = os.path.join(tmp, "ior")
+    os.makedirs(d, exist_ok=True)
+    S._write_om_material(d, mat)
+    q = np.stack([np.full(500, 300.0), np.concatenate([rng.uniform(wl[0], wl[-1], 496),
+                                                       np.float32(wl[[0, 5, 30, -1]])])], 1).astype(np.float32)
+    out = os.path.join(tmp, "ior.out")
+    harness("ior", os.path.join(d, "synthetic_ior.gltf"), f32file(tmp, "ior.in", q), out)
+    tab_n = np.stack([wl, nv], 1).astype(np.float32)
+    tab_k = np.stack([wl, kv], 1).astype(np.float32)
+    np.savez_compressed(os.path.join(HERE, "ior.npz"), q=q, y=np.fromfile(out, dtype=np.float32).reshape(-1, 2),
+                        table_n=tab_n, table_k=tab_k)
+
+
+def gen_env(tmp):
+    rng = np.random.default_rng(4)
+    img = S.make_sky(64, 32, rng) * np.float32(0.001)
+    img = S.rgbe_quantize(img)
+    hdr = os.path.join(tmp, "env.hdr")
+    S.write_hdr(hdr, img)
+    dirs = np.concatenate([unit(rng, 3000), np.eye(3), -np.eye(3),
+                           [[0.0, 1.0, 1e-7], [1e-7, 1.0, 0.0], [0.0, -1.0, 0.0]]]).astype(np.float32)
+    R = np.array([[1, 0, 0], [0, 0, 1], [0, -1, 0]], dtype=np.float32)
+    scale = np.float32(np.pi)
+    inp = np.concatenate([R.reshape(-1), [scale], dirs.reshape(-1)]).astype(np.float32)
+    out = os.path.join(tmp, "env.out")
+    harness("env", hdr, f32file(tmp, "env.in", inp), out)
+    np.savez_compressed(os.path.join(HERE, "env.npz"), image=S.read_hdr(hdr), rotation=R, scale=scale, dirs=dirs,
+                        y=np.fromfile(out, dtype=np.float32).reshape(-1, 3))
+
+
+def gen_camera(tmp):
+    sc = S.scene_c1(48, 40, 1)
+    d = os.path.join(tmp, "cam")
+    S.write_gltf(sc, d)
+    out = os.path.join(tmp, "cam.out")
+    harness("camera", os.path.join(d, "c1_camera.json"), 48, 40, 777, out)
+    y = np.fromfile(out, dtype=np.float32)
+    np.savez_compressed(os.path.join(HERE, "camera.npz"), width=48, height=40, seed=777, sizes=y[:3],
+                        rays=y[3:].reshape(-1, 6), json=str(sc.camera.json_props))
+
+
+def read_scene_dump(path):
+    raw = open(path, "rb").read()
+    off = 0
+
+    def i32():
+        nonlocal off
+        v = int(np.frombuffer(raw, np.int32, 1, off)[0])
+        off += 4
+        return v
+
+    def f32(n):
+        nonlocal off
+        v = np.frombuffer(raw, np.float32, n, off).copy()
+        off += 4 * n
+        return v
+
+    assert i32() == 0x4F4D5631
+    ok = i32()
+    out = {"ok": ok}
+    nm = i32()
+    verts, faces, mesh_mat = [], [], []
+    for _ in range(nm):
+        mid, vn, fn, mat, stride = i32(), i32(), i32(), i32(), i32()
+        mesh_mat.append(mat)
+        if vn > 0 and fn > 0:
+            faces.append(np.frombuffer(raw, np.uint32, 3 * fn, off).reshape(fn, 3).copy())
+            off += 12 * fn
+            verts.append(f32(10 * vn).reshape(vn, 10))
+        else:
+            faces.append(np.zeros((0, 3), np.uint32))
+            verts.append(np.zeros((0, 10), np.float32))
+    ni = i32()
+    xf, nmx, imesh = [], [], []
+    for _ in range(ni):
+        i32()
+        imesh.append(i32())
+        xf.append(f32(16).reshape(4, 4))
+        nmx.append(f32(9).reshape(3, 3))
+    nmat = i32()
+    mtype, mrec = [], []
+    for _ in range(nmat):
+        mtype.append(i32())
+        mrec.append(f32(16))
+    nl = i32()
+    lights = [f32(8) for _ in range(nl)]
+    out["has_background"] = i32()
+    out.update(mesh_material=np.array(mesh_mat, np.int32), inst_mesh=np.array(imesh, np.int32),
+               inst_xf=np.array(xf, np.float32).reshape(-1, 4, 4), inst_nrm=np.array(nmx, np.float32).reshape(-1, 3, 3),
+               mat_type=np.array(mtype, np.int32), mat_rec=np.array(mrec, np.float32).reshape(-1, 16),
+               lights=np.array(lights, np.float32).reshape(-1, 8))
+    for i, (v, f) in enumerate(zip(verts, faces)):
+        out[f"verts{i}"] = v
+        out[f"faces{i}"] = f
+    return out
+
+
+def render_reference(sc, tmp, exe="pathtracer", extra=(), log=None):
+    d = os.path.join(tmp, f"{sc.name}_{sc.camera.width}_{sc.render.samples_per_pixel}_{exe}")
+    out = S.write_gltf(sc, d)
+    env = dict(os.environ, OMV_REF_FILM=os.path.join(d, "film.bin"), OMV_REF_SCENE=os.path.join(d, "scene.bin"))
+    if log:
+        env["OMV_SHIM_LOG"] = log
+    r = run([os.path.join(BIN, exe), *out["flags"], "-C", "1", "-o", os.path.join(d, "out.png"), *extra], env=env)
+    line = [l for l in r.stderr.splitlines() if l.startswith("OMV_REF_RENDER")][0].split()
+    hdr = np.fromfile(os.path.join(d, "film.bin"), dtype=np.int32, count=2)
+    film = np.fromfile(os.path.join(d, "film.bin"), dtype=np.float32)[2:].reshape(hdr[1], hdr[0], 4)
+    return film, float(line[1]), int(line[2]), read_scene_dump(os.path.join(d, "scene.bin"))
+
+
+def gen_films(tmp, big=False):
+    jobs = [("film_c1_32x4", S.scene_c1(32, 32, 4)), ("film_mixed_32x8", S.scene_mixed(32, 32, 8)),
+            ("film_c1_64x1024", S.scene_c1(64, 64, 1024))]
+    if big:
+        jobs.append(("film_c1_256x4096", S.scene_c1(256, 256, 4096)))
+    for name, sc in jobs:
+        film, secs, rays, dump = render_reference(sc, tmp)
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), film=film, seconds=secs, rays=rays,
+                            width=sc.camera.width, height=sc.camera.height, spp=sc.render.samples_per_pixel)
+        if name in ("film_c1_32x4", "film_mixed_32x8"):
+            np.savez_compressed(os.path.join(HERE, f"scene_{sc.name}.npz"), **dump)
+        print(name, film.shape, secs, rays)
+
+
+def gen_ids(tmp):
+    sc = S.scene_c1(64, 64, 1)
+    log = os.path.join(tmp, "shim.log")
+    if os.path.exists(log):
+        os.remove(log)
+    render_reference(sc, tmp, exe="pathtracer_fc", extra=["-F", "mid"], log=log)
+    rec = np.fromfile(log, dtype=np.uint8).reshape(-1, 64)
+    f = rec[:, :32].copy().view(np.float32).reshape(-1, 8)
+    u = rec[:, 32:48].copy().view(np.uint32).reshape(-1, 4)
+    g = rec[:, 48:60].copy().view(np.float32).reshape(-1, 3)
+    assert len(rec) == 64 * 64, len(rec)
+    np.savez_compressed(os.path.join(HERE, "ids_c1_64.npz"), rays=f, hit=u[:, 0], geom=u[:, 1], inst=u[:, 2],
+                        prim=u[:, 3], u=g[:, 0], v=g[:, 1], t=g[:, 2])
+
+
+GENS = {"mt": gen_mt, "brdf": gen_brdf, "om": gen_om, "ior": gen_ior, "env": gen_env, "camera": gen_camera,
+        "films": gen_films, "ids": gen_ids}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", default="")
+    ap.add_argument("--big", action="store_true", help="also the 256x256 4096-spp C1 reference film")
+    a = ap.parse_args()
+    if not os.path.isdir(REF):
+        sys.exit(f"reference tree not found at {REF}")
+    run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "-j8", "ref", f"REF={REF}"])
+    names = [n for n in a.only.split(",") if n] or list(GENS)
+    with tempfile.TemporaryDirectory() as tmp:
+        for n in names:
+            if n == "films":
+                gen_films(tmp, a.big)
+            else:
+                GENS[n](tmp)
+            print("wrote", n)
+
+
+if __name__ == "__main__":
+    main()

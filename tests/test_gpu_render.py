@@ -1,0 +1,143 @@
+"""The GPU wavefront BDPT against the reference estimator.
+
+Random streams differ (counter-based Philox on the GPU, one std::mt19937 in the
+reference), so image parity is statistical: per pixel and channel
+z = (gpu - ref) / sqrt(se_gpu^2 + se_ref^2), with the per-sample variance
+measured by the GPU run (both sides sample the same estimator).  Bar: at most
+1% of the pixel-channels beyond 3 sigma (0.27% expected for a normal
+statistic) and the image mean within 3 combined standard errors."""
+import os
+
+import numpy as np
+import pytest
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _render(gpu, sc, spp, seed=1, variance=True, **kw):
+    rs = gpu.RenderScene(sc)
+    r = gpu.BDPTRenderer()
+    r.set_scene(rs)
+    r.set_parameters(gpu.RendererParameters.for_scene(sc, samplesPerPixel=spp, seed=seed,
+                                                      accumulate_variance=variance, **kw))
+    img, s, q, cnt = r.render(gpu.PinholeCamera.from_spec(sc.camera), sums=True)
+    return img, s, q, cnt, r.last_stats
+
+
+def _zstats(mean_a, n_a, mean_b, n_b, var):
+    se2 = var / n_a + var / n_b
+    live = se2 > 0
+    z = np.zeros_like(mean_a)
+    z[live] = (mean_a[live] - mean_b[live]) / np.sqrt(se2[live])
+    dead_equal = np.allclose(mean_a[~live], mean_b[~live], rtol=0, atol=1e-6)
+    tot_se = np.sqrt(se2.sum())
+    glob = (mean_a.sum() - mean_b.sum()) / tot_se if tot_se > 0 else 0.0
+    return z[live], dead_equal, glob
+
+
+def test_c1_statistically_matches_reference(gpu, scenes):
+    g = golden("film_c1_64x1024")
+    n_ref = int(g["spp"])
+    sc = scenes.scene_c1(64, 64, 1)
+    n = 4096
+    img, s, q, cnt, st = _render(gpu, sc, n)
+    assert (cnt == n).all()
+    mean = s / n
+    var = np.maximum(q / n - mean ** 2, 0.0)
+    ref = g["film"][..., :3].astype(np.float64)
+    z, dead_ok, glob = _zstats(mean, n, ref, n_ref, var)
+    assert dead_ok
+    frac3 = float(np.mean(np.abs(z) > 3))
+    assert frac3 < 0.01, (frac3, np.sort(np.abs(z))[-10:])
+    assert abs(glob) < 3, glob
+    assert np.allclose(img[..., :3], mean, rtol=1e-6, atol=1e-6)
+    assert st["shadow_rays"] > 0 and st["light_rays"] > 0
+
+
+def test_mixed_materials_statistically_match_oracle(gpu, oracle, scenes):
+    sc = scenes.scene_mixed(48, 48, 1)
+    n_cpu = 256
+    film, sumsq, _ = oracle.OracleScene(sc).render(params=_params(oracle, sc, n_cpu), mode=1,
+                                                   threads=os.cpu_count() or 8, seed=5, variance=True)
+    n = 4096
+    _, s, q, cnt, _ = _render(gpu, sc, n, seed=2)
+    mean = s / n
+    var = np.maximum(q / n - mean ** 2, 0.0)
+    z, dead_ok, glob = _zstats(mean, n, film[..., :3].astype(np.float64), n_cpu, var)
+    frac3 = float(np.mean(np.abs(z) > 3))
+    assert frac3 < 0.01, frac3
+    assert abs(glob) < 3, glob
+
+
+def _params(oracle, sc, spp):
+    p = oracle.capi.params_for(sc, spp=spp)
+    return p
+
+
+def test_environment_scene_statistically_matches_oracle(gpu, oracle, scenes):
+    """Instanced PBR scene lit by an HDRI (escape term, GGX/diffuse branches,
+    rotated and scaled instances), GPU vs oracle."""
+    sc = scenes.scene_c2(40, 24, 1, tri_scale=0.02, suns=False, sky_size=(256, 128))
+    n_cpu = 512
+    film, _, _ = oracle.OracleScene(sc).render(params=_params(oracle, sc, n_cpu), mode=1,
+                                               threads=os.cpu_count() or 8, seed=3)
+    n = 8192
+    _, s, q, cnt, st = _render(gpu, sc, n, seed=4)
+    mean = s / n
+    var = np.maximum(q / n - mean ** 2, 0.0)
+    z, dead_ok, glob = _zstats(mean, n, film[..., :3].astype(np.float64), n_cpu, var)
+    assert float(np.mean(np.abs(z) > 3)) < 0.01
+    assert abs(glob) < 3, glob
+    assert st["shadow_rays"] == 0 and st["light_rays"] == 0
+
+
+def test_same_seed_same_image_and_partition_invariance(gpu, scenes):
+    sc = scenes.scene_c1(64, 64, 1)
+    _, a, _, _, _ = _render(gpu, sc, 64, seed=9, variance=False)
+    _, b, _, _, _ = _render(gpu, sc, 64, seed=9, variance=False)
+    _, c, _, _, _ = _render(gpu, sc, 64, seed=9, variance=False, wave_paths=10007)
+    _, d, _, _, _ = _render(gpu, sc, 64, seed=10, variance=False)
+    scale = np.abs(a).max()
+    assert np.abs(a - b).max() <= 1e-6 * scale
+    assert np.abs(a - c).max() <= 1e-6 * scale
+    assert np.abs(a - d).max() > 1e-3 * scale
+
+
+def test_sample_offset_continues_the_sequence(gpu, scenes):
+    """Rendering spp in two calls (sample_offset) equals one call."""
+    sc = scenes.scene_c1(32, 32, 1)
+    _, a, _, _, _ = _render(gpu, sc, 32, seed=3, variance=False)
+    _, b1, _, _, _ = _render(gpu, sc, 16, seed=3, variance=False)
+    _, b2, _, _, _ = _render(gpu, sc, 16, seed=3, variance=False, sample_offset=16)
+    assert np.abs(a - (b1 + b2)).max() <= 1e-6 * np.abs(a).max()
+
+
+def test_large_scene_frame_properties(gpu, scenes):
+    sc = scenes.scene_c2(192, 108, 1)
+    img, s, q, cnt, st = _render(gpu, sc, 8, variance=False)
+    assert (cnt == 8).all()
+    assert np.isfinite(img).all() and (img[..., :3] >= 0).all()
+    assert (img[..., 3] == 1).all()
+    assert st["paths"] == 192 * 108 * 8
+    assert st["extension_rays"] >= st["paths"]
+    assert img[..., :3].mean() > 0
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(__file__), "golden", "film_c1_256x4096.npz")),
+                    reason="4096-spp reference film not generated")
+def test_c1_full_resolution_4096spp_rel_rmse(gpu, scenes):
+    """C1 at 256x256 and 4096 spp on both sides: every pixel within the
+    combined Monte Carlo error (3 sigma, at most 1% outliers) and relative RMSE
+    of the GPU image against the reference image under 1%."""
+    g = golden("film_c1_256x4096")
+    sc = scenes.scene_c1(256, 256, 1)
+    n = 4096
+    _, s, q, cnt, _ = _render(gpu, sc, n, seed=21)
+    mean = s / n
+    var = np.maximum(q / n - mean ** 2, 0.0)
+    ref = g["film"][..., :3].astype(np.float64)
+    z, dead_ok, glob = _zstats(mean, n, ref, int(g["spp"]), var)
+    assert float(np.mean(np.abs(z) > 3)) < 0.01
+    rel_rmse = np.sqrt(np.mean((mean - ref) ** 2)) / ref.mean()
+    assert rel_rmse < 0.01, rel_rmse

@@ -1,0 +1,137 @@
+"""GPU BVH build + traversal: identification (primary-hit) buffers bit-exact
+against the reference's false-colour pass and against the oracle's closest-hit
+query on the same rays."""
+import numpy as np
+import pytest
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+FLT_MAX = np.float32(3.402823466e38)
+
+
+def _hits_equal(a, b):
+    for k in ("inst", "geom", "prim", "material"):
+        if not np.array_equal(a[k], b[k]):
+            bad = np.nonzero(a[k] != b[k])[0]
+            return False, f"{k} differs at {bad[:8]} ({len(bad)} rays)"
+    for k in ("t", "u", "v"):
+        if not np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)):
+            bad = np.nonzero(a[k].view(np.uint32) != b[k].view(np.uint32))[0]
+            return False, f"{k} differs at {bad[:8]} ({len(bad)} rays)"
+    return True, ""
+
+
+def test_reference_rays_give_reference_ids(gpu, scenes):
+    """The exact rays the reference traced in its -F mid pass (logged at the
+    Embree boundary) give the same instance/geometry/primitive ids and t,u,v."""
+    g = golden("ids_c1_64")
+    rs = gpu.RenderScene(scenes.scene_c1(64, 64, 1))
+    hits = rs.trace(g["rays"])
+    hit = g["hit"].astype(bool)
+    assert np.array_equal(hits["inst"] != 0xFFFFFFFF, hit)
+    for k in ("geom", "inst", "prim"):
+        assert np.array_equal(hits[k][hit], g[k][hit]), k
+    for k in ("u", "v", "t"):
+        assert np.array_equal(hits[k][hit].view(np.uint32), g[k][hit].view(np.uint32)), k
+
+
+def test_id_pass_with_reference_jitter_full_c1(gpu, oracle, scenes):
+    """C1 material-ID pass at 256x256: GPU raygen + trace with the reference's
+    jitter stream equals the oracle replay (itself pinned bit-exact to the
+    reference binary) for every pixel."""
+    sc = scenes.scene_c1(256, 256, 1)
+    _, ref = oracle.OracleScene(sc).render_ids()
+    jitter = oracle.mt_uniforms(oracle.REFERENCE_SEED, 2 * 256 * 256)
+    rs = gpu.RenderScene(sc)
+    r = gpu.BDPTRenderer()
+    r.set_scene(rs)
+    hits, gprim = r.render_ids(gpu.PinholeCamera.from_spec(sc.camera), jitter=jitter)
+    ok, msg = _hits_equal(hits, ref)
+    assert ok, msg
+    faces = [len(m.faces) for m in sc.meshes]
+    pre = np.concatenate([[0], np.cumsum(faces)])
+    hit = hits["inst"] != 0xFFFFFFFF
+    assert np.array_equal(gprim[hit], pre[hits["geom"][hit]] + hits["prim"][hit])
+    assert set(np.unique(hits["material"][hit])) <= {0, 1}
+
+
+def _random_rays(rng, n, lo, hi, spread=1.0):
+    o = rng.uniform(lo, hi, (n, 3))
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    r = np.zeros((n, 8), np.float32)
+    r[:, 0:3], r[:, 4:7] = o, d * spread
+    r[:, 3] = 0.0
+    r[:, 7] = FLT_MAX
+    return r
+
+
+def test_large_instanced_scene_matches_oracle(gpu, oracle, scenes):
+    """1M-triangle scene, 64 rotated/scaled instances: GPU hits equal the
+    oracle's on camera rays and on random rays (bit-exact)."""
+    sc = scenes.scene_c2(160, 90, 1)
+    rs = gpu.RenderScene(sc)
+    os_ = oracle.OracleScene(sc)
+    rng = np.random.default_rng(5)
+    cam = rays_from_camera(oracle, sc)
+    rnd = _random_rays(rng, 20000, [-25, -25, -65], [25, 25, -15])
+    axis = _random_rays(rng, 3000, [-25, -25, -65], [25, 25, -15])
+    axis[:, 4:7] = np.eye(3, dtype=np.float32)[rng.integers(0, 3, 3000)] * np.where(
+        rng.uniform(size=(3000, 1)) < 0.5, -1, 1)
+    rays = np.concatenate([cam, rnd, axis])
+    ok, msg = _hits_equal(rs.trace(rays), os_.trace(rays))
+    assert ok, msg
+
+
+def rays_from_camera(oracle, sc):
+    W, H = sc.camera.width, sc.camera.height
+    jr = oracle.camera_rays(sc.camera, np.full(2 * W * H, 0.5, np.float32))
+    r = np.zeros((W * H, 8), np.float32)
+    r[:, 0:3], r[:, 4:7] = jr[:, 0:3], jr[:, 3:6]
+    r[:, 7] = FLT_MAX
+    return r
+
+
+def test_edge_cases_match_oracle(gpu, oracle, scenes):
+    """Shared edges (ties between the two ground triangles), vertices, grazing
+    rays, zero/NaN directions, empty intervals, origins on surfaces."""
+    sc = scenes.scene_mixed(8, 8, 1)
+    rs = gpu.RenderScene(sc)
+    os_ = oracle.OracleScene(sc)
+    rows = []
+    # rays through the ground quad's diagonal (shared edge) and its corners
+    for t in np.linspace(0.0, 1.0, 41):
+        p = np.array([-5 + 10 * t, -1.0, -5 + 10 * t - 5.0], np.float32)
+        rows.append([0, 3, -5, 0, *(p - np.array([0, 3, -5], np.float32)), FLT_MAX])
+    for c in ([-5, -1, -10], [5, -1, -10], [5, -1, 0], [-5, -1, 0]):
+        rows.append([0, 3, -5, 0, c[0], c[1] - 3, c[2] + 5, FLT_MAX])
+    # grazing along the ground plane, exactly in and slightly above it
+    for dy in (0.0, 1e-7, -1e-7):
+        rows.append([-6, -1 + dy, -5, 0, 1, 0, 0, FLT_MAX])
+    rows += [[0, 0, 0, 0, 0, 0, 0, FLT_MAX], [0, 0, 0, 0, np.nan, 0, -1, FLT_MAX],
+             [0, 0, 0, 5, 0, 0, -1, 1], [0, 0, 0, 0, 0, 0, -1, 0], [0, 0, 0, 0, 0, 0, -1, 4.3]]
+    rays = np.array(rows, np.float32)
+    rng = np.random.default_rng(9)
+    # origins on the spheres, shooting outwards and inwards
+    m = sc.meshes[1]
+    pts = m.positions[rng.integers(0, len(m.positions), 500)] + np.array([0, 0, -5], np.float32)
+    d = rng.normal(size=(500, 3)).astype(np.float32)
+    extra = np.zeros((500, 8), np.float32)
+    extra[:, 0:3], extra[:, 4:7], extra[:, 7] = pts, d, FLT_MAX
+    rays = np.concatenate([rays, extra])
+    ok, msg = _hits_equal(rs.trace(rays), os_.trace(rays))
+    assert ok, msg
+
+
+def test_alpha_masked_material_is_skipped_like_reference(gpu, oracle, scenes):
+    sc = scenes.scene_mixed(8, 8, 1)
+    sc.materials[3].alpha_mode = 1  # MASK with base alpha 0.5 < cutoff 0.75
+    sc.materials[3].alpha_cutoff = 0.75
+    rs = gpu.RenderScene(sc)
+    os_ = oracle.OracleScene(sc)
+    rays = rays_from_camera(oracle, scenes.scene_mixed(96, 96, 1))
+    a, b = rs.trace(rays), os_.trace(rays)
+    ok, msg = _hits_equal(a, b)
+    assert ok, msg
+    assert not np.any(a["material"] == 3)
