@@ -35,6 +35,9 @@ SOURCES = ["bvh_build.cu", "scene.cu", "render.cu", "capi.cu"]
 HEADERS = ["bvh_build.h", "omv_device.cuh", "omv_types.h", "scene.h", "trace.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
+# translation units whose device float math must round like the reference
+# (no implicit FMA contraction; explicit fmaf() calls in the traversal stay fused)
+NO_CONTRACT = {"render.cu", "scene.cu"}
 
 
 class OmvError(RuntimeError):
@@ -66,7 +69,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(src: str) -> str:
         obj = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
-        cmd = [nvcc, *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+        extra = ["--fmad=false"] if src in NO_CONTRACT else []
+        cmd = [nvcc, *NVCC_FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise OmvError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")

