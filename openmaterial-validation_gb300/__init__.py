@@ -96,9 +96,10 @@ def lib():
     global _lib
     if _lib is not None:
         return _lib
-    if not os.path.exists(LIB_PATH):
-        raise OmvError(f"{LIB_PATH} is missing: run build() first (no CPU fallback exists)")
-    L = C.CDLL(LIB_PATH)
+    path = os.environ.get("OMV_LIBRARY", LIB_PATH)  # a separately built libomv.so
+    if not os.path.exists(path):
+        raise OmvError(f"{path} is missing: run build() first (no CPU fallback exists)")
+    L = C.CDLL(path)
     vp = C.c_void_p
     st = C.c_int32
     L.omv_scene_create.argtypes = [C.POINTER(capi.SceneDesc), C.c_int32, C.POINTER(vp)]

@@ -35,6 +35,13 @@ def _render(gpu, sc, spp, seed=1, variance=True, **kw):
 
 def _zstats(mean_a, n_a, var_a, mean_b, n_b, var_b):
     """Returns (fraction of pixel-channels beyond 3 sigma, global z)."""
+    # non-finite means come from infinite samples (the reference's film has one:
+    # a single infinite contribution overflowed its FP32 sum); they are excluded
+    # and must stay rare
+    fin = np.isfinite(mean_a) & np.isfinite(mean_b) & np.isfinite(var_a) & np.isfinite(var_b)
+    assert np.count_nonzero(~fin) <= 1e-4 * mean_a.size + 3, np.count_nonzero(~fin)
+    mean_a, mean_b = np.where(fin, mean_a, 0.0), np.where(fin, mean_b, 0.0)
+    var_a, var_b = np.where(fin, var_a, 0.0), np.where(fin, var_b, 0.0)
     se2 = var_a / n_a + var_b / n_b
     live = se2 > 0
     z = np.zeros_like(mean_a)
@@ -151,5 +158,6 @@ def test_c1_full_resolution_4096spp_rel_rmse(gpu, scenes):
     frac3, glob = _zstats(mean, n, var, ref, int(g["spp"]), var)
     assert frac3 < 0.01, frac3
     assert abs(glob) < 3, glob
-    rel_rmse = np.sqrt(np.mean((mean - ref) ** 2)) / ref.mean()
+    fin = np.isfinite(ref)
+    rel_rmse = np.sqrt(np.mean((mean - ref)[fin] ** 2)) / ref[fin].mean()
     assert rel_rmse < 0.01, rel_rmse
