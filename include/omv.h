@@ -218,6 +218,39 @@ omv_status omv_render_device(omv_scene* scene, const omv_camera* camera, const o
                              double* d_sum_rgb, double* d_sumsq_rgb, uint32_t* d_count,
                              void* stream, omv_stats* stats);
 
+/* Capacity of the fixed device scratch used by omv_render_device_static. */
+#define OMV_STATIC_SCRATCH_BYTES ((size_t)32 << 20)
+
+/* omv_render_device without any device allocation; the reference has no
+ * counterpart (its BDPTRenderer::render renders on the host).
+ *
+ * For callers that may not allocate device memory while rendering: a host
+ * framework whose own pool owns the device memory, or a render loop that cannot
+ * take the device-wide synchronisation of cudaFree.  omv_render_device grows a
+ * per-scene scratch buffer with cudaMalloc; this call instead carves its wave
+ * queues out of one fixed array of OMV_STATIC_SCRATCH_BYTES in the library's
+ * device image and makes no cudaMalloc, cudaFree or other allocating call.
+ *
+ *   - Same film contract as omv_render_device: caller-owned device buffers,
+ *     accumulated into (zero them before the first call), asynchronous on
+ *     `stream` (NULL: the scene's stream).
+ *   - The scratch bounds the wave size: params->wave_paths = 0 picks the
+ *     largest wave that fits; a larger explicit wave_paths fails with
+ *     OMV_ERR_INVALID_ARGUMENT and a message giving the limit.  The number of
+ *     waves only changes the order of the FP64 film additions.
+ *   - Nothing in the scratch has to be zero on entry: the call clears its queue
+ *     and ray counters itself (cudaMemsetAsync on `stream`).
+ *   - No stats and no timing (it creates no CUDA events); time_kernels must be 0.
+ *   - The first call on each device resolves the scratch address
+ *     (cudaGetSymbolAddress, which may load the module on that device); make one
+ *     call before any stream capture.
+ *   - One scratch per device for all scenes: calls that overlap on the device
+ *     (different streams or threads, any scenes) race on it; keep them ordered
+ *     on one stream or serialise them. */
+omv_status omv_render_device_static(omv_scene* scene, const omv_camera* camera, const omv_params* params,
+                                    double* d_sum_rgb, double* d_sumsq_rgb, uint32_t* d_count,
+                                    void* stream);
+
 /* ----------------------------------------------------- rays / ID buffers --- */
 
 /* One closest-hit query (the reference's sceneIntersect, BDPTRenderer.cpp:75-102,

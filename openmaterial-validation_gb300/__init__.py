@@ -109,6 +109,7 @@ def lib():
                              C.POINTER(C.c_double), C.POINTER(C.c_uint32), C.POINTER(capi.Stats)]
     L.omv_render_device.argtypes = [vp, C.POINTER(capi.Camera), C.POINTER(capi.Params), vp, vp, vp, vp,
                                     C.POINTER(capi.Stats)]
+    L.omv_render_device_static.argtypes = [vp, C.POINTER(capi.Camera), C.POINTER(capi.Params), vp, vp, vp, vp]
     L.omv_trace_rays.argtypes = [vp, C.c_int64, capi.f32p, C.POINTER(capi.Hit)]
     L.omv_render_ids.argtypes = [vp, C.POINTER(capi.Camera), capi.f32p, C.c_uint64, C.POINTER(capi.Hit),
                                  C.POINTER(C.c_uint32)]
@@ -122,8 +123,8 @@ def lib():
     L.omv_params_default.restype = None
     L.omv_struct_sizes.argtypes = [C.POINTER(C.c_int64), C.c_int32]
     for n in ("omv_scene_create", "omv_scene_destroy", "omv_scene_get_info", "omv_render", "omv_render_device",
-              "omv_trace_rays", "omv_render_ids", "omv_brdf_eval_direct", "omv_brdf_sample_indirect",
-              "omv_om_fresnel", "omv_camera_rays", "omv_env_radiance", "omv_struct_sizes"):
+              "omv_render_device_static", "omv_trace_rays", "omv_render_ids", "omv_brdf_eval_direct",
+              "omv_brdf_sample_indirect", "omv_om_fresnel", "omv_camera_rays", "omv_env_radiance", "omv_struct_sizes"):
         getattr(L, n).restype = st
     _lib = L
     return L

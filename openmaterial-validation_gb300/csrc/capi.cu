@@ -177,6 +177,20 @@ omv_status omv_render_device(omv_scene* scene, const omv_camera* camera, const o
     });
 }
 
+omv_status omv_render_device_static(omv_scene* scene, const omv_camera* camera, const omv_params* params,
+                                    double* d_sum_rgb, double* d_sumsq_rgb, uint32_t* d_count, void* stream)
+{
+    return guarded([&] {
+        check_scene(scene);
+        check_camera(camera);
+        if (!params || !d_sum_rgb || !d_count) throw omv::ArgError("params, d_sum_rgb and d_count are required");
+        if (params->accumulate_variance && !d_sumsq_rgb) throw omv::ArgError("accumulate_variance needs d_sumsq_rgb");
+        cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : scene->h->stream;
+        omv::render_frame_static(*scene->h, *camera, *params, d_sum_rgb,
+                                 params->accumulate_variance ? d_sumsq_rgb : nullptr, d_count, st);
+    });
+}
+
 omv_status omv_render(omv_scene* scene, const omv_camera* camera, const omv_params* params, float* image_rgba,
                       double* sum_rgb, double* sumsq_rgb, uint32_t* count, omv_stats* stats)
 {

@@ -24,6 +24,8 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "omv_device.cuh"
@@ -695,15 +697,16 @@ inline int grid_for(int64_t n, int t) { return (int)std::max<int64_t>(1, (n + t 
 
 // -------------------------------------------------------------- host ---
 
-static void ensure_scratch(SceneHost& s, int64_t wave_cap, int light_slots, int shadow_slots)
+namespace {
+
+// Byte offsets of one wave's arrays inside a single scratch block (each array
+// starts on a 256-byte boundary).
+struct ScratchLayout {
+    size_t tp, rad, ltp, lrad, lmeta, lvp, lvr, rq0, rq1, hits, sq, ctr, stats, err, bytes;
+};
+
+ScratchLayout scratch_layout(int64_t wave_cap, int light_slots, int shadow_slots)
 {
-    RenderScratch& R = s.scratch;
-    if (R.base && R.wave_cap >= wave_cap && R.light_slots >= light_slots && R.shadow_slots >= shadow_slots) return;
-    if (R.base) {
-        OMV_CUDA(cudaStreamSynchronize(s.stream));
-        cudaFree(R.base);
-        R = RenderScratch{};
-    }
     const size_t W = (size_t)wave_cap;
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -711,50 +714,92 @@ static void ensure_scratch(SceneHost& s, int64_t wave_cap, int light_slots, int 
         off += (bytes + 255) & ~(size_t)255;
         return o;
     };
-    size_t o_tp = take(W * 16), o_rad = take(W * 16), o_ltp = take(W * 16), o_lrad = take(W * 16),
-           o_lmeta = take(W * 4), o_lvp = take((size_t)light_slots * W * 16), o_lvr = take((size_t)light_slots * W * 16),
-           o_rq0 = take(W * 32), o_rq1 = take(W * 32), o_hits = take(W * 16),
-           o_sq = take((size_t)shadow_slots * W * 48 + 48), o_ctr = take(kMaxCounters * 4), o_stats = take(16 * 8),
-           o_err = take(16 * 4);
-    OMV_CUDA(cudaMalloc(&R.base, off));
-    char* b = static_cast<char*>(R.base);
-    R.bytes = off;
+    ScratchLayout L;
+    L.tp = take(W * 16);
+    L.rad = take(W * 16);
+    L.ltp = take(W * 16);
+    L.lrad = take(W * 16);
+    L.lmeta = take(W * 4);
+    L.lvp = take((size_t)light_slots * W * 16);
+    L.lvr = take((size_t)light_slots * W * 16);
+    L.rq0 = take(W * 32);
+    L.rq1 = take(W * 32);
+    L.hits = take(W * 16);
+    L.sq = take((size_t)shadow_slots * W * 48 + 48);
+    L.ctr = take(kMaxCounters * 4);
+    L.stats = take(16 * 8);
+    L.err = take(16 * 4);
+    L.bytes = off;
+    return L;
+}
+
+// Scratch bytes of one path: tp rad ltp lrad (16 B each), lmeta 4, light
+// vertices 32 per slot, two ray-queue entries 64, hit 16, shadow entries 48 per
+// slot (each array is further rounded up to 256 bytes).
+size_t path_scratch_bytes(int light_slots, int shadow_slots)
+{
+    return 68 + 32 * (size_t)light_slots + 80 + 48 * (size_t)shadow_slots;
+}
+
+void carve_scratch(RenderScratch& R, void* base, int64_t wave_cap, int light_slots, int shadow_slots)
+{
+    const ScratchLayout L = scratch_layout(wave_cap, light_slots, shadow_slots);
+    char* b = static_cast<char*>(base);
+    R.base = base;
+    R.bytes = L.bytes;
     R.wave_cap = wave_cap;
     R.light_slots = light_slots;
     R.shadow_slots = shadow_slots;
-    R.tp = (float4*)(b + o_tp);
-    R.rad = (float4*)(b + o_rad);
-    R.ltp = (float4*)(b + o_ltp);
-    R.lrad = (float4*)(b + o_lrad);
-    R.lmeta = (uint32_t*)(b + o_lmeta);
-    R.lv_pos = (float4*)(b + o_lvp);
-    R.lv_rad = (float4*)(b + o_lvr);
-    R.rq[0] = (float4*)(b + o_rq0);
-    R.rq[1] = (float4*)(b + o_rq1);
-    R.hits = (uint4*)(b + o_hits);
-    R.sq = (float4*)(b + o_sq);
-    R.ctr = (uint32_t*)(b + o_ctr);
-    R.stats = (unsigned long long*)(b + o_stats);
-    R.err = (uint32_t*)(b + o_err);
+    R.tp = (float4*)(b + L.tp);
+    R.rad = (float4*)(b + L.rad);
+    R.ltp = (float4*)(b + L.ltp);
+    R.lrad = (float4*)(b + L.lrad);
+    R.lmeta = (uint32_t*)(b + L.lmeta);
+    R.lv_pos = (float4*)(b + L.lvp);
+    R.lv_rad = (float4*)(b + L.lvr);
+    R.rq[0] = (float4*)(b + L.rq0);
+    R.rq[1] = (float4*)(b + L.rq1);
+    R.hits = (uint4*)(b + L.hits);
+    R.sq = (float4*)(b + L.sq);
+    R.ctr = (uint32_t*)(b + L.ctr);
+    R.stats = (unsigned long long*)(b + L.stats);
+    R.err = (uint32_t*)(b + L.err);
 }
 
-void render_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, double* d_sum, double* d_sumsq,
-                  uint32_t* d_count, cudaStream_t st, omv_stats* stats)
+// Validated sizes of one frame: paths, wave capacity and vertex slots.
+struct FramePlan {
+    int64_t npix, total, cap;
+    int light_slots, shadow_slots;
+    bool lights;
+};
+
+// `cap` is the requested wave size (0: `default_cap`), clamped to the frame.
+FramePlan plan_frame(const SceneHost& s, const omv_camera& cam, const omv_params& p, int64_t default_cap)
 {
     if (cam.width <= 0 || cam.height <= 0) throw ArgError("camera resolution must be positive");
     if (p.samples_per_pixel < 0 || p.camera_bounces < 0 || p.light_bounces < 0)
         throw ArgError("negative sample or bounce count");
     if (p.camera_bounces > 60 || p.light_bounces > 60) throw ArgError("at most 60 bounces are supported");
-    const int64_t npix = (int64_t)cam.width * cam.height;
-    const int64_t total = npix * p.samples_per_pixel;
-    if (npix > (int64_t)0x7FFFFFFF) throw ArgError("image too large");
-    int64_t cap = p.wave_paths > 0 ? p.wave_paths : (int64_t)1 << 22;
-    cap = std::min<int64_t>(cap, std::max<int64_t>(total, 1));
-    const bool lights = s.num_lights > 0;
-    const int light_slots = lights ? p.light_bounces + 1 : 1;
-    const int shadow_slots = lights ? light_slots : 1;
-    ensure_scratch(s, cap, light_slots, shadow_slots);
-    RenderScratch& R = s.scratch;
+    FramePlan P;
+    P.npix = (int64_t)cam.width * cam.height;
+    P.total = P.npix * p.samples_per_pixel;
+    if (P.npix > (int64_t)0x7FFFFFFF) throw ArgError("image too large");
+    P.cap = p.wave_paths > 0 ? p.wave_paths : default_cap;
+    P.cap = std::min<int64_t>(P.cap, std::max<int64_t>(P.total, 1));
+    P.lights = s.num_lights > 0;
+    P.light_slots = P.lights ? p.light_bounces + 1 : 1;
+    P.shadow_slots = P.lights ? P.light_slots : 1;
+    return P;
+}
+
+// The wave loop of one frame on scratch R (at least P.cap paths).  With
+// `events` false no CUDA event is created: no frame or kernel timing, and
+// `stats` must be null.
+void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_camera& cam, const omv_params& p,
+               double* d_sum, double* d_sumsq, uint32_t* d_count, cudaStream_t st, omv_stats* stats, bool events)
+{
+    const int64_t total = P.total, npix = P.npix, cap = P.cap;
+    const bool lights = P.lights;
     OMV_CUDA(cudaMemsetAsync(R.stats, 0, 16 * 8, st));
     WaveArgs A;
     A.S = s.dev;
@@ -780,6 +825,7 @@ void render_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, doub
     int64_t launches = 0;
     // optional per-launch events around the closest-hit kernels
     std::vector<cudaEvent_t> ext_ev, sh_ev;
+    const bool time_kernels = events && p.time_kernels;
     auto timed = [&](std::vector<cudaEvent_t>& pool) -> cudaEvent_t {
         cudaEvent_t e;
         OMV_CUDA(cudaEventCreate(&e));
@@ -787,10 +833,12 @@ void render_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, doub
         pool.push_back(e);
         return e;
     };
-    cudaEvent_t e0, e1;
-    OMV_CUDA(cudaEventCreate(&e0));
-    OMV_CUDA(cudaEventCreate(&e1));
-    OMV_CUDA(cudaEventRecord(e0, st));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (events) {
+        OMV_CUDA(cudaEventCreate(&e0));
+        OMV_CUDA(cudaEventCreate(&e1));
+        OMV_CUDA(cudaEventRecord(e0, st));
+    }
     for (int64_t wb = 0; wb < total; wb += cap) {
         A.wave_base = wb;
         A.wave_n = (int32_t)std::min<int64_t>(cap, total - wb);
@@ -803,11 +851,11 @@ void render_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, doub
                 float4* in = R.rq[1];
                 float4* out = R.rq[0];
                 if (b % 2 == 0) std::swap(in, out);
-                if (p.time_kernels) timed(ext_ev);
+                if (time_kernels) timed(ext_ev);
                 k_extend<<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, in, R.hits,
                                                                R.ctr + kCtrLight + b, R.ctr + kCtrWork + work++,
                                                                R.stats, kStatLight);
-                if (p.time_kernels) timed(ext_ev);
+                if (time_kernels) timed(ext_ev);
                 k_light_shade<<<shade_grid, kShadeThreads, 0, st>>>(A, b, in, out);
                 launches += 2;
             }
@@ -817,23 +865,27 @@ void render_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, doub
         for (int b = 1; b <= p.camera_bounces; ++b) {
             float4* in = R.rq[(b + 1) % 2];
             float4* out = R.rq[b % 2];
-            if (p.time_kernels) timed(ext_ev);
+            if (time_kernels) timed(ext_ev);
             k_extend<<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, in, R.hits, R.ctr + kCtrCam + b,
                                                            R.ctr + kCtrWork + work++, R.stats, kStatExt);
-            if (p.time_kernels) timed(ext_ev);
+            if (time_kernels) timed(ext_ev);
             k_camera_shade<<<shade_grid, kShadeThreads, 0, st>>>(A, b, in, out);
             launches += 2;
             if (lights) {
-                if (p.time_kernels) timed(sh_ev);
+                if (time_kernels) timed(sh_ev);
                 k_shadow<<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, R.sq, R.ctr + kCtrShadow + b,
                                                                R.ctr + kCtrWork + work++, R.rad, R.stats);
-                if (p.time_kernels) timed(sh_ev);
+                if (time_kernels) timed(sh_ev);
                 ++launches;
             }
         }
         k_film<<<grid_for(A.wave_n, kShadeThreads), kShadeThreads, 0, st>>>(A, d_sum, d_sumsq, d_count);
         ++launches;
         OMV_CUDA(cudaGetLastError());
+    }
+    if (!events) {
+        OMV_CUDA(cudaGetLastError());
+        return;
     }
     OMV_CUDA(cudaEventRecord(e1, st));
     if (stats) {
@@ -871,6 +923,87 @@ void render_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, doub
     for (auto e : sh_ev) cudaEventDestroy(e);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+}
+
+}  // namespace
+
+static void ensure_scratch(SceneHost& s, int64_t wave_cap, int light_slots, int shadow_slots)
+{
+    RenderScratch& R = s.scratch;
+    if (R.base && R.wave_cap >= wave_cap && R.light_slots >= light_slots && R.shadow_slots >= shadow_slots) return;
+    if (R.base) {
+        OMV_CUDA(cudaStreamSynchronize(s.stream));
+        cudaFree(R.base);
+        R = RenderScratch{};
+    }
+    void* base = nullptr;
+    OMV_CUDA(cudaMalloc(&base, scratch_layout(wave_cap, light_slots, shadow_slots).bytes));
+    carve_scratch(R, base, wave_cap, light_slots, shadow_slots);
+}
+
+void render_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, double* d_sum, double* d_sumsq,
+                  uint32_t* d_count, cudaStream_t st, omv_stats* stats)
+{
+    const FramePlan P = plan_frame(s, cam, p, (int64_t)1 << 22);
+    ensure_scratch(s, P.cap, P.light_slots, P.shadow_slots);
+    run_waves(s, s.scratch, P, cam, p, d_sum, d_sumsq, d_count, st, stats, true);
+}
+
+// ------------------------------------------ render without allocation ---
+//
+// Callers that must not allocate device memory while they render: a host
+// framework that owns the device memory through its own pool and leaves no
+// headroom, or a loop that cannot afford cudaMalloc/cudaFree (cudaFree
+// synchronises the whole device).  The wave scratch then comes from one fixed
+// array in the library's device image instead of the scene's grown buffer.
+namespace {
+
+__device__ __align__(256) unsigned char g_static_scratch[OMV_STATIC_SCRATCH_BYTES];
+
+constexpr int kMaxDevices = 64;
+
+// Device address of g_static_scratch on `device` (current).  Resolved once per
+// device; the first call may load the module on that device.
+void* static_scratch_address(int device)
+{
+    static std::mutex mu;
+    static void* addr[kMaxDevices] = {};
+    if (device < 0 || device >= kMaxDevices) throw ArgError("device index out of range for the static scratch");
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[device]) OMV_CUDA(cudaGetSymbolAddress(&addr[device], g_static_scratch));
+    return addr[device];
+}
+
+}  // namespace
+
+int64_t static_wave_limit(int light_slots, int shadow_slots)
+{
+    const size_t per_path = path_scratch_bytes(light_slots, shadow_slots);
+    const size_t fixed = 48 + kMaxCounters * 4 + 16 * 8 + 16 * 4 + 14 * 256;
+    int64_t cap = (int64_t)((OMV_STATIC_SCRATCH_BYTES - fixed) / per_path) & ~(int64_t)31;
+    while (cap > 0 && scratch_layout(cap, light_slots, shadow_slots).bytes > OMV_STATIC_SCRATCH_BYTES) cap -= 32;
+    return cap;
+}
+
+void render_frame_static(SceneHost& s, const omv_camera& cam, const omv_params& p, double* d_sum, double* d_sumsq,
+                         uint32_t* d_count, cudaStream_t st)
+{
+    if (p.time_kernels) throw ArgError("time_kernels needs CUDA events, which the no-allocation render does not create");
+    FramePlan P = plan_frame(s, cam, p, 1);
+    const int64_t limit = static_wave_limit(P.light_slots, P.shadow_slots);
+    if (p.wave_paths > 0) {
+        const size_t need = scratch_layout(P.cap, P.light_slots, P.shadow_slots).bytes;
+        if (need > OMV_STATIC_SCRATCH_BYTES)
+            throw ArgError("wave_paths " + std::to_string(p.wave_paths) + " needs " + std::to_string(need) +
+                           " bytes of scratch; the static scratch holds " +
+                           std::to_string((size_t)OMV_STATIC_SCRATCH_BYTES) + " bytes (at most " +
+                           std::to_string(limit) + " paths per wave with these bounce counts)");
+    } else {
+        P.cap = std::min<int64_t>(limit, std::max<int64_t>(P.total, 1));
+    }
+    RenderScratch R;
+    carve_scratch(R, static_scratch_address(s.device), P.cap, P.light_slots, P.shadow_slots);
+    run_waves(s, R, P, cam, p, d_sum, d_sumsq, d_count, st, nullptr, false);
 }
 
 void render_ids(SceneHost& s, const omv_camera& cam, const float* d_jitter, uint64_t seed, omv_hit* d_hits,

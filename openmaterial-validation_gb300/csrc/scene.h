@@ -87,6 +87,11 @@ SceneHost* scene_create(const omv_scene_desc& desc, int device);
 
 void render_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, double* d_sum, double* d_sumsq,
                   uint32_t* d_count, cudaStream_t st, omv_stats* stats);
+// render_frame on the fixed scratch array; makes no device allocation
+void render_frame_static(SceneHost& s, const omv_camera& cam, const omv_params& p, double* d_sum, double* d_sumsq,
+                         uint32_t* d_count, cudaStream_t st);
+// largest wave of render_frame_static for these vertex-slot counts
+int64_t static_wave_limit(int light_slots, int shadow_slots);
 void render_ids(SceneHost& s, const omv_camera& cam, const float* d_jitter, uint64_t seed, omv_hit* d_hits,
                 uint32_t* d_gprim, cudaStream_t st);
 void trace_rays(SceneHost& s, int64_t n, const float* d_rays, omv_hit* d_hits, cudaStream_t st);

@@ -1,0 +1,95 @@
+"""omv_render_device_static (the render without device allocation) through the
+C ABI, against omv_render_device on the same scene, camera and parameters.
+
+The file sorts last so that, in a full run, these calls also come after every
+other GPU test in the same process; each test builds its own scene, so the file
+passes alone as well.  Films differ between the two entry points only in the
+order of the FP64 atomic additions (the static scratch may split the frame into
+more waves), so sums agree to 1e-9 of the film's largest value and sample counts
+exactly."""
+import ctypes as C
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+OMV_ERR_INVALID_ARGUMENT = 1
+
+
+def _setup(gpu, scenes, spp=16, **kw):
+    torch = pytest.importorskip("torch")
+    sc = scenes.scene_c1(64, 64, 1)
+    scene = gpu.RenderScene(sc)
+    cam = gpu.PinholeCamera.from_spec(sc.camera).to_c()
+    params = gpu.RendererParameters.for_scene(sc, samplesPerPixel=spp, seed=5, accumulate_variance=True, **kw).to_c()
+    return torch, sc, scene, cam, params
+
+
+def _film(torch, npix):
+    return (torch.zeros(3 * npix, dtype=torch.float64, device="cuda"),
+            torch.zeros(3 * npix, dtype=torch.float64, device="cuda"),
+            torch.zeros(npix, dtype=torch.int32, device="cuda"))
+
+
+def _render(gpu, torch, entry, scene, cam, params, film):
+    L = gpu.lib()
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    ptrs = [C.c_void_p(t.data_ptr()) for t in film]
+    if entry == "static":
+        st = L.omv_render_device_static(scene.handle, C.byref(cam), C.byref(params), *ptrs, stream)
+    else:
+        st = L.omv_render_device(scene.handle, C.byref(cam), C.byref(params), *ptrs, stream, None)
+    torch.cuda.synchronize()
+    return st
+
+
+def _assert_same_film(a, b, spp):
+    scale = float(a[0].abs().max())
+    assert scale > 0
+    assert float((a[0] - b[0]).abs().max()) <= 1e-9 * scale
+    assert float((a[1] - b[1]).abs().max()) <= 1e-9 * float(a[1].abs().max())
+    assert bool((a[2] == b[2]).all()) and int(a[2].min()) == spp
+
+
+def test_static_render_matches_device_render_on_two_calls_in_a_row(gpu, scenes):
+    torch, sc, scene, cam, params = _setup(gpu, scenes)
+    npix = cam.width * cam.height
+    ref = _film(torch, npix)
+    gpu.check(_render(gpu, torch, "device", scene, cam, params, ref))
+    for _ in range(2):
+        out = _film(torch, npix)
+        gpu.check(_render(gpu, torch, "static", scene, cam, params, out))
+        _assert_same_film(ref, out, params.samples_per_pixel)
+
+
+def test_static_render_with_explicit_wave_matches(gpu, scenes):
+    torch, sc, scene, cam, params = _setup(gpu, scenes, wave_paths=3001)
+    npix = cam.width * cam.height
+    ref = _film(torch, npix)
+    gpu.check(_render(gpu, torch, "device", scene, cam, params, ref))
+    out = _film(torch, npix)
+    gpu.check(_render(gpu, torch, "static", scene, cam, params, out))
+    _assert_same_film(ref, out, params.samples_per_pixel)
+
+
+def test_static_render_leaves_free_device_memory_unchanged(gpu, scenes):
+    torch, sc, scene, cam, params = _setup(gpu, scenes)
+    npix = cam.width * cam.height
+    films = [_film(torch, npix) for _ in range(3)]
+    gpu.check(_render(gpu, torch, "static", scene, cam, params, films[0]))  # first call per device: setup
+    free0 = torch.cuda.mem_get_info()[0]
+    for f in films[1:]:
+        gpu.check(_render(gpu, torch, "static", scene, cam, params, f))
+    assert torch.cuda.mem_get_info()[0] == free0
+
+
+def test_static_render_rejects_a_wave_beyond_the_scratch(gpu, scenes):
+    torch, sc, scene, cam, params = _setup(gpu, scenes, spp=1024, wave_paths=1 << 22)
+    film = _film(torch, cam.width * cam.height)
+    st = _render(gpu, torch, "static", scene, cam, params, film)
+    assert st == OMV_ERR_INVALID_ARGUMENT
+    assert b"static scratch holds" in gpu.lib().omv_last_error()
+    assert int(film[2].sum()) == 0  # nothing was launched
+    params.wave_paths = 0
+    params.time_kernels = 1
+    assert _render(gpu, torch, "static", scene, cam, params, film) == OMV_ERR_INVALID_ARGUMENT
