@@ -12,7 +12,8 @@
 //      octrees, and k-d trees", HPG 2012): one thread per internal node
 //   5. bottom-up boxes with arrival counters
 //   6. top-down collapse into 8-wide nodes (greedy: expand the child of largest
-//      surface area), leaves of at most kLeafMax triangles, child boxes
+//      surface area; children placed in octant slots), leaves of at most
+//      kLeafMax triangles, child boxes
 //      quantised to 16 bits per bound against the node box, rounded outward and
 //      verified in float so the decoded box always contains the true box.
 #include <cuda_runtime.h>
@@ -423,6 +424,44 @@ __global__ void k_collapse(int nwork, const Work* __restrict__ work, const Node2
     o.py = __fsub_rn(nb.lo[1], sc[1]);
     o.pz = __fsub_rn(nb.lo[2], sc[2]);
     const float p[3] = {o.px, o.py, o.pz};
+    // octant slot assignment (Ylitie, Karras, Laine, "Efficient incoherent ray
+    // traversal on GPUs through compressed wide BVHs", HPG 2017): slot s stands
+    // for the corner direction (+-1,+-1,+-1) given by its bits; children go to the
+    // slot their centroid offset points to (greedy on the largest projection), so
+    // visiting slots in the order s ^ octant(ray) is approximately front to back.
+    int at[8];
+    {
+        float score[8][8];
+        const float cx = 0.5f * (nb.lo[0] + nb.hi[0]), cy = 0.5f * (nb.lo[1] + nb.hi[1]),
+                    cz = 0.5f * (nb.lo[2] + nb.hi[2]);
+        for (int i = 0; i < ns; ++i) {
+            const float dx = 0.5f * (sb[i].lo[0] + sb[i].hi[0]) - cx;
+            const float dy = 0.5f * (sb[i].lo[1] + sb[i].hi[1]) - cy;
+            const float dz = 0.5f * (sb[i].lo[2] + sb[i].hi[2]) - cz;
+            for (int q = 0; q < 8; ++q)
+                score[i][q] = ((q & 1) ? dx : -dx) + ((q & 2) ? dy : -dy) + ((q & 4) ? dz : -dz);
+        }
+        for (int q = 0; q < 8; ++q) at[q] = -1;
+        uint32_t used_child = 0, used_slot = 0;
+        for (int k = 0; k < ns; ++k) {
+            float best = -3.0e38f;
+            int bi = -1, bq = -1;
+            for (int i = 0; i < ns; ++i) {
+                if (used_child & (1u << i)) continue;
+                for (int q = 0; q < 8; ++q) {
+                    if (used_slot & (1u << q)) continue;
+                    if (score[i][q] > best) {
+                        best = score[i][q];
+                        bi = i;
+                        bq = q;
+                    }
+                }
+            }
+            at[bq] = bi;
+            used_child |= 1u << bi;
+            used_slot |= 1u << bq;
+        }
+    }
     uint32_t imask = 0, meta[8];
     int rank = 0, off = 0;
     for (int s = 0; s < 8; ++s) {
@@ -432,10 +471,14 @@ __global__ void k_collapse(int nwork, const Work* __restrict__ work, const Node2
             o.qhi[a][s] = 0;
         }
     }
-    for (int s = 0; s < ns; ++s) {
-        int cnt = sl[s] - sf[s] + 1;
+    // internal children are stored in slot order: child(s) = child_base + popc(imask & ((1<<s)-1));
+    // leaf primitives in slot order from prim_base
+    for (int s = 0; s < 8; ++s) {
+        const int c = at[s];
+        if (c < 0) continue;
+        int cnt = sl[c] - sf[c] + 1;
         for (int a = 0; a < 3; ++a) {
-            float lo = sb[s].lo[a], hi = sb[s].hi[a];
+            float lo = sb[c].lo[a], hi = sb[c].hi[a];
             int ql = (int)floorf(__fdiv_rn(__fsub_rn(lo, p[a]), sc[a]));
             int qh = (int)ceilf(__fdiv_rn(__fsub_rn(hi, p[a]), sc[a]));
             ql = max(0, min(65535, ql));
@@ -451,12 +494,12 @@ __global__ void k_collapse(int nwork, const Work* __restrict__ work, const Node2
             imask |= 1u << s;
             meta[s] = (uint32_t)rank;
             uint32_t idx = atomicAdd(next_count, 1u);
-            next_work[idx] = Work{slot[s], cbase + (uint32_t)rank};
+            next_work[idx] = Work{slot[c], cbase + (uint32_t)rank};
             ++rank;
         } else {
             meta[s] = ((uint32_t)cnt << 5) | (uint32_t)off;
             for (int k = 0; k < cnt; ++k) {
-                uint32_t item = vals[sf[s] + k];
+                uint32_t item = vals[sf[c] + k];
                 uint32_t dst = pbase + (uint32_t)(off + k);
                 if (kTlas) {
                     out_items[dst] = item;
@@ -680,6 +723,8 @@ void validate_accel(const AccelResult& a, const std::vector<MeshGeom>& meshes, c
             for (int s = 0; s < 8; ++s) {
                 const uint32_t meta = ((s < 4 ? nd.meta_lo : nd.meta_hi) >> (8 * (s & 3))) & 0xFFu;
                 if ((imask >> s) & 1u) {
+                    if (meta != (uint32_t)__builtin_popcount(imask & ((1u << s) - 1u)))
+                        throw std::runtime_error("BVH validation: internal children not in slot order");
                     stack.push_back({nd.child_base + meta, depth + 1});
                 } else if (meta) {
                     const uint32_t cnt = meta >> 5, off = meta & 31u;

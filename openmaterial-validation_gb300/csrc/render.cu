@@ -227,6 +227,7 @@ struct WaveArgs {
     int32_t wave_n;
     int32_t wave_cap;
     int32_t npix;
+    int32_t spp;
     int32_t sample_offset;
     int32_t cam_bounces, light_bounces, max_len;
     int32_t atten_mode;
@@ -234,11 +235,15 @@ struct WaveArgs {
     RenderScratch R;
 };
 
+// Path g of the frame is sample g % spp of pixel g / spp: the samples of one
+// pixel are neighbours, so a warp's camera rays (and first shading points) are
+// nearly identical.  Random numbers are keyed by (pixel, sample), so the order
+// does not change the image.
 __device__ __forceinline__ void path_ids(const WaveArgs& A, int k, uint32_t& pixel, uint32_t& sample)
 {
     const int64_t g = A.wave_base + k;
-    pixel = (uint32_t)(g % A.npix);
-    sample = (uint32_t)(A.sample_offset + g / A.npix);
+    pixel = (uint32_t)(g / A.spp);
+    sample = (uint32_t)(A.sample_offset + g % A.spp);
 }
 
 // ------------------------------------------------------------ raygen ---
@@ -252,14 +257,17 @@ __global__ void __launch_bounds__(kShadeThreads) k_camera_gen(WaveArgs A)
         path_ids(A, k, pixel, sample);
         Rng4 r = rng4(A.seed, pixel, sample, 0u, kStreamCamera);
         camera_ray(A.cam, (int)(pixel % A.cam.width), (int)(pixel / A.cam.width), r.u[0], r.u[1], O, R);
-        A.R.tp[k] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-        A.R.rad[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        // throughput starts at 1 and radiance at 0: the first camera shade uses
+        // the constants and writes both, so only a frame without camera
+        // bounces needs the radiance cleared here
+        if (A.cam_bounces == 0) A.R.rad[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
-    const uint32_t slot = warp_append(&A.R.ctr[kCtrCam + 1], ok);
+    // every path emits a camera ray: queue slot = path index, no append
+    if (k == 0) A.R.ctr[kCtrCam + 1] = (uint32_t)A.wave_n;
     if (ok) {
         V3 so = shifted_origin(O, R, 1.0f);
-        A.R.rq[0][2 * (size_t)slot] = make_float4(so.x, so.y, so.z, 0.0f);
-        A.R.rq[0][2 * (size_t)slot + 1] = make_float4(R.x, R.y, R.z, __int_as_float(k));
+        A.R.rq[0][2 * (size_t)k] = make_float4(so.x, so.y, so.z, 0.0f);
+        A.R.rq[0][2 * (size_t)k + 1] = make_float4(R.x, R.y, R.z, __int_as_float(k));
     }
 }
 
@@ -314,12 +322,13 @@ __global__ void __launch_bounds__(kShadeThreads) k_light_gen(WaveArgs A)
         A.R.lv_pos[k] = make_float4(O.x, O.y, O.z, 0.0f);
         A.R.lv_rad[k] = make_float4(rad.x, rad.y, rad.z, 0.0f);
     }
+    // with light bounces every path emits a light ray: queue slot = path index
     const bool push = ok && A.light_bounces >= 1;
-    const uint32_t slot = warp_append(&A.R.ctr[kCtrLight + 1], push);
+    if (k == 0 && A.light_bounces >= 1) A.R.ctr[kCtrLight + 1] = (uint32_t)A.wave_n;
     if (push) {
         V3 so = shifted_origin(O, R, 1.0f);
-        A.R.rq[1][2 * (size_t)slot] = make_float4(so.x, so.y, so.z, 0.0f);
-        A.R.rq[1][2 * (size_t)slot + 1] = make_float4(R.x, R.y, R.z, __int_as_float(k));
+        A.R.rq[1][2 * (size_t)k] = make_float4(so.x, so.y, so.z, 0.0f);
+        A.R.rq[1][2 * (size_t)k + 1] = make_float4(R.x, R.y, R.z, __int_as_float(k));
     }
 }
 
@@ -451,19 +460,23 @@ __global__ void __launch_bounds__(kShadeThreads) k_camera_shade(WaveArgs A, int 
             k = __float_as_int(rb.w);
             tnear = ra.w;
             const V3 in = v3(rb.x, rb.y, rb.z);
-            const float4 tp4 = A.R.tp[k];
+            const bool first = b == 1;  // throughput 1, radiance 0 (not stored yet)
+            const float4 tp4 = first ? make_float4(1.0f, 1.0f, 1.0f, 0.0f) : A.R.tp[k];
             const V3 tp = v3(tp4.x, tp4.y, tp4.z);
             if (h.x == kInvalid) {
                 // escape: background x throughput when cp_len <= maxPathLength (:251-258)
                 if (S.env.present && b <= A.max_len) {
                     const V3 bg = env_radiance(S.env, in);
-                    float4 r = A.R.rad[k];
+                    float4 r = first ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : A.R.rad[k];
                     r.x += bg.x * tp.x;
                     r.y += bg.y * tp.y;
                     r.z += bg.z * tp.z;
                     A.R.rad[k] = r;
+                } else if (first) {
+                    A.R.rad[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 }
             } else {
+                if (first) A.R.rad[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 uint32_t pixel, sample;
                 path_ids(A, k, pixel, sample);
                 const Surf sp = surface_point(S, h.x, h.y, __uint_as_float(h.z), __uint_as_float(h.w), true);
@@ -585,22 +598,90 @@ __global__ void __launch_bounds__(kTraceThreads) k_shadow(DevScene S, const uint
 
 // -------------------------------------------------------------- film ---
 // PinholeCamera::hit (PinholeCamera.cpp:97-108), FP64 accumulation
+// Float-float accumulator (value = hi + lo, |lo| <= ulp(hi) / 2): sums of a
+// few hundred FP32 samples kept to about 2^-44 relative, in FP32 arithmetic
+// (FP64 throughput is a small fraction of FP32 on this GPU).  ff_add is
+// Knuth's TwoSum of the high parts with the low parts folded in.  Squares of
+// samples beyond 1.8e19 overflow to infinity (the FP32 range).
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ FF ff_add(FF a, FF b)
+{
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    const float hi = __fadd_rn(s, e);
+    if (fabsf(s) > kFltMax) return FF{s, 0.0f};  // an infinite sample stays infinite (not NaN)
+    return FF{hi, __fsub_rn(e, __fsub_rn(hi, s))};
+}
+// x * x exactly as a float-float (the FMA gives the rounding error of the product)
+__device__ __forceinline__ FF ff_sqr(float x)
+{
+    const float p = __fmul_rn(x, x);
+    return FF{p, fmaf(x, x, -p)};
+}
+
+// PinholeCamera::hit for every path of the wave, without atomics: the wave's
+// pixels are split between warps (one pixel per warp when spp >= 32, else
+// 32 / spp whole pixels), each warp sums its pixels' samples in a fixed order
+// and one lane per pixel adds the sums to the FP64 film.  No other thread of
+// the launch touches that pixel, so the order of additions is deterministic.
 __global__ void __launch_bounds__(kShadeThreads) k_film(WaveArgs A, double* sum, double* sumsq, uint32_t* count)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= A.wave_n) return;
-    uint32_t pixel, sample;
-    path_ids(A, k, pixel, sample);
-    const float4 r = A.R.rad[k];
-    atomicAdd(sum + 3 * (size_t)pixel, (double)r.x);
-    atomicAdd(sum + 3 * (size_t)pixel + 1, (double)r.y);
-    atomicAdd(sum + 3 * (size_t)pixel + 2, (double)r.z);
-    if (sumsq) {
-        atomicAdd(sumsq + 3 * (size_t)pixel, (double)r.x * r.x);
-        atomicAdd(sumsq + 3 * (size_t)pixel + 1, (double)r.y * r.y);
-        atomicAdd(sumsq + 3 * (size_t)pixel + 2, (double)r.z * r.z);
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t spp = A.spp;
+    const int64_t ppw = spp >= 32 ? 1 : 32 / spp;
+    const int64_t g_begin = A.wave_base, g_end = A.wave_base + A.wave_n;
+    const int64_t p0 = g_begin / spp + warp * ppw;
+    const int64_t p_end = (g_end - 1) / spp + 1;
+    if (p0 >= p_end) return;  // warp-uniform
+    const int64_t p1 = min(p0 + ppw, p_end);
+    const int64_t g0 = max(p0 * spp, g_begin), g1 = min(p1 * spp, g_end);
+    uint32_t key = 0xFFFFFFFFu, c = 0;
+    FF v[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) v[j] = FF{0.0f, 0.0f};
+    for (int64_t g = g0 + lane; g < g1; g += 32) {
+        const float4 r = A.R.rad[g - g_begin];
+        key = (uint32_t)(g / spp);
+        v[0] = ff_add(v[0], FF{r.x, 0.0f});
+        v[1] = ff_add(v[1], FF{r.y, 0.0f});
+        v[2] = ff_add(v[2], FF{r.z, 0.0f});
+        v[3] = ff_add(v[3], ff_sqr(r.x));
+        v[4] = ff_add(v[4], ff_sqr(r.y));
+        v[5] = ff_add(v[5], ff_sqr(r.z));
+        ++c;
     }
-    atomicAdd(count + pixel, 1u);
+    // lanes of one pixel are consecutive: segmented inclusive scan
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t pk = __shfl_up_sync(0xFFFFFFFFu, key, off);
+        const uint32_t oc = __shfl_up_sync(0xFFFFFFFFu, c, off);
+        FF ov[6];
+#pragma unroll
+        for (int j = 0; j < 6; ++j) {
+            ov[j].hi = __shfl_up_sync(0xFFFFFFFFu, v[j].hi, off);
+            ov[j].lo = __shfl_up_sync(0xFFFFFFFFu, v[j].lo, off);
+        }
+        if (lane >= off && pk == key) {
+#pragma unroll
+            for (int j = 0; j < 6; ++j) v[j] = ff_add(ov[j], v[j]);
+            c += oc;
+        }
+    }
+    const uint32_t next = __shfl_down_sync(0xFFFFFFFFu, key, 1);
+    if (c == 0 || (lane != 31 && next == key)) return;
+    double* ps = sum + 3 * (size_t)key;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) ps[j] += (double)v[j].hi + (double)v[j].lo;
+    if (sumsq) {
+        double* pq = sumsq + 3 * (size_t)key;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) pq[j] += (double)v[3 + j].hi + (double)v[3 + j].lo;
+    }
+    count[key] += c;
 }
 
 // ------------------------------------------------------------ ID pass ---
@@ -808,6 +889,7 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
     A.seed = p.seed;
     A.wave_cap = (int32_t)cap;
     A.npix = (int32_t)npix;
+    A.spp = p.samples_per_pixel;
     A.sample_offset = p.sample_offset;
     A.cam_bounces = p.camera_bounces;
     A.light_bounces = p.light_bounces;
@@ -879,7 +961,12 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
                 ++launches;
             }
         }
-        k_film<<<grid_for(A.wave_n, kShadeThreads), kShadeThreads, 0, st>>>(A, d_sum, d_sumsq, d_count);
+        {
+            const int64_t spp = p.samples_per_pixel, ppw = spp >= 32 ? 1 : 32 / spp;
+            const int64_t pixels = (A.wave_base + A.wave_n - 1) / spp - A.wave_base / spp + 1;
+            k_film<<<grid_for((pixels + ppw - 1) / ppw * 32, kShadeThreads), kShadeThreads, 0, st>>>(A, d_sum, d_sumsq,
+                                                                                                  d_count);
+        }
         ++launches;
         OMV_CUDA(cudaGetLastError());
     }
@@ -941,10 +1028,22 @@ static void ensure_scratch(SceneHost& s, int64_t wave_cap, int light_slots, int 
     carve_scratch(R, base, wave_cap, light_slots, shadow_slots);
 }
 
+// Default wave scratch: up to 32 GiB (and at most half of the free device
+// memory), enough for a full-HD frame at 64 spp in one wave.  Every wave pays
+// the latency of its last, nearly empty bounces once, so fewer waves are faster.
+constexpr size_t kWaveScratchBudget = (size_t)32 << 30;
+
 void render_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, double* d_sum, double* d_sumsq,
                   uint32_t* d_count, cudaStream_t st, omv_stats* stats)
 {
-    const FramePlan P = plan_frame(s, cam, p, (int64_t)1 << 22);
+    FramePlan P = plan_frame(s, cam, p, 1);
+    if (p.wave_paths <= 0) {
+        size_t free_b = 0, total_b = 0;
+        OMV_CUDA(cudaMemGetInfo(&free_b, &total_b));
+        const size_t budget = std::min(kWaveScratchBudget, (free_b + s.scratch.bytes) / 2);
+        const int64_t fit = (int64_t)(budget / path_scratch_bytes(P.light_slots, P.shadow_slots));
+        P.cap = std::max<int64_t>(1, std::min<int64_t>({fit, std::max<int64_t>(P.total, 1), (int64_t)0x7FFFFFFF}));
+    }
     ensure_scratch(s, P.cap, P.light_slots, P.shadow_slots);
     run_waves(s, s.scratch, P, cam, p, d_sum, d_sumsq, d_count, st, stats, true);
 }

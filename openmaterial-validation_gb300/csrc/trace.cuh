@@ -141,13 +141,6 @@ __device__ __forceinline__ bool tri_hit(const Shear& w, V3 o, float4 p0, float4 
 // 0 * inf NaN can appear (the triangle test uses the true direction)
 __device__ __forceinline__ float box_rcp(float d) { return 1.0f / (fabsf(d) < 1e-20f ? copysignf(1e-20f, d) : d); }
 
-__device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b)
-{
-    uint32_t lo = min(a, b), hi = max(a, b);
-    a = lo;
-    b = hi;
-}
-
 // world -> object space, 3x4 row-major inverse, fixed order
 __device__ __forceinline__ void to_object(const float* m, V3 o, V3 d, V3& ro, V3& rd)
 {
@@ -159,13 +152,29 @@ __device__ __forceinline__ void to_object(const float* m, V3 o, V3 d, V3& ro, V3
             __fadd_rn(__fadd_rn(__fmul_rn(m[8], d.x), __fmul_rn(m[9], d.y)), __fmul_rn(m[10], d.z)));
 }
 
+// 16-bit quantised plane of slot s (two slots per word) as a float: the bits
+// 0x4B00_0000 | q are the float 2^23 + q, so one byte permute and one exact
+// subtraction give float(q)
+__device__ __forceinline__ float qword(uint4 w, int s)
+{
+    const uint32_t x = (s >> 1) == 0 ? w.x : (s >> 1) == 1 ? w.y : (s >> 1) == 2 ? w.z : w.w;
+    return __uint_as_float(__byte_perm(x, 0x4B000000u, (s & 1) ? 0x7632u : 0x7610u)) - 8388608.0f;
+}
+
+__device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b)
+{
+    uint32_t lo = min(a, b), hi = max(a, b);
+    a = lo;
+    b = hi;
+}
+
 struct TraceCounters {
     uint32_t nodes;
     uint32_t tris;
 };
 
 // Closest hit; returns true and fills `hit` when a triangle is found.
-__device__ __noinline__ bool trace_closest(const DevScene& S, const uint32_t* __restrict__ tlas_items, V3 o, V3 d,
+__device__ __forceinline__ bool trace_closest(const DevScene& S, const uint32_t* __restrict__ tlas_items, V3 o, V3 d,
                                            float tnear, float tfar, RayHit& hit, TraceStack& st, TraceCounters& tc)
 {
     Shear sw;
@@ -228,6 +237,11 @@ __device__ __noinline__ bool trace_closest(const DevScene& S, const uint32_t* __
         const float sz = __uint_as_float(((exps >> 16) & 0xFFu) << 23);
         const float ax = sx * rid.x, ay = sy * rid.y, az = sz * rid.z;
         const float bx = (px - ro.x) * rid.x, by = (py - ro.y) * rid.y, bz = (pz - ro.z) * rid.z;
+        // entry and exit planes per axis from the ray direction: for a child with
+        // qlo <= qhi these are exactly min() and max() of the two slab distances
+        const uint4 nx = rid.x >= 0.0f ? qlx : qhx, fx = rid.x >= 0.0f ? qhx : qlx;
+        const uint4 ny = rid.y >= 0.0f ? qly : qhy, fy = rid.y >= 0.0f ? qhy : qly;
+        const uint4 nz = rid.z >= 0.0f ? qlz : qhz, fz = rid.z >= 0.0f ? qhz : qlz;
         const float lim = best_t;
         uint32_t key[8];
         uint32_t leafmask = 0;
@@ -236,29 +250,16 @@ __device__ __noinline__ bool trace_closest(const DevScene& S, const uint32_t* __
             const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> (8 * (s & 3))) & 0xFFu;
             const bool internal = (imask >> s) & 1u;
             const bool valid = internal || meta != 0u;
-            const int sh = 16 * (s & 1);
-            const uint32_t wlx = s < 2 ? qlx.x : s < 4 ? qlx.y : s < 6 ? qlx.z : qlx.w;
-            const uint32_t wly = s < 2 ? qly.x : s < 4 ? qly.y : s < 6 ? qly.z : qly.w;
-            const uint32_t wlz = s < 2 ? qlz.x : s < 4 ? qlz.y : s < 6 ? qlz.z : qlz.w;
-            const uint32_t whx = s < 2 ? qhx.x : s < 4 ? qhx.y : s < 6 ? qhx.z : qhx.w;
-            const uint32_t why = s < 2 ? qhy.x : s < 4 ? qhy.y : s < 6 ? qhy.z : qhy.w;
-            const uint32_t whz = s < 2 ? qhz.x : s < 4 ? qhz.y : s < 6 ? qhz.z : qhz.w;
-            const float tlx = fmaf((float)((wlx >> sh) & 0xFFFFu), ax, bx);
-            const float thx = fmaf((float)((whx >> sh) & 0xFFFFu), ax, bx);
-            const float tly = fmaf((float)((wly >> sh) & 0xFFFFu), ay, by);
-            const float thy = fmaf((float)((why >> sh) & 0xFFFFu), ay, by);
-            const float tlz = fmaf((float)((wlz >> sh) & 0xFFFFu), az, bz);
-            const float thz = fmaf((float)((whz >> sh) & 0xFFFFu), az, bz);
-            float tin = fmaxf(fmaxf(fminf(tlx, thx), fminf(tly, thy)), fminf(tlz, thz));
-            float tout = fminf(fminf(fmaxf(tlx, thx), fmaxf(tly, thy)), fmaxf(tlz, thz));
-            tin = fmaxf(tin * 0.99999952f, tnear);
-            tout = fminf(tout * 1.00000048f, lim);
-            const bool hit = valid && tin <= tout;
+            const float tnx = fmaf(qword(nx, s), ax, bx), tfx = fmaf(qword(fx, s), ax, bx);
+            const float tny = fmaf(qword(ny, s), ay, by), tfy = fmaf(qword(fy, s), ay, by);
+            const float tnz = fmaf(qword(nz, s), az, bz), tfz = fmaf(qword(fz, s), az, bz);
+            const float tin = fmaxf(fmaxf(fmaxf(tnx, tny), tnz) * 0.99999952f, tnear);
+            const float tout = fminf(fminf(fminf(tfx, tfy), tfz) * 1.00000048f, lim);
             key[s] = 0xFFFFFFFFu;
-            if (hit) {
+            if (valid && tin <= tout) {
                 if (!internal && in_blas)
                     leafmask |= 1u << s;
-                else
+                else  // entry distance rounded down to 8 ulp | slot
                     key[s] = (__float_as_uint(fmaxf(tin, 0.0f)) & ~7u) | (uint32_t)s;
             }
         }
