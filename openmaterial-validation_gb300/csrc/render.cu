@@ -623,65 +623,58 @@ __device__ __forceinline__ FF ff_sqr(float x)
     return FF{p, fmaf(x, x, -p)};
 }
 
-// PinholeCamera::hit for every path of the wave, without atomics: the wave's
-// pixels are split between warps (one pixel per warp when spp >= 32, else
-// 32 / spp whole pixels), each warp sums its pixels' samples in a fixed order
-// and one lane per pixel adds the sums to the FP64 film.  No other thread of
-// the launch touches that pixel, so the order of additions is deterministic.
-__global__ void __launch_bounds__(kShadeThreads) k_film(WaveArgs A, double* sum, double* sumsq, uint32_t* count)
+// PinholeCamera::hit for every path of the wave, without atomics: each pixel
+// of the wave gets an aligned group of `group` lanes (a power of two), lane j
+// sums samples j, j + group, ... of the pixel's paths in this wave, the group
+// reduces by xor butterfly and its first lane adds the totals to the FP64 film.
+// No other thread of the launch touches that pixel and the order of every
+// addition is fixed, so the film is deterministic for a given wave split.
+__global__ void __launch_bounds__(kShadeThreads) k_film(WaveArgs A, int group, double* sum, double* sumsq,
+                                                        uint32_t* count)
 {
-    const int lane = threadIdx.x & 31;
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = threadIdx.x & (group - 1);
     const int64_t spp = A.spp;
-    const int64_t ppw = spp >= 32 ? 1 : 32 / spp;
     const int64_t g_begin = A.wave_base, g_end = A.wave_base + A.wave_n;
-    const int64_t p0 = g_begin / spp + warp * ppw;
-    const int64_t p_end = (g_end - 1) / spp + 1;
-    if (p0 >= p_end) return;  // warp-uniform
-    const int64_t p1 = min(p0 + ppw, p_end);
-    const int64_t g0 = max(p0 * spp, g_begin), g1 = min(p1 * spp, g_end);
-    uint32_t key = 0xFFFFFFFFu, c = 0;
+    const int64_t p = g_begin / spp + t / group;
+    const bool live = p <= (g_end - 1) / spp;
+    uint32_t c = 0;
     FF v[6];
 #pragma unroll
-    for (int j = 0; j < 6; ++j) v[j] = FF{0.0f, 0.0f};
-    for (int64_t g = g0 + lane; g < g1; g += 32) {
-        const float4 r = A.R.rad[g - g_begin];
-        key = (uint32_t)(g / spp);
-        v[0] = ff_add(v[0], FF{r.x, 0.0f});
-        v[1] = ff_add(v[1], FF{r.y, 0.0f});
-        v[2] = ff_add(v[2], FF{r.z, 0.0f});
-        v[3] = ff_add(v[3], ff_sqr(r.x));
-        v[4] = ff_add(v[4], ff_sqr(r.y));
-        v[5] = ff_add(v[5], ff_sqr(r.z));
-        ++c;
-    }
-    // lanes of one pixel are consecutive: segmented inclusive scan
-    for (int off = 1; off < 32; off <<= 1) {
-        const uint32_t pk = __shfl_up_sync(0xFFFFFFFFu, key, off);
-        const uint32_t oc = __shfl_up_sync(0xFFFFFFFFu, c, off);
-        FF ov[6];
-#pragma unroll
-        for (int j = 0; j < 6; ++j) {
-            ov[j].hi = __shfl_up_sync(0xFFFFFFFFu, v[j].hi, off);
-            ov[j].lo = __shfl_up_sync(0xFFFFFFFFu, v[j].lo, off);
-        }
-        if (lane >= off && pk == key) {
-#pragma unroll
-            for (int j = 0; j < 6; ++j) v[j] = ff_add(ov[j], v[j]);
-            c += oc;
+    for (int q = 0; q < 6; ++q) v[q] = FF{0.0f, 0.0f};
+    if (live) {
+        const int64_t g0 = max(p * spp, g_begin), g1 = min((p + 1) * spp, g_end);
+        for (int64_t g = g0 + j; g < g1; g += group) {
+            const float4 r = A.R.rad[g - g_begin];
+            v[0] = ff_add(v[0], FF{r.x, 0.0f});
+            v[1] = ff_add(v[1], FF{r.y, 0.0f});
+            v[2] = ff_add(v[2], FF{r.z, 0.0f});
+            v[3] = ff_add(v[3], ff_sqr(r.x));
+            v[4] = ff_add(v[4], ff_sqr(r.y));
+            v[5] = ff_add(v[5], ff_sqr(r.z));
+            ++c;
         }
     }
-    const uint32_t next = __shfl_down_sync(0xFFFFFFFFu, key, 1);
-    if (c == 0 || (lane != 31 && next == key)) return;
-    double* ps = sum + 3 * (size_t)key;
+    for (int off = group >> 1; off > 0; off >>= 1) {
+        c += __shfl_xor_sync(0xFFFFFFFFu, c, off);
 #pragma unroll
-    for (int j = 0; j < 3; ++j) ps[j] += (double)v[j].hi + (double)v[j].lo;
+        for (int q = 0; q < 6; ++q) {
+            FF o;
+            o.hi = __shfl_xor_sync(0xFFFFFFFFu, v[q].hi, off);
+            o.lo = __shfl_xor_sync(0xFFFFFFFFu, v[q].lo, off);
+            v[q] = (j & off) ? ff_add(o, v[q]) : ff_add(v[q], o);  // same operand order on both lanes
+        }
+    }
+    if (!live || j != 0 || c == 0) return;
+    double* ps = sum + 3 * (size_t)p;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) ps[q] += (double)v[q].hi + (double)v[q].lo;
     if (sumsq) {
-        double* pq = sumsq + 3 * (size_t)key;
+        double* pq = sumsq + 3 * (size_t)p;
 #pragma unroll
-        for (int j = 0; j < 3; ++j) pq[j] += (double)v[3 + j].hi + (double)v[3 + j].lo;
+        for (int q = 0; q < 3; ++q) pq[q] += (double)v[3 + q].hi + (double)v[3 + q].lo;
     }
-    count[key] += c;
+    count[p] += c;
 }
 
 // ------------------------------------------------------------ ID pass ---
@@ -962,12 +955,15 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
             }
         }
         {
-            const int64_t spp = p.samples_per_pixel, ppw = spp >= 32 ? 1 : 32 / spp;
+            // about 8 samples per lane: group = power of two <= spp / 8, in [1, 32]
+            const int64_t spp = p.samples_per_pixel;
+            int group = 1;
+            while (group < 32 && group * 16 <= spp) group *= 2;
             const int64_t pixels = (A.wave_base + A.wave_n - 1) / spp - A.wave_base / spp + 1;
-            k_film<<<grid_for((pixels + ppw - 1) / ppw * 32, kShadeThreads), kShadeThreads, 0, st>>>(A, d_sum, d_sumsq,
-                                                                                                  d_count);
+            k_film<<<grid_for(pixels * group, kShadeThreads), kShadeThreads, 0, st>>>(A, group, d_sum, d_sumsq,
+                                                                                     d_count);
+            ++launches;
         }
-        ++launches;
         OMV_CUDA(cudaGetLastError());
     }
     if (!events) {
