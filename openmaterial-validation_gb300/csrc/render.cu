@@ -58,6 +58,61 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want)
     return base + __popc(m & ((1u << lane) - 1u));
 }
 
+// Direction bin of a ray: the cube face its direction points to (dominant
+// axis and sign) and the quadrant on that face, 24 bins.
+constexpr int kDirBins = 24;
+__device__ __forceinline__ uint32_t direction_bin(V3 d)
+{
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    uint32_t f;
+    float u, v;
+    if (ax >= ay && ax >= az) {
+        f = d.x < 0.0f ? 1u : 0u;
+        u = d.y;
+        v = d.z;
+    } else if (ay >= az) {
+        f = d.y < 0.0f ? 3u : 2u;
+        u = d.z;
+        v = d.x;
+    } else {
+        f = d.z < 0.0f ? 5u : 4u;
+        u = d.x;
+        v = d.y;
+    }
+    return 4u * f + (u < 0.0f ? 2u : 0u) + (v < 0.0f ? 1u : 0u);
+}
+
+struct BinScratch {
+    uint32_t count[kDirBins];
+    uint32_t base;
+};
+
+// Block-wide append to a queue with the block's entries grouped by bin, so
+// that the warps tracing the queue get rays of similar direction from nearby
+// pixels.  One atomic per block; every thread of the block must call it.
+__device__ __forceinline__ uint32_t block_append_binned(uint32_t* counter, bool want, uint32_t bin, BinScratch& sh)
+{
+    if (threadIdx.x < kDirBins) sh.count[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t rank = want ? atomicAdd(&sh.count[bin], 1u) : 0u;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        // exclusive scan of the bin counts in the first warp; lane 31 reserves
+        const uint32_t c = threadIdx.x < kDirBins ? sh.count[threadIdx.x] : 0u;
+        uint32_t x = c;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+            if ((int)threadIdx.x >= o) x += y;
+        }
+        if (threadIdx.x < kDirBins) sh.count[threadIdx.x] = x - c;
+        if (threadIdx.x == 31) sh.base = x ? atomicAdd(counter, x) : 0u;
+    }
+    __syncthreads();
+    const uint32_t slot = sh.base + sh.count[bin] + rank;
+    __syncthreads();  // the scratch is reused by the next call
+    return slot;
+}
+
 struct Surf {
     V3 pos, nrm, tan, bin;
     float tw;
@@ -443,9 +498,10 @@ __global__ void __launch_bounds__(kShadeThreads) k_light_shade(WaveArgs A, int b
 // ------------------------------------------------------ camera shade ---
 // BDPTRenderer::computePath for the camera subpath (inv = true), vertex b, plus
 // the escape term and the connections of computePaths (:251-298) at vertex b
-__global__ void __launch_bounds__(kShadeThreads) k_camera_shade(WaveArgs A, int b, const float4* rq_in,
+__global__ void __launch_bounds__(kShadeThreads, 3) k_camera_shade(WaveArgs A, int b, const float4* rq_in,
                                                                  float4* rq_out)
 {
+    __shared__ BinScratch bins;
     const uint32_t n = A.R.ctr[kCtrCam + b];
     const DevScene& S = A.S;
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
@@ -527,7 +583,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_camera_shade(WaveArgs A, int 
                 }
             }
         }
-        const uint32_t slot = warp_append(&A.R.ctr[kCtrCam + b + 1], push);
+        const uint32_t slot = block_append_binned(&A.R.ctr[kCtrCam + b + 1], push, direction_bin(O), bins);
         if (push) {
             rq_out[2 * (size_t)slot] = make_float4(so.x, so.y, so.z, tnear);
             rq_out[2 * (size_t)slot + 1] = make_float4(O.x, O.y, O.z, __int_as_float(k));
