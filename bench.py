@@ -48,7 +48,7 @@ def _peaks():
 
 def _traffic_per_launch():
     """dram bytes per k_extend launch from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "k_extend_c2_launches.md")
+    p = os.path.join(ROOT, "profiles", "k_extend_c2_480x270x16.md")
     try:
         for line in open(p):
             if line.strip().startswith("dram_bytes_per_launch:"):
