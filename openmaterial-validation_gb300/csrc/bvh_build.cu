@@ -94,20 +94,35 @@ __global__ void k_tri_boxes(int n, const float* __restrict__ pos, const uint32_t
     }
 }
 
-__global__ void k_box_centroid_bounds(int n, const Box* boxes, uint32_t* cbounds)
+// World bounds of one instance: every vertex its faces reference, through the
+// instance transform (double arithmetic, rounded to float), reduced into six
+// ordered ints (lo xyz, hi xyz).  Tighter than the box of the transformed
+// object box, which a rotation inflates.
+struct Xf34 {
+    float m[12];
+};
+__global__ void k_instance_bounds(int nfaces, const float* __restrict__ pos, const uint32_t* __restrict__ faces,
+                                  Xf34 xf, uint32_t* out6)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    bool ok = i < n;
+    float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * nfaces; i += gridDim.x * blockDim.x) {
+        const float* p = pos + 3 * (size_t)faces[i];
+        for (int a = 0; a < 3; ++a) {
+            const double w = (double)xf.m[4 * a] * p[0] + (double)xf.m[4 * a + 1] * p[1] +
+                             (double)xf.m[4 * a + 2] * p[2] + (double)xf.m[4 * a + 3];
+            lo[a] = fminf(lo[a], (float)w);
+            hi[a] = fmaxf(hi[a], (float)w);
+        }
+    }
     for (int a = 0; a < 3; ++a) {
-        float c = ok ? 0.5f * (boxes[i].lo[a] + boxes[i].hi[a]) : 0.f;
-        uint32_t lo = ok ? f2ord(c) : 0xFFFFFFFFu, hi = ok ? f2ord(c) : 0u;
+        uint32_t l = f2ord(lo[a]), h = f2ord(hi[a]);
         for (int o = 16; o; o >>= 1) {
-            lo = min(lo, __shfl_xor_sync(0xFFFFFFFFu, lo, o));
-            hi = max(hi, __shfl_xor_sync(0xFFFFFFFFu, hi, o));
+            l = min(l, __shfl_xor_sync(0xFFFFFFFFu, l, o));
+            h = max(h, __shfl_xor_sync(0xFFFFFFFFu, h, o));
         }
         if ((threadIdx.x & 31) == 0) {
-            atomicMin(&cbounds[a], lo);
-            atomicMax(&cbounds[3 + a], hi);
+            atomicMin(&out6[a], l);
+            atomicMax(&out6[3 + a], h);
         }
     }
 }
@@ -560,6 +575,90 @@ void radix_sort(int n, uint32_t* keys, uint32_t* vals, uint32_t* k2, uint32_t* v
 
 // Builds one tree over n items whose boxes are in `item_boxes` (device).
 // Appends nodes at node_base... of `out_nodes`, primitives at prim_base... .
+static uint32_t collapse_tree(bool tlas, int n, const Node2* nodes, const uint32_t* vals, const Box* item_boxes,
+                              const float* pos, const uint32_t* faces, Bvh8Node* out_nodes, uint32_t* node_counter,
+                              uint32_t node_cap, float4* out_tris, uint32_t* out_items, uint32_t* prim_counter,
+                              uint32_t* overflow, cudaStream_t st);
+
+// Binary tree by a full-sweep SAH split (every split position on every axis,
+// items ordered by box centroid), leaves of one item: for the few instances of
+// a top-level tree.  nodes[0] is the root; `order` receives the item order the
+// node ranges refer to.
+static void host_sah_tree(const std::vector<Box>& boxes, std::vector<Node2>& nodes, std::vector<uint32_t>& order)
+{
+    const int n = (int)boxes.size();
+    order.resize(n);
+    for (int i = 0; i < n; ++i) order[i] = (uint32_t)i;
+    nodes.clear();
+    if (n < 2) return;
+    nodes.reserve(n - 1);
+    auto area = [](const Box& b) {
+        const float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+        return dx * dy + dy * dz + dz * dx;
+    };
+    auto unite = [](const Box& a, const Box& b) {
+        Box u;
+        for (int k = 0; k < 3; ++k) {
+            u.lo[k] = std::min(a.lo[k], b.lo[k]);
+            u.hi[k] = std::max(a.hi[k], b.hi[k]);
+        }
+        return u;
+    };
+    struct Task {
+        int first, last, node, parent, side;
+    };
+    std::vector<Task> todo{{0, n - 1, -1, -1, 0}};
+    std::vector<float> right_area(n);
+    while (!todo.empty()) {
+        Task t = todo.back();
+        todo.pop_back();
+        const int cnt = t.last - t.first + 1;
+        int ref;
+        if (cnt == 1) {
+            ref = ~t.first;
+        } else {
+            ref = (int)nodes.size();
+            nodes.push_back(Node2{});
+            float best = 3.0e38f;
+            int best_axis = 0, best_split = t.first;
+            for (int a = 0; a < 3; ++a) {
+                std::stable_sort(order.begin() + t.first, order.begin() + t.last + 1, [&](uint32_t x, uint32_t y) {
+                    return boxes[x].lo[a] + boxes[x].hi[a] < boxes[y].lo[a] + boxes[y].hi[a];
+                });
+                Box acc = boxes[order[t.last]];
+                for (int k = t.last; k > t.first; --k) {
+                    acc = unite(acc, boxes[order[k]]);
+                    right_area[k] = area(acc);
+                }
+                acc = boxes[order[t.first]];
+                for (int k = t.first; k < t.last; ++k) {
+                    acc = unite(acc, boxes[order[k]]);
+                    const float c = area(acc) * (float)(k - t.first + 1) + right_area[k + 1] * (float)(t.last - k);
+                    if (c < best) {
+                        best = c;
+                        best_axis = a;
+                        best_split = k;
+                    }
+                }
+            }
+            std::stable_sort(order.begin() + t.first, order.begin() + t.last + 1, [&](uint32_t x, uint32_t y) {
+                return boxes[x].lo[best_axis] + boxes[x].hi[best_axis] < boxes[y].lo[best_axis] + boxes[y].hi[best_axis];
+            });
+            Box b = boxes[order[t.first]];
+            for (int k = t.first + 1; k <= t.last; ++k) b = unite(b, boxes[order[k]]);
+            Node2& nd = nodes[ref];
+            nd.first = t.first;
+            nd.last = t.last;
+            nd.parent = t.node;
+            nd.box = b;
+            nd.left = nd.right = 0;
+            todo.push_back({best_split + 1, t.last, ref, ref, 1});
+            todo.push_back({t.first, best_split, ref, ref, 0});
+        }
+        if (t.node >= 0) (t.side ? nodes[t.node].right : nodes[t.node].left) = ref;
+    }
+}
+
 static uint32_t build_tree(bool tlas, int n, Box* item_boxes, uint32_t* cbounds, const float* pos,
                            const uint32_t* faces, Bvh8Node* out_nodes, uint32_t* node_counter, uint32_t node_cap,
                            float4* out_tris, uint32_t* out_items, uint32_t* prim_counter, uint32_t* overflow,
@@ -572,14 +671,23 @@ static uint32_t build_tree(bool tlas, int n, Box* item_boxes, uint32_t* cbounds,
     DBuf<Node2> nodes(ni);
     DBuf<int> leaf_parent(n), arrivals(ni);
     OMV_CK(cudaMemsetAsync(arrivals.p, 0, sizeof(int) * ni, st));
-    Work root{};
     if (n > 1) {
         k_karras<<<blocks(n - 1, 256), 256, 0, st>>>(n, keys.p, nodes.p, leaf_parent.p);
         k_bottom_up<<<blocks(n, 256), 256, 0, st>>>(n, vals.p, item_boxes, nodes.p, leaf_parent.p, arrivals.p);
-        root.node2 = 0;
-    } else {
-        root.node2 = ~0;
     }
+    return collapse_tree(tlas, n, nodes.p, vals.p, item_boxes, pos, faces, out_nodes, node_counter, node_cap, out_tris,
+                         out_items, prim_counter, overflow, st);
+}
+
+// Top-down collapse of a binary tree (nodes[0] the root when n > 1) into 8-wide
+// nodes appended to out_nodes; returns the root's index.
+static uint32_t collapse_tree(bool tlas, int n, const Node2* nodes, const uint32_t* vals, const Box* item_boxes,
+                              const float* pos, const uint32_t* faces, Bvh8Node* out_nodes, uint32_t* node_counter,
+                              uint32_t node_cap, float4* out_tris, uint32_t* out_items, uint32_t* prim_counter,
+                              uint32_t* overflow, cudaStream_t st)
+{
+    Work root{};
+    root.node2 = n > 1 ? 0 : ~0;
     uint32_t root_index = 0;
     OMV_CK(cudaMemcpyAsync(&root_index, node_counter, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     OMV_CK(cudaStreamSynchronize(st));
@@ -595,11 +703,11 @@ static uint32_t build_tree(bool tlas, int n, Box* item_boxes, uint32_t* cbounds,
         if (level > 200) throw std::runtime_error("BVH collapse did not terminate");
         OMV_CK(cudaMemsetAsync(cnt.p, 0, sizeof(uint32_t), st));
         if (tlas)
-            k_collapse<true><<<blocks(nwork, 128), 128, 0, st>>>(nwork, cur, nodes.p, vals.p, item_boxes, out_nodes,
+            k_collapse<true><<<blocks(nwork, 128), 128, 0, st>>>(nwork, cur, nodes, vals, item_boxes, out_nodes,
                                                                  node_counter, nxt, cnt.p, out_tris, out_items,
                                                                  prim_counter, pos, faces, node_cap, overflow);
         else
-            k_collapse<false><<<blocks(nwork, 128), 128, 0, st>>>(nwork, cur, nodes.p, vals.p, item_boxes, out_nodes,
+            k_collapse<false><<<blocks(nwork, 128), 128, 0, st>>>(nwork, cur, nodes, vals, item_boxes, out_nodes,
                                                                   node_counter, nxt, cnt.p, out_tris, out_items,
                                                                   prim_counter, pos, faces, node_cap, overflow);
         OMV_CK(cudaGetLastError());
@@ -638,49 +746,68 @@ void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<Instance
         out.blas_root[mi] = build_tree(false, m.num_faces, boxes.p, cb.p, m.d_pos, m.d_faces, out.nodes, counters.p,
                                        node_cap, out.tris, nullptr, counters.p + 1, counters.p + 2, st);
     }
-    // top level: world boxes of the valid instances, widened so that no
-    // object-space hit is ever culled by world-space rounding
-    std::vector<Box> ib;
+    // top level: world boxes of the valid instances (their referenced vertices
+    // through the instance transform), widened so that no object-space hit is
+    // ever culled by world-space rounding
     std::vector<uint32_t> ids;
-    for (size_t i = 0; i < insts.size(); ++i) {
-        const InstanceGeom& g = insts[i];
-        if (!g.valid) continue;
-        const float* lo = meshes[g.mesh].lo;
-        const float* hi = meshes[g.mesh].hi;
-        Box b;
-        for (int a = 0; a < 3; ++a) {
-            b.lo[a] = 3e38f;
-            b.hi[a] = -3e38f;
-        }
-        for (int c = 0; c < 8; ++c) {
-            double p[3] = {(c & 1) ? hi[0] : lo[0], (c & 2) ? hi[1] : lo[1], (c & 4) ? hi[2] : lo[2]};
+    for (size_t i = 0; i < insts.size(); ++i)
+        if (insts[i].valid) ids.push_back((uint32_t)i);
+    std::vector<Box> ib(ids.size());
+    if (!ids.empty()) {
+        DBuf<uint32_t> ob(6 * ids.size());
+        std::vector<uint32_t> init(6 * ids.size());
+        for (size_t j = 0; j < ids.size(); ++j)
             for (int a = 0; a < 3; ++a) {
-                double w = (double)g.xf[a][0] * p[0] + (double)g.xf[a][1] * p[1] + (double)g.xf[a][2] * p[2] +
-                           (double)g.xf[a][3];
-                b.lo[a] = std::min(b.lo[a], (float)w);
-                b.hi[a] = std::max(b.hi[a], (float)w);
+                init[6 * j + a] = 0xFFFFFFFFu;
+                init[6 * j + 3 + a] = 0u;
+            }
+        OMV_CK(cudaMemcpyAsync(ob.p, init.data(), sizeof(uint32_t) * init.size(), cudaMemcpyHostToDevice, st));
+        for (size_t j = 0; j < ids.size(); ++j) {
+            const InstanceGeom& g = insts[ids[j]];
+            const MeshGeom& m = meshes[g.mesh];
+            Xf34 xf;
+            for (int a = 0; a < 3; ++a)
+                for (int c = 0; c < 4; ++c) xf.m[4 * a + c] = g.xf[a][c];
+            const int nb = std::max(1, std::min(64, blocks((size_t)3 * m.num_faces, 256)));
+            k_instance_bounds<<<nb, 256, 0, st>>>(m.num_faces, m.d_pos, m.d_faces, xf, ob.p + 6 * j);
+        }
+        OMV_CK(cudaGetLastError());
+        OMV_CK(cudaMemcpyAsync(init.data(), ob.p, sizeof(uint32_t) * init.size(), cudaMemcpyDeviceToHost, st));
+        OMV_CK(cudaStreamSynchronize(st));
+        auto dec = [](uint32_t u) {
+            const uint32_t b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+            float f;
+            std::memcpy(&f, &b, 4);
+            return f;
+        };
+        for (size_t j = 0; j < ids.size(); ++j) {
+            Box& b = ib[j];
+            for (int a = 0; a < 3; ++a) {
+                b.lo[a] = dec(init[6 * j + a]);
+                b.hi[a] = dec(init[6 * j + 3 + a]);
+                const float pad = (b.hi[a] - b.lo[a]) * 1e-5f + (std::fabs(b.lo[a]) + std::fabs(b.hi[a])) * 1e-5f + 1e-20f;
+                b.lo[a] -= pad;
+                b.hi[a] += pad;
             }
         }
-        for (int a = 0; a < 3; ++a) {
-            float pad = (b.hi[a] - b.lo[a]) * 1e-5f + (std::fabs(b.lo[a]) + std::fabs(b.hi[a])) * 1e-5f + 1e-20f;
-            b.lo[a] -= pad;
-            b.hi[a] += pad;
-        }
-        ib.push_back(b);
-        ids.push_back((uint32_t)i);
     }
     out.num_valid_instances = (uint32_t)ib.size();
     if (!ib.empty()) {
-        int n = (int)ib.size();
+        const int n = (int)ib.size();
+        std::vector<Node2> h_nodes;
+        std::vector<uint32_t> h_order;
+        host_sah_tree(ib, h_nodes, h_order);
         DBuf<Box> boxes(n);
-        DBuf<uint32_t> idmap(n);
+        DBuf<uint32_t> vals(n);
+        DBuf<Node2> d_nodes(std::max<size_t>(1, h_nodes.size()));
         OMV_CK(cudaMemcpyAsync(boxes.p, ib.data(), sizeof(Box) * n, cudaMemcpyHostToDevice, st));
-        uint32_t init[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
-        OMV_CK(cudaMemcpyAsync(cb.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
-        k_box_centroid_bounds<<<blocks(n, 256), 256, 0, st>>>(n, boxes.p, cb.p);
+        OMV_CK(cudaMemcpyAsync(vals.p, h_order.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, st));
+        if (!h_nodes.empty())
+            OMV_CK(cudaMemcpyAsync(d_nodes.p, h_nodes.data(), sizeof(Node2) * h_nodes.size(), cudaMemcpyHostToDevice,
+                                   st));
         OMV_CK(cudaMemsetAsync(counters.p + 1, 0, sizeof(uint32_t), st));
-        out.tlas_root = build_tree(true, n, boxes.p, cb.p, nullptr, nullptr, out.nodes, counters.p, node_cap, nullptr,
-                                   out.tlas_items, counters.p + 1, counters.p + 2, st);
+        out.tlas_root = collapse_tree(true, n, d_nodes.p, vals.p, boxes.p, nullptr, nullptr, out.nodes, counters.p,
+                                      node_cap, nullptr, out.tlas_items, counters.p + 1, counters.p + 2, st);
         // TLAS items are positions in `ids`; translate to instance indices
         std::vector<uint32_t> items(n);
         OMV_CK(cudaMemcpyAsync(items.data(), out.tlas_items, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, st));
