@@ -25,6 +25,8 @@
 #include <stdexcept>
 #include <string>
 #include <vector>
+#include <atomic>
+#include <thread>
 
 #include "bvh_build.h"
 #include "omv_types.h"
@@ -580,10 +582,16 @@ static uint32_t collapse_tree(bool tlas, int n, const Node2* nodes, const uint32
                               uint32_t node_cap, float4* out_tris, uint32_t* out_items, uint32_t* prim_counter,
                               uint32_t* overflow, cudaStream_t st);
 
-// Binary tree by a full-sweep SAH split (every split position on every axis,
-// items ordered by box centroid), leaves of one item: for the few instances of
-// a top-level tree.  nodes[0] is the root; `order` receives the item order the
-// node ranges refer to.
+// Binary tree by the surface area heuristic, leaves of one item: binned
+// (kSahBins bins per axis over the centroid bounds) on ranges of more than
+// kSweepMax items, a full sweep over every split position below.  nodes[0] is
+// the root; `order` receives the item order the node ranges refer to.  Runs on
+// the host: for the top-level tree and for bottom-level trees of up to
+// kHostSahMaxTris triangles (one thread per mesh).
+constexpr int kSahBins = 32;
+constexpr int kSweepMax = 32;
+constexpr int kHostSahMaxTris = 1 << 21;
+
 static void host_sah_tree(const std::vector<Box>& boxes, std::vector<Node2>& nodes, std::vector<uint32_t>& order)
 {
     const int n = (int)boxes.size();
@@ -604,13 +612,21 @@ static void host_sah_tree(const std::vector<Box>& boxes, std::vector<Node2>& nod
         }
         return u;
     };
+    Box empty;
+    for (int k = 0; k < 3; ++k) {
+        empty.lo[k] = 3.0e38f;
+        empty.hi[k] = -3.0e38f;
+    }
+    std::vector<float> c2(3 * (size_t)n);  // twice the centroid
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k) c2[3 * (size_t)i + k] = boxes[i].lo[k] + boxes[i].hi[k];
     struct Task {
-        int first, last, node, parent, side;
+        int first, last, parent, side;
     };
-    std::vector<Task> todo{{0, n - 1, -1, -1, 0}};
+    std::vector<Task> todo{{0, n - 1, -1, 0}};
     std::vector<float> right_area(n);
     while (!todo.empty()) {
-        Task t = todo.back();
+        const Task t = todo.back();
         todo.pop_back();
         const int cnt = t.last - t.first + 1;
         int ref;
@@ -619,43 +635,108 @@ static void host_sah_tree(const std::vector<Box>& boxes, std::vector<Node2>& nod
         } else {
             ref = (int)nodes.size();
             nodes.push_back(Node2{});
-            float best = 3.0e38f;
-            int best_axis = 0, best_split = t.first;
-            for (int a = 0; a < 3; ++a) {
-                std::stable_sort(order.begin() + t.first, order.begin() + t.last + 1, [&](uint32_t x, uint32_t y) {
-                    return boxes[x].lo[a] + boxes[x].hi[a] < boxes[y].lo[a] + boxes[y].hi[a];
-                });
-                Box acc = boxes[order[t.last]];
-                for (int k = t.last; k > t.first; --k) {
-                    acc = unite(acc, boxes[order[k]]);
-                    right_area[k] = area(acc);
-                }
-                acc = boxes[order[t.first]];
-                for (int k = t.first; k < t.last; ++k) {
-                    acc = unite(acc, boxes[order[k]]);
-                    const float c = area(acc) * (float)(k - t.first + 1) + right_area[k + 1] * (float)(t.last - k);
-                    if (c < best) {
-                        best = c;
-                        best_axis = a;
-                        best_split = k;
+            Box b = empty;
+            for (int k = t.first; k <= t.last; ++k) b = unite(b, boxes[order[k]]);
+            int split = t.first + cnt / 2 - 1;  // fallback: halves in the current order
+            if (cnt <= kSweepMax) {
+                float best = 3.0e38f;
+                int best_axis = -1;
+                for (int a = 0; a < 3; ++a) {
+                    std::stable_sort(order.begin() + t.first, order.begin() + t.last + 1,
+                                     [&](uint32_t x, uint32_t y) { return c2[3 * (size_t)x + a] < c2[3 * (size_t)y + a]; });
+                    Box acc = boxes[order[t.last]];
+                    for (int k = t.last; k > t.first; --k) {
+                        acc = unite(acc, boxes[order[k]]);
+                        right_area[k] = area(acc);
+                    }
+                    acc = boxes[order[t.first]];
+                    for (int k = t.first; k < t.last; ++k) {
+                        acc = unite(acc, boxes[order[k]]);
+                        const float c = area(acc) * (float)(k - t.first + 1) + right_area[k + 1] * (float)(t.last - k);
+                        if (c < best) {
+                            best = c;
+                            best_axis = a;
+                            split = k;
+                        }
                     }
                 }
+                if (best_axis >= 0)
+                    std::stable_sort(order.begin() + t.first, order.begin() + t.last + 1, [&](uint32_t x, uint32_t y) {
+                        return c2[3 * (size_t)x + best_axis] < c2[3 * (size_t)y + best_axis];
+                    });
+            } else {
+                float cmin[3], cmax[3];
+                for (int k = 0; k < 3; ++k) {
+                    cmin[k] = 3.0e38f;
+                    cmax[k] = -3.0e38f;
+                }
+                for (int k = t.first; k <= t.last; ++k)
+                    for (int a = 0; a < 3; ++a) {
+                        cmin[a] = std::min(cmin[a], c2[3 * (size_t)order[k] + a]);
+                        cmax[a] = std::max(cmax[a], c2[3 * (size_t)order[k] + a]);
+                    }
+                float best = 3.0e38f;
+                int best_axis = -1, best_bin = 0;
+                for (int a = 0; a < 3; ++a) {
+                    const float ext = cmax[a] - cmin[a];
+                    if (!(ext > 0.0f)) continue;
+                    const float scale = (float)kSahBins / ext;
+                    auto bin = [&](uint32_t it) {  // clamped before the conversion (scale may overflow)
+                        return (int)std::min((float)(kSahBins - 1), (c2[3 * (size_t)it + a] - cmin[a]) * scale);
+                    };
+                    int bc[kSahBins] = {};
+                    Box bb[kSahBins];
+                    for (int q = 0; q < kSahBins; ++q) bb[q] = empty;
+                    for (int k = t.first; k <= t.last; ++k) {
+                        const uint32_t it = order[k];
+                        const int q = bin(it);
+                        ++bc[q];
+                        bb[q] = unite(bb[q], boxes[it]);
+                    }
+                    float ra[kSahBins];
+                    int rc[kSahBins];
+                    Box acc = empty;
+                    int accn = 0;
+                    for (int q = kSahBins - 1; q > 0; --q) {
+                        acc = unite(acc, bb[q]);
+                        accn += bc[q];
+                        ra[q] = accn ? area(acc) : 0.0f;
+                        rc[q] = accn;
+                    }
+                    acc = empty;
+                    accn = 0;
+                    for (int q = 0; q < kSahBins - 1; ++q) {
+                        acc = unite(acc, bb[q]);
+                        accn += bc[q];
+                        if (accn == 0 || rc[q + 1] == 0) continue;
+                        const float c = area(acc) * (float)accn + ra[q + 1] * (float)rc[q + 1];
+                        if (c < best) {
+                            best = c;
+                            best_axis = a;
+                            best_bin = q;
+                        }
+                    }
+                }
+                if (best_axis >= 0) {
+                    const int a = best_axis;
+                    const float scale = (float)kSahBins / (cmax[a] - cmin[a]);
+                    auto mid = std::stable_partition(order.begin() + t.first, order.begin() + t.last + 1, [&](uint32_t it) {
+                        return (int)std::min((float)(kSahBins - 1), (c2[3 * (size_t)it + a] - cmin[a]) * scale) <=
+                               best_bin;
+                    });
+                    split = (int)(mid - order.begin()) - 1;
+                }
             }
-            std::stable_sort(order.begin() + t.first, order.begin() + t.last + 1, [&](uint32_t x, uint32_t y) {
-                return boxes[x].lo[best_axis] + boxes[x].hi[best_axis] < boxes[y].lo[best_axis] + boxes[y].hi[best_axis];
-            });
-            Box b = boxes[order[t.first]];
-            for (int k = t.first + 1; k <= t.last; ++k) b = unite(b, boxes[order[k]]);
             Node2& nd = nodes[ref];
             nd.first = t.first;
             nd.last = t.last;
-            nd.parent = t.node;
+            nd.parent = t.parent;
             nd.box = b;
             nd.left = nd.right = 0;
-            todo.push_back({best_split + 1, t.last, ref, ref, 1});
-            todo.push_back({t.first, best_split, ref, ref, 0});
+            todo.push_back({split + 1, t.last, ref, 1});
+            todo.push_back({t.first, split, ref, 0});
         }
-        if (t.node >= 0) (t.side ? nodes[t.node].right : nodes[t.node].left) = ref;
+        if (t.parent >= 0) (t.side ? nodes[t.parent].right : nodes[t.parent].left) = ref;
     }
 }
 
@@ -735,9 +816,68 @@ void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<Instance
     OMV_CK(cudaMemsetAsync(counters.p, 0, sizeof(uint32_t) * 3, st));
     DBuf<uint32_t> cb(6);
     out.blas_root.assign(meshes.size(), 0xFFFFFFFFu);
+    // host SAH trees for the meshes that are small enough, one thread per mesh
+    struct HostTree {
+        std::vector<Box> boxes;
+        std::vector<Node2> nodes;
+        std::vector<uint32_t> order;
+    };
+    std::vector<HostTree> ht(meshes.size());
+    {
+        std::vector<size_t> todo;
+        for (size_t mi = 0; mi < meshes.size(); ++mi)
+            if (meshes[mi].valid && meshes[mi].num_faces > 0 && meshes[mi].num_faces <= kHostSahMaxTris &&
+                meshes[mi].h_pos && meshes[mi].h_faces)
+                todo.push_back(mi);
+        std::atomic<size_t> next{0};
+        auto worker = [&]() {
+            for (size_t j; (j = next.fetch_add(1)) < todo.size();) {
+                const MeshGeom& m = meshes[todo[j]];
+                HostTree& t = ht[todo[j]];
+                t.boxes.resize(m.num_faces);
+                for (int f = 0; f < m.num_faces; ++f) {
+                    Box& b = t.boxes[f];
+                    for (int a = 0; a < 3; ++a) {
+                        b.lo[a] = 3.0e38f;
+                        b.hi[a] = -3.0e38f;
+                    }
+                    for (int k = 0; k < 3; ++k) {
+                        const float* p = m.h_pos + 3 * (size_t)m.h_faces[3 * (size_t)f + k];
+                        for (int a = 0; a < 3; ++a) {
+                            b.lo[a] = std::min(b.lo[a], p[a]);
+                            b.hi[a] = std::max(b.hi[a], p[a]);
+                        }
+                    }
+                }
+                host_sah_tree(t.boxes, t.nodes, t.order);
+            }
+        };
+        const unsigned nt = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), (unsigned)todo.size()));
+        std::vector<std::thread> pool;
+        for (unsigned k = 1; k < nt; ++k) pool.emplace_back(worker);
+        worker();
+        for (auto& th : pool) th.join();
+    }
     for (size_t mi = 0; mi < meshes.size(); ++mi) {
         const MeshGeom& m = meshes[mi];
         if (!m.valid || m.num_faces <= 0) continue;
+        const HostTree& t = ht[mi];
+        if (!t.boxes.empty()) {
+            const int n = m.num_faces;
+            DBuf<Box> boxes(n);
+            DBuf<uint32_t> vals(n);
+            DBuf<Node2> d_nodes(std::max<size_t>(1, t.nodes.size()));
+            OMV_CK(cudaMemcpyAsync(boxes.p, t.boxes.data(), sizeof(Box) * n, cudaMemcpyHostToDevice, st));
+            OMV_CK(cudaMemcpyAsync(vals.p, t.order.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, st));
+            if (!t.nodes.empty())
+                OMV_CK(cudaMemcpyAsync(d_nodes.p, t.nodes.data(), sizeof(Node2) * t.nodes.size(),
+                                       cudaMemcpyHostToDevice, st));
+            out.blas_root[mi] = collapse_tree(false, n, d_nodes.p, vals.p, boxes.p, m.d_pos, m.d_faces, out.nodes,
+                                              counters.p, node_cap, out.tris, nullptr, counters.p + 1, counters.p + 2,
+                                              st);
+            continue;
+        }
+        // very large meshes: device LBVH
         DBuf<Box> boxes(m.num_faces);
         uint32_t init[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
         OMV_CK(cudaMemcpyAsync(cb.p, init, sizeof(init), cudaMemcpyHostToDevice, st));

@@ -15,6 +15,8 @@ struct MeshGeom {
     int num_faces = 0;
     const float* d_pos = nullptr;       // device, 3 floats per vertex
     const uint32_t* d_faces = nullptr;  // device, 3 indices per face
+    const float* h_pos = nullptr;       // the same positions and faces on the host
+    const uint32_t* h_faces = nullptr;
     float lo[3] = {0, 0, 0};            // exact bounds of the referenced vertices
     float hi[3] = {0, 0, 0};
 };

@@ -415,6 +415,8 @@ SceneHost* scene_create(const omv_scene_desc& d, int device)
                                  cudaMemcpyHostToDevice, s->stream));
         geo[i].d_pos = dp;
         geo[i].d_faces = df;
+        geo[i].h_pos = pos3[i].data();
+        geo[i].h_faces = d.meshes[i].faces;
     }
     AccelResult acc;
     build_accel(geo, igeo, acc, s->stream);
