@@ -251,6 +251,49 @@ omv_status omv_render_device_static(omv_scene* scene, const omv_camera* camera, 
                                     double* d_sum_rgb, double* d_sumsq_rgb, uint32_t* d_count,
                                     void* stream);
 
+/* -------------------------------------------------------------- batches --- */
+
+/* One render job of a batch.  Jobs share the scene geometry, lights, HDRI and
+ * the bounce / cutoff parameters; each has its own camera (and resolution),
+ * samples per pixel, sample offset, seed and material set, and accumulates
+ * into its own caller-owned DEVICE film like omv_render_device (not cleared).
+ * The reference renders one camera per process (main.cpp:426-511); a batch is
+ * the same render loop for many cameras and material variants at once. */
+typedef struct omv_job {
+    omv_camera camera;
+    int32_t samples_per_pixel;
+    int32_t sample_offset;
+    uint64_t seed;
+    int32_t material_set;   /* index into omv_batch_set_materials' sets; -1: the scene's materials */
+    int32_t pad;
+    double* d_sum_rgb;      /* 3 * width * height */
+    double* d_sumsq_rgb;    /* may be NULL (required when params->accumulate_variance) */
+    uint32_t* d_count;      /* width * height */
+} omv_job;
+
+/* Material variants for batch jobs: num_sets consecutive groups of
+ * num_materials descriptors, in the scene's material order (the missing
+ * material is appended to every set).  Which materials are alpha-masked may
+ * not change.  Replaces the previous sets. */
+omv_status omv_batch_set_materials(omv_scene* scene, int32_t num_sets, const omv_material_desc* sets);
+
+enum { OMV_BATCH_GRAPH = 1 };  /* capture the batch once as a CUDA graph; replay it for an identical job list */
+
+/* Renders all jobs through one wave pipeline: the jobs' paths are concatenated
+ * (job by job, pixel by pixel, sample by sample) into waves that the same
+ * persistent kernels process, with a device job table giving each path its
+ * camera, material set and film.  params->samples_per_pixel, seed,
+ * sample_offset and wave_paths are ignored (per job / autotuned).
+ * Asynchronous on `stream` (NULL: the scene's stream) unless stats is given. */
+omv_status omv_render_batch(omv_scene* scene, int32_t num_jobs, const omv_job* jobs, const omv_params* params,
+                            void* stream, int32_t flags, omv_stats* stats);
+
+/* Times a few wave sizes on this job list (renders it several times into the
+ * jobs' films: clear them afterwards) and keeps the fastest for the scene's
+ * later batches; *chosen_wave_paths (may be NULL) receives it. */
+omv_status omv_batch_autotune(omv_scene* scene, int32_t num_jobs, const omv_job* jobs, const omv_params* params,
+                              void* stream, int64_t* chosen_wave_paths);
+
 /* ----------------------------------------------------- rays / ID buffers --- */
 
 /* One closest-hit query (the reference's sceneIntersect, BDPTRenderer.cpp:75-102,

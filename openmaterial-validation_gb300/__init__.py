@@ -110,6 +110,11 @@ def lib():
     L.omv_render_device.argtypes = [vp, C.POINTER(capi.Camera), C.POINTER(capi.Params), vp, vp, vp, vp,
                                     C.POINTER(capi.Stats)]
     L.omv_render_device_static.argtypes = [vp, C.POINTER(capi.Camera), C.POINTER(capi.Params), vp, vp, vp, vp]
+    L.omv_batch_set_materials.argtypes = [vp, C.c_int32, C.POINTER(capi.MaterialDesc)]
+    L.omv_render_batch.argtypes = [vp, C.c_int32, C.POINTER(capi.Job), C.POINTER(capi.Params), vp, C.c_int32,
+                                   C.POINTER(capi.Stats)]
+    L.omv_batch_autotune.argtypes = [vp, C.c_int32, C.POINTER(capi.Job), C.POINTER(capi.Params), vp,
+                                     C.POINTER(C.c_int64)]
     L.omv_trace_rays.argtypes = [vp, C.c_int64, capi.f32p, C.POINTER(capi.Hit)]
     L.omv_render_ids.argtypes = [vp, C.POINTER(capi.Camera), capi.f32p, C.c_uint64, C.POINTER(capi.Hit),
                                  C.POINTER(C.c_uint32)]
@@ -123,7 +128,8 @@ def lib():
     L.omv_params_default.restype = None
     L.omv_struct_sizes.argtypes = [C.POINTER(C.c_int64), C.c_int32]
     for n in ("omv_scene_create", "omv_scene_destroy", "omv_scene_get_info", "omv_render", "omv_render_device",
-              "omv_render_device_static", "omv_trace_rays", "omv_render_ids", "omv_brdf_eval_direct",
+              "omv_render_device_static", "omv_batch_set_materials", "omv_render_batch", "omv_batch_autotune",
+              "omv_trace_rays", "omv_render_ids", "omv_brdf_eval_direct",
               "omv_brdf_sample_indirect", "omv_om_fresnel", "omv_camera_rays", "omv_env_radiance", "omv_struct_sizes"):
         getattr(L, n).restype = st
     _lib = L
@@ -263,6 +269,50 @@ class RenderScene:
         out = np.zeros((len(dirs), 3), dtype=np.float32)
         check(lib().omv_env_radiance(self.handle, len(dirs), capi.fptr(dirs), capi.fptr(out)))
         return out
+
+
+class BatchRenderer:
+    """Many render jobs of one scene through omv_render_batch: each job has its
+    own camera, samples per pixel, seed and material set and a device film
+    (torch tensors on the scene's GPU: sums (H, W, 3) float64, counts (H, W)
+    int32)."""
+
+    def __init__(self, scene: RenderScene, params: RendererParameters) -> None:
+        self.scene = scene
+        self.params = params
+        self._keep: list = []
+
+    def set_material_sets(self, sets) -> None:
+        keep: list = []
+        descs = capi.material_set_descs(sets, keep)
+        check(lib().omv_batch_set_materials(self.scene.handle, len(sets), descs))
+        self._keep = keep
+
+    @staticmethod
+    def job(camera: "PinholeCamera", spp: int, film, seed: int = 0, material_set: int = -1,
+            sample_offset: int = 0) -> "capi.Job":
+        j = capi.Job()
+        j.camera = camera.to_c()
+        j.samples_per_pixel, j.sample_offset, j.seed, j.material_set = spp, sample_offset, seed, material_set
+        j.d_sum_rgb = film[0].data_ptr()
+        j.d_sumsq_rgb = film[1].data_ptr() if film[1] is not None else None
+        j.d_count = film[2].data_ptr()
+        return j
+
+    def render(self, jobs, stream=None, graph: bool = False, stats: bool = False):
+        arr = (capi.Job * len(jobs))(*jobs)
+        p = self.params.to_c()
+        st = capi.Stats() if stats else None
+        check(lib().omv_render_batch(self.scene.handle, len(jobs), arr, C.byref(p), stream,
+                                     capi.OMV_BATCH_GRAPH if graph else 0, C.byref(st) if st else None))
+        return st
+
+    def autotune(self, jobs, stream=None) -> int:
+        arr = (capi.Job * len(jobs))(*jobs)
+        p = self.params.to_c()
+        chosen = C.c_int64(0)
+        check(lib().omv_batch_autotune(self.scene.handle, len(jobs), arr, C.byref(p), stream, C.byref(chosen)))
+        return chosen.value
 
 
 class BDPTRenderer:

@@ -91,6 +91,15 @@ HIT_DTYPE = np.dtype([("inst", "<u4"), ("geom", "<u4"), ("prim", "<u4"), ("mater
                       ("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("pad", "<u4")])
 
 
+class Job(C.Structure):
+    _fields_ = [("camera", Camera), ("samples_per_pixel", C.c_int32), ("sample_offset", C.c_int32),
+                ("seed", C.c_uint64), ("material_set", C.c_int32), ("pad", C.c_int32),
+                ("d_sum_rgb", C.c_void_p), ("d_sumsq_rgb", C.c_void_p), ("d_count", C.c_void_p)]
+
+
+OMV_BATCH_GRAPH = 1
+
+
 def fptr(a: np.ndarray):
     return a.ctypes.data_as(f32p)
 
@@ -124,6 +133,34 @@ def camera_struct(cam) -> Camera:
             c.rotation[i][j] = float(cam.rotation[i, j])
     c.half_width, c.half_height, c.focus = cam.half_width, cam.half_height, cam.focus
     return c
+
+
+def material_descs(materials, keep: List[Any]):
+    """omv_material_desc array for a list of scenes.Material; the IOR tables
+    are appended to `keep`."""
+    mats = (MaterialDesc * max(1, len(materials)))()
+    for i, mat in enumerate(materials):
+        md = mats[i]
+        md.type = mat.type
+        for c in range(4):
+            md.base_color[c] = mat.base_color[c]
+        md.metallic, md.roughness, md.ior = mat.metallic, mat.roughness, mat.ior
+        md.alpha_mode, md.alpha_cutoff = mat.alpha_mode, mat.alpha_cutoff
+        md.double_sided = 1 if mat.double_sided else 0
+        md.temperature = mat.temperature
+        if mat.ior_n is not None:
+            tn = np.ascontiguousarray(np.asarray(mat.ior_n, dtype=np.float64).astype(np.float32))
+            tk = np.ascontiguousarray(np.asarray(mat.ior_k, dtype=np.float64).astype(np.float32))
+            keep += [tn, tk]
+            md.ior_n_count, md.ior_n = len(tn), fptr(tn)
+            md.ior_k_count, md.ior_k = len(tk), fptr(tk)
+    return mats
+
+
+def material_set_descs(sets, keep: List[Any]):
+    """Flat omv_material_desc array of several material sets (set after set)."""
+    flat = [m for row in sets for m in row]
+    return material_descs(flat, keep)
 
 
 class DescHolder:
@@ -160,22 +197,7 @@ class DescHolder:
                 for c in range(4):
                     insts[i].transform[r][c] = float(M[r, c])
             insts[i].mesh = inst.mesh
-        mats = (MaterialDesc * max(1, len(scene.materials)))()
-        for i, mat in enumerate(scene.materials):
-            md = mats[i]
-            md.type = mat.type
-            for c in range(4):
-                md.base_color[c] = mat.base_color[c]
-            md.metallic, md.roughness, md.ior = mat.metallic, mat.roughness, mat.ior
-            md.alpha_mode, md.alpha_cutoff = mat.alpha_mode, mat.alpha_cutoff
-            md.double_sided = 1 if mat.double_sided else 0
-            md.temperature = mat.temperature
-            if mat.ior_n is not None:
-                tn = np.ascontiguousarray(np.asarray(mat.ior_n, dtype=np.float64).astype(np.float32))
-                tk = np.ascontiguousarray(np.asarray(mat.ior_k, dtype=np.float64).astype(np.float32))
-                self.keep += [tn, tk]
-                md.ior_n_count, md.ior_n = len(tn), fptr(tn)
-                md.ior_k_count, md.ior_k = len(tk), fptr(tk)
+        mats = material_descs(scene.materials, self.keep)
         lights = (LightDesc * max(1, len(scene.lights)))()
         for i, l in enumerate(scene.lights):
             for c in range(3):

@@ -127,7 +127,7 @@ int32_t omv_struct_sizes(int64_t* out, int32_t n)
                              (int64_t)sizeof(omv_hdri_desc),  (int64_t)sizeof(omv_scene_desc),
                              (int64_t)sizeof(omv_scene_info), (int64_t)sizeof(omv_camera),
                              (int64_t)sizeof(omv_params),     (int64_t)sizeof(omv_stats),
-                             (int64_t)sizeof(omv_hit)};
+                             (int64_t)sizeof(omv_hit),        (int64_t)sizeof(omv_job)};
     const int32_t m = (int32_t)(sizeof(sizes) / sizeof(sizes[0]));
     if (!out) return m;
     const int32_t k = std::min(n, m);
@@ -188,6 +188,38 @@ omv_status omv_render_device_static(omv_scene* scene, const omv_camera* camera, 
         cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : scene->h->stream;
         omv::render_frame_static(*scene->h, *camera, *params, d_sum_rgb,
                                  params->accumulate_variance ? d_sumsq_rgb : nullptr, d_count, st);
+    });
+}
+
+omv_status omv_batch_set_materials(omv_scene* scene, int32_t num_sets, const omv_material_desc* sets)
+{
+    return guarded([&] {
+        check_scene(scene);
+        omv::set_material_sets(*scene->h, num_sets, sets);
+    });
+}
+
+omv_status omv_render_batch(omv_scene* scene, int32_t num_jobs, const omv_job* jobs, const omv_params* params,
+                            void* stream, int32_t flags, omv_stats* stats)
+{
+    return guarded([&] {
+        check_scene(scene);
+        if (!params) throw omv::ArgError("params is NULL");
+        if (params->time_kernels && (flags & OMV_BATCH_GRAPH))
+            throw omv::ArgError("time_kernels cannot be combined with OMV_BATCH_GRAPH");
+        cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : scene->h->stream;
+        omv::render_batch(*scene->h, num_jobs, jobs, *params, st, stats, (flags & OMV_BATCH_GRAPH) != 0);
+    });
+}
+
+omv_status omv_batch_autotune(omv_scene* scene, int32_t num_jobs, const omv_job* jobs, const omv_params* params,
+                              void* stream, int64_t* chosen_wave_paths)
+{
+    return guarded([&] {
+        check_scene(scene);
+        if (!params) throw omv::ArgError("params is NULL");
+        cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : scene->h->stream;
+        omv::autotune_batch(*scene->h, num_jobs, jobs, *params, st, chosen_wave_paths);
     });
 }
 

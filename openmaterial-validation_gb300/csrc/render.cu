@@ -284,6 +284,11 @@ struct WaveArgs {
     int32_t npix;
     int32_t spp;
     int32_t sample_offset;
+    uint32_t base_q, base_r;  // wave_base / spp, wave_base % spp (batch: first global pixel, unused)
+    uint32_t last_pixel;      // pixel of the wave's last path (batch: global pixel)
+    const DevJob* jobs;       // batch job table (num_jobs == 0: one frame with the fields above)
+    int32_t num_jobs;
+    uint32_t* path_job;       // batch: job of each path of the wave
     int32_t cam_bounces, light_bounces, max_len;
     int32_t atten_mode;
     float light_scale, min_dist, cut;
@@ -296,9 +301,51 @@ struct WaveArgs {
 // does not change the image.
 __device__ __forceinline__ void path_ids(const WaveArgs& A, int k, uint32_t& pixel, uint32_t& sample)
 {
+    const uint32_t t = A.base_r + (uint32_t)k;  // < spp + 2^31
+    pixel = A.base_q + t / (uint32_t)A.spp;
+    sample = (uint32_t)A.sample_offset + t % (uint32_t)A.spp;
+}
+
+// What a path needs to know about its job: pixel and sample within the job,
+// the job's seed and material table (one frame: the frame's).
+struct PathCtx {
+    uint32_t pixel, sample;
+    uint64_t seed;
+    const DevMaterial* mats;
+};
+__device__ __forceinline__ PathCtx path_ctx(const WaveArgs& A, int k)
+{
+    PathCtx c;
+    if (A.num_jobs == 0) {
+        path_ids(A, k, c.pixel, c.sample);
+        c.seed = A.seed;
+        c.mats = A.S.mats;
+    } else {
+        const DevJob& J = A.jobs[A.path_job[k]];
+        const uint32_t local = (uint32_t)(A.wave_base + k - J.path_base);
+        c.pixel = local / (uint32_t)J.spp;
+        c.sample = (uint32_t)J.sample_offset + local % (uint32_t)J.spp;
+        c.seed = J.seed;
+        c.mats = J.mats;
+    }
+    return c;
+}
+
+// batch: the job of every path of the wave (largest job whose first path <= g)
+__global__ void __launch_bounds__(kShadeThreads) k_job_ids(WaveArgs A)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= A.wave_n) return;
     const int64_t g = A.wave_base + k;
-    pixel = (uint32_t)(g / A.spp);
-    sample = (uint32_t)(A.sample_offset + g % A.spp);
+    int lo = 0, hi = A.num_jobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (A.jobs[mid].path_base <= g)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    A.path_job[k] = (uint32_t)lo;
 }
 
 // ------------------------------------------------------------ raygen ---
@@ -309,9 +356,12 @@ __global__ void __launch_bounds__(kShadeThreads) k_camera_gen(WaveArgs A)
     uint32_t pixel = 0, sample = 0;
     V3 O = v3(0, 0, 0), R = v3(0, 0, 1);
     if (ok) {
-        path_ids(A, k, pixel, sample);
-        Rng4 r = rng4(A.seed, pixel, sample, 0u, kStreamCamera);
-        camera_ray(A.cam, (int)(pixel % A.cam.width), (int)(pixel / A.cam.width), r.u[0], r.u[1], O, R);
+        const PathCtx c = path_ctx(A, k);
+        pixel = c.pixel;
+        sample = c.sample;
+        const omv_camera& cam = A.num_jobs ? A.jobs[A.path_job[k]].cam : A.cam;
+        Rng4 r = rng4(c.seed, pixel, sample, 0u, kStreamCamera);
+        camera_ray(cam, (int)(pixel % (uint32_t)cam.width), (int)(pixel / (uint32_t)cam.width), r.u[0], r.u[1], O, R);
         // throughput starts at 1 and radiance at 0: the first camera shade uses
         // the constants and writes both, so only a frame without camera
         // bounces needs the radiance cleared here
@@ -333,11 +383,11 @@ __global__ void __launch_bounds__(kShadeThreads) k_light_gen(WaveArgs A)
     const bool ok = k < A.wave_n;
     V3 O = v3(0, 0, 0), R = v3(0, 0, 1);
     if (ok) {
-        uint32_t pixel, sample;
-        path_ids(A, k, pixel, sample);
+        const PathCtx c = path_ctx(A, k);
+        const uint32_t pixel = c.pixel, sample = c.sample;
         const DevScene& S = A.S;
         // DistanceRandom::getValue (DistanceRandom.h:98-115)
-        const float d = rng4(A.seed, pixel, sample, 0u, kStreamLight).u[0] * S.light_max;
+        const float d = rng4(c.seed, pixel, sample, 0u, kStreamLight).u[0] * S.light_max;
         int li = 0;
         const int N = S.num_lights;
         if (N > 1) {
@@ -361,7 +411,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_light_gen(WaveArgs A)
         V3 v = v3(1.0f, 0.0f, 0.0f);
         float sl = 1.0f;
         for (uint32_t t = 0; t < 64; ++t) {
-            Rng4 r = rng4(A.seed, pixel, sample, 1u + t, kStreamLight);
+            Rng4 r = rng4(c.seed, pixel, sample, 1u + t, kStreamLight);
             v = v3(r.u[0], r.u[1], r.u[2]);
             sl = dot(v, v);
             if (!(sl > 1.0f || sl < kEps)) break;
@@ -454,12 +504,12 @@ __global__ void __launch_bounds__(kShadeThreads) k_light_shade(WaveArgs A, int b
             k = __float_as_int(rb.w);
             tnear = ra.w;
             if (h.x != kInvalid) {
-                uint32_t pixel, sample;
-                path_ids(A, k, pixel, sample);
+                const PathCtx c = path_ctx(A, k);
+                const uint32_t pixel = c.pixel, sample = c.sample;
                 const Surf sp = surface_point(S, h.x, h.y, __uint_as_float(h.z), __uint_as_float(h.w), true);
-                const DevMaterial M = S.mats[sp.mat];
+                const DevMaterial M = c.mats[sp.mat];
                 const V3 in = v3(rb.x, rb.y, rb.z);
-                const Rng4 u = rng4(A.seed, pixel, sample, kDimLightBounce + (uint32_t)b, kStreamLight);
+                const Rng4 u = rng4(c.seed, pixel, sample, kDimLightBounce + (uint32_t)b, kStreamLight);
                 const V3 brdf = material_sample(S, M, sp, in, false, u, O);
                 const float ct = fabsf(dot(in, sp.nrm));
                 const float4 tp0 = A.R.ltp[k];
@@ -533,11 +583,11 @@ __global__ void __launch_bounds__(kShadeThreads, 3) k_camera_shade(WaveArgs A, i
                 }
             } else {
                 if (first) A.R.rad[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                uint32_t pixel, sample;
-                path_ids(A, k, pixel, sample);
+                const PathCtx c = path_ctx(A, k);
+                const uint32_t pixel = c.pixel, sample = c.sample;
                 const Surf sp = surface_point(S, h.x, h.y, __uint_as_float(h.z), __uint_as_float(h.w), true);
-                const DevMaterial M = S.mats[sp.mat];
-                const Rng4 u = rng4(A.seed, pixel, sample, (uint32_t)b, kStreamCamera);
+                const DevMaterial M = c.mats[sp.mat];
+                const Rng4 u = rng4(c.seed, pixel, sample, (uint32_t)b, kStreamCamera);
                 const V3 brdf = material_sample(S, M, sp, in, true, u, O);
                 const float ct = fabsf(dot(O, sp.nrm));
                 const V3 tpn = v3(tp.x * brdf.x * ct, tp.y * brdf.y * ct, tp.z * brdf.z * ct);
@@ -692,14 +742,37 @@ __global__ void __launch_bounds__(kShadeThreads) k_film(WaveArgs A, int group, d
     const int j = threadIdx.x & (group - 1);
     const int64_t spp = A.spp;
     const int64_t g_begin = A.wave_base, g_end = A.wave_base + A.wave_n;
-    const int64_t p = g_begin / spp + t / group;
-    const bool live = p <= (g_end - 1) / spp;
+    const int64_t p = (int64_t)A.base_q + t / group;
+    const bool live = p <= (int64_t)A.last_pixel;
+    // the pixel's paths, film and index in it (batch: p is a pixel of the
+    // concatenated job films)
+    int64_t first_path = p * spp, npp = spp, lp = p;
+    double* fsum = sum;
+    double* fsq = sumsq;
+    uint32_t* fcnt = count;
+    if (A.num_jobs > 0 && live) {
+        int lo = 0, hi = A.num_jobs - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if ((int64_t)A.jobs[mid].pixel_base <= p)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const DevJob& J = A.jobs[lo];
+        lp = p - (int64_t)J.pixel_base;
+        npp = J.spp;
+        first_path = J.path_base + lp * npp;
+        fsum = J.sum;
+        fsq = J.sumsq;
+        fcnt = J.count;
+    }
     uint32_t c = 0;
     FF v[6];
 #pragma unroll
     for (int q = 0; q < 6; ++q) v[q] = FF{0.0f, 0.0f};
     if (live) {
-        const int64_t g0 = max(p * spp, g_begin), g1 = min((p + 1) * spp, g_end);
+        const int64_t g0 = max(first_path, g_begin), g1 = min(first_path + npp, g_end);
         for (int64_t g = g0 + j; g < g1; g += group) {
             const float4 r = A.R.rad[g - g_begin];
             v[0] = ff_add(v[0], FF{r.x, 0.0f});
@@ -722,15 +795,15 @@ __global__ void __launch_bounds__(kShadeThreads) k_film(WaveArgs A, int group, d
         }
     }
     if (!live || j != 0 || c == 0) return;
-    double* ps = sum + 3 * (size_t)p;
+    double* ps = fsum + 3 * (size_t)lp;
 #pragma unroll
     for (int q = 0; q < 3; ++q) ps[q] += (double)v[q].hi + (double)v[q].lo;
-    if (sumsq) {
-        double* pq = sumsq + 3 * (size_t)p;
+    if (fsq) {
+        double* pq = fsq + 3 * (size_t)lp;
 #pragma unroll
         for (int q = 0; q < 3; ++q) pq[q] += (double)v[3 + q].hi + (double)v[3 + q].lo;
     }
-    count[p] += c;
+    fcnt[lp] += c;
 }
 
 // ------------------------------------------------------------ ID pass ---
@@ -832,7 +905,7 @@ namespace {
 // Byte offsets of one wave's arrays inside a single scratch block (each array
 // starts on a 256-byte boundary).
 struct ScratchLayout {
-    size_t tp, rad, ltp, lrad, lmeta, lvp, lvr, rq0, rq1, hits, sq, ctr, stats, err, bytes;
+    size_t tp, rad, ltp, lrad, lmeta, lvp, lvr, rq0, rq1, hits, pjob, sq, ctr, stats, err, bytes;
 };
 
 ScratchLayout scratch_layout(int64_t wave_cap, int light_slots, int shadow_slots)
@@ -855,6 +928,7 @@ ScratchLayout scratch_layout(int64_t wave_cap, int light_slots, int shadow_slots
     L.rq0 = take(W * 32);
     L.rq1 = take(W * 32);
     L.hits = take(W * 16);
+    L.pjob = take(W * 4);
     L.sq = take((size_t)shadow_slots * W * 48 + 48);
     L.ctr = take(kMaxCounters * 4);
     L.stats = take(16 * 8);
@@ -864,11 +938,11 @@ ScratchLayout scratch_layout(int64_t wave_cap, int light_slots, int shadow_slots
 }
 
 // Scratch bytes of one path: tp rad ltp lrad (16 B each), lmeta 4, light
-// vertices 32 per slot, two ray-queue entries 64, hit 16, shadow entries 48 per
-// slot (each array is further rounded up to 256 bytes).
+// vertices 32 per slot, two ray-queue entries 64, hit 16, batch job 4, shadow
+// entries 48 per slot (each array is further rounded up to 256 bytes).
 size_t path_scratch_bytes(int light_slots, int shadow_slots)
 {
-    return 68 + 32 * (size_t)light_slots + 80 + 48 * (size_t)shadow_slots;
+    return 68 + 32 * (size_t)light_slots + 84 + 48 * (size_t)shadow_slots;
 }
 
 void carve_scratch(RenderScratch& R, void* base, int64_t wave_cap, int light_slots, int shadow_slots)
@@ -890,6 +964,7 @@ void carve_scratch(RenderScratch& R, void* base, int64_t wave_cap, int light_slo
     R.rq[0] = (float4*)(b + L.rq0);
     R.rq[1] = (float4*)(b + L.rq1);
     R.hits = (uint4*)(b + L.hits);
+    R.path_job = (uint32_t*)(b + L.pjob);
     R.sq = (float4*)(b + L.sq);
     R.ctr = (uint32_t*)(b + L.ctr);
     R.stats = (unsigned long long*)(b + L.stats);
@@ -922,11 +997,33 @@ FramePlan plan_frame(const SceneHost& s, const omv_camera& cam, const omv_params
     return P;
 }
 
-// The wave loop of one frame on scratch R (at least P.cap paths).  With
-// `events` false no CUDA event is created: no frame or kernel timing, and
-// `stats` must be null.
+// A batch as the wave loop sees it: the device job table and its host copy.
+struct BatchPlan {
+    const DevJob* d_jobs;
+    const std::vector<DevJob>* h_jobs;
+    int min_spp;
+};
+
+// pixel of the concatenated job films that holds global path g
+uint32_t batch_global_pixel(const std::vector<DevJob>& jobs, int64_t g)
+{
+    size_t lo = 0, hi = jobs.size() - 1;
+    while (lo < hi) {
+        const size_t mid = (lo + hi + 1) / 2;
+        if (jobs[mid].path_base <= g)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return jobs[lo].pixel_base + (uint32_t)((g - jobs[lo].path_base) / jobs[lo].spp);
+}
+
+// The wave loop of one frame (or, with `batch`, of all jobs of a batch) on
+// scratch R (at least P.cap paths).  With `events` false no CUDA event is
+// created: no frame or kernel timing, and `stats` must be null.
 void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_camera& cam, const omv_params& p,
-               double* d_sum, double* d_sumsq, uint32_t* d_count, cudaStream_t st, omv_stats* stats, bool events)
+               double* d_sum, double* d_sumsq, uint32_t* d_count, cudaStream_t st, omv_stats* stats, bool events,
+               const BatchPlan* batch = nullptr)
 {
     const int64_t total = P.total, npix = P.npix, cap = P.cap;
     const bool lights = P.lights;
@@ -948,6 +1045,9 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
     A.min_dist = p.light_min_distance;
     A.cut = p.ray_cut_value;
     A.R = R;
+    A.jobs = batch ? batch->d_jobs : nullptr;
+    A.num_jobs = batch ? (int32_t)batch->h_jobs->size() : 0;
+    A.path_job = R.path_job;
     int occ_t = 0, occ_s = 0;
     OMV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, k_extend, kTraceThreads, 0));
     OMV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_camera_shade, kShadeThreads, 0));
@@ -973,8 +1073,21 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
     for (int64_t wb = 0; wb < total; wb += cap) {
         A.wave_base = wb;
         A.wave_n = (int32_t)std::min<int64_t>(cap, total - wb);
+        if (batch) {
+            A.base_q = batch_global_pixel(*batch->h_jobs, wb);
+            A.base_r = 0;
+            A.last_pixel = batch_global_pixel(*batch->h_jobs, wb + A.wave_n - 1);
+        } else {
+            A.base_q = (uint32_t)(wb / p.samples_per_pixel);
+            A.base_r = (uint32_t)(wb % p.samples_per_pixel);
+            A.last_pixel = (uint32_t)((wb + A.wave_n - 1) / p.samples_per_pixel);
+        }
         OMV_CUDA(cudaMemsetAsync(R.ctr, 0, kMaxCounters * 4, st));
         int work = 0;
+        if (batch) {
+            k_job_ids<<<grid_for(A.wave_n, kShadeThreads), kShadeThreads, 0, st>>>(A);
+            ++launches;
+        }
         if (lights) {
             k_light_gen<<<grid_for(A.wave_n, kShadeThreads), kShadeThreads, 0, st>>>(A);
             ++launches;
@@ -1012,10 +1125,10 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
         }
         {
             // about 8 samples per lane: group = power of two <= spp / 8, in [1, 32]
-            const int64_t spp = p.samples_per_pixel;
+            const int64_t spp = batch ? batch->min_spp : p.samples_per_pixel;
             int group = 1;
             while (group < 32 && group * 16 <= spp) group *= 2;
-            const int64_t pixels = (A.wave_base + A.wave_n - 1) / spp - A.wave_base / spp + 1;
+            const int64_t pixels = (int64_t)A.last_pixel - (int64_t)A.base_q + 1;
             k_film<<<grid_for(pixels * group, kShadeThreads), kShadeThreads, 0, st>>>(A, group, d_sum, d_sumsq,
                                                                                      d_count);
             ++launches;
@@ -1074,6 +1187,11 @@ static void ensure_scratch(SceneHost& s, int64_t wave_cap, int light_slots, int 
         OMV_CUDA(cudaStreamSynchronize(s.stream));
         cudaFree(R.base);
         R = RenderScratch{};
+        if (s.batch_graph) {  // it refers to the old scratch
+            cudaGraphExecDestroy(s.batch_graph);
+            s.batch_graph = nullptr;
+            s.batch_key.clear();
+        }
     }
     void* base = nullptr;
     OMV_CUDA(cudaMalloc(&base, scratch_layout(wave_cap, light_slots, shadow_slots).bytes));
@@ -1098,6 +1216,190 @@ void render_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, doub
     }
     ensure_scratch(s, P.cap, P.light_slots, P.shadow_slots);
     run_waves(s, s.scratch, P, cam, p, d_sum, d_sumsq, d_count, st, stats, true);
+}
+
+// ------------------------------------------------------------- batches ---
+
+namespace {
+
+// Checked device job table of a batch (host copy) with its totals.
+struct BatchJobs {
+    std::vector<DevJob> jobs;
+    int64_t total_paths = 0;
+    int min_spp = 0;
+};
+
+BatchJobs make_batch(const SceneHost& s, int n, const omv_job* jobs, const omv_params& p)
+{
+    if (n <= 0 || !jobs) throw ArgError("a batch needs at least one job");
+    if (p.camera_bounces < 0 || p.light_bounces < 0) throw ArgError("negative bounce count");
+    if (p.camera_bounces > 60 || p.light_bounces > 60) throw ArgError("at most 60 bounces are supported");
+    BatchJobs B;
+    B.jobs.resize(n);
+    int64_t paths = 0, pixels = 0;
+    B.min_spp = 1 << 30;
+    for (int i = 0; i < n; ++i) {
+        const omv_job& j = jobs[i];
+        if (j.camera.width <= 0 || j.camera.height <= 0) throw ArgError("batch job with a non-positive resolution");
+        if (j.samples_per_pixel <= 0) throw ArgError("batch job with no samples");
+        if (!j.d_sum_rgb || !j.d_count) throw ArgError("batch job without a film");
+        if (p.accumulate_variance && !j.d_sumsq_rgb) throw ArgError("accumulate_variance needs every job's d_sumsq_rgb");
+        if (j.material_set < -1 || j.material_set >= s.num_mat_sets) throw ArgError("batch job material set out of range");
+        const int64_t npix = (int64_t)j.camera.width * j.camera.height;
+        if (npix * j.samples_per_pixel > (int64_t)0x7FFFFFFF) throw ArgError("batch job too large");
+        DevJob& d = B.jobs[i];
+        d = DevJob{};
+        d.cam = j.camera;
+        d.path_base = paths;
+        d.pixel_base = (uint32_t)pixels;
+        d.spp = j.samples_per_pixel;
+        d.sample_offset = j.sample_offset;
+        d.seed = j.seed;
+        d.mats = j.material_set < 0 ? s.dev.mats : s.mat_sets + (size_t)j.material_set * s.num_materials;
+        d.sum = j.d_sum_rgb;
+        d.sumsq = p.accumulate_variance ? j.d_sumsq_rgb : nullptr;
+        d.count = j.d_count;
+        paths += npix * j.samples_per_pixel;
+        pixels += npix;
+        B.min_spp = std::min(B.min_spp, j.samples_per_pixel);
+    }
+    if (pixels > (int64_t)0xFFFFFFFFu) throw ArgError("batch has too many pixels");
+    B.total_paths = paths;
+    return B;
+}
+
+FramePlan batch_frame_plan(SceneHost& s, const BatchJobs& B, const omv_params& p, int64_t wave_paths)
+{
+    FramePlan P;
+    P.npix = 0;
+    P.total = B.total_paths;
+    P.lights = s.num_lights > 0;
+    P.light_slots = P.lights ? p.light_bounces + 1 : 1;
+    P.shadow_slots = P.lights ? P.light_slots : 1;
+    int64_t cap = wave_paths;
+    if (cap <= 0) {
+        size_t free_b = 0, total_b = 0;
+        OMV_CUDA(cudaMemGetInfo(&free_b, &total_b));
+        const size_t budget = std::min(kWaveScratchBudget, (free_b + s.scratch.bytes) / 2);
+        cap = (int64_t)(budget / path_scratch_bytes(P.light_slots, P.shadow_slots));
+    }
+    P.cap = std::max<int64_t>(1, std::min<int64_t>({cap, std::max<int64_t>(P.total, 1), (int64_t)0x7FFFFFFF}));
+    return P;
+}
+
+void upload_jobs(SceneHost& s, const BatchJobs& B, cudaStream_t st)
+{
+    if (s.jobs_cap < B.jobs.size()) {
+        OMV_CUDA(cudaStreamSynchronize(s.stream));
+        OMV_CUDA(cudaStreamSynchronize(st));
+        if (s.d_jobs) cudaFree(s.d_jobs);
+        s.d_jobs = nullptr;
+        s.jobs_cap = 0;
+        if (s.batch_graph) {  // it refers to the old table
+            cudaGraphExecDestroy(s.batch_graph);
+            s.batch_graph = nullptr;
+            s.batch_key.clear();
+        }
+        const size_t cap = std::max<size_t>(64, B.jobs.size());
+        OMV_CUDA(cudaMalloc(&s.d_jobs, sizeof(DevJob) * cap));
+        s.jobs_cap = cap;
+    }
+    // synchronous: the table must be in place before a captured batch replays
+    OMV_CUDA(cudaStreamSynchronize(st));
+    OMV_CUDA(cudaMemcpy(s.d_jobs, B.jobs.data(), sizeof(DevJob) * B.jobs.size(), cudaMemcpyHostToDevice));
+}
+
+}  // namespace
+
+void render_batch(SceneHost& s, int n, const omv_job* jobs, const omv_params& p, cudaStream_t st, omv_stats* stats,
+                  bool use_graph)
+{
+    const BatchJobs B = make_batch(s, n, jobs, p);
+    const FramePlan P = batch_frame_plan(s, B, p, s.batch_wave_paths);
+    ensure_scratch(s, P.cap, P.light_slots, P.shadow_slots);
+    upload_jobs(s, B, st);
+    const BatchPlan plan{s.d_jobs, &B.jobs, B.min_spp};
+    omv_camera cam0 = B.jobs[0].cam;
+    if (!use_graph) {
+        run_waves(s, s.scratch, P, cam0, p, nullptr, nullptr, nullptr, st, stats, stats != nullptr, &plan);
+        return;
+    }
+    // the captured graph is valid for this job table, these parameters and this wave size
+    std::vector<unsigned char> key(sizeof(DevJob) * B.jobs.size() + sizeof(omv_params) + sizeof(int64_t));
+    std::memcpy(key.data(), B.jobs.data(), sizeof(DevJob) * B.jobs.size());
+    omv_params pk = p;
+    pk.time_kernels = 0;
+    std::memcpy(key.data() + sizeof(DevJob) * B.jobs.size(), &pk, sizeof(pk));
+    std::memcpy(key.data() + sizeof(DevJob) * B.jobs.size() + sizeof(pk), &P.cap, sizeof(int64_t));
+    if (!s.batch_graph || s.batch_key != key) {
+        if (s.batch_graph) {
+            cudaGraphExecDestroy(s.batch_graph);
+            s.batch_graph = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        OMV_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        try {
+            run_waves(s, s.scratch, P, cam0, pk, nullptr, nullptr, nullptr, st, nullptr, false, &plan);
+        } catch (...) {
+            cudaStreamEndCapture(st, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        OMV_CUDA(cudaStreamEndCapture(st, &g));
+        cudaGraphExec_t ge = nullptr;
+        const cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        OMV_CUDA(e);
+        s.batch_graph = ge;
+        s.batch_key = key;
+    }
+    OMV_CUDA(cudaGraphLaunch(s.batch_graph, st));
+    if (stats) {
+        OMV_CUDA(cudaStreamSynchronize(st));
+        *stats = omv_stats{};
+        stats->paths = B.total_paths;
+    }
+}
+
+void autotune_batch(SceneHost& s, int n, const omv_job* jobs, const omv_params& p, cudaStream_t st,
+                    int64_t* chosen)
+{
+    const BatchJobs B = make_batch(s, n, jobs, p);
+    const FramePlan Pmax = batch_frame_plan(s, B, p, 0);
+    std::vector<int64_t> cand;
+    for (int64_t c = (int64_t)1 << 22; c < Pmax.cap; c *= 4) cand.push_back(c);
+    cand.push_back(Pmax.cap);
+    cudaEvent_t e0, e1;
+    OMV_CUDA(cudaEventCreate(&e0));
+    OMV_CUDA(cudaEventCreate(&e1));
+    int64_t best = Pmax.cap;
+    float best_ms = 3.0e38f;
+    const int64_t saved = s.batch_wave_paths;
+    try {
+        for (int64_t c : cand) {
+            s.batch_wave_paths = c;
+            render_batch(s, n, jobs, p, st, nullptr, false);  // warm-up (and scratch)
+            OMV_CUDA(cudaEventRecord(e0, st));
+            render_batch(s, n, jobs, p, st, nullptr, false);
+            OMV_CUDA(cudaEventRecord(e1, st));
+            OMV_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.0f;
+            OMV_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = c;
+            }
+        }
+    } catch (...) {
+        s.batch_wave_paths = saved;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    s.batch_wave_paths = best;
+    if (chosen) *chosen = best;
 }
 
 // ------------------------------------------ render without allocation ---
@@ -1130,7 +1432,7 @@ void* static_scratch_address(int device)
 int64_t static_wave_limit(int light_slots, int shadow_slots)
 {
     const size_t per_path = path_scratch_bytes(light_slots, shadow_slots);
-    const size_t fixed = 48 + kMaxCounters * 4 + 16 * 8 + 16 * 4 + 14 * 256;
+    const size_t fixed = 48 + kMaxCounters * 4 + 16 * 8 + 16 * 4 + 15 * 256;
     int64_t cap = (int64_t)((OMV_STATIC_SCRATCH_BYTES - fixed) / per_path) & ~(int64_t)31;
     while (cap > 0 && scratch_layout(cap, light_slots, shadow_slots).bytes > OMV_STATIC_SCRATCH_BYTES) cap -= 32;
     return cap;

@@ -219,6 +219,9 @@ SceneHost::~SceneHost()
     if (stream) cudaStreamSynchronize(stream);
     for (void* p : allocs) cudaFree(p);
     if (scratch.base) cudaFree(scratch.base);
+    if (mat_sets) cudaFree(mat_sets);
+    if (d_jobs) cudaFree(d_jobs);
+    if (batch_graph) cudaGraphExecDestroy(batch_graph);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -229,6 +232,78 @@ void* SceneHost::alloc(size_t bytes)
     allocs.push_back(p);
     device_bytes += (int64_t)bytes;
     return p;
+}
+
+DevMaterial material_from_desc(const omv_material_desc& md)
+{
+    DevMaterial m{};
+    if (md.type == OMV_MATERIAL_OPENMATERIAL) {
+        m.type = kMatOm;
+        m.om_valid = md.ior_n_count >= 2 && md.ior_k_count >= 2 && md.ior_n && md.ior_k;
+        for (int c = 0; c < 3 && m.om_valid; ++c) {
+            const float wl = kRgbWl[c];
+            if (wl < std::max(md.ior_n[0], md.ior_k[0]) ||
+                wl > std::min(md.ior_n[2 * (md.ior_n_count - 1)], md.ior_k[2 * (md.ior_k_count - 1)]))
+                throw ArgError("OpenMATERIAL IOR table does not cover the RGB wavelengths");
+            m.om_n[c] = ior_lookup(md.ior_n, md.ior_n_count, wl);
+            m.om_k[c] = ior_lookup(md.ior_k, md.ior_k_count, wl);
+        }
+    } else if (md.type == OMV_MATERIAL_PBR) {
+        m.type = kMatPbr;
+        for (int c = 0; c < 4; ++c) m.color[c] = 1.0f * md.base_color[c];
+        if (md.alpha_mode != OMV_ALPHA_BLEND) m.color[3] = 1.0f;
+        m.transmissive = (md.double_sided || m.color[3] < 1.0f) ? 1 : 0;
+        m.metal = md.metallic;
+        float rough = md.roughness;
+        rough = std::max(0.00001f, std::min(rough, 0.99999f));
+        m.alpha = std::pow(rough, 2.0f);
+        m.eta = 1.0f / (md.double_sided ? 1.0f : md.ior);
+        m.masked = (md.alpha_mode == OMV_ALPHA_MASK && md.base_color[3] < md.alpha_cutoff) ? 1 : 0;
+    } else {
+        throw ArgError("unknown material type");
+    }
+    return m;
+}
+
+// DiffuseColorMaterial (DiffuseColorMaterial.cpp:41-108): the pink stand-in
+DevMaterial missing_material()
+{
+    DevMaterial m{};
+    m.type = kMatMissing;
+    const float pdf = 1.0f / kPi;
+    const float bp = 1.0f / (pdf * kPi);
+    m.color[0] = bp * 1000.0f;
+    m.color[1] = bp * 0.0f;
+    m.color[2] = bp * 1000.0f;
+    m.color[3] = 1.0f;
+    return m;
+}
+
+void set_material_sets(SceneHost& s, int num_sets, const omv_material_desc* descs)
+{
+    if (num_sets < 0 || (num_sets > 0 && !descs)) throw ArgError("material sets: NULL descriptors");
+    const int per = s.num_materials;  // including the missing material
+    std::vector<DevMaterial> all((size_t)num_sets * per);
+    for (int k = 0; k < num_sets; ++k) {
+        for (int i = 0; i + 1 < per; ++i) {
+            const DevMaterial m = material_from_desc(descs[(size_t)k * (per - 1) + i]);
+            if (m.masked != s.h_mats[i].masked)
+                throw ArgError("material sets cannot change which materials are alpha-masked");
+            all[(size_t)k * per + i] = m;
+        }
+        all[(size_t)k * per + per - 1] = missing_material();
+    }
+    if (s.mat_sets) {
+        OMV_CUDA(cudaStreamSynchronize(s.stream));
+        cudaFree(s.mat_sets);
+        s.mat_sets = nullptr;
+        s.num_mat_sets = 0;
+    }
+    if (num_sets > 0) {
+        OMV_CUDA(cudaMalloc(&s.mat_sets, sizeof(DevMaterial) * all.size()));
+        OMV_CUDA(cudaMemcpy(s.mat_sets, all.data(), sizeof(DevMaterial) * all.size(), cudaMemcpyHostToDevice));
+    }
+    s.num_mat_sets = num_sets;
 }
 
 SceneHost* scene_create(const omv_scene_desc& d, int device)
@@ -253,48 +328,11 @@ SceneHost* scene_create(const omv_scene_desc& d, int device)
     std::vector<DevMaterial> mats(nmat);
     std::vector<int> mat_type(nmat);
     for (int i = 0; i < d.num_materials; ++i) {
-        const omv_material_desc& md = d.materials[i];
-        DevMaterial m{};
-        if (md.type == OMV_MATERIAL_OPENMATERIAL) {
-            m.type = kMatOm;
-            m.om_valid = md.ior_n_count >= 2 && md.ior_k_count >= 2 && md.ior_n && md.ior_k;
-            for (int c = 0; c < 3 && m.om_valid; ++c) {
-                const float wl = kRgbWl[c];
-                if (wl < std::max(md.ior_n[0], md.ior_k[0]) ||
-                    wl > std::min(md.ior_n[2 * (md.ior_n_count - 1)], md.ior_k[2 * (md.ior_k_count - 1)]))
-                    throw ArgError("OpenMATERIAL IOR table does not cover the RGB wavelengths");
-                m.om_n[c] = ior_lookup(md.ior_n, md.ior_n_count, wl);
-                m.om_k[c] = ior_lookup(md.ior_k, md.ior_k_count, wl);
-            }
-        } else if (md.type == OMV_MATERIAL_PBR) {
-            m.type = kMatPbr;
-            for (int c = 0; c < 4; ++c) m.color[c] = 1.0f * md.base_color[c];
-            if (md.alpha_mode != OMV_ALPHA_BLEND) m.color[3] = 1.0f;
-            m.transmissive = (md.double_sided || m.color[3] < 1.0f) ? 1 : 0;
-            m.metal = md.metallic;
-            float rough = md.roughness;
-            rough = std::max(0.00001f, std::min(rough, 0.99999f));
-            m.alpha = std::pow(rough, 2.0f);
-            m.eta = 1.0f / (md.double_sided ? 1.0f : md.ior);
-            m.masked = (md.alpha_mode == OMV_ALPHA_MASK && md.base_color[3] < md.alpha_cutoff) ? 1 : 0;
-        } else {
-            throw ArgError("unknown material type");
-        }
-        mat_type[i] = m.type;
-        mats[i] = m;
+        mats[i] = material_from_desc(d.materials[i]);
+        mat_type[i] = mats[i].type;
     }
-    {
-        DevMaterial m{};
-        m.type = kMatMissing;
-        const float pdf = 1.0f / kPi;
-        const float bp = 1.0f / (pdf * kPi);
-        m.color[0] = bp * 1000.0f;
-        m.color[1] = bp * 0.0f;
-        m.color[2] = bp * 1000.0f;
-        m.color[3] = 1.0f;
-        mats[nmat - 1] = m;
-        mat_type[nmat - 1] = kMatMissing;
-    }
+    mats[nmat - 1] = missing_material();
+    mat_type[nmat - 1] = kMatMissing;
 
     // ---- meshes
     s->num_meshes = d.num_meshes;
@@ -441,6 +479,7 @@ SceneHost* scene_create(const omv_scene_desc& d, int device)
     D.mats = s->upload(mats);
     D.num_materials = nmat;
     s->num_materials = nmat;
+    s->h_mats = mats;
     s->d_face_prefix = s->upload(s->mesh_face_prefix);
 
     // ---- lights (RenderLightPoint::set, DistanceRandom CDF)

@@ -44,6 +44,7 @@ struct RenderScratch {
     float4* lv_rad = nullptr;    // [light_slots][wave_cap]
     float4* rq[2] = {nullptr, nullptr};  // ray queues: 2 float4 per entry
     uint4* hits = nullptr;       // per queue entry
+    uint32_t* path_job = nullptr;  // batch: job of each path
     float4* sq = nullptr;        // shadow queue: 3 float4 per entry
     uint32_t* ctr = nullptr;     // per-wave queue and work counters
     unsigned long long* stats = nullptr;  // cumulative ray counters
@@ -51,6 +52,23 @@ struct RenderScratch {
 };
 
 constexpr int kMaxCounters = 512;
+
+// One job of a batch render (device copy): its camera, samples, seed and
+// material table, its film, and where its paths and pixels start in the
+// batch's concatenated path and pixel ranges.
+struct DevJob {
+    omv_camera cam;
+    int64_t path_base;
+    uint32_t pixel_base;
+    int32_t spp;
+    int32_t sample_offset;
+    int32_t pad;
+    uint64_t seed;
+    const DevMaterial* mats;
+    double* sum;
+    double* sumsq;
+    uint32_t* count;
+};
 
 struct SceneHost {
     int device = 0;
@@ -71,6 +89,14 @@ struct SceneHost {
     std::vector<uint32_t> mesh_face_prefix;  // global primitive id base per mesh
     uint32_t* d_face_prefix = nullptr;
     RenderScratch scratch;
+    std::vector<DevMaterial> h_mats;         // the scene's materials (host copy)
+    DevMaterial* mat_sets = nullptr;         // batch material sets: num_mat_sets x num_materials
+    int num_mat_sets = 0;
+    DevJob* d_jobs = nullptr;                // batch job table
+    size_t jobs_cap = 0;
+    cudaGraphExec_t batch_graph = nullptr;   // captured batch render, replayed for an identical job list
+    std::vector<unsigned char> batch_key;    // what batch_graph was captured for
+    int64_t batch_wave_paths = 0;            // autotuned wave size for batches (0: automatic)
 
     ~SceneHost();
     void* alloc(size_t bytes);
@@ -87,6 +113,18 @@ SceneHost* scene_create(const omv_scene_desc& desc, int device);
 
 void render_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, double* d_sum, double* d_sumsq,
                   uint32_t* d_count, cudaStream_t st, omv_stats* stats);
+DevMaterial material_from_desc(const omv_material_desc& md);
+DevMaterial missing_material();
+// material sets for batch jobs: num_sets x (scene materials without the missing one)
+void set_material_sets(SceneHost& s, int num_sets, const omv_material_desc* descs);
+// all jobs through one wave pipeline (optionally captured once as a CUDA graph
+// and replayed for an identical job list)
+void render_batch(SceneHost& s, int num_jobs, const omv_job* jobs, const omv_params& p, cudaStream_t st,
+                  omv_stats* stats, bool use_graph);
+// times candidate wave sizes on the job list and keeps the fastest for batches
+void autotune_batch(SceneHost& s, int num_jobs, const omv_job* jobs, const omv_params& p, cudaStream_t st,
+                    int64_t* chosen);
+
 // render_frame on the fixed scratch array; makes no device allocation
 void render_frame_static(SceneHost& s, const omv_camera& cam, const omv_params& p, double* d_sum, double* d_sumsq,
                          uint32_t* d_count, cudaStream_t st);

@@ -373,6 +373,83 @@ def scene_c2(width: int = 1920, height: int = 1080, spp: int = 64, seed: int = 0
     return Scene("c2", meshes, insts, mats, [], hdri, cam, RenderSpec(spp, 10, 10, 10))
 
 
+def _tessellation_for(tris: int):
+    """(icosphere subdivision, torus nu, nv) for 4 icospheres and 4 tori of
+    about `tris` triangles in total: the icospheres take the largest power-of-4
+    size within half the budget, the tori the rest."""
+    sub = 1
+    while sub < 7 and 4 * 20 * 4 ** (sub + 1) <= tris // 2:
+        sub += 1
+    per_torus = max(96, (tris - 4 * 20 * 4 ** sub) // 4)
+    nv = max(6, int(round((per_torus / 2 / 2.67) ** 0.5)))
+    nu = max(8, int(round(per_torus / 2 / nv)))
+    return sub, nu, nv
+
+
+def scene_materials(width: int = 512, height: int = 512, spp: int = 32, tris: int = 100_000,
+                    n_materials: int = 8, seed: int = 0, bounces: int = 6) -> Scene:
+    """Material-study scene (batched sweeps, adjoint, inverse fits): 8 objects
+    (tori and displaced icospheres, about `tris` triangles in total) on a
+    10x10 ground quad under one point light, seen by a 45-degree pinhole camera.
+    Materials alternate glTF PBR (base colour, roughness, metallic) and
+    OpenMATERIAL conductors (complex IOR at the RGB wavelengths); the ground
+    uses material 0."""
+    rng = np.random.default_rng(seed)
+    sub, nu, nv = _tessellation_for(tris)
+    meshes, insts = [], []
+    for i in range(8):
+        if i % 2 == 0:
+            R = rng.uniform(0.5, 0.8)
+            p, n, f = torus(R, rng.uniform(0.15, 0.3), nu, nv)
+            m = Mesh(positions=p.astype(F32), normals=n.astype(F32), faces=f, material=i % n_materials,
+                     name=f"torus{i}")
+        else:
+            p, f = displaced_icosphere(sub, rng, amplitude=0.12)
+            p = (p * 0.7).astype(F32)
+            m = Mesh(positions=p, normals=None, faces=f, material=i % n_materials, name=f"blob{i}")
+        meshes.append(m)
+        M = np.eye(4)
+        M[:3, :3] = random_rotation(rng)
+        M[:3, 3] = (-3.0 + 2.0 * (i % 4), -0.2 + 0.3 * rng.uniform(), -4.0 - 2.2 * (i // 4))
+        insts.append(Instance(M.astype(F32), i))
+    qv = np.array([[-6, -1, 1], [6, -1, 1], [6, -1, -11], [-6, -1, -11]], dtype=F32)
+    qf = np.array([[0, 1, 2], [0, 2, 3]], dtype=np.uint32)
+    meshes.append(Mesh(positions=qv, normals=np.tile(np.array([0, 1, 0], dtype=F32), (4, 1)), faces=qf,
+                       material=0, name="ground"))
+    insts.append(Instance(np.eye(4, dtype=F32), 8))
+    mats = []
+    for i in range(n_materials):
+        if i % 2 == 0:
+            mats.append(Material(type=0, base_color=(float(rng.uniform(0.2, 0.9)), float(rng.uniform(0.2, 0.9)),
+                                                     float(rng.uniform(0.2, 0.9)), 1.0),
+                                 roughness=float(rng.uniform(0.2, 0.9)), metallic=float(rng.uniform(0.0, 1.0)),
+                                 name=f"pbr{i}"))
+        else:
+            mats.append(_om_conductor(tuple(rng.uniform(0.1, 4.0, 3)), tuple(rng.uniform(0.1, 4.0, 3)),
+                                      name=f"om{i}"))
+    light = Light(position=(2.0, 4.0, 0.0), intensity=(50.0, 50.0, 50.0))
+    focus = (height / 2.0) / math.tan(math.radians(22.5))
+    cam = camera_from_json(width, height, width / height, focus, 45.0, position=(0.0, 1.5, 4.0))
+    return Scene("materials", meshes, insts, mats, [light], None, cam, RenderSpec(spp, bounces, bounces, bounces))
+
+
+def material_variants(scene: Scene, n_sets: int, seed: int = 1) -> List[List[Material]]:
+    """Per-job material sets for a batched sweep: conductors get n, k in
+    U[0.1, 4] per RGB channel, PBR materials a roughness in U[0.02, 1] (other
+    fields as in the scene)."""
+    rng = np.random.default_rng(seed)
+    sets = []
+    for _ in range(n_sets):
+        row = []
+        for m in scene.materials:
+            if m.type == 1:
+                row.append(_om_conductor(tuple(rng.uniform(0.1, 4.0, 3)), tuple(rng.uniform(0.1, 4.0, 3)), m.name))
+            else:
+                row.append(dataclasses.replace(m, roughness=float(rng.uniform(0.02, 1.0))))
+        sets.append(row)
+    return sets
+
+
 def scene_mixed(width: int = 32, height: int = 32, spp: int = 8) -> Scene:
     """Parity scene covering every material branch of the reference: the
     OpenMATERIAL conductor, a rough PBR metal (specular GGX branch), a
