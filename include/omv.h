@@ -294,6 +294,33 @@ omv_status omv_render_batch(omv_scene* scene, int32_t num_jobs, const omv_job* j
 omv_status omv_batch_autotune(omv_scene* scene, int32_t num_jobs, const omv_job* jobs, const omv_params* params,
                               void* stream, int64_t* chosen_wave_paths);
 
+/* ------------------------------------------------------- differentiation --- */
+
+/* Parameters per material, in this order: base colour r, g, b, roughness and
+ * metallic (glTF PBR materials); complex IOR n at 650/510/440 nm and k at
+ * 650/510/440 nm (OpenMATERIAL conductors).  A material uses the slots of its
+ * type (PBR 5, OpenMATERIAL 6); the others stay zero. */
+#define OMV_MATERIAL_PARAMS 11
+
+/* Replaces the scene's materials (num_materials descriptors, as given to
+ * omv_scene_create, whose alpha-mask status may not change).  Geometry and
+ * acceleration structure are kept. */
+omv_status omv_scene_set_materials(omv_scene* scene, int32_t num_materials, const omv_material_desc* materials);
+
+/* Gradient of an image loss with respect to the material parameters by path
+ * replay: d_adjoint_rgb (DEVICE, width*height*3 floats) is dLoss/dImage for
+ * the normalised image (film sum / sample count); the paths of `params`
+ * (samples_per_pixel, seed, sample_offset, bounces) are replayed and
+ * d_grad (DEVICE, num_materials * OMV_MATERIAL_PARAMS floats, material order
+ * of the scene without the missing material) is ACCUMULATED into.  Sampled
+ * directions are held fixed (GGX-sampled vertices add the score of their
+ * half-vector density), so the result estimates the gradient of the expected
+ * image; luminance cutoffs are not differentiated.  At most 15 camera and 15
+ * light bounces and 16 materials.  Asynchronous on `stream` (NULL: the
+ * scene's stream).  The reference has no counterpart (it renders only). */
+omv_status omv_adjoint(omv_scene* scene, const omv_camera* camera, const omv_params* params,
+                       const float* d_adjoint_rgb, float* d_grad, void* stream);
+
 /* ----------------------------------------------------- rays / ID buffers --- */
 
 /* One closest-hit query (the reference's sceneIntersect, BDPTRenderer.cpp:75-102,

@@ -31,13 +31,13 @@ REPO_DIR = os.path.dirname(PKG_DIR)
 CSRC = os.path.join(PKG_DIR, "csrc")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "libomv.so")
-SOURCES = ["bvh_build.cu", "scene.cu", "render.cu", "capi.cu"]
-HEADERS = ["bvh_build.h", "omv_device.cuh", "omv_types.h", "scene.h", "trace.cuh"]
+SOURCES = ["bvh_build.cu", "scene.cu", "render.cu", "adjoint.cu", "capi.cu"]
+HEADERS = ["bvh_build.h", "omv_device.cuh", "omv_types.h", "scene.h", "trace.cuh", "shade.cuh", "dual.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
 # translation units whose device float math must round like the reference
 # (no implicit FMA contraction; explicit fmaf() calls in the traversal stay fused)
-NO_CONTRACT = {"render.cu", "scene.cu"}
+NO_CONTRACT = {"render.cu", "scene.cu", "adjoint.cu"}
 
 
 class OmvError(RuntimeError):
@@ -115,6 +115,8 @@ def lib():
                                    C.POINTER(capi.Stats)]
     L.omv_batch_autotune.argtypes = [vp, C.c_int32, C.POINTER(capi.Job), C.POINTER(capi.Params), vp,
                                      C.POINTER(C.c_int64)]
+    L.omv_scene_set_materials.argtypes = [vp, C.c_int32, C.POINTER(capi.MaterialDesc)]
+    L.omv_adjoint.argtypes = [vp, C.POINTER(capi.Camera), C.POINTER(capi.Params), vp, vp, vp]
     L.omv_trace_rays.argtypes = [vp, C.c_int64, capi.f32p, C.POINTER(capi.Hit)]
     L.omv_render_ids.argtypes = [vp, C.POINTER(capi.Camera), capi.f32p, C.c_uint64, C.POINTER(capi.Hit),
                                  C.POINTER(C.c_uint32)]
@@ -129,6 +131,7 @@ def lib():
     L.omv_struct_sizes.argtypes = [C.POINTER(C.c_int64), C.c_int32]
     for n in ("omv_scene_create", "omv_scene_destroy", "omv_scene_get_info", "omv_render", "omv_render_device",
               "omv_render_device_static", "omv_batch_set_materials", "omv_render_batch", "omv_batch_autotune",
+              "omv_scene_set_materials", "omv_adjoint",
               "omv_trace_rays", "omv_render_ids", "omv_brdf_eval_direct",
               "omv_brdf_sample_indirect", "omv_om_fresnel", "omv_camera_rays", "omv_env_radiance", "omv_struct_sizes"):
         getattr(L, n).restype = st

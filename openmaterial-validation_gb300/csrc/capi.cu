@@ -223,6 +223,26 @@ omv_status omv_batch_autotune(omv_scene* scene, int32_t num_jobs, const omv_job*
     });
 }
 
+omv_status omv_scene_set_materials(omv_scene* scene, int32_t num_materials, const omv_material_desc* materials)
+{
+    return guarded([&] {
+        check_scene(scene);
+        omv::set_scene_materials(*scene->h, num_materials, materials);
+    });
+}
+
+omv_status omv_adjoint(omv_scene* scene, const omv_camera* camera, const omv_params* params,
+                       const float* d_adjoint_rgb, float* d_grad, void* stream)
+{
+    return guarded([&] {
+        check_scene(scene);
+        check_camera(camera);
+        if (!params) throw omv::ArgError("params is NULL");
+        cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : scene->h->stream;
+        omv::adjoint_frame(*scene->h, *camera, *params, d_adjoint_rgb, d_grad, st);
+    });
+}
+
 omv_status omv_render(omv_scene* scene, const omv_camera* camera, const omv_params* params, float* image_rgba,
                       double* sum_rgb, double* sumsq_rgb, uint32_t* count, omv_stats* stats)
 {

@@ -338,10 +338,21 @@ __device__ __forceinline__ bool refract3(V3 I, V3 N, float eta, V3& R)
     return true;
 }
 
+// What bsdf_sample_indirect decided, for differentiating its weight with the
+// sampled direction held fixed: the evaluate kind (-1: zero weight), half
+// vector, branch probability and the normal it used.
+struct SampleInfo {
+    int kind;
+    V3 H, N;
+    float p;
+};
+
 // BSDFModel::sampleIndirect (BRDFModel.h:265-337) with the three uniforms
 // (branch, phi, radial) supplied; returns the weight, writes the direction.
-__device__ __forceinline__ V3 bsdf_sample_indirect(BsdfIn d, float u0, float u1, float u2, V3& O)
+__device__ __forceinline__ V3 bsdf_sample_indirect(BsdfIn d, float u0, float u1, float u2, V3& O,
+                                                   SampleInfo* info = nullptr)
 {
+    if (info) info->kind = -1;
     float VdotN = -dot(d.I, d.N);
     V3 binorm = cross(d.N, d.T);
     V3 b0 = d.T, b1 = binorm;
@@ -362,17 +373,20 @@ __device__ __forceinline__ V3 bsdf_sample_indirect(BsdfIn d, float u0, float u1,
             V3 H = normalize(to_basis(b0, b1, d.N, ggx_hemisphere(d.alpha * d.alpha, u1, u2)));
             if (refract3(d.I, H, eta, O) && dot(d.N, O) < 0.0f) {
                 O = normalize(O);
+                if (info) *info = SampleInfo{2, H, d.N, p};
                 return bsdf_evaluate(d.I, O, d.N, d.color, d.metal, d.alpha, 2, H, p);
             }
             return v3(0.0f, 0.0f, 0.0f);
         }
         O = normalize(to_basis(b0, b1, d.N, cosine_hemisphere(u1, u2)));
+        if (info) *info = SampleInfo{0, O, d.N, p};
         return bsdf_evaluate(d.I, O, d.N, d.color, d.metal, d.alpha, 0, O, p);
     }
     V3 H = normalize(to_basis(b0, b1, d.N, ggx_hemisphere(d.alpha * d.alpha, u1, u2)));
     O = reflect3(d.I, H);
     if (dot(d.N, O) > 0.0f) {
         O = normalize(O);
+        if (info) *info = SampleInfo{1, H, d.N, p};
         return bsdf_evaluate(d.I, O, d.N, d.color, d.metal, d.alpha, 1, H, p);
     }
     return v3(0.0f, 0.0f, 0.0f);

@@ -306,6 +306,23 @@ void set_material_sets(SceneHost& s, int num_sets, const omv_material_desc* desc
     s.num_mat_sets = num_sets;
 }
 
+void set_scene_materials(SceneHost& s, int num, const omv_material_desc* descs)
+{
+    if (num != s.num_materials - 1 || (num > 0 && !descs))
+        throw ArgError("omv_scene_set_materials needs the scene's number of materials");
+    std::vector<DevMaterial> mats(s.num_materials);
+    for (int i = 0; i < num; ++i) {
+        mats[i] = material_from_desc(descs[i]);
+        if (mats[i].masked != s.h_mats[i].masked)
+            throw ArgError("omv_scene_set_materials cannot change which materials are alpha-masked");
+    }
+    mats[num] = missing_material();
+    OMV_CUDA(cudaStreamSynchronize(s.stream));
+    OMV_CUDA(cudaMemcpy(const_cast<DevMaterial*>(s.dev.mats), mats.data(), sizeof(DevMaterial) * mats.size(),
+                        cudaMemcpyHostToDevice));
+    s.h_mats = mats;
+}
+
 SceneHost* scene_create(const omv_scene_desc& d, int device)
 {
     if (d.num_meshes < 0 || d.num_instances < 0 || d.num_materials < 0 || d.num_lights < 0)

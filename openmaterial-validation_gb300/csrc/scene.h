@@ -125,6 +125,12 @@ void render_batch(SceneHost& s, int num_jobs, const omv_job* jobs, const omv_par
 void autotune_batch(SceneHost& s, int num_jobs, const omv_job* jobs, const omv_params& p, cudaStream_t st,
                     int64_t* chosen);
 
+// replaces the scene's own materials (same count, same alpha-mask status)
+void set_scene_materials(SceneHost& s, int num, const omv_material_desc* descs);
+// path-replay gradient of an image loss with respect to the material parameters
+void adjoint_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, const float* d_adjoint, float* d_grad,
+                   cudaStream_t st);
+
 // render_frame on the fixed scratch array; makes no device allocation
 void render_frame_static(SceneHost& s, const omv_camera& cam, const omv_params& p, double* d_sum, double* d_sumsq,
                          uint32_t* d_count, cudaStream_t st);
