@@ -239,6 +239,91 @@ def run_batched(args, dev):
             "scene": f"{rs.info()['triangles']} triangles, 8 materials (4 PBR, 4 OpenMATERIAL conductors), point light, 6 bounces"}
 
 
+def run_adjoint(args, dev):
+    """Adjoint: 512x512 L2 loss against a 1024-spp target of a 100k-triangle
+    scene with 8 materials (4 PBR: base colour, roughness, metallic; 4
+    OpenMATERIAL conductors: n, k per RGB: 44 active parameters of 88 slots),
+    32 spp forward.  The path-replay gradient (forward + replay) is timed
+    against central differences (eps 1e-3, common random numbers: 2 renders per
+    parameter) at the same spp; both are compared with a 512-spp path-replay
+    reference gradient, and gradients/s are compared at equal RMSE (time grows
+    with the inverse square of the RMSE)."""
+    import numpy as np
+    import torch
+
+    S = importlib.import_module("openmaterial-validation_gb300.scenes")
+    diff = importlib.import_module("openmaterial-validation_gb300.diff")
+    spp = args.adjoint_spp
+    sc = S.scene_materials(512, 512, spp, tris=100_000, bounces=6)
+    P0 = diff.params_from_materials(sc.materials)
+    active = diff.active_mask(sc.materials)
+    Pt = P0.copy()
+    Pt[:, 0:3] = np.clip(Pt[:, 0:3] * 0.7 + 0.1, 0.05, 0.95)
+    Pt[:, 3] = np.clip(Pt[:, 3] * 0.8 + 0.1, 0.05, 0.95)
+    Pt[:, 4] = 1.0 - Pt[:, 4]
+    Pt[:, 5:11] = Pt[:, 5:11] * 0.8
+    Rt = diff.MaterialRenderer(sc, spp=1024, seed=99)
+    Rt.set_params(Pt)
+    s, c = Rt.render_sums(torch)
+    T = (s / c.unsqueeze(-1)).detach()
+    del Rt, s, c
+    R = diff.MaterialRenderer(sc, spp=spp, seed=1)
+
+    # the estimator can produce an infinite sample (so does the reference's):
+    # pixels whose target or image is not finite are left out of the loss
+    def l2(I):
+        ok = torch.isfinite(T) & torch.isfinite(I)
+        d = torch.where(ok, I - torch.where(ok, T, torch.zeros_like(T)), torch.zeros_like(I))
+        return (d ** 2).sum() / max(1, int(ok.sum()))
+
+    def ad_grad(renderer):
+        P = torch.tensor(P0, dtype=torch.float64, requires_grad=True)
+        L = l2(renderer.image(P))
+        L.backward()
+        return P.grad.detach().cpu().numpy()
+
+    def loss(Px):
+        R.set_params(Px)
+        s_, c_ = R.render_sums(torch)
+        return float(l2(s_ / c_.unsqueeze(-1)))
+
+    def fd_grad():
+        g = np.zeros_like(P0)
+        for i, k in zip(*np.nonzero(active)):
+            Pp, Pm = P0.copy(), P0.copy()
+            Pp[i, k] += 1e-3
+            Pm[i, k] -= 1e-3
+            g[i, k] = (loss(Pp) - loss(Pm)) / 2e-3
+        return g
+
+    ad_grad(R)  # warm-up
+    t0 = time.perf_counter()
+    g_ad = ad_grad(R)
+    t_ad = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    g_fd = fd_grad()
+    t_fd = time.perf_counter() - t0
+    Rref = diff.MaterialRenderer(sc, spp=512, seed=5)
+    g_ref = ad_grad(Rref)
+    exact = active.copy()
+    exact[:, 3] = False
+
+    def rmse(g, m):
+        return float(np.sqrt(np.mean((g[m] - g_ref[m]) ** 2)))
+
+    out = {"params": int(active.sum()), "slots": int(active.size), "spp": spp,
+           "adjoint_s": round(t_ad, 4), "fd_s": round(t_fd, 4), "fd_renders": int(2 * active.sum())}
+    for name, m in (("all", active), ("no_roughness", exact)):
+        ra, rf = rmse(g_ad, m), rmse(g_fd, m)
+        t_fd_eq = t_fd * max(1.0, (rf / ra) ** 2) if ra > 0 else t_fd
+        out[name] = {"rmse_adjoint": ra, "rmse_fd": rf, "adjoint_gradients_per_s": round(1.0 / t_ad, 3),
+                     "fd_gradients_per_s_at_equal_rmse": round(1.0 / t_fd_eq, 5),
+                     "speedup_at_equal_rmse": round(t_fd_eq / t_ad, 2)}
+    out["reference"] = "path-replay gradient at 512 spp, other seed"
+    out["timing"] = "host wall clock with device synchronisation"
+    return out
+
+
 def run_ours(args, scene, ws, rank, local):
     import numpy as np
     import torch
@@ -366,6 +451,8 @@ def run_ours(args, scene, ws, rank, local):
                 "gpu_launches": agg["kernel_launches"], "scene_build_ms": round(info["build_ms"], 1)}
         if ws == 1 and not args.no_batched:
             line["batched"] = run_batched(args, dev)
+        if ws == 1 and not args.no_adjoint:
+            line["adjoint"] = run_adjoint(args, dev)
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -385,6 +472,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched material sweep")
     ap.add_argument("--batch-jobs", type=int, default=256)
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-vs-finite-difference leg")
+    ap.add_argument("--adjoint-spp", type=int, default=32)
     args = ap.parse_args()
     ws, rank, local = _dist()
     if args.impl == "reference" and rank != 0:

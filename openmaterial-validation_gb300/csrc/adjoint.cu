@@ -122,6 +122,13 @@ __device__ __forceinline__ V3 eval_with_grad(const DevMaterial& M, const Surf& s
     return f;
 }
 
+// adds t to a gradient slot unless it is not finite: a degenerate path (an
+// infinite sample of the forward estimator) must not poison the sum
+__device__ __forceinline__ void add_finite(float& slot, float t)
+{
+    if (fabsf(t) <= kFltMax) slot += t;
+}
+
 // adds sum_c a[c] * g.d[c][i] to the material's parameter slots
 __device__ __forceinline__ void accumulate(float* acc, const DevMaterial& M, uint32_t mat, int nmat, V3 a,
                                            const LocalGrad& g)
@@ -132,16 +139,16 @@ __device__ __forceinline__ void accumulate(float* acc, const DevMaterial& M, uin
     if (M.type == kMatPbr) {
         const float rough = sqrtf(M.alpha);  // alpha = roughness^2
         for (int c = 0; c < 3; ++c) {
-            o[0] += av[c] * g.d[c][0];
-            o[1] += av[c] * g.d[c][1];
-            o[2] += av[c] * g.d[c][2];
-            o[3] += av[c] * g.d[c][3] * 2.0f * rough;
-            o[4] += av[c] * g.d[c][4];
+            add_finite(o[0], av[c] * g.d[c][0]);
+            add_finite(o[1], av[c] * g.d[c][1]);
+            add_finite(o[2], av[c] * g.d[c][2]);
+            add_finite(o[3], av[c] * g.d[c][3] * 2.0f * rough);
+            add_finite(o[4], av[c] * g.d[c][4]);
         }
     } else if (M.type == kMatOm) {
         for (int c = 0; c < 3; ++c) {
-            o[5 + c] += av[c] * g.d[c][c];
-            o[8 + c] += av[c] * g.d[c][3 + c];
+            add_finite(o[5 + c], av[c] * g.d[c][c]);
+            add_finite(o[8 + c], av[c] * g.d[c][3 + c]);
         }
     }
 }

@@ -175,7 +175,9 @@ template <int K>
 __device__ __forceinline__ Dual<K> d_smith_g1(float c, Dual<K> alpha)
 {
     if (!(alpha.v > 0.0f || c < 0.99f)) return dconst<K>(1.0f);
-    const Dual<K> a = c / (alpha * sqrtf(1.0f - c * c));
+    const float s = sqrtf(1.0f - c * c);
+    if (!(s > 0.0f)) return dconst<K>(1.0f);  // c = 1: the float code's limit (a infinite, G1 = 1)
+    const Dual<K> a = c / (alpha * s);
     const Dual<K> lam = (dsqrt(1.0f + 1.0f / (a * a)) - 1.0f) * 0.5f;
     return 1.0f / (1.0f + lam);
 }
