@@ -83,6 +83,11 @@ class MaterialRenderer:
         self.materials = list(scene.materials)
         self._keep: list = []
 
+    def set_seeds(self, seed: int, adjoint_seed: int) -> None:
+        """Random streams of the next forward render and of the replay."""
+        self.params.seed = seed
+        self.adj_params.seed = adjoint_seed
+
     def set_params(self, P) -> None:
         mats = materials_from_params(self.materials, P)
         keep: list = []

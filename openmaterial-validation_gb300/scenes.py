@@ -387,13 +387,14 @@ def _tessellation_for(tris: int):
 
 
 def scene_materials(width: int = 512, height: int = 512, spp: int = 32, tris: int = 100_000,
-                    n_materials: int = 8, seed: int = 0, bounces: int = 6) -> Scene:
+                    n_materials: int = 8, seed: int = 0, bounces: int = 6, sky: bool = False) -> Scene:
     """Material-study scene (batched sweeps, adjoint, inverse fits): 8 objects
     (tori and displaced icospheres, about `tris` triangles in total) on a
     10x10 ground quad under one point light, seen by a 45-degree pinhole camera.
     Materials alternate glTF PBR (base colour, roughness, metallic) and
     OpenMATERIAL conductors (complex IOR at the RGB wavelengths); the ground
-    uses material 0."""
+    uses material 0.  With `sky`, a 512x256 log-normal sky (no sun lobes) lights
+    the scene as well, so the mirror-like conductors show something to fit."""
     rng = np.random.default_rng(seed)
     sub, nu, nv = _tessellation_for(tris)
     meshes, insts = [], []
@@ -430,7 +431,11 @@ def scene_materials(width: int = 512, height: int = 512, spp: int = 32, tris: in
     light = Light(position=(2.0, 4.0, 0.0), intensity=(50.0, 50.0, 50.0))
     focus = (height / 2.0) / math.tan(math.radians(22.5))
     cam = camera_from_json(width, height, width / height, focus, 45.0, position=(0.0, 1.5, 4.0))
-    return Scene("materials", meshes, insts, mats, [light], None, cam, RenderSpec(spp, bounces, bounces, bounces))
+    hdri = None
+    if sky:
+        R = np.array([[1, 0, 0], [0, 0, 1], [0, -1, 0]], dtype=F32)  # main.cpp:401-405 (y-up)
+        hdri = Hdri(make_sky(512, 256, np.random.default_rng(seed + 7), suns=False), R, float(F32(math.pi)))
+    return Scene("materials", meshes, insts, mats, [light], hdri, cam, RenderSpec(spp, bounces, bounces, bounces))
 
 
 def material_variants(scene: Scene, n_sets: int, seed: int = 1) -> List[List[Material]]:
