@@ -351,6 +351,51 @@ omv_status omv_trace_rays(omv_scene* scene, int64_t n, const float* rays, omv_hi
 omv_status omv_render_ids(omv_scene* scene, const omv_camera* camera, const float* jitter,
                           uint64_t seed, omv_hit* hits, uint32_t* global_prim);
 
+/* --------------------------------------------------- image development --- */
+
+/* The tail of a render in the reference's main (main.cpp:505-521) on device
+ * buffers: PinholeCamera::getImpression after stop() (PinholeCamera.cpp:70-78),
+ * gammaCorrection (ToneMapping.cpp:24-53), saveImage's 8-bit conversion
+ * (main.cpp:92) and SimpleDenoiserMedian (Denoiser.h:24-64).  Images are
+ * row-major RGBA float (16 bytes per pixel) or RGBA uint8 in DEVICE memory of
+ * the current device; `stream` is a cudaStream_t (NULL: the legacy default
+ * stream).  Asynchronous; nothing is allocated.
+ *
+ * omv_develop: one pass over a film (sums and counts as omv_render_device
+ * accumulates them): the normalised linear image (rgb / count, alpha 1), the
+ * gamma-corrected image gammaCorrection(img, W, H, A, gamma) gives, and its
+ * 8-bit rgba (rows flipped when `flip`, the order stb writes with
+ * flipVerticallyOnWrite(true)).  Any of the three outputs may be NULL.
+ * The reference's call is gammaCorrection(img, W, H, 1.0f, rparams.gamma),
+ * gamma 0.5 by default (RendererParameters.h:95). */
+omv_status omv_develop(const double* d_sum_rgb, const uint32_t* d_count, int32_t width, int32_t height, float A,
+                       float gamma, float* d_linear_rgba, float* d_tonemapped_rgba, uint8_t* d_rgba8, int32_t flip,
+                       void* stream);
+
+/* gammaCorrection (ToneMapping.cpp:24-53) in place on `pixels` RGBA pixels. */
+omv_status omv_tonemap(float* d_rgba, int64_t pixels, float A, float gamma, void* stream);
+
+/* SimpleDenoiserMedian<half_size> (Denoiser.h:24-64): the per-channel median
+ * of the (2 half_size + 1)^2 window for every pixel at least half_size from
+ * each edge (alpha 1 there); border pixels are copied unchanged.  The reference
+ * filters in place through a temporary image; here input and output must be
+ * distinct buffers.  half_size 1 (the reference's), 2 or 3. */
+omv_status omv_denoise_median(const float* d_in_rgba, float* d_out_rgba, int32_t width, int32_t height,
+                              int32_t half_size, void* stream);
+
+/* saveImage's conversion (main.cpp:92): unsigned char(255 f) per channel of an
+ * image in [0, 1] (values outside are clamped), rows flipped when `flip`. */
+omv_status omv_rgba8(const float* d_rgba, uint8_t* d_out, int32_t width, int32_t height, int32_t flip,
+                     void* stream);
+
+/* saveImage (main.cpp:86-120) of a HOST RGBA float image with
+ * ImageSaver::flipVerticallyOnWrite(true): by extension, .pfm (ImageSaver::savePfm,
+ * the float rgb as stored) or .png / .bmp / .tga (8 bits per channel, the
+ * buffer's last row at the top).  The reference writes those three through
+ * stb_image_write; these files hold the same pixels but are not compressed.
+ * .jpg is not written (OMV_ERR_INVALID_ARGUMENT). */
+omv_status omv_save_image(const char* path, const float* rgba, int32_t width, int32_t height);
+
 /* ------------------------------------------------------ kernel test hooks --- */
 
 /* Device evaluation of the material model on host SoA inputs, for parity tests

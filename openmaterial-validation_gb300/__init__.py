@@ -31,13 +31,13 @@ REPO_DIR = os.path.dirname(PKG_DIR)
 CSRC = os.path.join(PKG_DIR, "csrc")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "libomv.so")
-SOURCES = ["bvh_build.cu", "scene.cu", "render.cu", "adjoint.cu", "capi.cu"]
+SOURCES = ["bvh_build.cu", "scene.cu", "render.cu", "adjoint.cu", "post.cu", "capi.cu"]
 HEADERS = ["bvh_build.h", "omv_device.cuh", "omv_types.h", "scene.h", "trace.cuh", "shade.cuh", "dual.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
 # translation units whose device float math must round like the reference
 # (no implicit FMA contraction; explicit fmaf() calls in the traversal stay fused)
-NO_CONTRACT = {"render.cu", "scene.cu", "adjoint.cu"}
+NO_CONTRACT = {"render.cu", "scene.cu", "adjoint.cu", "post.cu"}
 
 
 class OmvError(RuntimeError):
@@ -124,6 +124,11 @@ def lib():
         getattr(L, n).argtypes = [C.c_int64, capi.f32p, capi.f32p]
     L.omv_camera_rays.argtypes = [C.POINTER(capi.Camera), capi.f32p, capi.f32p]
     L.omv_env_radiance.argtypes = [vp, C.c_int64, capi.f32p, capi.f32p]
+    L.omv_develop.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_float, C.c_float, vp, vp, vp, C.c_int32, vp]
+    L.omv_tonemap.argtypes = [vp, C.c_int64, C.c_float, C.c_float, vp]
+    L.omv_denoise_median.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_int32, vp]
+    L.omv_rgba8.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_int32, vp]
+    L.omv_save_image.argtypes = [C.c_char_p, capi.f32p, C.c_int32, C.c_int32]
     L.omv_last_error.restype = C.c_char_p
     L.omv_version.restype = C.c_char_p
     L.omv_params_default.argtypes = [C.POINTER(capi.Params)]
@@ -133,7 +138,8 @@ def lib():
               "omv_render_device_static", "omv_batch_set_materials", "omv_render_batch", "omv_batch_autotune",
               "omv_scene_set_materials", "omv_adjoint",
               "omv_trace_rays", "omv_render_ids", "omv_brdf_eval_direct",
-              "omv_brdf_sample_indirect", "omv_om_fresnel", "omv_camera_rays", "omv_env_radiance", "omv_struct_sizes"):
+              "omv_brdf_sample_indirect", "omv_om_fresnel", "omv_camera_rays", "omv_env_radiance", "omv_struct_sizes",
+              "omv_develop", "omv_tonemap", "omv_denoise_median", "omv_rgba8", "omv_save_image"):
         getattr(L, n).restype = st
     _lib = L
     return L

@@ -383,4 +383,39 @@ omv_status omv_camera_rays(const omv_camera* camera, const float* jitter, float*
     });
 }
 
+/* ------------------------------------------------------- image development */
+
+omv_status omv_develop(const double* d_sum_rgb, const uint32_t* d_count, int32_t width, int32_t height, float A,
+                       float gamma, float* d_linear_rgba, float* d_tonemapped_rgba, uint8_t* d_rgba8, int32_t flip,
+                       void* stream)
+{
+    return guarded([&] {
+        omv::develop_film(d_sum_rgb, d_count, width, height, A, gamma, d_linear_rgba, d_tonemapped_rgba, d_rgba8,
+                          flip != 0, static_cast<cudaStream_t>(stream));
+    });
+}
+
+omv_status omv_tonemap(float* d_rgba, int64_t pixels, float A, float gamma, void* stream)
+{
+    return guarded([&] { omv::tonemap(d_rgba, pixels, A, gamma, static_cast<cudaStream_t>(stream)); });
+}
+
+omv_status omv_denoise_median(const float* d_in_rgba, float* d_out_rgba, int32_t width, int32_t height,
+                              int32_t half_size, void* stream)
+{
+    return guarded([&] {
+        omv::denoise_median(d_in_rgba, d_out_rgba, width, height, half_size, static_cast<cudaStream_t>(stream));
+    });
+}
+
+omv_status omv_rgba8(const float* d_rgba, uint8_t* d_out, int32_t width, int32_t height, int32_t flip, void* stream)
+{
+    return guarded([&] { omv::rgba8(d_rgba, d_out, width, height, flip != 0, static_cast<cudaStream_t>(stream)); });
+}
+
+omv_status omv_save_image(const char* path, const float* rgba, int32_t width, int32_t height)
+{
+    return guarded([&] { omv::save_image(path, rgba, width, height); });
+}
+
 }  // extern "C"

@@ -142,6 +142,14 @@ void trace_rays(SceneHost& s, int64_t n, const float* d_rays, omv_hit* d_hits, c
 void env_radiance(SceneHost& s, int64_t n, const float* d_dirs, float* d_rgb, cudaStream_t st);
 
 // kernel-level hooks (no scene)
+// image development and writers (post.cu)
+void develop_film(const double* d_sum, const uint32_t* d_count, int w, int h, float A, float gamma, float* d_linear,
+                  float* d_toned, uint8_t* d_rgba8, bool flip, cudaStream_t st);
+void tonemap(float* d_rgba, int64_t pixels, float A, float gamma, cudaStream_t st);
+void denoise_median(const float* d_in, float* d_out, int w, int h, int half, cudaStream_t st);
+void rgba8(const float* d_in, uint8_t* d_out, int w, int h, bool flip, cudaStream_t st);
+void save_image(const char* path, const float* rgba, int w, int h);
+
 void hook_eval_direct(int64_t n, const float* d_in, float* d_out, cudaStream_t st);
 void hook_sample_indirect(int64_t n, const float* d_in, float* d_out, cudaStream_t st);
 void hook_om_fresnel(int64_t n, const float* d_in, float* d_out, cudaStream_t st);

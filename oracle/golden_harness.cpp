@@ -17,7 +17,13 @@
  *   golden_harness camera props W H seed out   PinholeCamera::getRay (PinholeCamera.cpp:80)
  *       out: halfW halfH focus, then 6 floats/pixel (row-major) from one RandomSampler(seed)
  *   golden_harness mt     seed n out      RandomSampler::rand (RandomSampler.h:59)
+ *   golden_harness tonemap W H gamma in out   gammaCorrection(img, W, H, 1, gamma) (ToneMapping.cpp:24)
+ *       in/out: W*H*4 floats (rgba, row-major)
+ *   golden_harness median  W H in out     SimpleDenoiserMedian<1> (Denoiser.h:24); in/out as tonemap
+ *   golden_harness rgba8   W H in out     saveImage's conversion (main.cpp:92): unsigned char(255 f),
+ *       out: W*H*4 bytes
  */
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -29,6 +35,8 @@
 #include "OpenMaterial.h"
 #include "PinholeCamera.h"
 #include "RandomSampler.h"
+#include "ToneMapping.h"
+#include "Denoiser.h"
 #include "materials/AssetMaterial.h"
 #include "materials/AssetMaterialIor.h"
 
@@ -164,6 +172,31 @@ int main(int argc, char** argv)
         long n = std::atol(argv[3]);
         for (long i = 0; i < n; ++i) out.push_back(rs.rand());
         write_floats(argv[4], out);
+    } else if ((mode == "tonemap" && argc == 7) || ((mode == "median" || mode == "rgba8") && argc == 6)) {
+        const int W = std::atoi(argv[2]), H = std::atoi(argv[3]);
+        const bool tm = mode == "tonemap";
+        auto img = read_floats(argv[tm ? 5 : 4]);
+        if (img.size() != (size_t)4 * W * H) {
+            std::fprintf(stderr, "image size mismatch\n");
+            return 1;
+        }
+        const char* dst = argv[tm ? 6 : 5];
+        auto px = reinterpret_cast<fvec4*>(img.data());
+        if (tm) {
+            gammaCorrection(px, W, H, 1.0f, (float)std::atof(argv[4]));
+        } else if (mode == "median") {
+            SimpleDenoiserMedian<1>(px, W, H);
+        } else {
+            std::vector<unsigned char> q(img.size());
+            std::transform(img.begin(), img.end(), q.begin(), [](float f) { return static_cast<unsigned char>(255.0f * f); });
+            FILE* f = std::fopen(dst, "wb");
+            if (!f) return 2;
+            std::fwrite(q.data(), 1, q.size(), f);
+            std::fclose(f);
+            return 0;
+        }
+        write_floats(dst, img);
+        return 0;
     } else {
         std::fprintf(stderr, "bad arguments\n");
         return 1;

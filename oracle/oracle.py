@@ -1,7 +1,7 @@
 """ORACLE -- test infrastructure only.
 
 ctypes wrapper of liboracle.so, the C restatement of the reference renderer's
-hot path (oc_render.c / oc_bvh.c).  Used by the tests as the checker, by
+hot path (oc_render.c / oc_bvh.c) and of its image post-processing (oc_post.c).  Used by the tests as the checker, by
 __graft_entry__.smoke() as the checker and by bench.py as the timed CPU
 reference; never by the product path.
 """
@@ -35,7 +35,7 @@ def build(force: bool = False) -> str:
 
 def _stale() -> bool:
     t = os.path.getmtime(LIB_PATH)
-    for f in ("oc_render.c", "oc_bvh.c", "oc_core.h", "oc_bvh.h", "oc_render.h"):
+    for f in ("oc_render.c", "oc_bvh.c", "oc_post.c", "oc_core.h", "oc_bvh.h", "oc_render.h"):
         if os.path.getmtime(os.path.join(HERE, f)) > t:
             return True
     return os.path.getmtime(os.path.join(ROOT, "include", "omv.h")) > t
@@ -67,6 +67,9 @@ def lib():
                                          C.POINTER(C.c_int32)]
         L.oc_scene_mesh_vertices.argtypes = [vp, C.c_int32, capi.f32p]
         L.oc_scene_normal_matrix.argtypes = [vp, C.c_int32, capi.f32p]
+        L.oc_tonemap.argtypes = [capi.f32p, C.c_int64, C.c_float, C.c_float]
+        L.oc_median.argtypes = [capi.f32p, C.c_int, C.c_int, C.c_int]
+        L.oc_rgba8.argtypes = [capi.f32p, C.c_int64, C.POINTER(C.c_uint8)]
         _lib = L
     return _lib
 
@@ -183,3 +186,25 @@ def mt_uniforms(seed: int, n: int) -> np.ndarray:
 def ior_lookup(table: np.ndarray, wl: float) -> float:
     t = np.ascontiguousarray(table, dtype=np.float32)
     return float(lib().oc_ior_lookup(capi.fptr(t), len(t), wl))
+
+
+def tonemap(img: np.ndarray, gamma: float, A: float = 1.0) -> np.ndarray:
+    """gammaCorrection (ToneMapping.cpp:24) of an (H, W, 4) float image, returned as a copy."""
+    out = np.array(img, dtype=np.float32, order="C", copy=True)
+    lib().oc_tonemap(capi.fptr(out), out.size // 4, A, gamma)
+    return out
+
+
+def median(img: np.ndarray, half: int = 1) -> np.ndarray:
+    """SimpleDenoiserMedian<half> (Denoiser.h:24) of an (H, W, 4) float image, as a copy."""
+    out = np.array(img, dtype=np.float32, order="C", copy=True)
+    lib().oc_median(capi.fptr(out), out.shape[1], out.shape[0], half)
+    return out
+
+
+def rgba8(img: np.ndarray) -> np.ndarray:
+    """saveImage's conversion (main.cpp:92): unsigned char(255 f) per channel."""
+    x = np.ascontiguousarray(img, dtype=np.float32)
+    out = np.zeros(x.shape, dtype=np.uint8)
+    lib().oc_rgba8(capi.fptr(x), x.size, out.ctypes.data_as(C.POINTER(C.c_uint8)))
+    return out

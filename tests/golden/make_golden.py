@@ -18,6 +18,8 @@ Fixtures (numpy .npz):
                     matrices, material ids, lights) dumped after commitScene
   film_<s>.npz      linear film (PinholeCamera after stop) of a -C 1 render + ray count
   ids_c1_64.npz     primary rays and hits of the false-colour (-F mid) pass
+  post.npz          gammaCorrection (two gammas), SimpleDenoiserMedian<1> and
+                    saveImage's 8-bit conversion on a seeded 23x37 HDR image
 """
 from __future__ import annotations
 
@@ -267,8 +269,32 @@ def gen_ids(tmp):
                         prim=u[:, 3], u=g[:, 0], v=g[:, 1], t=g[:, 2])
 
 
+def gen_post(tmp):
+    rng = np.random.default_rng(9)
+    W, H = 23, 37
+    img = rng.lognormal(-1.5, 1.5, size=(H, W, 4)).astype(np.float32)
+    img[rng.random((H, W)) < 0.08] = 0.0                       # black pixels: l = 0
+    img[rng.random((H, W)) < 0.04, :3] = np.float32(1e-8)       # below FLT_EPSILON
+    img[rng.random((H, W)) < 0.05] *= np.float32(40.0)          # fireflies, clamped
+    img[:4, :4, :3] = np.floor(img[:4, :4, :3] * 4) / 4         # ties in the median windows
+    src = f32file(tmp, "post.in", img)
+    out = {"image": img}
+    for name, g in (("tonemap_0.5", 0.5), ("tonemap_0.4545", 0.4545)):
+        o = os.path.join(tmp, name)
+        harness("tonemap", W, H, g, src, o)
+        out[name] = np.fromfile(o, dtype=np.float32).reshape(H, W, 4)
+    tm = f32file(tmp, "post.tm", out["tonemap_0.5"])
+    o = os.path.join(tmp, "post.med")
+    harness("median", W, H, tm, o)
+    out["median"] = np.fromfile(o, dtype=np.float32).reshape(H, W, 4)
+    o = os.path.join(tmp, "post.u8")
+    harness("rgba8", W, H, tm, o)
+    out["rgba8"] = np.fromfile(o, dtype=np.uint8).reshape(H, W, 4)
+    np.savez_compressed(os.path.join(HERE, "post.npz"), **out)
+
+
 GENS = {"mt": gen_mt, "brdf": gen_brdf, "om": gen_om, "ior": gen_ior, "env": gen_env, "camera": gen_camera,
-        "films": gen_films, "ids": gen_ids}
+        "films": gen_films, "ids": gen_ids, "post": gen_post}
 
 
 def main():

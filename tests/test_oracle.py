@@ -161,3 +161,15 @@ def test_live_reference_full_c1_bit_exact(oracle, scenes, tmp_path):
     assert np.array_equal(hits["inst"] != 0xFFFFFFFF, hit)
     assert np.array_equal(hits["geom"][hit], u[hit, 1])
     assert np.array_equal(hits["prim"][hit], u[hit, 3])
+
+
+def test_post_processing_matches_reference(oracle):
+    """gammaCorrection at two gammas, SimpleDenoiserMedian<1> and the 8-bit
+    conversion of saveImage, bit for bit on the reference's outputs."""
+    g = golden("post")
+    for name, gamma in (("tonemap_0.5", 0.5), ("tonemap_0.4545", 0.4545)):
+        y = oracle.tonemap(g["image"], gamma)
+        assert np.array_equal(y.view(np.uint32), g[name].view(np.uint32)), name
+    m = oracle.median(g["tonemap_0.5"], 1)
+    assert np.array_equal(m.view(np.uint32), g["median"].view(np.uint32))
+    assert np.array_equal(oracle.rgba8(g["tonemap_0.5"]), g["rgba8"])
