@@ -225,8 +225,10 @@ def run_batched(args, dev):
     zero()
     t_batch = timed(lambda: br.render(jobs, graph=True))
     # shadow-ray contributions reach a path's radiance through FP32 atomics, whose
-    # order varies from run to run: sums agree to FP32 rounding, counts exactly
-    match = all(bool((f[2] == c).all()) and float((f[0] - r).abs().max()) <= 1e-6 * max(1e-30, float(r.abs().max()))
+    # order varies from run to run: a path's radiance is an FP32 sum of up to
+    # (light bounces + 1) x camera bounces terms, so sums agree to ~50 FP32
+    # roundings of the largest pixel, counts exactly
+    match = all(bool((f[2] == c).all()) and float((f[0] - r).abs().max()) <= 3e-6 * max(1e-30, float(r.abs().max()))
                 for f, r, c in zip(films, ref_sum, ref_cnt))
     del films, ref_sum, ref_cnt
     torch.cuda.empty_cache()
@@ -237,6 +239,77 @@ def run_batched(args, dev):
             "timing": "host wall clock with device synchronisation, one pass over all jobs",
             "equal_rmse": "same estimator, jobs and spp: identical films up to summation order",
             "scene": f"{rs.info()['triangles']} triangles, 8 materials (4 PBR, 4 OpenMATERIAL conductors), point light, 6 bounces"}
+
+
+def run_post(args, dev, film, count, W, H, flush):
+    """Image development of the frame just rendered (the reference main's tail,
+    main.cpp:505-521): omv_develop (film -> normalised -> gamma 0.5 -> 8-bit,
+    flipped) and the 3x3 median, each timed alone with CUDA events on the
+    launching stream, L2 flushed before every launch.  Algorithmic bytes per
+    pixel: develop 24 + 4 read, 16 + 16 + 4 written; median 16 read, 16 written.
+    CPU side: the oracle's gamma correction and median of the same image, one
+    thread (the reference runs both single-threaded)."""
+    import numpy as np
+    import torch
+
+    omv = importlib.import_module("openmaterial-validation_gb300")
+    L = omv.lib()
+    npix = W * H
+    lin = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
+    toned = torch.empty_like(lin)
+    med = torch.empty_like(lin)
+    u8 = torch.empty((H, W, 4), dtype=torch.uint8, device=dev)
+    st = torch.cuda.current_stream(dev)
+    sp = C.c_void_p(st.cuda_stream)
+
+    def develop():
+        omv.check(L.omv_develop(C.c_void_p(film.data_ptr()), C.c_void_p(count.data_ptr()), W, H, 1.0, 0.5,
+                                C.c_void_p(lin.data_ptr()), C.c_void_p(toned.data_ptr()), C.c_void_p(u8.data_ptr()),
+                                1, sp))
+
+    def median():
+        omv.check(L.omv_denoise_median(C.c_void_p(toned.data_ptr()), C.c_void_p(med.data_ptr()), W, H, 1, sp))
+
+    def timed(fn, reps):
+        for _ in range(3):
+            fn()
+        ms = []
+        for _ in range(reps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            fn()
+            e1.record(st)
+            torch.cuda.synchronize(dev)
+            ms.append(e0.elapsed_time(e1))
+        return statistics.median(ms)
+
+    hbm, kind = _peaks()
+    reps = max(5, args.steps * 4)
+    out = {"image": f"{W}x{H}", "l2": "flushed by a 256 MiB write before each launch", "peak_gbs": hbm,
+           "peak_source": kind}
+    for name, fn, bpp in (("develop", develop, 64), ("median3", median, 32)):
+        t = timed(fn, reps)
+        gbs = npix * bpp / (t / 1e3) / 1e9
+        out[name] = {"ms": round(t, 4), "bytes_per_pixel": bpp, "achieved_gbs": round(gbs, 1),
+                     "frac": round(gbs / hbm, 4), "mpix_per_s": round(npix / (t / 1e3) / 1e6, 1)}
+    if not args.no_cpu_baseline:
+        import oracle
+
+        oracle.build()
+        img = lin.cpu().numpy()
+        t0 = time.perf_counter()
+        tm = oracle.tonemap(img, 0.5)
+        t1 = time.perf_counter()
+        oracle.median(tm, 1)
+        t2 = time.perf_counter()
+        out["cpu_baseline"] = {"kind": "port", "cores": 1, "gamma_ms": round((t1 - t0) * 1e3, 2),
+                               "median_ms": round((t2 - t1) * 1e3, 2),
+                               "sample": f"the whole {W}x{H} image"}
+        # parity on the benchmark frame itself
+        out["median_matches_oracle"] = bool(np.array_equal(med.cpu().numpy(), oracle.median(toned.cpu().numpy(), 1)))
+    return out
 
 
 def run_adjoint(args, dev):
@@ -449,6 +522,8 @@ def run_ours(args, scene, ws, rank, local):
                 "mrays_per_s": round(rays / (max_ms / 1e3) / 1e6, 4), "film_counts_ok": cnt_ok,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clock,
                 "gpu_launches": agg["kernel_launches"], "scene_build_ms": round(info["build_ms"], 1)}
+        if ws == 1 and not args.no_post:
+            line["post"] = run_post(args, dev, film, count, W, H, flush)
         if ws == 1 and not args.no_batched:
             line["batched"] = run_batched(args, dev)
         if ws == 1 and not args.no_adjoint:
@@ -471,6 +546,7 @@ def main():
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched material sweep")
+    ap.add_argument("--no-post", action="store_true", help="skip the image development leg")
     ap.add_argument("--batch-jobs", type=int, default=256)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-vs-finite-difference leg")
     ap.add_argument("--adjoint-spp", type=int, default=32)

@@ -351,6 +351,61 @@ omv_status omv_trace_rays(omv_scene* scene, int64_t n, const float* rays, omv_hi
 omv_status omv_render_ids(omv_scene* scene, const omv_camera* camera, const float* jitter,
                           uint64_t seed, omv_hit* hits, uint32_t* global_prim);
 
+/* ------------------------------------------------ false-colour validation --- */
+
+/* Subjects of the FC_VALIDATION build's -F option (FCSubject.h:189-470, chosen
+ * by name in RenderScene::setFalseColorSubject, RenderScene.cpp:130-146).  An
+ * unknown name is the EmptySubject (black). */
+enum {
+    OMV_FC_EMPTY = 0,
+    OMV_FC_PID = 1, /* global primitive id, hashed colour */
+    OMV_FC_GID = 2, /* mesh (geometry) id, hashed colour */
+    OMV_FC_MID = 3, /* material id: (0, G, B) of its hashed colour; missing material pink */
+    OMV_FC_MMP = 4, /* PBR metallic factor: white -> blue */
+    OMV_FC_RMP = 5, /* PBR roughness factor: white -> green */
+    OMV_FC_MD = 6,  /* relative mesh density (log of 1/area between the scene's extremes): white -> red */
+    OMV_FC_SG = 7,  /* pointwise surface gradient (vertex normals vs the face normal): 1 - g grey */
+    OMV_FC_MN = 8,  /* material kind: OpenMATERIAL green, PBR blue, missing pink */
+    OMV_FC_IN = 9   /* inverted normal (ray direction along the face normal): red, else green */
+};
+
+/* Subject code of an -F name ("pid", "gid", "mid", "mmp", "rmp", "md", "sg",
+ * "mn", "in"); OMV_FC_EMPTY for any other name, like fcSetSubject
+ * (FCHandler.cpp:82-90). */
+int32_t omv_fc_subject_from_name(const char* name);
+
+/* The false-colour pass (main.cpp:261-270 with -F): one jittered primary ray
+ * per pixel, the hit material paints the subject's argument
+ * (PhysicallyBasedMaterial.cpp:202-240, OpenMaterial.cpp:165-210,
+ * DiffuseColorMaterial.cpp:49-89) and the colour is the pixel's value
+ * (BDPTRenderer.cpp:165-168); misses are black.
+ *   uniforms  HOST, 4 floats per pixel: jitter dx+.5, dy+.5 and the two
+ *             uniform-hemisphere draws a missing-material hit consumes
+ *             (RenderMaterial.cpp:51-58); NULL: Philox keyed by `seed`
+ *   palette   HOST 0xRRGGBB per category for pid/gid/mid (the reference
+ *             draws them from an entropy-seeded generator, FCSubject.h:126-135);
+ *             ids at or beyond palette_size paint black, as in the reference
+ * Outputs (HOST, any may be NULL): image_rgba W*H*4 floats (alpha 1), args W*H
+ * (the 4 bytes of GenericFCArgument: enumerator, clamped float bits, name
+ * bytes or 0/1; 0 on a miss), hits W*H omv_hit.  The reference then applies
+ * gammaCorrection to the image (omv_develop / omv_tonemap). */
+omv_status omv_render_fc(omv_scene* scene, const omv_camera* camera, int32_t subject, const float* uniforms,
+                         uint64_t seed, const uint32_t* palette, int32_t palette_size, float* image_rgba,
+                         uint32_t* args, omv_hit* hits);
+
+/* World bounding box of the scene's valid instances (every vertex of each
+ * instanced mesh through its instance transform): AssetGeometry::getBBox
+ * (AssetGeometry.cpp:230-236, Node.h:132-166, Mesh.cpp:56-65) for a scene
+ * flattened without the CLI's centring transform. */
+omv_status omv_scene_bounds(omv_scene* scene, float lo[3], float hi[3]);
+
+/* The light-box views (-V, main.cpp:434-458): for each of the 8 corners p of
+ * the box [lo, hi] (BoundingBox::getCorners order), a camera at 2p - C looking
+ * at the centre C with up (0, 1, 0), and the default intrinsics
+ * (adjustToResolution, setYFoV(60), PinholeCamera.cpp:156-174).  Host only. */
+omv_status omv_lightbox_cameras(const float lo[3], const float hi[3], int32_t width, int32_t height,
+                                omv_camera cameras[8]);
+
 /* --------------------------------------------------- image development --- */
 
 /* The tail of a render in the reference's main (main.cpp:505-521) on device

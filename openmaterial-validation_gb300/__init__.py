@@ -31,13 +31,13 @@ REPO_DIR = os.path.dirname(PKG_DIR)
 CSRC = os.path.join(PKG_DIR, "csrc")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "libomv.so")
-SOURCES = ["bvh_build.cu", "scene.cu", "render.cu", "adjoint.cu", "post.cu", "capi.cu"]
+SOURCES = ["bvh_build.cu", "scene.cu", "render.cu", "adjoint.cu", "fc.cu", "post.cu", "capi.cu"]
 HEADERS = ["bvh_build.h", "omv_device.cuh", "omv_types.h", "scene.h", "trace.cuh", "shade.cuh", "dual.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
 # translation units whose device float math must round like the reference
 # (no implicit FMA contraction; explicit fmaf() calls in the traversal stay fused)
-NO_CONTRACT = {"render.cu", "scene.cu", "adjoint.cu", "post.cu"}
+NO_CONTRACT = {"render.cu", "scene.cu", "adjoint.cu", "fc.cu", "post.cu"}
 
 
 class OmvError(RuntimeError):
@@ -124,6 +124,13 @@ def lib():
         getattr(L, n).argtypes = [C.c_int64, capi.f32p, capi.f32p]
     L.omv_camera_rays.argtypes = [C.POINTER(capi.Camera), capi.f32p, capi.f32p]
     L.omv_env_radiance.argtypes = [vp, C.c_int64, capi.f32p, capi.f32p]
+    L.omv_fc_subject_from_name.argtypes = [C.c_char_p]
+    L.omv_fc_subject_from_name.restype = C.c_int32
+    L.omv_render_fc.argtypes = [vp, C.POINTER(capi.Camera), C.c_int32, capi.f32p, C.c_uint64,
+                                C.POINTER(C.c_uint32), C.c_int32, capi.f32p, C.POINTER(C.c_uint32),
+                                C.POINTER(capi.Hit)]
+    L.omv_scene_bounds.argtypes = [vp, capi.f32p, capi.f32p]
+    L.omv_lightbox_cameras.argtypes = [capi.f32p, capi.f32p, C.c_int32, C.c_int32, C.POINTER(capi.Camera)]
     L.omv_develop.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_float, C.c_float, vp, vp, vp, C.c_int32, vp]
     L.omv_tonemap.argtypes = [vp, C.c_int64, C.c_float, C.c_float, vp]
     L.omv_denoise_median.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_int32, vp]
@@ -139,7 +146,8 @@ def lib():
               "omv_scene_set_materials", "omv_adjoint",
               "omv_trace_rays", "omv_render_ids", "omv_brdf_eval_direct",
               "omv_brdf_sample_indirect", "omv_om_fresnel", "omv_camera_rays", "omv_env_radiance", "omv_struct_sizes",
-              "omv_develop", "omv_tonemap", "omv_denoise_median", "omv_rgba8", "omv_save_image"):
+              "omv_develop", "omv_tonemap", "omv_denoise_median", "omv_rgba8", "omv_save_image",
+              "omv_render_fc", "omv_scene_bounds", "omv_lightbox_cameras"):
         getattr(L, n).restype = st
     _lib = L
     return L
@@ -273,6 +281,13 @@ class RenderScene:
                                    hits.ctypes.data_as(C.POINTER(capi.Hit))))
         return hits
 
+    def bounds(self):
+        """World bounding box of the valid instances (AssetGeometry::getBBox)."""
+        lo = np.zeros(3, dtype=np.float32)
+        hi = np.zeros(3, dtype=np.float32)
+        check(lib().omv_scene_bounds(self.handle, capi.fptr(lo), capi.fptr(hi)))
+        return lo, hi
+
     def env_radiance(self, dirs: np.ndarray) -> np.ndarray:
         dirs = np.ascontiguousarray(dirs, dtype=np.float32)
         out = np.zeros((len(dirs), 3), dtype=np.float32)
@@ -301,7 +316,7 @@ class BatchRenderer:
     def job(camera: "PinholeCamera", spp: int, film, seed: int = 0, material_set: int = -1,
             sample_offset: int = 0) -> "capi.Job":
         j = capi.Job()
-        j.camera = camera.to_c()
+        j.camera = camera.to_c() if hasattr(camera, "to_c") else camera
         j.samples_per_pixel, j.sample_offset, j.seed, j.material_set = spp, sample_offset, seed, material_set
         j.d_sum_rgb = film[0].data_ptr()
         j.d_sumsq_rgb = film[1].data_ptr() if film[1] is not None else None
@@ -381,6 +396,50 @@ class BDPTRenderer:
         return hits, gp
 
 
+# --------------------------------------------------- validation (-F / -V) --
+
+FC_SUBJECTS = ("pid", "gid", "mid", "mmp", "rmp", "md", "sg", "mn", "in")
+
+
+def fc_subject(name: str) -> int:
+    """Subject code of an -F name (0, the empty subject, for unknown names)."""
+    return int(lib().omv_fc_subject_from_name(name.encode()))
+
+
+def render_fc(scene: "RenderScene", camera, subject, palette=None, uniforms=None, seed: int = 0):
+    """The false-colour pass (main.cpp:261-270 with -F <subject>): returns
+    (rgba (H, W, 4) float32, args (H, W) uint32, hits (H*W,)).  `subject` is a
+    name or an OMV_FC_* code; `palette` 0xRRGGBB per id for pid/gid/mid;
+    `uniforms` (H, W, 4) replaces the device's Philox draws."""
+    code = fc_subject(subject) if isinstance(subject, str) else int(subject)
+    cam = camera.to_c() if hasattr(camera, "to_c") else camera
+    W, H = cam.width, cam.height
+    rgba = np.zeros((H, W, 4), dtype=np.float32)
+    args = np.zeros((H, W), dtype=np.uint32)
+    hits = np.zeros(W * H, dtype=capi.HIT_DTYPE)
+    pal = None if palette is None else np.ascontiguousarray(palette, dtype=np.uint32)
+    uni = None
+    if uniforms is not None:
+        uni = np.ascontiguousarray(uniforms, dtype=np.float32).reshape(-1)
+        if len(uni) != 4 * W * H:
+            raise ValueError("uniforms must hold 4 floats per pixel")
+    check(lib().omv_render_fc(scene.handle, C.byref(cam), code, capi.fptr(uni) if uni is not None else None, seed,
+                              pal.ctypes.data_as(C.POINTER(C.c_uint32)) if pal is not None else None,
+                              0 if pal is None else len(pal), capi.fptr(rgba),
+                              args.ctypes.data_as(C.POINTER(C.c_uint32)), hits.ctypes.data_as(C.POINTER(capi.Hit))))
+    return rgba, args, hits
+
+
+def lightbox_cameras(lo, hi, width: int, height: int):
+    """The 8 light-box views (-V, main.cpp:434-458) of the box [lo, hi] as C
+    cameras, in BoundingBox::getCorners order."""
+    cams = (capi.Camera * 8)()
+    lo = np.ascontiguousarray(lo, dtype=np.float32)
+    hi = np.ascontiguousarray(hi, dtype=np.float32)
+    check(lib().omv_lightbox_cameras(capi.fptr(lo), capi.fptr(hi), width, height, cams))
+    return list(cams)
+
+
 # ------------------------------------------------------ kernel test hooks --
 
 def _hook(name: str, win: int, wout: int, x: np.ndarray) -> np.ndarray:
@@ -411,4 +470,5 @@ def camera_rays(camera: PinholeCamera, jitter: np.ndarray) -> np.ndarray:
 
 
 __all__ = ["build", "lib", "OmvError", "RendererParameters", "PinholeCamera", "RenderScene", "BDPTRenderer",
+           "BatchRenderer", "render_fc", "fc_subject", "lightbox_cameras", "FC_SUBJECTS",
            "brdf_eval_direct", "brdf_sample_indirect", "om_fresnel", "camera_rays", "scenes", "capi"]

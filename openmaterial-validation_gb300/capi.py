@@ -125,6 +125,8 @@ def params_for(scene, spp: int = None, seed: int = 0, variance: bool = False) ->
 
 
 def camera_struct(cam) -> Camera:
+    if isinstance(cam, Camera):
+        return cam
     c = Camera()
     c.width, c.height = cam.width, cam.height
     for i in range(3):

@@ -383,6 +383,39 @@ omv_status omv_camera_rays(const omv_camera* camera, const float* jitter, float*
     });
 }
 
+/* ------------------------------------------------- false-colour validation */
+
+int32_t omv_fc_subject_from_name(const char* name) { return omv::fc_subject_from_name(name); }
+
+omv_status omv_render_fc(omv_scene* scene, const omv_camera* camera, int32_t subject, const float* uniforms,
+                         uint64_t seed, const uint32_t* palette, int32_t palette_size, float* image_rgba,
+                         uint32_t* args, omv_hit* hits)
+{
+    return guarded([&] {
+        check_scene(scene);
+        check_camera(camera);
+        omv::render_fc(*scene->h, *camera, subject, uniforms, seed, palette, palette_size, image_rgba, args, hits);
+    });
+}
+
+omv_status omv_scene_bounds(omv_scene* scene, float lo[3], float hi[3])
+{
+    return guarded([&] {
+        check_scene(scene);
+        if (!lo || !hi) throw omv::ArgError("lo and hi are required");
+        omv::scene_bounds(*scene->h, lo, hi);
+    });
+}
+
+omv_status omv_lightbox_cameras(const float lo[3], const float hi[3], int32_t width, int32_t height,
+                                omv_camera cameras[8])
+{
+    return guarded([&] {
+        if (!lo || !hi || !cameras) throw omv::ArgError("lo, hi and cameras are required");
+        omv::lightbox_cameras(lo, hi, width, height, cameras);
+    });
+}
+
 /* ------------------------------------------------------- image development */
 
 omv_status omv_develop(const double* d_sum_rgb, const uint32_t* d_count, int32_t width, int32_t height, float A,

@@ -64,7 +64,7 @@ struct alignas(16) DevMaterial {
     float metal;
     float alpha;  // roughness^2
     float eta;    // 1 / ior, or 1 when double sided
-    float pad0;
+    float rough;  // roughness factor as given (the rmp validation subject)
     float om_n[4];
     float om_k[4];
 };

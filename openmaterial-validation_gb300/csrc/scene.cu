@@ -254,6 +254,7 @@ DevMaterial material_from_desc(const omv_material_desc& md)
         if (md.alpha_mode != OMV_ALPHA_BLEND) m.color[3] = 1.0f;
         m.transmissive = (md.double_sided || m.color[3] < 1.0f) ? 1 : 0;
         m.metal = md.metallic;
+        m.rough = md.roughness;
         float rough = md.roughness;
         rough = std::max(0.00001f, std::min(rough, 0.99999f));
         m.alpha = std::pow(rough, 2.0f);
@@ -359,6 +360,7 @@ SceneHost* scene_create(const omv_scene_desc& d, int device)
     std::vector<MeshGeom> geo(d.num_meshes);
     std::vector<std::vector<float>> pos3(d.num_meshes);
     s->mesh_face_prefix.assign(d.num_meshes + 1, 0);
+    s->mesh_vert_count.assign(d.num_meshes, 0);
     for (int i = 0; i < d.num_meshes; ++i) {
         const omv_mesh_desc& md = d.meshes[i];
         const bool valid = md.num_vertices > 0 && md.num_faces > 0 && md.positions && md.faces;
@@ -371,6 +373,7 @@ SceneHost* scene_create(const omv_scene_desc& d, int device)
         mesh_mat[i] = (uint32_t)mat;
         s->mesh_face_prefix[i + 1] = s->mesh_face_prefix[i] + (valid ? (uint32_t)md.num_faces : 0u);
         if (!valid) continue;
+        s->mesh_vert_count[i] = (uint32_t)md.num_vertices;
         if (md.position_stride < 3 || (md.normals && md.normal_stride < 3) || (md.tangents && md.tangent_stride < 4) ||
             (md.texcoord0 && md.texcoord_stride < 2))
             throw ArgError("mesh stride smaller than its element size");

@@ -87,6 +87,9 @@ struct SceneHost {
     int64_t device_bytes = 0;
     double build_ms = 0.0;
     std::vector<uint32_t> mesh_face_prefix;  // global primitive id base per mesh
+    std::vector<uint32_t> mesh_vert_count;   // vertices per mesh (0: invalid mesh)
+    bool fc_density_ready = false;           // triangle density extremes (the md validation subject)
+    float fc_density_min = 0.0f, fc_density_max = 0.0f;
     uint32_t* d_face_prefix = nullptr;
     RenderScratch scratch;
     std::vector<DevMaterial> h_mats;         // the scene's materials (host copy)
@@ -142,6 +145,13 @@ void trace_rays(SceneHost& s, int64_t n, const float* d_rays, omv_hit* d_hits, c
 void env_radiance(SceneHost& s, int64_t n, const float* d_dirs, float* d_rgb, cudaStream_t st);
 
 // kernel-level hooks (no scene)
+// false-colour validation pass and light-box views (fc.cu)
+int fc_subject_from_name(const char* name);
+void render_fc(SceneHost& s, const omv_camera& cam, int subject, const float* uniforms, uint64_t seed,
+               const uint32_t* palette, int palette_size, float* rgba, uint32_t* args, omv_hit* hits);
+void scene_bounds(SceneHost& s, float lo[3], float hi[3]);
+void lightbox_cameras(const float lo[3], const float hi[3], int width, int height, omv_camera out[8]);
+
 // image development and writers (post.cu)
 void develop_film(const double* d_sum, const uint32_t* d_count, int w, int h, float A, float gamma, float* d_linear,
                   float* d_toned, uint8_t* d_rgba8, bool flip, cudaStream_t st);

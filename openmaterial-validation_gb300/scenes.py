@@ -492,7 +492,44 @@ def scene_mixed(width: int = 32, height: int = 32, spp: int = 8) -> Scene:
     return Scene("mixed", meshes, inst, mats, [light], None, cam, RenderSpec(spp, 4, 4, 5), gltf_nodes=[nodes])
 
 
-SCENES = {"c1": scene_c1, "c2": scene_c2, "mixed": scene_mixed}
+def scene_validation(width: int = 64, height: int = 48) -> Scene:
+    """Scene for the false-colour subjects: triangle densities over three
+    orders of magnitude (icospheres of 80, 320 and 1280 faces, a 2-face
+    ground), one ball wound inside out with outward vertex normals (inverted
+    normals, surface gradient 1), an OpenMATERIAL conductor, PBR materials with
+    distinct metallic / roughness factors (one roughness above 1, clamped by the
+    subject) and a mesh without material.  C1's light and camera model."""
+    meshes = []
+    specs = [(2, (-1.6, -0.3, 0.0), 0, False), (1, (0.0, -0.3, -0.8), 1, False), (3, (1.6, -0.3, 0.0), 2, False),
+             (1, (-0.8, 0.9, -1.2), 3, True), (2, (0.9, 0.9, -1.5), -1, False)]
+    scale = F32(0.7)
+    for i, (sub, c, mat, flip) in enumerate(specs):
+        v, f = icosphere(sub)
+        n = (v / np.linalg.norm(v, axis=1, keepdims=True)).astype(F32)
+        p = (v.astype(F32) * scale + np.array(c, dtype=F32)).astype(F32)
+        faces = f[:, [0, 2, 1]].copy() if flip else f
+        meshes.append(Mesh(positions=p, normals=n, faces=np.ascontiguousarray(faces), material=mat, name=f"ball{i}"))
+    qv = np.array([[-5, -1, -5], [5, -1, -5], [5, -1, 5], [-5, -1, 5]], dtype=F32)
+    qf = np.array([[0, 2, 1], [0, 3, 2]], dtype=np.uint32)
+    meshes.append(Mesh(positions=qv, normals=None, faces=qf, material=4, name="ground"))
+    mats = [_om_conductor((0.18, 0.42, 1.37), (3.42, 2.35, 1.77)),
+            Material(type=0, base_color=(0.9, 0.6, 0.3, 1.0), metallic=1.0, roughness=0.3, name="rough_metal"),
+            Material(type=0, base_color=(0.8, 0.9, 1.0, 1.0), metallic=0.25, roughness=1.3, double_sided=True,
+                     name="over_rough"),
+            Material(type=0, base_color=(0.2, 0.8, 0.3, 1.0), metallic=0.6, roughness=0.8, name="inside_out"),
+            Material(type=0, base_color=(0.5, 0.5, 0.5, 1.0), metallic=0.0, roughness=1.0, name="ground_diffuse")]
+    root_t = np.eye(4, dtype=F32)
+    root_t[2, 3] = -5.0
+    inst = [Instance(root_t.copy(), i) for i in range(len(meshes))]
+    light = Light(position=(2.0, 4.0, -3.0), intensity=(50.0, 50.0, 50.0))
+    focus = (height / 2.0) / math.tan(math.radians(22.5))
+    cam = camera_from_json(width, height, width / height, focus, 45.0)
+    nodes = {"root_translation": (0.0, 0.0, -5.0), "light_translation": (2.0, 4.0, 2.0),
+             "light_color": (1.0, 1.0, 1.0), "light_intensity": 50.0}
+    return Scene("validation", meshes, inst, mats, [light], None, cam, RenderSpec(1, 1, 1, 8), gltf_nodes=[nodes])
+
+
+SCENES = {"c1": scene_c1, "c2": scene_c2, "mixed": scene_mixed, "validation": scene_validation}
 
 
 # -------------------------------------------------------------------- RGBE --

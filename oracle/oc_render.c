@@ -1363,3 +1363,232 @@ void omv_params_default(omv_params* p)
     p->seed = 0;
     p->estimator = OMV_ESTIMATOR_REFERENCE;
 }
+
+/* ----------------------------------------------- false-colour validation --- */
+
+/* RenderMesh::getMinMaxDensity (RenderMesh.cpp:277-297) over every instance,
+ * as RenderScene::commitScene collects it (RenderScene.cpp:196-203) */
+static void density_range(const oc_scene* s, float* dmin, float* dmax)
+{
+    float lo = INFINITY, hi = 0.0f;
+    for (int i = 0; i < s->n_inst; ++i) {
+        const oc_inst_r* in = &s->inst[i];
+        if (in->mesh < 0) continue;
+        const oc_mesh_r* m = &s->meshes[in->mesh];
+        for (int f = 0; f < m->fn; ++f) {
+            float V[3][3], N[3];
+            for (int k = 0; k < 3; ++k)
+                oc_xform_point((const float(*)[4])in->M, m->v + (size_t)m->faces[3 * (size_t)f + k] * 10, V[k]);
+            const float E1[3] = {V[1][0] - V[0][0], V[1][1] - V[0][1], V[1][2] - V[0][2]};
+            const float E2[3] = {V[2][0] - V[0][0], V[2][1] - V[0][1], V[2][2] - V[0][2]};
+            oc_cross3(E1, E2, N);
+            const float area = oc_length3(N) / 2.0f;
+            if (area > OC_EPS) {
+                const float d = 1.0f / (0.0f + area);
+                lo = oc_min(lo, d);
+                hi = oc_max(hi, d);
+            }
+        }
+    }
+    *dmin = lo;
+    *dmax = hi;
+}
+
+/* the FC_VALIDATION tail of RenderMesh::computeSurfacePoint (RenderMesh.cpp:
+ * 197-207, pointwise surface gradient) and of BDPTRenderer::computeSurfacePoint
+ * (BDPTRenderer.cpp:68-72): relative mesh density and average gradient */
+static void fc_surface_terms(const oc_scene* s, const oc_sp* sp, float dmin, float dmax, float* density,
+                             float* gradient)
+{
+    const oc_inst_r* in = &s->inst[sp->inst];
+    const oc_mesh_r* m = &s->meshes[sp->mesh];
+    const uint32_t* fi = m->faces + 3 * (size_t)sp->face;
+    float V[3][3], tfn[3];
+    for (int k = 0; k < 3; ++k) oc_xform_point((const float(*)[4])in->M, m->v + (size_t)fi[k] * 10, V[k]);
+    const float E1[3] = {V[1][0] - V[0][0], V[1][1] - V[0][1], V[1][2] - V[0][2]};
+    const float E2[3] = {V[2][0] - V[0][0], V[2][1] - V[0][1], V[2][2] - V[0][2]};
+    oc_cross3(E1, E2, tfn);
+    float ref = 1.0f / (0.0f + oc_length3(tfn) / 2.0f);
+    oc_normalize3(tfn);
+    float ag = 0.0f;
+    for (int k = 0; k < 3; ++k) {
+        float tvn[3];
+        oc_mat3_vec((const float(*)[3])in->N, m->v + (size_t)fi[k] * 10 + 3, tvn);
+        oc_normalize_if_needed3(tvn);
+        ag = ag + sqrtf((1.0f - oc_clamp(oc_dot3(tvn, tfn), -1.0f, 1.0f)) / 2.0f);
+    }
+    *gradient = powf(oc_clamp(ag / 3.0f, 1e-6f, 1.0f), 0.286f);
+    *density = oc_clamp01(1.0f - logf(dmax / oc_clamp(ref, dmin, dmax)) / logf(dmax / dmin));
+}
+
+static float fc_clamped(float v) { return oc_clamp(v, 0.0f, 1.0f); } /* GenericFCArgument ClampedFloat */
+
+static void fc_lerp_paint(float t, const float* lower, const float* upper, float* c)
+{
+    for (int i = 0; i < 3; ++i) c[i] = oc_lerp(lower[i], upper[i], t);
+}
+
+/* The false-colour pass of the FC_VALIDATION build (main.cpp:261-270): spp 1,
+ * one bounce, no lights, no background.  Each pixel's jittered primary ray is
+ * traced; the hit material's getRayAndBrdf hands the subject's argument to
+ * GenericFCSubject::paint (PhysicallyBasedMaterial.cpp:202-240,
+ * OpenMaterial.cpp:165-210, DiffuseColorMaterial.cpp:49-89) and the colour
+ * becomes the pixel's radiance (BDPTRenderer.cpp:165-168).  Outputs per pixel
+ * (each may be NULL): rgba (colour, alpha 1: the film after stop), the 4
+ * argument bytes, the uniforms drawn (dx, dy, and the missing material's two
+ * hemisphere draws, else 0) and the hit. */
+int32_t oc_render_fc(const oc_scene* s, const omv_camera* cam, uint32_t seed, int32_t subject,
+                     const uint32_t* palette, int32_t palette_size, float* rgba, uint32_t* args, float* uniforms,
+                     omv_hit* hits)
+{
+    static const float white[3] = {1.0f, 1.0f, 1.0f}, blue[3] = {0.0f, 0.0f, 1.0f}, green[3] = {0.0f, 1.0f, 0.0f},
+                       red[3] = {1.0f, 0.0f, 0.0f};
+    oc_mt mt;
+    oc_mt_seed(&mt, seed);
+    draw_src rs = {&mt, NULL, 0};
+    omv_params p;
+    omv_params_default(&p);
+    ctx c = {s, &p, 0};
+    float dmin = 0.0f, dmax = 0.0f;
+    if (subject == OMV_FC_MD) density_range(s, &dmin, &dmax);
+    uint32_t face_base = 0;
+    for (int y = 0; y < cam->height; ++y) {
+        for (int x = 0; x < cam->width; ++x) {
+            const size_t id = (size_t)y * cam->width + x;
+            float u[4] = {draw(&rs), draw(&rs), 0.0f, 0.0f};
+            float O[3], R[3];
+            camera_ray(cam, x, y, u[0], u[1], O, R);
+            oc_rh h;
+            memset(&h, 0, sizeof(h));
+            set_ray(O, R, &h, 1.0f);
+            oc_sp sp;
+            const int hit = scene_intersect(&c, &h, &sp);
+            float col[3] = {0.0f, 0.0f, 0.0f};
+            uint32_t arg = 0;
+            if (hit) {
+                const oc_mat* m = &s->mats[s->meshes[sp.mesh].mat];
+                apply_texture_normal(&sp, (const float[3]){0.0f, 0.0f, 1.0f}); /* modifyFrame */
+                float inV[3] = {R[0], R[1], R[2]};
+                if (m->type == MAT_MISSING) { /* RenderMaterial::getRayAndBrdf: hemisphere, then getBrdf(-out, -in) */
+                    float v[3], outV[3];
+                    u[2] = draw(&rs);
+                    u[3] = draw(&rs);
+                    uniform_hemisphere(v, u[2], u[3]);
+                    oc_to_normal_space(sp.tan, sp.bin, sp.nrm, v, outV);
+                    inV[0] = -outV[0];
+                    inV[1] = -outV[1];
+                    inV[2] = -outV[2];
+                }
+                float f = 0.0f;
+                face_base = 0;
+                for (int k = 0; k < sp.mesh; ++k) face_base += (uint32_t)s->meshes[k].fn;
+                switch (subject) {
+                case OMV_FC_PID:
+                case OMV_FC_GID: {
+                    arg = subject == OMV_FC_PID ? face_base + (uint32_t)sp.face : (uint32_t)sp.mesh;
+                    const uint32_t n = (palette && arg < (uint32_t)palette_size) ? palette[arg] : 0u;
+                    col[0] = (float)((n >> 16) & 0xFFu) / 255.0f;
+                    col[1] = (float)((n >> 8) & 0xFFu) / 255.0f;
+                    col[2] = (float)(n & 0xFFu) / 255.0f;
+                    break;
+                }
+                case OMV_FC_MID:
+                    if (m->type == MAT_MISSING) {
+                        arg = 0xFFFFFFFFu;
+                        col[0] = 1000.0f;
+                        col[2] = 1000.0f;
+                    } else {
+                        arg = (uint32_t)s->meshes[sp.mesh].mat;
+                        const uint32_t n = (palette && arg < (uint32_t)palette_size) ? palette[arg] : 0u;
+                        col[1] = (float)((n >> 8) & 0xFFu) / 255.0f;
+                        col[2] = (float)(n & 0xFFu) / 255.0f;
+                    }
+                    break;
+                case OMV_FC_MMP:
+                case OMV_FC_RMP:
+                    if (m->type == MAT_PBR) f = fc_clamped(subject == OMV_FC_MMP ? m->metal : m->rough);
+                    memcpy(&arg, &f, 4);
+                    fc_lerp_paint(f, white, subject == OMV_FC_MMP ? blue : green, col);
+                    break;
+                case OMV_FC_MD:
+                case OMV_FC_SG: {
+                    float dens, grad;
+                    fc_surface_terms(s, &sp, dmin, dmax, &dens, &grad);
+                    f = fc_clamped(subject == OMV_FC_MD ? dens : grad);
+                    memcpy(&arg, &f, 4);
+                    if (subject == OMV_FC_MD)
+                        fc_lerp_paint(f, white, red, col);
+                    else
+                        col[0] = col[1] = col[2] = 1.0f - f;
+                    break;
+                }
+                case OMV_FC_MN: {
+                    const char* nm = m->type == MAT_PBR ? "pbr" : (m->type == MAT_OM ? "om" : "mm");
+                    unsigned char b[4] = {0, 0, 0, 0};
+                    memcpy(b, nm, strlen(nm));
+                    memcpy(&arg, b, 4);
+                    if (m->type == MAT_PBR) col[2] = 1.0f;
+                    else if (m->type == MAT_OM) col[1] = 1.0f;
+                    else col[0] = col[2] = 1000.0f;
+                    break;
+                }
+                case OMV_FC_IN: {
+                    float tfn[3];
+                    face_normal(s, &sp, tfn);
+                    const int inv = oc_dot3(inV, tfn) > 0.0f;
+                    arg = (uint32_t)inv;
+                    col[0] = (float)inv;
+                    col[1] = 1.0f - (float)inv;
+                    break;
+                }
+                default: /* EmptySubject */
+                    break;
+                }
+            }
+            if (rgba) {
+                rgba[4 * id] = col[0];
+                rgba[4 * id + 1] = col[1];
+                rgba[4 * id + 2] = col[2];
+                rgba[4 * id + 3] = 1.0f;
+            }
+            if (args) args[id] = arg;
+            if (uniforms) memcpy(uniforms + 4 * id, u, sizeof(u));
+            if (hits) fill_hit(s, &h, hit, &hits[id]);
+        }
+    }
+    return 0;
+}
+
+/* RenderMesh::getMinMaxDensity over all instances (for the density checks) */
+void oc_density_range(const oc_scene* s, float* out2) { density_range(s, &out2[0], &out2[1]); }
+
+/* The light-box loop (main.cpp:491-521): the views rendered one after another
+ * by BDPTRenderer::render at -C 1, all drawing from the scene's one
+ * mt19937(seed) generator (RenderScene.cpp:20), each film normalised by stop.
+ * films: n * W*H*4 floats (every camera has the same resolution). */
+int32_t oc_render_views(const oc_scene* s, int32_t n, const omv_camera* cams, const omv_params* p, uint32_t seed,
+                        float* films)
+{
+    if (!s || !cams || !p || !films || n < 0) return -1;
+    oc_mt mt;
+    oc_mt_seed(&mt, seed);
+    const size_t px = (size_t)cams[0].width * cams[0].height;
+    for (int v = 0; v < n; ++v) {
+        if ((size_t)cams[v].width * cams[v].height != px) return -1;
+        job j;
+        j.s = s;
+        j.cam = &cams[v];
+        j.p = p;
+        j.mode = 0;
+        j.seed = seed;
+        j.row_end = cams[v].height;
+        atomic_init(&j.next_row, 0);
+        j.film = films + 4 * px * (size_t)v;
+        memset(j.film, 0, sizeof(float) * 4 * px);
+        j.sumsq = NULL;
+        atomic_init(&j.rays, 0ULL);
+        render_rows(&j, &mt);
+        oc_film_stop(j.film, (int64_t)px);
+    }
+    return 0;
+}

@@ -44,11 +44,26 @@ int32_t oc_render(const oc_scene* s, const omv_camera* cam, const omv_params* p,
                   uint64_t* rays_out);
 /* PinholeCamera::stop (PinholeCamera.cpp:70-78) */
 void oc_film_stop(float* film, int64_t pixels);
+/* The light-box loop (main.cpp:491-521): n views of equal resolution rendered
+ * in turn from one mt19937(seed) stream, each film normalised (n*W*H*4). */
+int32_t oc_render_views(const oc_scene* s, int32_t n, const omv_camera* cams, const omv_params* p, uint32_t seed,
+                        float* films);
 
 /* Replay of the false-colour / ID pass (main.cpp:261-270: spp 1, one bounce, no
  * lights, no background) with one mt19937(seed) stream: per pixel the jittered
  * primary ray (org, dir: 6 floats) and its hit. */
 int32_t oc_render_ids(const oc_scene* s, const omv_camera* cam, uint32_t seed, float* rays, omv_hit* hits);
+
+/* The false-colour pass of the FC_VALIDATION build for one subject
+ * (OMV_FC_* of omv.h) with one mt19937(seed) stream; per pixel (each output
+ * may be NULL) the colour (rgba, alpha 1), the 4 argument bytes, the 4
+ * uniforms drawn (dx, dy, hemisphere pair of a missing-material hit, else 0)
+ * and the hit.  `palette` colours the enumerated subjects (0xRRGGBB). */
+int32_t oc_render_fc(const oc_scene* s, const omv_camera* cam, uint32_t seed, int32_t subject,
+                     const uint32_t* palette, int32_t palette_size, float* rgba, uint32_t* args, float* uniforms,
+                     omv_hit* hits);
+/* scene minimum and maximum triangle density (1 / area) */
+void oc_density_range(const oc_scene* s, float* out2);
 
 /* closest-hit queries (sceneIntersect incl. the alpha-mask retry loop) */
 int32_t oc_trace_rays(const oc_scene* s, int64_t n, const float* rays, omv_hit* hits);

@@ -67,6 +67,11 @@ def lib():
                                          C.POINTER(C.c_int32)]
         L.oc_scene_mesh_vertices.argtypes = [vp, C.c_int32, capi.f32p]
         L.oc_scene_normal_matrix.argtypes = [vp, C.c_int32, capi.f32p]
+        L.oc_render_fc.argtypes = [vp, C.POINTER(capi.Camera), C.c_uint32, C.c_int32, C.POINTER(C.c_uint32),
+                                   C.c_int32, capi.f32p, C.POINTER(C.c_uint32), capi.f32p, C.POINTER(capi.Hit)]
+        L.oc_density_range.argtypes = [vp, capi.f32p]
+        L.oc_render_views.argtypes = [vp, C.c_int32, C.POINTER(capi.Camera), C.POINTER(capi.Params), C.c_uint32,
+                                      capi.f32p]
         L.oc_tonemap.argtypes = [capi.f32p, C.c_int64, C.c_float, C.c_float]
         L.oc_median.argtypes = [capi.f32p, C.c_int, C.c_int, C.c_int]
         L.oc_rgba8.argtypes = [capi.f32p, C.c_int64, C.POINTER(C.c_uint8)]
@@ -119,6 +124,38 @@ class OracleScene:
         hits = np.zeros(n, dtype=capi.HIT_DTYPE)
         lib().oc_render_ids(self.h, C.byref(cam), seed, capi.fptr(rays), hits.ctypes.data_as(C.POINTER(capi.Hit)))
         return rays, hits
+
+    def render_fc(self, subject: int, palette=None, camera=None, seed: int = REFERENCE_SEED):
+        """The false-colour pass: (rgba (H, W, 4), args uint32 (H, W), uniforms
+        (H, W, 4), hits (H*W,))."""
+        cam = capi.camera_struct(camera or self.scene.camera)
+        W, H = cam.width, cam.height
+        rgba = np.zeros((H, W, 4), dtype=np.float32)
+        args = np.zeros((H, W), dtype=np.uint32)
+        uni = np.zeros((H, W, 4), dtype=np.float32)
+        hits = np.zeros(W * H, dtype=capi.HIT_DTYPE)
+        pal = None if palette is None else np.ascontiguousarray(palette, dtype=np.uint32)
+        lib().oc_render_fc(self.h, C.byref(cam), seed, subject,
+                           pal.ctypes.data_as(C.POINTER(C.c_uint32)) if pal is not None else None,
+                           0 if pal is None else len(pal), capi.fptr(rgba), args.ctypes.data_as(C.POINTER(C.c_uint32)),
+                           capi.fptr(uni), hits.ctypes.data_as(C.POINTER(capi.Hit)))
+        return rgba, args, uni, hits
+
+    def density_range(self):
+        out = np.zeros(2, dtype=np.float32)
+        lib().oc_density_range(self.h, capi.fptr(out))
+        return out
+
+    def render_views(self, cams, params=None, seed: int = REFERENCE_SEED):
+        """Light-box loop: normalised films (n, H, W, 4) of the cameras rendered
+        in turn from one generator."""
+        arr = (capi.Camera * len(cams))(*cams)
+        p = params or capi.params_for(self.scene)
+        W, H = cams[0].width, cams[0].height
+        films = np.zeros((len(cams), H, W, 4), dtype=np.float32)
+        if lib().oc_render_views(self.h, len(cams), arr, C.byref(p), seed, capi.fptr(films)) != 0:
+            raise RuntimeError("oracle render_views failed")
+        return films
 
     def trace(self, rays8: np.ndarray):
         rays8 = np.ascontiguousarray(rays8, dtype=np.float32)

@@ -5,12 +5,16 @@
  *
  *   gammaCorrection (ToneMapping.cpp:24)   -> OMV_REF_FILM: the linear film as
  *       produced by PinholeCamera::stop/getImpression (W*H*4 float32), then the
- *       real tone mapping runs unchanged;
+ *       real tone mapping runs unchanged; a "%d" in the path is replaced by
+ *       the call's index (one film per view of a light-box run);
  *   RenderScene::commitScene (RenderScene.cpp:155) -> OMV_REF_SCENE: the
  *       flattened, committed scene (meshes with derived normals/tangents,
  *       instances with normal matrices, materials, lights);
  *   BDPTRenderer::render (BDPTRenderer.cpp:372) -> one line on stderr
- *       "OMV_REF_RENDER <seconds> <rays>" (steady clock, shim ray counter).
+ *       "OMV_REF_RENDER <seconds> <rays>" (steady clock, shim ray counter),
+ *       and with OMV_REF_CAMERAS set, 15 floats appended per call: the
+ *       sensor's ViewPoint (position, rotation rows) and the pinhole's
+ *       half width, half height and focus.
  */
 #include <chrono>
 #include <cstdio>
@@ -23,6 +27,7 @@
 #include "DiffuseColorMaterial.h"
 #include "OpenMaterial.h"
 #include "PhysicallyBasedMaterial.h"
+#include "PinholeCamera.h"
 #include "RenderLightPoint.h"
 #include "RenderScene.h"
 #include "embree4/rtcore.h"
@@ -35,7 +40,14 @@ void __real__ZN12BDPTRenderer6renderEP12RenderSensor(BDPTRenderer* self, RenderS
 
 void __wrap__Z15gammaCorrectionPA4_fiiff(fvec4* img, int iw, int ih, float A, float gamma)
 {
+    static int calls = 0;
     const char* p = std::getenv("OMV_REF_FILM");
+    char path[4096];
+    if (p && *p && std::strstr(p, "%d")) {
+        std::snprintf(path, sizeof(path), p, calls);
+        p = path;
+    }
+    ++calls;
     if (p && *p) {
         FILE* f = std::fopen(p, "wb");
         if (f) {
@@ -147,5 +159,19 @@ void __wrap__ZN12BDPTRenderer6renderEP12RenderSensor(BDPTRenderer* self, RenderS
     auto t1 = std::chrono::steady_clock::now();
     unsigned long long r1 = omvShimRayCount();
     std::fprintf(stderr, "OMV_REF_RENDER %.9f %llu\n", std::chrono::duration<double>(t1 - t0).count(), r1 - r0);
+    const char* cp = std::getenv("OMV_REF_CAMERAS");
+    const PinholeCamera* pc = dynamic_cast<const PinholeCamera*>(s);
+    if (cp && *cp && pc) {
+        FILE* f = std::fopen(cp, "ab");
+        if (f) {
+            const ViewPoint vp = pc->getViewPoint();
+            const auto hw = pc->getRealSizes();
+            const float rec[3] = {hw.first, hw.second, pc->getFocus()};
+            put_f(f, vp.m_position, 3);
+            put_f(f, &vp.m_rotation[0][0], 9);
+            put_f(f, rec, 3);
+            std::fclose(f);
+        }
+    }
 }
 }

@@ -20,6 +20,10 @@ Fixtures (numpy .npz):
   ids_c1_64.npz     primary rays and hits of the false-colour (-F mid) pass
   post.npz          gammaCorrection (two gammas), SimpleDenoiserMedian<1> and
                     saveImage's 8-bit conversion on a seeded 23x37 HDR image
+  fc.npz            false-colour films (-F pid gid mid mmp rmp md sg mn in, and an
+                    unknown name) of the validation scene, before tone mapping
+  lightbox.npz      the 8 light-box views (-V) of the mixed scene: cameras
+                    (ViewPoint, half sizes, focus) and linear films
 """
 from __future__ import annotations
 
@@ -293,8 +297,43 @@ def gen_post(tmp):
     np.savez_compressed(os.path.join(HERE, "post.npz"), **out)
 
 
+FC_SUBJECTS = ["pid", "gid", "mid", "mmp", "rmp", "md", "sg", "mn", "in", "nosuch"]
+
+
+def gen_fc(tmp):
+    sc = S.scene_validation(64, 48)
+    out = {}
+    for name in FC_SUBJECTS:
+        film, _, _, dump = render_reference(sc, tmp, exe="pathtracer_fc", extra=["-F", name])
+        out[name] = film
+    out["width"], out["height"] = sc.camera.width, sc.camera.height
+    np.savez_compressed(os.path.join(HERE, "fc.npz"), **out)
+    np.savez_compressed(os.path.join(HERE, "scene_validation.npz"), **dump)
+
+
+def gen_lightbox(tmp):
+    sc = S.scene_mixed(32, 32, 32)
+    d = os.path.join(tmp, "lightbox")
+    o = S.write_gltf(sc, d)
+    cams = os.path.join(d, "cameras.bin")
+    if os.path.exists(cams):
+        os.remove(cams)
+    env = dict(os.environ, OMV_REF_FILM=os.path.join(d, "film_%d.bin"), OMV_REF_CAMERAS=cams)
+    run([os.path.join(BIN, "pathtracer"), *o["flags"], "-C", "1", "-V", "-o", os.path.join(d, "out.png")], env=env)
+    films = []
+    for k in range(8):
+        p = os.path.join(d, f"film_{k}.bin")
+        hdr = np.fromfile(p, dtype=np.int32, count=2)
+        films.append(np.fromfile(p, dtype=np.float32)[2:].reshape(hdr[1], hdr[0], 4))
+    c = np.fromfile(cams, dtype=np.float32).reshape(-1, 15)
+    assert len(c) == 8, c.shape
+    np.savez_compressed(os.path.join(HERE, "lightbox.npz"), films=np.stack(films), position=c[:, 0:3],
+                        rotation=c[:, 3:12].reshape(8, 3, 3), half_width=c[:, 12], half_height=c[:, 13],
+                        focus=c[:, 14], spp=sc.render.samples_per_pixel)
+
+
 GENS = {"mt": gen_mt, "brdf": gen_brdf, "om": gen_om, "ior": gen_ior, "env": gen_env, "camera": gen_camera,
-        "films": gen_films, "ids": gen_ids, "post": gen_post}
+        "films": gen_films, "ids": gen_ids, "post": gen_post, "fc": gen_fc, "lightbox": gen_lightbox}
 
 
 def main():
