@@ -60,6 +60,7 @@ typedef struct omv_mesh_desc {
     const float* tangents;   int32_t tangent_stride;   /* xyz + handedness w */
     const float* texcoord0;  int32_t texcoord_stride;
     int32_t material;               /* <0 or >= num_materials: the missing material */
+    const float* texcoord1;         /* TEXCOORD_1 (same stride as texcoord0) or NULL */
 } omv_mesh_desc;
 
 /* RenderScene::setInstance (RenderScene.cpp:101-109): row-major 4x4 object-to-world. */
@@ -70,6 +71,27 @@ typedef struct omv_instance_desc {
 
 enum { OMV_MATERIAL_PBR = 0, OMV_MATERIAL_OPENMATERIAL = 1 };
 enum { OMV_ALPHA_OPAQUE = 0, OMV_ALPHA_MASK = 1, OMV_ALPHA_BLEND = 2 };
+
+/* Bitmap texture (RenderScene::setTexture, BitmapTexture.cpp:20-36): 8-bit RGBA
+ * texels, rows in image order (texture coordinate v = 0 is the first row), as
+ * ImageData::load converts a glTF image (ImageData.cpp:33-100). */
+typedef struct omv_texture_desc {
+    int32_t width;
+    int32_t height;
+    const uint8_t* rgba;            /* width * height * 4 */
+} omv_texture_desc;
+
+/* One texture slot of a PBR material (PbrMaterial::TextureData, PbrMaterial.h:24-34;
+ * loaded at PbrMaterial.cpp:122-190).  `texture` is 1 + the index into
+ * omv_scene_desc.textures (0: no texture), `texcoord` the TEXCOORD set (0 or 1),
+ * and with has_transform the KHR_texture_transform rows: (u', v') = M (u, v, 1)
+ * (getTextureTransform, PbrMaterial.cpp:25-57); otherwise the identity. */
+typedef struct omv_texture_ref {
+    int32_t texture;
+    int32_t texcoord;
+    int32_t has_transform;
+    float transform[2][3];
+} omv_texture_ref;
 
 /* PBR: PhysicallyBasedMaterial over PbrMaterial factors (PbrMaterial.cpp:100-204).
  * OpenMaterial: OpenMaterial over AssetMaterialIor (OpenMaterial.cpp, AssetMaterialIor.cpp):
@@ -90,6 +112,17 @@ typedef struct omv_material_desc {
     const float* ior_n;             /* ior_n_count (wavelength, n) pairs */
     int32_t ior_k_count;
     const float* ior_k;             /* ior_k_count (wavelength, k) pairs */
+    /* PBR textures (PhysicallyBasedMaterial.cpp:27-124, 147-167, 280-316); a
+     * zero-filled block means none */
+    omv_texture_ref base_color_texture;
+    omv_texture_ref metallic_roughness_texture;   /* G roughness, B metallic, R occlusion */
+    omv_texture_ref normal_texture;
+    omv_texture_ref occlusion_texture;
+    omv_texture_ref emissive_texture;
+    float normal_scale;             /* normalTexture.scale (glTF default 1; used with a normal texture) */
+    float occlusion_strength;       /* occlusionTexture.strength (glTF default 1; used with an occlusion
+                                       or metallic-roughness texture) */
+    float emissive_factor[3];       /* emission needs the factor and an emissive texture */
 } omv_material_desc;
 
 /* RenderLightPoint::set (RenderLightPoint.cpp:20-26).  `intensity` is the
@@ -121,6 +154,8 @@ typedef struct omv_scene_desc {
     int32_t num_lights;
     const omv_light_desc* lights;
     const omv_hdri_desc* hdri;      /* NULL: no background */
+    int32_t num_textures;
+    const omv_texture_desc* textures;
 } omv_scene_desc;
 
 typedef struct omv_scene omv_scene;
@@ -468,6 +503,11 @@ omv_status omv_brdf_eval_direct(int64_t n, const float* in, float* out);
 omv_status omv_brdf_sample_indirect(int64_t n, const float* in, float* out);
 omv_status omv_om_fresnel(int64_t n, const float* in, float* out);
 
+/* BitmapTexture::texture(u, v, fvec4) (BitmapTexture.cpp:73-125) on the device:
+ * one width x height RGBA8 image, n (u, v) pairs in, 4 floats each out. */
+omv_status omv_texture_sample(int32_t width, int32_t height, const uint8_t* rgba, int64_t n, const float* uv,
+                              float* out);
+
 /* Camera rays for given jitter uniforms (2 per pixel, row-major), 6 floats per
  * pixel out (org, dir).  Device evaluation of PinholeCamera::getRay. */
 omv_status omv_camera_rays(const omv_camera* camera, const float* jitter, float* rays);
@@ -482,7 +522,8 @@ const char* omv_version(void);
 
 /* sizeof of the public structs in this order: omv_mesh_desc, omv_instance_desc,
  * omv_material_desc, omv_light_desc, omv_hdri_desc, omv_scene_desc,
- * omv_scene_info, omv_camera, omv_params, omv_stats, omv_hit -- for binding
+ * omv_scene_info, omv_camera, omv_params, omv_stats, omv_hit, omv_job,
+ * omv_texture_desc, omv_texture_ref -- for binding
  * layout checks (no reference counterpart).  With out == NULL returns the
  * count; otherwise writes min(n, count) sizes and returns that number. */
 int32_t omv_struct_sizes(int64_t* out, int32_t n);

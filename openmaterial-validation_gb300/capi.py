@@ -25,18 +25,33 @@ class MeshDesc(C.Structure):
                 ("normals", f32p), ("normal_stride", C.c_int32),
                 ("tangents", f32p), ("tangent_stride", C.c_int32),
                 ("texcoord0", f32p), ("texcoord_stride", C.c_int32),
-                ("material", C.c_int32)]
+                ("material", C.c_int32), ("texcoord1", f32p)]
 
 
 class InstanceDesc(C.Structure):
     _fields_ = [("transform", (C.c_float * 4) * 4), ("mesh", C.c_int32)]
 
 
+class TextureDesc(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("rgba", C.POINTER(C.c_uint8))]
+
+
+class TextureRef(C.Structure):
+    _fields_ = [("texture", C.c_int32), ("texcoord", C.c_int32), ("has_transform", C.c_int32),
+                ("transform", (C.c_float * 3) * 2)]
+
+
+TEXTURE_SLOTS = ("base_color_texture", "metallic_roughness_texture", "normal_texture", "occlusion_texture",
+                 "emissive_texture")
+
+
 class MaterialDesc(C.Structure):
     _fields_ = [("type", C.c_int32), ("base_color", C.c_float * 4), ("metallic", C.c_float),
                 ("roughness", C.c_float), ("ior", C.c_float), ("alpha_mode", C.c_int32),
                 ("alpha_cutoff", C.c_float), ("double_sided", C.c_int32), ("temperature", C.c_float),
-                ("ior_n_count", C.c_int32), ("ior_n", f32p), ("ior_k_count", C.c_int32), ("ior_k", f32p)]
+                ("ior_n_count", C.c_int32), ("ior_n", f32p), ("ior_k_count", C.c_int32), ("ior_k", f32p)] + \
+        [(n, TextureRef) for n in TEXTURE_SLOTS] + \
+        [("normal_scale", C.c_float), ("occlusion_strength", C.c_float), ("emissive_factor", C.c_float * 3)]
 
 
 class LightDesc(C.Structure):
@@ -53,7 +68,8 @@ class SceneDesc(C.Structure):
                 ("num_instances", C.c_int32), ("instances", C.POINTER(InstanceDesc)),
                 ("num_materials", C.c_int32), ("materials", C.POINTER(MaterialDesc)),
                 ("num_lights", C.c_int32), ("lights", C.POINTER(LightDesc)),
-                ("hdri", C.POINTER(HdriDesc))]
+                ("hdri", C.POINTER(HdriDesc)), ("num_textures", C.c_int32),
+                ("textures", C.POINTER(TextureDesc))]
 
 
 class SceneInfo(C.Structure):
@@ -150,6 +166,23 @@ def material_descs(materials, keep: List[Any]):
         md.alpha_mode, md.alpha_cutoff = mat.alpha_mode, mat.alpha_cutoff
         md.double_sided = 1 if mat.double_sided else 0
         md.temperature = mat.temperature
+        md.normal_scale = getattr(mat, "normal_scale", 1.0)
+        md.occlusion_strength = getattr(mat, "occlusion_strength", 1.0)
+        for c in range(3):
+            md.emissive_factor[c] = getattr(mat, "emissive_factor", (0.0, 0.0, 0.0))[c]
+        for slot in TEXTURE_SLOTS:
+            ref = getattr(mat, slot, None)
+            if ref is None:
+                continue
+            tr = getattr(md, slot)
+            tr.texture = int(ref.texture) + 1
+            tr.texcoord = int(ref.texcoord)
+            if ref.transform is not None:
+                tr.has_transform = 1
+                T = np.asarray(ref.transform, dtype=np.float32)
+                for r in range(2):
+                    for c in range(3):
+                        tr.transform[r][c] = float(T[r, c])
         if mat.ior_n is not None:
             tn = np.ascontiguousarray(np.asarray(mat.ior_n, dtype=np.float64).astype(np.float32))
             tk = np.ascontiguousarray(np.asarray(mat.ior_k, dtype=np.float64).astype(np.float32))
@@ -191,6 +224,12 @@ class DescHolder:
                 uv = np.ascontiguousarray(m.texcoord0, dtype=np.float32)
                 self.keep.append(uv)
                 md.texcoord0, md.texcoord_stride = fptr(uv), 2
+            if getattr(m, "texcoord1", None) is not None:
+                if m.texcoord0 is None:
+                    raise ValueError("texcoord1 needs texcoord0")
+                uv1 = np.ascontiguousarray(m.texcoord1, dtype=np.float32)
+                self.keep.append(uv1)
+                md.texcoord1 = fptr(uv1)
             md.material = m.material
         insts = (InstanceDesc * max(1, len(scene.instances)))()
         for i, inst in enumerate(scene.instances):
@@ -225,4 +264,16 @@ class DescHolder:
         d.num_materials, d.materials = len(scene.materials), mats
         d.num_lights, d.lights = len(scene.lights), lights
         d.hdri = C.pointer(self.hdri) if self.hdri is not None else None
+        texs = getattr(scene, "textures", None) or []
+        if texs:
+            tds = (TextureDesc * len(texs))()
+            for i, t in enumerate(texs):
+                a = np.ascontiguousarray(t, dtype=np.uint8)
+                if a.ndim != 3 or a.shape[2] != 4:
+                    raise ValueError("textures are (H, W, 4) uint8 RGBA")
+                self.keep.append(a)
+                tds[i].height, tds[i].width = a.shape[0], a.shape[1]
+                tds[i].rgba = a.ctypes.data_as(C.POINTER(C.c_uint8))
+            self.keep.append(tds)
+            d.num_textures, d.textures = len(texs), tds
         self.desc = d

@@ -127,7 +127,8 @@ int32_t omv_struct_sizes(int64_t* out, int32_t n)
                              (int64_t)sizeof(omv_hdri_desc),  (int64_t)sizeof(omv_scene_desc),
                              (int64_t)sizeof(omv_scene_info), (int64_t)sizeof(omv_camera),
                              (int64_t)sizeof(omv_params),     (int64_t)sizeof(omv_stats),
-                             (int64_t)sizeof(omv_hit),        (int64_t)sizeof(omv_job)};
+                             (int64_t)sizeof(omv_hit),        (int64_t)sizeof(omv_job),
+                             (int64_t)sizeof(omv_texture_desc), (int64_t)sizeof(omv_texture_ref)};
     const int32_t m = (int32_t)(sizeof(sizes) / sizeof(sizes[0]));
     if (!out) return m;
     const int32_t k = std::min(n, m);

@@ -49,24 +49,32 @@ F32 = np.float32
 RGB_WAVELENGTHS = (6.50000004e-07, 5.10000007e-07, 4.40000008e-07)
 
 
-def _libm_tanf():
-    name = ctypes.util.find_library("m") or "libm.so.6"
-    lib = ctypes.CDLL(name)
-    f = lib.tanf
-    f.restype = ctypes.c_float
-    f.argtypes = [ctypes.c_float]
+_LIBM_F = {}
+
+
+def _libm_f(name: str):
+    """A float function of the C library (tanf, cosf, sinf)."""
+    f = _LIBM_F.get(name)
+    if f is None:
+        lib = ctypes.CDLL(ctypes.util.find_library("m") or "libm.so.6")
+        f = getattr(lib, name)
+        f.restype = ctypes.c_float
+        f.argtypes = [ctypes.c_float]
+        _LIBM_F[name] = f
     return f
-
-
-_TANF = None
 
 
 def tanf(x: float) -> float:
     """float tangent through the C library, as std::tan(float) evaluates it."""
-    global _TANF
-    if _TANF is None:
-        _TANF = _libm_tanf()
-    return float(_TANF(float(F32(x))))
+    return float(_libm_f("tanf")(float(F32(x))))
+
+
+def cosf(x: float) -> float:
+    return float(_libm_f("cosf")(float(F32(x))))
+
+
+def sinf(x: float) -> float:
+    return float(_libm_f("sinf")(float(F32(x))))
 
 
 # ----------------------------------------------------------------- geometry --
@@ -161,6 +169,7 @@ class Mesh:
     texcoord0: Optional[np.ndarray] = None
     material: int = -1
     name: str = "mesh"
+    texcoord1: Optional[np.ndarray] = None
 
 
 @dataclasses.dataclass
@@ -183,6 +192,37 @@ class Material:
     ior_n: Optional[np.ndarray] = None  # (K,2) wavelength[m], n
     ior_k: Optional[np.ndarray] = None
     name: str = "material"
+    # PBR texture slots (TextureRef or None) and their factors
+    base_color_texture: Optional["TextureRef"] = None
+    metallic_roughness_texture: Optional["TextureRef"] = None
+    normal_texture: Optional["TextureRef"] = None
+    occlusion_texture: Optional["TextureRef"] = None
+    emissive_texture: Optional["TextureRef"] = None
+    normal_scale: float = 1.0
+    occlusion_strength: float = 1.0
+    emissive_factor: tuple = (0.0, 0.0, 0.0)
+
+
+@dataclasses.dataclass
+class TextureRef:
+    """A material's use of scene texture `texture` through TEXCOORD_`texcoord`,
+    with KHR_texture_transform (offset, rotation, scale) when given."""
+    texture: int
+    texcoord: int = 0
+    offset: Optional[tuple] = None
+    rotation: Optional[float] = None
+    scale: Optional[tuple] = None
+
+    @property
+    def transform(self) -> Optional[np.ndarray]:
+        """Rows 0-1 of getTextureTransform's matrix (PbrMaterial.cpp:25-57), float32."""
+        if self.offset is None and self.rotation is None and self.scale is None:
+            return None
+        off = [F32(x) for x in (self.offset or (0.0, 0.0))]
+        sc = [F32(x) for x in (self.scale or (1.0, 1.0))]
+        rot = F32(self.rotation or 0.0)
+        c, s = F32(cosf(rot)), F32(sinf(rot))
+        return np.array([[sc[0] * c, sc[0] * s, off[0]], [-(sc[1] * s), sc[1] * c, off[1]]], dtype=F32)
 
 
 @dataclasses.dataclass
@@ -230,6 +270,7 @@ class Scene:
     camera: CameraSpec
     render: RenderSpec
     gltf_nodes: list = dataclasses.field(default_factory=list)  # for the writer
+    textures: list = dataclasses.field(default_factory=list)    # (H, W, 4) uint8 RGBA images
 
     @property
     def num_triangles(self) -> int:
@@ -529,7 +570,102 @@ def scene_validation(width: int = 64, height: int = 48) -> Scene:
     return Scene("validation", meshes, inst, mats, [light], None, cam, RenderSpec(1, 1, 1, 8), gltf_nodes=[nodes])
 
 
-SCENES = {"c1": scene_c1, "c2": scene_c2, "mixed": scene_mixed, "validation": scene_validation}
+def _texture_images(seed: int = 7) -> List[np.ndarray]:
+    """Seeded RGBA8 images: base colour with a varying alpha (64x32), packed
+    occlusion/roughness/metallic (32x32), a tangent-space normal map including
+    texels with z <= 0.5 (32x32), a separate occlusion map (16x16) and an
+    emission map (16x16)."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:32, 0:64]
+    base = np.zeros((32, 64, 4), np.uint8)
+    chk = ((x // 8 + y // 8) % 2).astype(np.float64)
+    base[..., 0] = np.clip(60 + 160 * chk + rng.integers(0, 30, chk.shape), 0, 255)
+    base[..., 1] = np.clip(200 - 120 * chk + rng.integers(0, 30, chk.shape), 0, 255)
+    base[..., 2] = rng.integers(20, 200, chk.shape)
+    base[..., 3] = np.clip(255 * (0.5 + 0.5 * np.sin(x / 5.0) * np.cos(y / 3.0)), 0, 255)
+    y2, x2 = np.mgrid[0:32, 0:32]
+    mr = np.zeros((32, 32, 4), np.uint8)
+    mr[..., 0] = 128 + (127 * np.cos(x2 / 4.0)).astype(np.int64)
+    mr[..., 1] = np.clip(40 + 7 * x2, 0, 255)
+    mr[..., 2] = np.clip(255 - 8 * y2, 0, 255)
+    mr[..., 3] = 255
+    nrm = np.zeros((32, 32, 4), np.uint8)
+    nx = 0.6 * np.sin(x2 / 3.0)
+    ny = 0.6 * np.cos(y2 / 2.0)
+    nz = np.sqrt(np.clip(1.0 - nx ** 2 - ny ** 2, 0.0, 1.0))
+    nz[:4, :4] = -0.2  # stored z below 0.5: clamped to 0.5 + FLT_EPSILON
+    nrm[..., 0] = np.clip(np.rint(127.5 * (nx + 1.0)), 0, 255)
+    nrm[..., 1] = np.clip(np.rint(127.5 * (ny + 1.0)), 0, 255)
+    nrm[..., 2] = np.clip(np.rint(127.5 * (nz + 1.0)), 0, 255)
+    nrm[..., 3] = 255
+    occ = np.full((16, 16, 4), 255, np.uint8)
+    occ[..., 0] = rng.integers(60, 256, (16, 16))
+    em = np.zeros((16, 16, 4), np.uint8)
+    em[..., :3] = rng.integers(0, 256, (16, 16, 3)) * (rng.random((16, 16, 1)) < 0.3)
+    em[..., 3] = 255
+    return [base, mr, nrm, occ, em]
+
+
+def _sphere_uv(v: np.ndarray) -> np.ndarray:
+    d = v / np.linalg.norm(v, axis=1, keepdims=True)
+    u = 0.5 + np.arctan2(d[:, 2], d[:, 0]) / (2 * math.pi)
+    w = 0.5 - np.arcsin(np.clip(d[:, 1], -1, 1)) / math.pi
+    return np.stack([u, w], 1).astype(F32)
+
+
+def scene_textured(width: int = 32, height: int = 32, spp: int = 8) -> Scene:
+    """Parity scene for the PBR texture paths: base colour (with KHR texture
+    transform and wrapping coordinates), packed metallic-roughness-occlusion,
+    a normal map, a separate occlusion map, an emissive ball, an alpha-masked
+    and an alpha-blended textured material, a second coordinate set, and the
+    OpenMATERIAL conductor; C1's light and camera model, bounces 4."""
+    v, f = icosphere(2)
+    n = (v / np.linalg.norm(v, axis=1, keepdims=True)).astype(F32)
+    uv = _sphere_uv(v)
+    uv1 = (uv * F32(2.0) + F32(0.25)).astype(F32)
+    meshes = []
+    centers = [(-1.6, -0.3, 0.0), (0.0, -0.3, -0.8), (1.6, -0.3, 0.0), (-0.8, 0.9, -1.2), (0.9, 0.9, -1.5)]
+    mats_of = [1, 2, 3, 4, 5]
+    scale = F32(0.7)
+    for i, c in enumerate(centers):
+        p = (v.astype(F32) * scale + np.array(c, dtype=F32)).astype(F32)
+        meshes.append(Mesh(positions=p, normals=n.copy(), faces=f, material=mats_of[i], name=f"ball{i}",
+                           texcoord0=uv.copy(), texcoord1=uv1.copy() if i == 3 else None))
+    qv = np.array([[-5, -1, -5], [5, -1, -5], [5, -1, 5], [-5, -1, 5]], dtype=F32)
+    qf = np.array([[0, 2, 1], [0, 3, 2]], dtype=np.uint32)
+    quv = np.array([[-1.5, -1.5], [2.5, -1.5], [2.5, 2.5], [-1.5, 2.5]], dtype=F32)
+    meshes.append(Mesh(positions=qv, normals=None, faces=qf, material=0, name="ground", texcoord0=quv))
+    T = TextureRef
+    mats = [
+        Material(type=0, base_color=(0.9, 0.9, 0.9, 1.0), metallic=0.8, roughness=0.9, name="ground_textured",
+                 base_color_texture=T(0, 0, offset=(0.1, 0.2), rotation=0.3, scale=(2.0, 1.5)),
+                 metallic_roughness_texture=T(1), normal_texture=T(2), normal_scale=0.8,
+                 occlusion_texture=T(3, scale=(3.0, 3.0)), occlusion_strength=0.7),
+        _om_conductor((0.18, 0.42, 1.37), (3.42, 2.35, 1.77)),
+        Material(type=0, base_color=(1.0, 0.8, 0.6, 1.0), metallic=1.0, roughness=1.0, name="emissive_ball",
+                 base_color_texture=T(0), metallic_roughness_texture=T(1), occlusion_texture=T(1),
+                 occlusion_strength=0.5, emissive_texture=T(4, rotation=1.0), emissive_factor=(1.0, 0.5, 0.2)),
+        Material(type=0, base_color=(0.8, 0.9, 1.0, 0.9), metallic=0.1, roughness=0.4, alpha_mode=1,
+                 alpha_cutoff=0.5, double_sided=True, name="masked", base_color_texture=T(0, 0, scale=(3.0, 2.0))),
+        Material(type=0, base_color=(0.9, 0.9, 0.9, 0.8), metallic=0.3, roughness=0.6, alpha_mode=2, name="blend",
+                 base_color_texture=T(0, 1), normal_texture=T(2, 1), normal_scale=1.2),
+        Material(type=0, base_color=(0.5, 0.7, 0.9, 1.0), metallic=0.0, roughness=0.5, name="second_set",
+                 metallic_roughness_texture=T(1, offset=(0.5, 0.5))),
+    ]
+    root_t = np.eye(4, dtype=F32)
+    root_t[2, 3] = -5.0
+    inst = [Instance(root_t.copy(), i) for i in range(len(meshes))]
+    light = Light(position=(2.0, 4.0, -3.0), intensity=(50.0, 50.0, 50.0))
+    focus = (height / 2.0) / math.tan(math.radians(22.5))
+    cam = camera_from_json(width, height, width / height, focus, 45.0)
+    nodes = {"root_translation": (0.0, 0.0, -5.0), "light_translation": (2.0, 4.0, 2.0),
+             "light_color": (1.0, 1.0, 1.0), "light_intensity": 50.0}
+    return Scene("textured", meshes, inst, mats, [light], None, cam, RenderSpec(spp, 4, 4, 5), gltf_nodes=[nodes],
+                 textures=_texture_images())
+
+
+SCENES = {"c1": scene_c1, "c2": scene_c2, "mixed": scene_mixed, "validation": scene_validation,
+          "textured": scene_textured}
 
 
 # -------------------------------------------------------------------- RGBE --
@@ -636,6 +772,39 @@ def _write_om_material(dirname: str, mat: Material) -> str:
     return mat_file
 
 
+def write_png(path: str, rgba: np.ndarray) -> None:
+    """8-bit RGBA PNG (filter 0 on every row, zlib-compressed)."""
+    import struct
+    import zlib
+
+    a = np.ascontiguousarray(rgba, dtype=np.uint8)
+    h, w = a.shape[:2]
+    raw = b"".join(b"\x00" + a[y].tobytes() for y in range(h))
+
+    def chunk(t: bytes, data: bytes) -> bytes:
+        return struct.pack(">I", len(data)) + t + data + struct.pack(">I", zlib.crc32(t + data) & 0xFFFFFFFF)
+
+    with open(path, "wb") as fh:
+        fh.write(b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0)) +
+                 chunk(b"IDAT", zlib.compress(raw, 6)) + chunk(b"IEND", b""))
+
+
+def _gltf_texture_info(ref: "TextureRef", extra: dict = None) -> dict:
+    info = {"index": int(ref.texture), "texCoord": int(ref.texcoord)}
+    if extra:
+        info.update(extra)
+    if ref.offset is not None or ref.rotation is not None or ref.scale is not None:
+        t = {}
+        if ref.offset is not None:
+            t["offset"] = [float(x) for x in ref.offset]
+        if ref.rotation is not None:
+            t["rotation"] = float(ref.rotation)
+        if ref.scale is not None:
+            t["scale"] = [float(x) for x in ref.scale]
+        info["extensions"] = {"KHR_texture_transform": t}
+    return info
+
+
 def write_gltf(scene: Scene, dirname: str) -> dict:
     """Writes <name>.gltf/.bin (+ material, IOR, camera and HDR files) and returns
     the reference command-line flags (main.cpp:161-193) that render it."""
@@ -672,6 +841,20 @@ def write_gltf(scene: Scene, dirname: str) -> dict:
             if mat.alpha_mode:
                 gm["alphaMode"] = ["OPAQUE", "MASK", "BLEND"][mat.alpha_mode]
                 gm["alphaCutoff"] = float(mat.alpha_cutoff)
+            pmr = gm["pbrMetallicRoughness"]
+            if mat.base_color_texture is not None:
+                pmr["baseColorTexture"] = _gltf_texture_info(mat.base_color_texture)
+            if mat.metallic_roughness_texture is not None:
+                pmr["metallicRoughnessTexture"] = _gltf_texture_info(mat.metallic_roughness_texture)
+            if mat.normal_texture is not None:
+                gm["normalTexture"] = _gltf_texture_info(mat.normal_texture, {"scale": float(mat.normal_scale)})
+            if mat.occlusion_texture is not None:
+                gm["occlusionTexture"] = _gltf_texture_info(mat.occlusion_texture,
+                                                            {"strength": float(mat.occlusion_strength)})
+            if mat.emissive_texture is not None:
+                gm["emissiveTexture"] = _gltf_texture_info(mat.emissive_texture)
+            if any(float(x) != 0.0 for x in mat.emissive_factor):
+                gm["emissiveFactor"] = [float(x) for x in mat.emissive_factor]
             gl_mats.append(gm)
         mat_index[mi] = mi
     for m in scene.meshes:
@@ -682,6 +865,8 @@ def write_gltf(scene: Scene, dirname: str) -> dict:
             attrs["TANGENT"] = add(np.ascontiguousarray(m.tangents, dtype=F32), 5126, "VEC4")
         if m.texcoord0 is not None:
             attrs["TEXCOORD_0"] = add(np.ascontiguousarray(m.texcoord0, dtype=F32), 5126, "VEC2")
+            if m.texcoord1 is not None:
+                attrs["TEXCOORD_1"] = add(np.ascontiguousarray(m.texcoord1, dtype=F32), 5126, "VEC2")
         ind = add(np.ascontiguousarray(m.faces, dtype=np.uint32).reshape(-1), 5125, "SCALAR")
         prim = {"attributes": attrs, "indices": ind}
         if 0 <= m.material < len(scene.materials):
@@ -715,6 +900,21 @@ def write_gltf(scene: Scene, dirname: str) -> dict:
            "scene": 0, "scenes": [{"nodes": scene_nodes}], "nodes": nodes, "meshes": gl_meshes,
            "materials": gl_mats, "accessors": accessors, "bufferViews": views,
            "buffers": [{"uri": bin_name, "byteLength": len(blob)}]}
+    if scene.textures:
+        images = []
+        for i, img in enumerate(scene.textures):
+            name = f"{scene.name}_tex{i}.png"
+            write_png(os.path.join(dirname, name), img)
+            images.append({"uri": name})
+        doc["images"] = images
+        doc["samplers"] = [{}]
+        doc["textures"] = [{"source": i, "sampler": 0} for i in range(len(images))]
+        refs = [getattr(m, slot) for m in scene.materials for slot in
+                ("base_color_texture", "metallic_roughness_texture", "normal_texture", "occlusion_texture",
+                 "emissive_texture")]
+        if any(r is not None and (r.offset is not None or r.rotation is not None or r.scale is not None)
+               for r in refs):
+            used.append("KHR_texture_transform")
     if extensions:
         doc["extensions"] = extensions
     if used:

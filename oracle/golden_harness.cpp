@@ -22,6 +22,8 @@
  *   golden_harness median  W H in out     SimpleDenoiserMedian<1> (Denoiser.h:24); in/out as tonemap
  *   golden_harness rgba8   W H in out     saveImage's conversion (main.cpp:92): unsigned char(255 f),
  *       out: W*H*4 bytes
+ *   golden_harness texture W H img uv out BitmapTexture::texture(u, v, fvec4) (BitmapTexture.cpp:108-125)
+ *       img: W*H*4 bytes; uv: 2 floats/case; out: 4 floats/case
  */
 #include <algorithm>
 #include <cstdio>
@@ -37,6 +39,7 @@
 #include "RandomSampler.h"
 #include "ToneMapping.h"
 #include "Denoiser.h"
+#include "BitmapTexture.h"
 #include "materials/AssetMaterial.h"
 #include "materials/AssetMaterialIor.h"
 
@@ -172,6 +175,21 @@ int main(int argc, char** argv)
         long n = std::atol(argv[3]);
         for (long i = 0; i < n; ++i) out.push_back(rs.rand());
         write_floats(argv[4], out);
+    } else if (mode == "texture" && argc == 7) {
+        const int W = std::atoi(argv[2]), H = std::atoi(argv[3]);
+        FILE* f = std::fopen(argv[4], "rb");
+        if (!f) return 2;
+        std::vector<unsigned char> img((size_t)W * H * 4);
+        if (std::fread(img.data(), 1, img.size(), f) != img.size()) return 2;
+        std::fclose(f);
+        BitmapTexture tex(W, H, reinterpret_cast<ubvec4*>(img.data()));
+        auto uv = read_floats(argv[5]);
+        for (size_t i = 0; i + 2 <= uv.size(); i += 2) {
+            fvec4 t;
+            tex.texture(uv[i], uv[i + 1], t);
+            out.insert(out.end(), t, t + 4);
+        }
+        write_floats(argv[6], out);
     } else if ((mode == "tonemap" && argc == 7) || ((mode == "median" || mode == "rgba8") && argc == 6)) {
         const int W = std::atoi(argv[2]), H = std::atoi(argv[3]);
         const bool tm = mode == "tonemap";

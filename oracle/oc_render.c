@@ -25,6 +25,15 @@
 
 enum { MAT_PBR = 0, MAT_OM = 1, MAT_MISSING = 2 };
 
+/* PbrMaterial::TextureData (PbrMaterial.h:24-34): image index (-1: none),
+ * TEXCOORD set and the first two rows of the 3x3 transformation */
+typedef struct oc_tref {
+    int tex, ch;
+    float m[2][3];
+} oc_tref;
+
+enum { TEX_BASE = 0, TEX_METROUGH = 1, TEX_NORMAL = 2, TEX_OCCLUSION = 3, TEX_EMISSIVE = 4, TEX_SLOTS = 5 };
+
 typedef struct oc_mat {
     int type;
     float color[4];
@@ -34,13 +43,22 @@ typedef struct oc_mat {
     int double_sided;
     float om_n[3], om_k[3];
     int has_ior;
+    oc_tref tref[TEX_SLOTS];
+    float normal_scale, occl_strength, emissive[3];
 } oc_mat;
+
+/* BitmapTexture (BitmapTexture.cpp): 8-bit RGBA texels */
+typedef struct oc_tex {
+    int w, h;
+    unsigned char* rgba;
+} oc_tex;
 
 typedef struct oc_mesh_r {
     int valid;
     int vn, fn, mat;
     uint32_t* faces;
     float* v; /* vn * 10: position, normal, tangent(4) */
+    float* uv[2]; /* TEXCOORD_0 / _1: vn * 2, or NULL */
     oc_tri_mesh geo;
 } oc_mesh_r;
 
@@ -69,6 +87,8 @@ struct oc_scene {
     float* bg; /* bg_w*bg_h*3 */
     float bg_R[3][3];
     float bg_scale;
+    int n_tex;
+    oc_tex* tex;
 };
 
 /* ------------------------------------------------------------ commit --- */
@@ -210,6 +230,35 @@ oc_scene* oc_scene_create(const omv_scene_desc* d)
             m->alpha_mode = md->alpha_mode;
             m->cutoff = md->alpha_cutoff;
             m->double_sided = md->double_sided;
+            const omv_texture_ref* refs[TEX_SLOTS] = {&md->base_color_texture, &md->metallic_roughness_texture,
+                                                     &md->normal_texture, &md->occlusion_texture,
+                                                     &md->emissive_texture};
+            for (int k = 0; k < TEX_SLOTS; ++k) {
+                oc_tref* t = &m->tref[k];
+                t->tex = refs[k]->texture - 1;
+                t->ch = refs[k]->texcoord;
+                for (int a = 0; a < 2; ++a)
+                    for (int b = 0; b < 3; ++b)
+                        t->m[a][b] = refs[k]->has_transform ? refs[k]->transform[a][b] : (a == b ? 1.0f : 0.0f);
+            }
+            m->normal_scale = md->normal_scale;
+            m->occl_strength = md->occlusion_strength;
+            memcpy(m->emissive, md->emissive_factor, sizeof(m->emissive));
+        }
+    }
+    for (int i = 0; i < s->n_mat; ++i)
+        if (s->mats[i].type != MAT_PBR)
+            for (int k = 0; k < TEX_SLOTS; ++k) s->mats[i].tref[k].tex = -1;
+    s->n_tex = d->num_textures > 0 ? d->num_textures : 0;
+    s->tex = (oc_tex*)calloc((size_t)(s->n_tex > 0 ? s->n_tex : 1), sizeof(oc_tex));
+    for (int i = 0; i < s->n_tex; ++i) {
+        const omv_texture_desc* td = &d->textures[i];
+        oc_tex* t = &s->tex[i];
+        t->w = td->width;
+        t->h = td->height;
+        if (td->rgba && t->w > 0 && t->h > 0) {
+            t->rgba = (unsigned char*)malloc((size_t)t->w * t->h * 4);
+            memcpy(t->rgba, td->rgba, (size_t)t->w * t->h * 4);
         }
     }
     oc_mat* miss = &s->mats[s->n_mat - 1]; /* DiffuseColorMaterial(BDPT_MISSING_MATERIAL_COLOR) */
@@ -234,17 +283,25 @@ oc_scene* oc_scene_create(const omv_scene_desc* d)
             if (md->normals) memcpy(m->v + (size_t)k * 10 + 3, md->normals + (size_t)k * md->normal_stride, 3 * sizeof(float));
             if (md->tangents) memcpy(m->v + (size_t)k * 10 + 6, md->tangents + (size_t)k * md->tangent_stride, 4 * sizeof(float));
         }
-        /* RenderScene::commitScene material resolution (RenderScene.cpp:158-176) */
+        const float* uvs[2] = {md->texcoord0, md->texcoord0 ? md->texcoord1 : NULL};
+        for (int c = 0; c < 2; ++c) {
+            if (!uvs[c]) continue;
+            m->uv[c] = (float*)malloc(sizeof(float) * 2 * (size_t)m->vn);
+            for (int k = 0; k < m->vn; ++k)
+                memcpy(m->uv[c] + 2 * (size_t)k, uvs[c] + (size_t)k * md->texcoord_stride, 2 * sizeof(float));
+        }
+        /* RenderScene::commitScene material resolution (RenderScene.cpp:158-176):
+         * PhysicallyBasedMaterial::getNormalTextureChannel = normalTexture.texCoord */
         int norm_ch = -1;
-        if (m->mat >= 0 && m->mat < s->n_mat) {
-            norm_ch = s->mats[m->mat].type == MAT_PBR ? 0 : -1; /* PBR: normalTexture.texCoord (default 0) */
+        if (m->mat >= 0 && m->mat < s->n_mat - 1) {
+            norm_ch = s->mats[m->mat].type == MAT_PBR ? d->materials[m->mat].normal_texture.texcoord : -1;
         } else {
             m->mat = s->n_mat - 1;
         }
         if (!md->normals) compute_normals(m);
         if (!md->tangents) {
-            if (norm_ch == 0 && md->texcoord0)
-                compute_tangents_uv(m, md->texcoord0, md->texcoord_stride);
+            if (norm_ch >= 0 && norm_ch < 2 && m->uv[norm_ch])
+                compute_tangents_uv(m, m->uv[norm_ch], 2);
             else
                 for (int k = 0; k < m->vn; ++k) random_tangent(m->v + (size_t)k * 10 + 3, m->v + (size_t)k * 10 + 6);
         }
@@ -319,6 +376,8 @@ void oc_scene_destroy(oc_scene* s)
     for (int i = 0; i < s->n_mesh; ++i) {
         free(s->meshes[i].faces);
         free(s->meshes[i].v);
+        free(s->meshes[i].uv[0]);
+        free(s->meshes[i].uv[1]);
         oc_free_bvh(&s->meshes[i].geo.bvh);
     }
     free(s->meshes);
@@ -331,6 +390,8 @@ void oc_scene_destroy(oc_scene* s)
     free(s->lrange);
     free(s->lcdf);
     free(s->bg);
+    for (int i = 0; i < s->n_tex; ++i) free(s->tex[i].rgba);
+    free(s->tex);
     free(s);
 }
 
@@ -451,6 +512,125 @@ static void face_normal(const oc_scene* s, const oc_sp* sp, float* tfn)
     oc_cross3(E1, E2, fn);
     oc_mat3_vec((const float(*)[3])s->inst[sp->inst].N, fn, tfn);
     oc_normalize3(tfn);
+}
+
+/* ---------------------------------------------------------- textures --- */
+
+/* BitmapTexture::getPixCoords + texture(u, v, fvec4) (BitmapTexture.cpp:73-125):
+ * bilinear, wrapping, texels scaled by 1/255 */
+static void tex_sample(const oc_tex* t, float u, float v, float* out)
+{
+    if (!t->rgba) {
+        out[0] = out[1] = out[2] = 0.5f;
+        out[3] = 1.0f;
+        return;
+    }
+    const int W = t->w, H = t->h;
+    float upage = floorf(u - 0.5f / (float)W);
+    float vpage = floorf(v - 0.5f / (float)H);
+    u -= upage;
+    v -= vpage;
+    u *= (float)W;
+    v *= (float)H;
+    int iu = (int)u, iv = (int)v;
+    float kui = u - (float)iu, kvi = v - (float)iv;
+    float ku = 1.0f - kui, kv = 1.0f - kvi;
+    int l = iu % W, r = (iu + 1) % W, b = iv % H, tp = (iv + 1) % H;
+    const int id[4] = {b * W + l, b * W + r, tp * W + l, tp * W + r};
+    const float w[4] = {ku * kv, kui * kv, ku * kvi, kui * kvi};
+    const float sc = 1.0f / 255.0f;
+    for (int i = 0; i < 4; ++i)
+        out[i] = (float)t->rgba[4 * (size_t)id[0] + i] * w[0] * sc + (float)t->rgba[4 * (size_t)id[1] + i] * w[1] * sc +
+                 (float)t->rgba[4 * (size_t)id[2] + i] * w[2] * sc + (float)t->rgba[4 * (size_t)id[3] + i] * w[3] * sc;
+}
+
+/* SurfacePoint::getTexCoords -> RenderMesh::getTexCoord (RenderMesh.cpp:146-157):
+ * barycentric interpolation of the channel's coordinates; (0, 0) and false
+ * when the mesh has no such channel */
+static int tex_coords(const oc_scene* s, const oc_sp* sp, int ch, float* tc)
+{
+    tc[0] = tc[1] = 0.0f;
+    const oc_mesh_r* m = &s->meshes[sp->mesh];
+    if (ch < 0 || ch > 1 || !m->uv[ch] || sp->face < 0 || sp->face >= m->fn) return 0;
+    const uint32_t* fi = m->faces + 3 * (size_t)sp->face;
+    const float* uv[3] = {m->uv[ch] + 2 * (size_t)fi[0], m->uv[ch] + 2 * (size_t)fi[1], m->uv[ch] + 2 * (size_t)fi[2]};
+    const float* bc = sp->bary;
+    tc[0] = uv[0][0] * bc[0] + uv[1][0] * bc[1] + uv[2][0] * bc[2];
+    tc[1] = uv[0][1] * bc[0] + uv[1][1] * bc[1] + uv[2][1] * bc[2];
+    return 1;
+}
+
+static int tex_valid(const oc_scene* s, int id) { return 0 <= id && id < s->n_tex; }
+
+/* multVector3(TM, (u, v, 1)) then BitmapTexture::texture */
+static void tex_transformed(const oc_scene* s, const oc_tref* t, const float* uv, float* out)
+{
+    const float uu = t->m[0][0] * uv[0] + t->m[0][1] * uv[1] + t->m[0][2] * 1.0f;
+    const float vv = t->m[1][0] * uv[0] + t->m[1][1] * uv[1] + t->m[1][2] * 1.0f;
+    tex_sample(&s->tex[t->tex], uu, vv, out);
+}
+
+/* a texture slot as the Helper reads it: sampled only if the map exists and
+ * the mesh has the slot's coordinate set */
+static int tex_slot(const oc_scene* s, const oc_mat* m, int slot, const oc_sp* sp, float* out)
+{
+    const oc_tref* t = &m->tref[slot];
+    float uv[2];
+    if (!tex_valid(s, t->tex) || !tex_coords(s, sp, t->ch, uv)) return 0;
+    tex_transformed(s, t, uv, out);
+    return 1;
+}
+
+/* Helper::getTextureOccMetRoughValues (PhysicallyBasedMaterial.cpp:54-90) */
+static void pbr_omr(const oc_scene* s, const oc_mat* m, const oc_sp* sp, float* omr)
+{
+    omr[0] = 1.0f;
+    omr[1] = m->metal;
+    omr[2] = m->rough;
+    float tb[4];
+    if (tex_slot(s, m, TEX_METROUGH, sp, tb)) {
+        omr[0] *= tb[0];
+        omr[1] *= tb[2];
+        omr[2] *= tb[1];
+    }
+    if (m->tref[TEX_OCCLUSION].tex != m->tref[TEX_METROUGH].tex && tex_slot(s, m, TEX_OCCLUSION, sp, tb))
+        omr[0] = tb[0];
+}
+
+/* PhysicallyBasedMaterial::modifyFrame (:147-167) */
+static void pbr_modify_frame(const oc_scene* s, const oc_mat* m, oc_sp* sp)
+{
+    float tn[4] = {0.0f, 0.0f, 1.0f, 0.0f};
+    if (tex_slot(s, m, TEX_NORMAL, sp, tn)) {
+        if (tn[2] <= 0.5f) tn[2] = 0.5f + OC_EPS;
+        for (int i = 0; i < 3; ++i) tn[i] = oc_linf(2.0f, -1.0f, tn[i]);
+        for (int i = 0; i < 2; ++i) tn[i] = m->normal_scale * tn[i];
+        oc_normalize3(tn);
+    }
+    apply_texture_normal(sp, tn);
+}
+
+/* modifyFrame of each material type (OpenMaterial.cpp:66-70, DiffuseColorMaterial.cpp:35-39) */
+static void modify_frame(const oc_scene* s, const oc_mat* m, oc_sp* sp)
+{
+    static const float tn[3] = {0.0f, 0.0f, 1.0f};
+    if (m->type == MAT_PBR)
+        pbr_modify_frame(s, m, sp);
+    else
+        apply_texture_normal(sp, tn);
+}
+
+/* PhysicallyBasedMaterial::getEmissivity + Helper::getTextureEmissivity
+ * (:96-117, :293-299) at the emissive channel's coordinates */
+static void pbr_emission(const oc_scene* s, const oc_mat* m, const oc_sp* sp, float* erad)
+{
+    float euv[2];
+    tex_coords(s, sp, m->tref[TEX_EMISSIVE].ch, euv);
+    if (!(oc_length3(m->emissive) > OC_EPS)) return;
+    if (!tex_valid(s, m->tref[TEX_EMISSIVE].tex)) return;
+    float tb[4];
+    tex_transformed(s, &m->tref[TEX_EMISSIVE], euv, tb);
+    for (int i = 0; i < 3; ++i) erad[i] = tb[i] * m->emissive[i];
 }
 
 /* ------------------------------------------------------------- BRDF --- */
@@ -687,16 +867,21 @@ static void om_brdf_channels(const float* n, const float* k, float fCos, float* 
     }
 }
 
-/* PhysicallyBasedMaterial: BSDFData from the material factors (no textures):
- * getTextureRGBA, getTextureOccMetRoughValues, occluseColor (PhysicallyBasedMaterial.cpp:27-95) */
-static void pbr_data(const oc_mat* m, bsdf_data* d)
+/* PhysicallyBasedMaterial: BSDFData from the material factors and textures:
+ * getTextureRGBA, getTextureOccMetRoughValues, occluseColor (PhysicallyBasedMaterial.cpp:27-95,
+ * 178-200, 261-276) */
+static void pbr_data(const oc_scene* s, const oc_mat* m, const oc_sp* sp, bsdf_data* d)
 {
-    for (int i = 0; i < 4; ++i) d->color[i] = 1.0f * m->color[i];
+    float rgba[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+    tex_slot(s, m, TEX_BASE, sp, rgba);
+    for (int i = 0; i < 4; ++i) d->color[i] = rgba[i] * m->color[i];
     if (m->alpha_mode != OMV_ALPHA_BLEND) d->color[3] = 1.0f;
     d->transmissive = m->double_sided || d->color[3] < 1.0f;
-    for (int i = 0; i < 3; ++i) d->color[i] = oc_lerp(d->color[i], 1.0f * d->color[i], 1.0f);
-    d->metal = m->metal;
-    d->rough = oc_clamp(m->rough, 0.00001f, 0.99999f);
+    float omr[3];
+    pbr_omr(s, m, sp, omr);
+    for (int i = 0; i < 3; ++i) d->color[i] = oc_lerp(d->color[i], omr[0] * d->color[i], m->occl_strength);
+    d->metal = omr[1];
+    d->rough = oc_clamp(omr[2], 0.00001f, 0.99999f);
     d->alpha = powf(d->rough, 2.0f);
 }
 
@@ -710,7 +895,7 @@ static void material_get_brdf(const oc_scene* s, const oc_mat* m, const float* i
         memcpy(d.I, inV, sizeof(d.I));
         memcpy(d.O, outV, sizeof(d.O));
         memcpy(d.N, sp->nrm, sizeof(d.N));
-        pbr_data(m, &d);
+        pbr_data(s, m, sp, &d);
         if (oc_dot3(inV, sp->nrm) > 0.0f && d.transmissive) {
             d.N[0] = -d.N[0]; d.N[1] = -d.N[1]; d.N[2] = -d.N[2];
         }
@@ -745,10 +930,11 @@ static void material_ray_and_brdf(const oc_scene* s, const oc_mat* m, const floa
         memcpy(d.I, inV, sizeof(d.I));
         memcpy(d.N, sp->nrm, sizeof(d.N));
         memcpy(d.T, sp->tan, sizeof(d.T));
-        pbr_data(m, &d);
+        pbr_data(s, m, sp, &d);
         d.eta = 1.0f / (m->double_sided ? 1.0f : m->ior);
         bsdf_sample_indirect(&d, rs, brdf);
         memcpy(outV, d.O, sizeof(d.O));
+        pbr_emission(s, m, sp, erad);
     } else if (m->type == MAT_OM) { /* OpenMaterial::defineNextDirection + getRayAndBrdf (:72-93, :165-232) */
         oc_reflect3(inV, sp->nrm, outV);
         float tfn[3];
@@ -780,12 +966,19 @@ static void material_ray_and_brdf(const oc_scene* s, const oc_mat* m, const floa
     }
 }
 
-/* PhysicallyBasedMaterial::isMasked (:301-316) without a base colour texture */
-static int material_masked(const oc_mat* m)
+/* PhysicallyBasedMaterial::isMasked (:301-316): the base colour texture's
+ * alpha at the untransformed coordinates (BitmapTexture::texture(sp, ...),
+ * BitmapTexture.cpp:142-156: 1 where the mesh lacks the coordinate set) */
+static int material_masked(const oc_scene* s, const oc_mat* m, const oc_sp* sp)
 {
     if (m->type != MAT_PBR || m->alpha_mode != OMV_ALPHA_MASK) return 0;
     float alpha = m->color[3];
     if (alpha < m->cutoff) return 1;
+    if (tex_valid(s, m->tref[TEX_BASE].tex)) {
+        float tc[4] = {0.5f, 0.5f, 0.5f, 1.0f}, uv[2];
+        if (tex_coords(s, sp, m->tref[TEX_BASE].ch, uv)) tex_sample(&s->tex[m->tref[TEX_BASE].tex], uv[0], uv[1], tc);
+        alpha *= tc[3];
+    }
     return alpha < m->cutoff;
 }
 
@@ -833,7 +1026,7 @@ static int scene_intersect(ctx* c, oc_rh* h, oc_sp* sp)
         if (h->geom == OC_INVALID) return 0;
         compute_surface_point(c->s, h, sp);
         const oc_mat* m = &c->s->mats[c->s->meshes[sp->mesh].mat];
-        if (!material_masked(m)) return 1;
+        if (!material_masked(c->s, m, sp)) return 1;
         float org[3] = {h->org[0] + h->tfar * h->dir[0], h->org[1] + h->tfar * h->dir[1], h->org[2] + h->tfar * h->dir[2]};
         float v = oc_max_abs(org, 1.0f);
         v = v > h->tfar ? v : h->tfar;
@@ -903,8 +1096,7 @@ static int compute_path(ctx* c, part* P, int max_n, const float* O, const float*
             break;
         }
         const oc_mat* m = &c->s->mats[c->s->meshes[P[i].sp.mesh].mat];
-        static const float tn[3] = {0.0f, 0.0f, 1.0f};
-        apply_texture_normal(&P[i].sp, tn); /* modifyFrame of every material without a normal map */
+        modify_frame(c->s, m, &P[i].sp);
         material_ray_and_brdf(c->s, m, P[i - 1].out_ray, &P[i].sp, P[i].out_ray, brdf, erad, inv, rs);
         float ct = fabsf(inv ? oc_dot3(P[i].out_ray, P[i].sp.nrm) : oc_dot3(P[i - 1].out_ray, P[i].sp.nrm));
         for (int k = 0; k < 3; ++k) P[i].out_factor[k] = P[i - 1].out_factor[k] * brdf[k] * ct;
@@ -1467,7 +1659,7 @@ int32_t oc_render_fc(const oc_scene* s, const omv_camera* cam, uint32_t seed, in
             uint32_t arg = 0;
             if (hit) {
                 const oc_mat* m = &s->mats[s->meshes[sp.mesh].mat];
-                apply_texture_normal(&sp, (const float[3]){0.0f, 0.0f, 1.0f}); /* modifyFrame */
+                modify_frame(s, m, &sp);
                 float inV[3] = {R[0], R[1], R[2]};
                 if (m->type == MAT_MISSING) { /* RenderMaterial::getRayAndBrdf: hemisphere, then getBrdf(-out, -in) */
                     float v[3], outV[3];
@@ -1506,7 +1698,11 @@ int32_t oc_render_fc(const oc_scene* s, const omv_camera* cam, uint32_t seed, in
                     break;
                 case OMV_FC_MMP:
                 case OMV_FC_RMP:
-                    if (m->type == MAT_PBR) f = fc_clamped(subject == OMV_FC_MMP ? m->metal : m->rough);
+                    if (m->type == MAT_PBR) {
+                        float omr[3];
+                        pbr_omr(s, m, &sp, omr);
+                        f = fc_clamped(subject == OMV_FC_MMP ? omr[1] : omr[2]);
+                    }
                     memcpy(&arg, &f, 4);
                     fc_lerp_paint(f, white, subject == OMV_FC_MMP ? blue : green, col);
                     break;
@@ -1591,4 +1787,11 @@ int32_t oc_render_views(const oc_scene* s, int32_t n, const omv_camera* cams, co
         oc_film_stop(j.film, (int64_t)px);
     }
     return 0;
+}
+
+/* BitmapTexture::texture(u, v, fvec4) on one RGBA8 image for n coordinate pairs */
+void oc_texture_sample(int32_t w, int32_t h, const uint8_t* rgba, int64_t n, const float* uv, float* out)
+{
+    oc_tex t = {w, h, (unsigned char*)rgba};
+    for (int64_t i = 0; i < n; ++i) tex_sample(&t, uv[2 * i], uv[2 * i + 1], out + 4 * i);
 }

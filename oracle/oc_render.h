@@ -76,6 +76,8 @@ void oc_camera_rays(const omv_camera* cam, const float* jitter, float* rays);
 void oc_env_radiance(const oc_scene* s, int64_t n, const float* dirs, float* rgb);
 /* AssetMaterialIor::getIor linear branch (AssetMaterialIor.cpp:133-145) */
 float oc_ior_lookup(const float* table, int32_t count, float wl);
+/* BitmapTexture::texture(u, v, fvec4) (BitmapTexture.cpp:73-125): n pairs in, 4 floats each out */
+void oc_texture_sample(int32_t w, int32_t h, const uint8_t* rgba, int64_t n, const float* uv, float* out);
 /* first n uniforms of std::mt19937(seed) + uniform_real_distribution<float> */
 void oc_mt_uniforms(uint32_t seed, int64_t n, float* out);
 

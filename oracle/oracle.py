@@ -70,6 +70,7 @@ def lib():
         L.oc_render_fc.argtypes = [vp, C.POINTER(capi.Camera), C.c_uint32, C.c_int32, C.POINTER(C.c_uint32),
                                    C.c_int32, capi.f32p, C.POINTER(C.c_uint32), capi.f32p, C.POINTER(capi.Hit)]
         L.oc_density_range.argtypes = [vp, capi.f32p]
+        L.oc_texture_sample.argtypes = [C.c_int32, C.c_int32, C.POINTER(C.c_uint8), C.c_int64, capi.f32p, capi.f32p]
         L.oc_render_views.argtypes = [vp, C.c_int32, C.POINTER(capi.Camera), C.POINTER(capi.Params), C.c_uint32,
                                       capi.f32p]
         L.oc_tonemap.argtypes = [capi.f32p, C.c_int64, C.c_float, C.c_float]
@@ -244,4 +245,14 @@ def rgba8(img: np.ndarray) -> np.ndarray:
     x = np.ascontiguousarray(img, dtype=np.float32)
     out = np.zeros(x.shape, dtype=np.uint8)
     lib().oc_rgba8(capi.fptr(x), x.size, out.ctypes.data_as(C.POINTER(C.c_uint8)))
+    return out
+
+
+def texture_sample(img: np.ndarray, uv: np.ndarray) -> np.ndarray:
+    """BitmapTexture::texture of an (H, W, 4) uint8 image at n (u, v) pairs."""
+    a = np.ascontiguousarray(img, dtype=np.uint8)
+    x = np.ascontiguousarray(uv, dtype=np.float32).reshape(-1, 2)
+    out = np.zeros((len(x), 4), dtype=np.float32)
+    lib().oc_texture_sample(a.shape[1], a.shape[0], a.ctypes.data_as(C.POINTER(C.c_uint8)), len(x), capi.fptr(x),
+                            capi.fptr(out))
     return out

@@ -20,6 +20,10 @@ Fixtures (numpy .npz):
   ids_c1_64.npz     primary rays and hits of the false-colour (-F mid) pass
   post.npz          gammaCorrection (two gammas), SimpleDenoiserMedian<1> and
                     saveImage's 8-bit conversion on a seeded 23x37 HDR image
+  texture.npz       BitmapTexture::texture on seeded images and coordinates
+                    (wrapping, negative, texel-centre and edge cases)
+  film_textured_32x8.npz / scene_textured.npz
+                    -C 1 film and committed scene of the textured PBR scene
   fc.npz            false-colour films (-F pid gid mid mmp rmp md sg mn in, and an
                     unknown name) of the validation scene, before tone mapping
   lightbox.npz      the 8 light-box views (-V) of the mixed scene: cameras
@@ -297,6 +301,33 @@ def gen_post(tmp):
     np.savez_compressed(os.path.join(HERE, "post.npz"), **out)
 
 
+def gen_texture(tmp):
+    rng = np.random.default_rng(12)
+    out = {}
+    for k, (W, H) in enumerate(((7, 5), (64, 32), (1, 1))):
+        img = rng.integers(0, 256, (H, W, 4), dtype=np.uint8)
+        uv = np.concatenate([rng.uniform(-3.0, 3.0, (3000, 2)),
+                             (np.stack(np.meshgrid(np.arange(W + 1), np.arange(H + 1)), -1).reshape(-1, 2) + 0.5)
+                             / np.array([W, H]),
+                             [[0.0, 0.0], [1.0, 1.0], [-1e-7, 1e-7], [0.5 / W, 0.5 / H], [1.0 - 1e-7, 0.9999999]]]
+                            ).astype(np.float32)
+        pi = os.path.join(tmp, f"tex{k}.bin")
+        img.tofile(pi)
+        o = os.path.join(tmp, f"tex{k}.out")
+        harness("texture", W, H, pi, f32file(tmp, f"uv{k}.bin", uv), o)
+        out[f"img{k}"], out[f"uv{k}"] = img, uv
+        out[f"y{k}"] = np.fromfile(o, dtype=np.float32).reshape(-1, 4)
+    np.savez_compressed(os.path.join(HERE, "texture.npz"), **out)
+
+
+def gen_textured(tmp):
+    sc = S.scene_textured(32, 32, 8)
+    film, secs, rays, dump = render_reference(sc, tmp)
+    np.savez_compressed(os.path.join(HERE, "film_textured_32x8.npz"), film=film, seconds=secs, rays=rays,
+                        width=32, height=32, spp=8)
+    np.savez_compressed(os.path.join(HERE, "scene_textured.npz"), **dump)
+
+
 FC_SUBJECTS = ["pid", "gid", "mid", "mmp", "rmp", "md", "sg", "mn", "in", "nosuch"]
 
 
@@ -333,7 +364,8 @@ def gen_lightbox(tmp):
 
 
 GENS = {"mt": gen_mt, "brdf": gen_brdf, "om": gen_om, "ior": gen_ior, "env": gen_env, "camera": gen_camera,
-        "films": gen_films, "ids": gen_ids, "post": gen_post, "fc": gen_fc, "lightbox": gen_lightbox}
+        "films": gen_films, "ids": gen_ids, "post": gen_post, "fc": gen_fc, "lightbox": gen_lightbox,
+        "textured": gen_textured, "texture": gen_texture}
 
 
 def main():
