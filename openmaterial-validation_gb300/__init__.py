@@ -130,6 +130,7 @@ def lib():
                                 C.POINTER(C.c_uint32), C.c_int32, capi.f32p, C.POINTER(C.c_uint32),
                                 C.POINTER(capi.Hit)]
     L.omv_scene_bounds.argtypes = [vp, capi.f32p, capi.f32p]
+    L.omv_texture_sample.argtypes = [C.c_int32, C.c_int32, C.POINTER(C.c_uint8), C.c_int64, capi.f32p, capi.f32p]
     L.omv_lightbox_cameras.argtypes = [capi.f32p, capi.f32p, C.c_int32, C.c_int32, C.POINTER(capi.Camera)]
     L.omv_develop.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_float, C.c_float, vp, vp, vp, C.c_int32, vp]
     L.omv_tonemap.argtypes = [vp, C.c_int64, C.c_float, C.c_float, vp]
@@ -147,7 +148,7 @@ def lib():
               "omv_trace_rays", "omv_render_ids", "omv_brdf_eval_direct",
               "omv_brdf_sample_indirect", "omv_om_fresnel", "omv_camera_rays", "omv_env_radiance", "omv_struct_sizes",
               "omv_develop", "omv_tonemap", "omv_denoise_median", "omv_rgba8", "omv_save_image",
-              "omv_render_fc", "omv_scene_bounds", "omv_lightbox_cameras"):
+              "omv_render_fc", "omv_scene_bounds", "omv_lightbox_cameras", "omv_texture_sample"):
         getattr(L, n).restype = st
     _lib = L
     return L
@@ -459,6 +460,16 @@ def brdf_sample_indirect(x: np.ndarray) -> np.ndarray:
 
 def om_fresnel(x: np.ndarray) -> np.ndarray:
     return _hook("omv_om_fresnel", 7, 3, x)
+
+
+def texture_sample(img: np.ndarray, uv: np.ndarray) -> np.ndarray:
+    """BitmapTexture::texture on the device: (H, W, 4) uint8 image, (n, 2) coordinates."""
+    a = np.ascontiguousarray(img, dtype=np.uint8)
+    x = np.ascontiguousarray(uv, dtype=np.float32).reshape(-1, 2)
+    out = np.zeros((len(x), 4), dtype=np.float32)
+    check(lib().omv_texture_sample(a.shape[1], a.shape[0], a.ctypes.data_as(C.POINTER(C.c_uint8)), len(x),
+                                   capi.fptr(x), capi.fptr(out)))
+    return out
 
 
 def camera_rays(camera: PinholeCamera, jitter: np.ndarray) -> np.ndarray:

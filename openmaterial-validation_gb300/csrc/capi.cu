@@ -369,6 +369,24 @@ omv_status omv_om_fresnel(int64_t n, const float* in, float* out)
     return run_hook(n, in, out, 7, 3, omv::hook_om_fresnel);
 }
 
+omv_status omv_texture_sample(int32_t width, int32_t height, const uint8_t* rgba, int64_t n, const float* uv,
+                              float* out)
+{
+    return guarded([&] {
+        if (width <= 0 || height <= 0 || !rgba) throw omv::ArgError("texture needs a positive size and texels");
+        if (n < 0 || (n > 0 && (!uv || !out))) throw omv::ArgError("invalid buffers");
+        if (n == 0) return;
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) throw omv::CudaError("no CUDA device available");
+        const size_t tb = (size_t)width * height * 4;
+        DevTmp dt(tb), du(sizeof(float) * 2 * n), dout(sizeof(float) * 4 * n), dtab(64);
+        OMV_CUDA(cudaMemcpy(dt.p, rgba, tb, cudaMemcpyHostToDevice));
+        OMV_CUDA(cudaMemcpy(du.p, uv, sizeof(float) * 2 * n, cudaMemcpyHostToDevice));
+        omv::hook_texture_sample(width, height, dt.as<uint8_t>(), n, du.as<float>(), dout.as<float>(), dtab.p, nullptr);
+        OMV_CUDA(cudaMemcpy(out, dout.p, sizeof(float) * 4 * n, cudaMemcpyDeviceToHost));
+    });
+}
+
 omv_status omv_camera_rays(const omv_camera* camera, const float* jitter, float* rays)
 {
     return guarded([&] {

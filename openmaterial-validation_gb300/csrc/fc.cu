@@ -167,8 +167,8 @@ __global__ void __launch_bounds__(kFcThreads) k_fc(DevScene S, const uint32_t* i
     uint32_t arg = 0;
     const bool hit = scene_intersect(S, items, so, R, tnear, kFltMax, h, st, tc);
     if (hit) {
-        const Surf sp = surface_point(S, h.inst, h.prim, h.u, h.v, true);  // includes modifyFrame
-        const DevMaterial& M = S.mats[sp.mat];
+        const DevMaterial& M = S.mats[__ldg(&S.insts[h.inst].material)];
+        const Surf sp = surface_point(S, h.inst, h.prim, h.u, h.v, true, &M);  // includes modifyFrame
         const DevInstance* I = S.insts + h.inst;
         const uint32_t mesh = __ldg(&I->mesh);
         V3 inV = R;
@@ -195,7 +195,11 @@ __global__ void __launch_bounds__(kFcThreads) k_fc(DevScene S, const uint32_t* i
             break;
         case OMV_FC_MMP:
         case OMV_FC_RMP: {
-            const float f = M.type == kMatPbr ? clamp01(a.subject == OMV_FC_MMP ? M.metal : M.rough) : 0.0f;
+            float f = 0.0f;
+            if (M.type == kMatPbr) {  // getTextureOccMetRoughValues (PhysicallyBasedMaterial.cpp:54-90)
+                const PbrParams P = pbr_params(S, M, sp);
+                f = clamp01(a.subject == OMV_FC_MMP ? P.omr_metal : P.omr_rough);
+            }
             arg = float_bits(f);
             col = lerp_paint(f, a.subject == OMV_FC_MMP ? v3(0.0f, 0.0f, 1.0f) : v3(0.0f, 1.0f, 0.0f));
             break;
@@ -308,7 +312,28 @@ void ensure_density_range(SceneHost& s)
     s.fc_density_ready = true;
 }
 
+__global__ void k_texture_hook(DevScene S, int64_t n, const float2* uv, float4* out)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = tex_sample(S, 0, uv[i].x, uv[i].y);
+}
+
 }  // namespace
+
+void hook_texture_sample(int w, int h, const uint8_t* d_rgba, int64_t n, const float* d_uv, float* d_out,
+                         void* d_table, cudaStream_t st)
+{
+    DevScene S{};
+    S.texels = reinterpret_cast<const uchar4*>(d_rgba);
+    S.textures = static_cast<const DevTexture*>(d_table);
+    S.num_textures = 1;
+    const DevTexture t{0u, w, h, d_rgba ? 1 : 0};
+    OMV_CUDA(cudaMemcpyAsync(d_table, &t, sizeof(t), cudaMemcpyHostToDevice, st));
+    if (n > 0)
+        k_texture_hook<<<(int)((n + 255) / 256), 256, 0, st>>>(S, n, reinterpret_cast<const float2*>(d_uv),
+                                                             reinterpret_cast<float4*>(d_out));
+    OMV_CUDA(cudaGetLastError());
+}
 
 int fc_subject_from_name(const char* name)
 {

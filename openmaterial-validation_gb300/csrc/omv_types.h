@@ -5,7 +5,7 @@
 //             trees and the instance TLAS live in one array
 //   tris    : 48 B per triangle in BLAS-leaf order: 3 x float4 (v0.xyz + primID,
 //             v1.xyz, v2.xyz), object space of its mesh
-//   verts   : 48 B per vertex: (p.xyz, n.x) (n.yz, t.xy) (t.zw, 0, 0)
+//   verts   : 48 B per vertex: (p.xyz, n.x) (n.yz, t.xy) (t.zw, uv0)
 //   faces   : 3 x u32 per face, vertex indices local to the mesh
 //   insts   : per instance object<->world transforms, normal matrix and ids
 //   env     : equirectangular RGB as float4 texels
@@ -48,10 +48,27 @@ struct alignas(16) DevInstance {
     uint32_t face_base;
     uint32_t vert_base;
     uint32_t valid;
-    uint32_t pad[1];
+    uint32_t uv_mask;  // the mesh's coordinate sets: bit 0 TEXCOORD_0, bit 1 TEXCOORD_1
 };
 
 enum : int32_t { kMatPbr = 0, kMatOm = 1, kMatMissing = 2 };
+
+// PBR texture slots
+enum : int32_t { kTexBase = 0, kTexMetRough = 1, kTexNormal = 2, kTexOcclusion = 3, kTexEmissive = 4, kTexSlots = 5 };
+
+// one texture slot: image (-1: none), TEXCOORD set, rows 0-1 of the transform
+struct DevTexRef {
+    int32_t tex;
+    int32_t ch;
+    float m[6];
+};
+
+// one RGBA8 image in the texel pool
+struct alignas(16) DevTexture {
+    uint32_t offset;  // first texel
+    int32_t width, height;
+    int32_t present;  // 0: BitmapTexture without an image (samples 0.5 0.5 0.5 1)
+};
 
 // material constants precomputed at commit (PhysicallyBasedMaterial with no
 // textures, OpenMaterial with IOR evaluated at the RGB wavelengths)
@@ -67,6 +84,17 @@ struct alignas(16) DevMaterial {
     float rough;  // roughness factor as given (the rmp validation subject)
     float om_n[4];
     float om_k[4];
+    // textured PBR (textured != 0): the per-vertex values are resolved from
+    // these at shading time; the constants above then hold the factors
+    int32_t textured;       // some slot has a valid image
+    int32_t alpha_mode;
+    int32_t double_sided;
+    float cutoff;
+    float factor[4];        // base colour factors as given
+    float normal_scale, occl_strength;
+    float emissive[3];
+    int32_t emissive_on;    // |emissive factor| > FLT_EPSILON and an emissive image
+    DevTexRef tex[kTexSlots];
 };
 
 struct DevEnv {
@@ -93,6 +121,10 @@ struct DevScene {
     const float* light_cdf;
     float light_max;
     DevEnv env;
+    const uchar4* texels;        // all images, RGBA8
+    const DevTexture* textures;
+    int32_t num_textures;
+    const float2* uv1;           // TEXCOORD_1 per vertex (TEXCOORD_0 is in verts), or null
 };
 
 // hit record of a closest-hit query

@@ -347,11 +347,11 @@ __global__ void __launch_bounds__(kShadeThreads) k_light_shade(WaveArgs A, int b
             if (h.x != kInvalid) {
                 const PathCtx c = path_ctx(A, k);
                 const uint32_t pixel = c.pixel, sample = c.sample;
-                const Surf sp = surface_point(S, h.x, h.y, __uint_as_float(h.z), __uint_as_float(h.w), true);
-                const DevMaterial M = c.mats[sp.mat];
+                const DevMaterial& M = c.mats[__ldg(&S.insts[h.x].material)];
+                const Surf sp = surface_point(S, h.x, h.y, __uint_as_float(h.z), __uint_as_float(h.w), true, &M);
                 const V3 in = v3(rb.x, rb.y, rb.z);
                 const Rng4 u = rng4(c.seed, pixel, sample, kDimLightBounce + (uint32_t)b, kStreamLight);
-                const V3 brdf = material_sample(S, M, sp, in, false, u, O);
+                const V3 brdf = material_sample(S, M, pbr_params(S, M, sp), sp, in, false, u, O);
                 const float ct = fabsf(dot(in, sp.nrm));
                 const float4 tp0 = A.R.ltp[k];
                 float4 lr = A.R.lrad[k];
@@ -426,12 +426,21 @@ __global__ void __launch_bounds__(kShadeThreads, 3) k_camera_shade(WaveArgs A, i
                 if (first) A.R.rad[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 const PathCtx c = path_ctx(A, k);
                 const uint32_t pixel = c.pixel, sample = c.sample;
-                const Surf sp = surface_point(S, h.x, h.y, __uint_as_float(h.z), __uint_as_float(h.w), true);
-                const DevMaterial M = c.mats[sp.mat];
+                const DevMaterial& M = c.mats[__ldg(&S.insts[h.x].material)];
+                const Surf sp = surface_point(S, h.x, h.y, __uint_as_float(h.z), __uint_as_float(h.w), true, &M);
+                const PbrParams P = pbr_params(S, M, sp);
                 const Rng4 u = rng4(c.seed, pixel, sample, (uint32_t)b, kStreamCamera);
-                const V3 brdf = material_sample(S, M, sp, in, true, u, O);
+                const V3 brdf = material_sample(S, M, P, sp, in, true, u, O);
                 const float ct = fabsf(dot(O, sp.nrm));
                 const V3 tpn = v3(tp.x * brdf.x * ct, tp.y * brdf.y * ct, tp.z * brdf.z * ct);
+                if (M.type == kMatPbr && M.emissive_on) {  // Rad += outFactor x emission (:171-173)
+                    const V3 e = pbr_emission(S, M, sp);
+                    float4 r = A.R.rad[k];
+                    r.x += tpn.x * e.x;
+                    r.y += tpn.y * e.y;
+                    r.z += tpn.z * e.z;
+                    A.R.rad[k] = r;
+                }
                 if (S.num_lights > 0) {
                     const uint32_t meta = A.R.lmeta[k];
                     const int lp_len = (int)(meta >> 16);
@@ -457,7 +466,7 @@ __global__ void __launch_bounds__(kShadeThreads, 3) k_camera_shade(WaveArgs A, i
                         const float c = fabsf(dot(LC, sp.nrm));
                         V3 lc = v3(lRad.x * c * tp.x, lRad.y * c * tp.y, lRad.z * c * tp.z);
                         if (intensity(lc) < A.cut) continue;
-                        V3 f = material_eval(M, sp, LC, outV) * c;
+                        V3 f = material_eval(M, P, sp, LC, outV) * c;
                         lc = v3(f.x * tp.x * lRad.x, f.y * tp.y * lRad.y, f.z * tp.z * lRad.z);
                         if (intensity(lc) < A.cut) continue;
                         const uint32_t sl = atomicAdd(&A.R.ctr[kCtrShadow + b], 1u);

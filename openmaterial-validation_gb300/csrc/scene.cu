@@ -234,7 +234,7 @@ void* SceneHost::alloc(size_t bytes)
     return p;
 }
 
-DevMaterial material_from_desc(const omv_material_desc& md)
+DevMaterial material_from_desc(const omv_material_desc& md, int num_textures)
 {
     DevMaterial m{};
     if (md.type == OMV_MATERIAL_OPENMATERIAL) {
@@ -260,6 +260,33 @@ DevMaterial material_from_desc(const omv_material_desc& md)
         m.alpha = std::pow(rough, 2.0f);
         m.eta = 1.0f / (md.double_sided ? 1.0f : md.ior);
         m.masked = (md.alpha_mode == OMV_ALPHA_MASK && md.base_color[3] < md.alpha_cutoff) ? 1 : 0;
+        // textures (PhysicallyBasedMaterial.cpp:27-124): a slot counts when its
+        // image index is in range (rangeCheck, :21-22)
+        const omv_texture_ref* refs[kTexSlots] = {&md.base_color_texture, &md.metallic_roughness_texture,
+                                                  &md.normal_texture, &md.occlusion_texture, &md.emissive_texture};
+        for (int k = 0; k < kTexSlots; ++k) {
+            DevTexRef& t = m.tex[k];
+            t.tex = refs[k]->texture - 1;
+            if (t.tex < 0 || t.tex >= num_textures) t.tex = -1;
+            t.ch = refs[k]->texcoord;
+            for (int r = 0; r < 2; ++r)
+                for (int c = 0; c < 3; ++c)
+                    t.m[3 * r + c] = refs[k]->has_transform ? refs[k]->transform[r][c] : (r == c ? 1.0f : 0.0f);
+            if (t.tex >= 0) m.textured = 1;
+        }
+        m.alpha_mode = md.alpha_mode;
+        m.double_sided = md.double_sided;
+        m.cutoff = md.alpha_cutoff;
+        for (int c = 0; c < 4; ++c) m.factor[c] = md.base_color[c];
+        m.normal_scale = md.normal_scale;
+        m.occl_strength = md.occlusion_strength;
+        for (int c = 0; c < 3; ++c) m.emissive[c] = md.emissive_factor[c];
+        const float el = std::sqrt(md.emissive_factor[0] * md.emissive_factor[0] +
+                                   md.emissive_factor[1] * md.emissive_factor[1] +
+                                   md.emissive_factor[2] * md.emissive_factor[2]);
+        m.emissive_on = (el > kEps && m.tex[kTexEmissive].tex >= 0) ? 1 : 0;
+        // isMasked (:301-316): the factor alone, else the base colour texture's alpha per hit
+        if (!m.masked && md.alpha_mode == OMV_ALPHA_MASK && m.tex[kTexBase].tex >= 0) m.masked = 2;
     } else {
         throw ArgError("unknown material type");
     }
@@ -287,9 +314,12 @@ void set_material_sets(SceneHost& s, int num_sets, const omv_material_desc* desc
     std::vector<DevMaterial> all((size_t)num_sets * per);
     for (int k = 0; k < num_sets; ++k) {
         for (int i = 0; i + 1 < per; ++i) {
-            const DevMaterial m = material_from_desc(descs[(size_t)k * (per - 1) + i]);
-            if (m.masked != s.h_mats[i].masked)
-                throw ArgError("material sets cannot change which materials are alpha-masked");
+            const DevMaterial m = material_from_desc(descs[(size_t)k * (per - 1) + i], s.num_textures);
+            if (m.masked != s.h_mats[i].masked ||
+                (m.masked == 2 && (m.tex[kTexBase].tex != s.h_mats[i].tex[kTexBase].tex ||
+                                   m.tex[kTexBase].ch != s.h_mats[i].tex[kTexBase].ch ||
+                                   m.factor[3] != s.h_mats[i].factor[3] || m.cutoff != s.h_mats[i].cutoff)))
+                throw ArgError("material sets cannot change which materials are alpha-masked, or how");
             all[(size_t)k * per + i] = m;
         }
         all[(size_t)k * per + per - 1] = missing_material();
@@ -313,7 +343,7 @@ void set_scene_materials(SceneHost& s, int num, const omv_material_desc* descs)
         throw ArgError("omv_scene_set_materials needs the scene's number of materials");
     std::vector<DevMaterial> mats(s.num_materials);
     for (int i = 0; i < num; ++i) {
-        mats[i] = material_from_desc(descs[i]);
+        mats[i] = material_from_desc(descs[i], s.num_textures);
         if (mats[i].masked != s.h_mats[i].masked)
             throw ArgError("omv_scene_set_materials cannot change which materials are alpha-masked");
     }
@@ -343,10 +373,11 @@ SceneHost* scene_create(const omv_scene_desc& d, int device)
 
     // ---- materials (+ the missing material, RenderScene.cpp:62-68)
     const int nmat = d.num_materials + 1;
+    s->num_textures = std::max(0, d.num_textures);
     std::vector<DevMaterial> mats(nmat);
     std::vector<int> mat_type(nmat);
     for (int i = 0; i < d.num_materials; ++i) {
-        mats[i] = material_from_desc(d.materials[i]);
+        mats[i] = material_from_desc(d.materials[i], std::max(0, d.num_textures));
         mat_type[i] = mats[i].type;
     }
     mats[nmat - 1] = missing_material();
@@ -357,6 +388,8 @@ SceneHost* scene_create(const omv_scene_desc& d, int device)
     std::vector<float4> verts;
     std::vector<uint32_t> faces;
     std::vector<uint32_t> face_base(d.num_meshes, 0), vert_base(d.num_meshes, 0), mesh_mat(d.num_meshes, 0);
+    std::vector<uint32_t> mesh_uv_mask(d.num_meshes, 0);
+    std::vector<float2> uv1;  // TEXCOORD_1 per vertex (only when some mesh has it)
     std::vector<MeshGeom> geo(d.num_meshes);
     std::vector<std::vector<float>> pos3(d.num_meshes);
     s->mesh_face_prefix.assign(d.num_meshes + 1, 0);
@@ -365,9 +398,9 @@ SceneHost* scene_create(const omv_scene_desc& d, int device)
         const omv_mesh_desc& md = d.meshes[i];
         const bool valid = md.num_vertices > 0 && md.num_faces > 0 && md.positions && md.faces;
         int mat = md.material;
-        int norm_ch = -1;
-        if (mat >= 0 && mat < nmat)
-            norm_ch = mat_type[mat] == kMatPbr ? 0 : -1;
+        int norm_ch = -1;  // PhysicallyBasedMaterial::getNormalTextureChannel = normalTexture.texCoord
+        if (mat >= 0 && mat < nmat - 1)
+            norm_ch = mat_type[mat] == kMatPbr ? d.materials[mat].normal_texture.texcoord : -1;
         else
             mat = nmat - 1;
         mesh_mat[i] = (uint32_t)mat;
@@ -390,8 +423,9 @@ SceneHost* scene_create(const omv_scene_desc& d, int device)
         }
         if (!md.normals) compute_normals(v, md.faces, vn, fn);
         if (!md.tangents) {
-            if (norm_ch == 0 && md.texcoord0)
-                compute_tangents_uv(v, md.faces, vn, fn, md.texcoord0, md.texcoord_stride);
+            const float* tuv = norm_ch == 0 ? md.texcoord0 : (norm_ch == 1 && md.texcoord0 ? md.texcoord1 : nullptr);
+            if (tuv)
+                compute_tangents_uv(v, md.faces, vn, fn, tuv, md.texcoord_stride);
             else
                 for (int k = 0; k < vn; ++k) random_tangent(&v[(size_t)k * 10 + 3], &v[(size_t)k * 10 + 6]);
         }
@@ -401,7 +435,16 @@ SceneHost* scene_create(const omv_scene_desc& d, int device)
             const float* x = &v[(size_t)k * 10];
             verts.push_back(make_float4(x[0], x[1], x[2], x[3]));
             verts.push_back(make_float4(x[4], x[5], x[6], x[7]));
-            verts.push_back(make_float4(x[8], x[9], 0.0f, 0.0f));
+            const float* t0 = md.texcoord0 ? md.texcoord0 + (size_t)k * md.texcoord_stride : nullptr;
+            verts.push_back(make_float4(x[8], x[9], t0 ? t0[0] : 0.0f, t0 ? t0[1] : 0.0f));
+        }
+        mesh_uv_mask[i] = (md.texcoord0 ? 1u : 0u) | (md.texcoord0 && md.texcoord1 ? 2u : 0u);
+        if (md.texcoord0 && md.texcoord1) {
+            uv1.resize(verts.size() / 3, make_float2(0.0f, 0.0f));
+            for (int k = 0; k < vn; ++k) {
+                const float* t1 = md.texcoord1 + (size_t)k * md.texcoord_stride;
+                uv1[vert_base[i] + k] = make_float2(t1[0], t1[1]);
+            }
         }
         faces.insert(faces.end(), md.faces, md.faces + 3 * (size_t)fn);
         MeshGeom& g = geo[i];
@@ -452,6 +495,7 @@ SceneHost* scene_create(const omv_scene_desc& d, int device)
         I.material = valid ? mesh_mat[id.mesh] : (uint32_t)(nmat - 1);
         I.face_base = valid ? face_base[id.mesh] : 0u;
         I.vert_base = valid ? vert_base[id.mesh] : 0u;
+        I.uv_mask = valid ? mesh_uv_mask[id.mesh] : 0u;
         igeo[i].valid = valid;
         igeo[i].mesh = valid ? id.mesh : -1;
         std::memcpy(igeo[i].xf, xf, sizeof(xf));
@@ -498,6 +542,35 @@ SceneHost* scene_create(const omv_scene_desc& d, int device)
     D.faces = s->upload(faces);
     D.mats = s->upload(mats);
     D.num_materials = nmat;
+    if (!uv1.empty()) {
+        uv1.resize(verts.size() / 3, make_float2(0.0f, 0.0f));
+        D.uv1 = s->upload(uv1);
+    }
+    // ---- textures (RenderScene::setTexture): one texel pool
+    if (s->num_textures > 0) {
+        if (!d.textures) throw ArgError("num_textures > 0 with NULL textures");
+        std::vector<DevTexture> tt(s->num_textures);
+        std::vector<uchar4> texels;
+        for (int i = 0; i < s->num_textures; ++i) {
+            const omv_texture_desc& td = d.textures[i];
+            const bool ok = td.rgba && td.width > 0 && td.height > 0;
+            if (ok && (int64_t)td.width * td.height > ((int64_t)1 << 28)) throw ArgError("texture too large");
+            tt[i].offset = (uint32_t)texels.size();
+            tt[i].width = ok ? td.width : 1;
+            tt[i].height = ok ? td.height : 1;
+            tt[i].present = ok ? 1 : 0;
+            if (ok) {
+                const uchar4* p = reinterpret_cast<const uchar4*>(td.rgba);
+                texels.insert(texels.end(), p, p + (size_t)td.width * td.height);
+            }
+            if (texels.size() > 0xFFFFFFFFull) throw ArgError("texel pool too large");
+        }
+        if (texels.empty()) texels.push_back(make_uchar4(0, 0, 0, 0));
+        D.texels = s->upload(texels);
+        D.textures = s->upload(tt);
+        D.num_textures = s->num_textures;
+        s->device_bytes += (int64_t)texels.size() * 4;
+    }
     s->num_materials = nmat;
     s->h_mats = mats;
     s->d_face_prefix = s->upload(s->mesh_face_prefix);

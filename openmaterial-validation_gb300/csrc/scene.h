@@ -81,6 +81,7 @@ struct SceneHost {
     int num_instances = 0;
     int num_materials = 0;  // including the missing material
     int num_lights = 0;
+    int num_textures = 0;
     int64_t num_triangles = 0;
     int64_t blas_nodes = 0;
     int64_t tlas_nodes = 0;
@@ -116,7 +117,7 @@ SceneHost* scene_create(const omv_scene_desc& desc, int device);
 
 void render_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, double* d_sum, double* d_sumsq,
                   uint32_t* d_count, cudaStream_t st, omv_stats* stats);
-DevMaterial material_from_desc(const omv_material_desc& md);
+DevMaterial material_from_desc(const omv_material_desc& md, int num_textures);
 DevMaterial missing_material();
 // material sets for batch jobs: num_sets x (scene materials without the missing one)
 void set_material_sets(SceneHost& s, int num_sets, const omv_material_desc* descs);
@@ -151,6 +152,9 @@ void render_fc(SceneHost& s, const omv_camera& cam, int subject, const float* un
                const uint32_t* palette, int palette_size, float* rgba, uint32_t* args, omv_hit* hits);
 void scene_bounds(SceneHost& s, float lo[3], float hi[3]);
 void lightbox_cameras(const float lo[3], const float hi[3], int width, int height, omv_camera out[8]);
+// BitmapTexture::texture on the device for one image (d_table: 16 bytes of scratch)
+void hook_texture_sample(int w, int h, const uint8_t* d_rgba, int64_t n, const float* d_uv, float* d_out,
+                         void* d_table, cudaStream_t st);
 
 // image development and writers (post.cu)
 void develop_film(const double* d_sum, const uint32_t* d_count, int w, int h, float A, float gamma, float* d_linear,

@@ -17,7 +17,157 @@ struct Surf {
     uint32_t face;
     uint32_t vert_base;
     uint32_t face_base;
+    float bu, bv;       // hit barycentrics (u, v); the first weight is 1 - u - v
+    uint32_t uv_mask;   // coordinate sets of the mesh
 };
+
+// ------------------------------------------------------------ textures ---
+
+// BitmapTexture::getPixCoords + texture(u, v, fvec4) (BitmapTexture.cpp:73-125):
+// bilinear over the four wrapped neighbours, texels scaled by 1/255
+__device__ __forceinline__ float4 tex_sample(const DevScene& S, int t, float u, float v)
+{
+    const DevTexture T = S.textures[t];
+    if (!T.present) return make_float4(0.5f, 0.5f, 0.5f, 1.0f);
+    const int W = T.width, H = T.height;
+    const float upage = floorf(u - 0.5f / (float)W);
+    const float vpage = floorf(v - 0.5f / (float)H);
+    u -= upage;
+    v -= vpage;
+    u *= (float)W;
+    v *= (float)H;
+    const int iu = (int)u, iv = (int)v;
+    const float kui = u - (float)iu, kvi = v - (float)iv;
+    const float ku = 1.0f - kui, kv = 1.0f - kvi;
+    const int l = iu % W, r = (iu + 1) % W, b = iv % H, tp = (iv + 1) % H;
+    const uchar4* px = S.texels + T.offset;
+    const uchar4 c0 = __ldg(px + b * W + l), c1 = __ldg(px + b * W + r);
+    const uchar4 c2 = __ldg(px + tp * W + l), c3 = __ldg(px + tp * W + r);
+    const float w0 = ku * kv, w1 = kui * kv, w2 = ku * kvi, w3 = kui * kvi;
+    constexpr float sc = 1.0f / 255.0f;
+    return make_float4((float)c0.x * w0 * sc + (float)c1.x * w1 * sc + (float)c2.x * w2 * sc + (float)c3.x * w3 * sc,
+                       (float)c0.y * w0 * sc + (float)c1.y * w1 * sc + (float)c2.y * w2 * sc + (float)c3.y * w3 * sc,
+                       (float)c0.z * w0 * sc + (float)c1.z * w1 * sc + (float)c2.z * w2 * sc + (float)c3.z * w3 * sc,
+                       (float)c0.w * w0 * sc + (float)c1.w * w1 * sc + (float)c2.w * w2 * sc + (float)c3.w * w3 * sc);
+}
+
+__device__ __forceinline__ float2 vertex_uv(const DevScene& S, int ch, uint32_t vi)
+{
+    if (ch == 0) {
+        const float4 w = __ldg(S.verts + 3 * (size_t)vi + 2);
+        return make_float2(w.z, w.w);
+    }
+    return __ldg(S.uv1 + vi);
+}
+
+// SurfacePoint::getTexCoords -> RenderMesh::getTexCoord (RenderMesh.cpp:146-157):
+// (0, 0) and false when the mesh lacks the coordinate set
+__device__ __forceinline__ bool tex_coords(const DevScene& S, const Surf& sp, int ch, float2& tc)
+{
+    tc = make_float2(0.0f, 0.0f);
+    if (ch < 0 || ch > 1 || !(sp.uv_mask & (1u << ch))) return false;
+    const uint32_t* F = S.faces + 3 * (size_t)(sp.face_base + sp.face);
+    const float2 a = vertex_uv(S, ch, sp.vert_base + __ldg(F));
+    const float2 b = vertex_uv(S, ch, sp.vert_base + __ldg(F + 1));
+    const float2 c = vertex_uv(S, ch, sp.vert_base + __ldg(F + 2));
+    const float b0 = 1.0f - sp.bu - sp.bv, b1 = sp.bu, b2 = sp.bv;
+    tc = make_float2(a.x * b0 + b.x * b1 + c.x * b2, a.y * b0 + b.y * b1 + c.y * b2);
+    return true;
+}
+
+// multVector3(TM, (u, v, 1)) then the bitmap lookup
+__device__ __forceinline__ float4 tex_transformed(const DevScene& S, const DevTexRef& t, float2 uv)
+{
+    const float uu = t.m[0] * uv.x + t.m[1] * uv.y + t.m[2] * 1.0f;
+    const float vv = t.m[3] * uv.x + t.m[4] * uv.y + t.m[5] * 1.0f;
+    return tex_sample(S, t.tex, uu, vv);
+}
+
+// a slot as PhysicallyBasedMaterial::Helper reads it: only when the image
+// exists and the mesh has the slot's coordinate set
+__device__ __forceinline__ bool tex_slot(const DevScene& S, const DevMaterial& M, int slot, const Surf& sp,
+                                         float4& out)
+{
+    const DevTexRef& t = M.tex[slot];
+    float2 uv;
+    if (t.tex < 0 || !tex_coords(S, sp, t.ch, uv)) return false;
+    out = tex_transformed(S, t, uv);
+    return true;
+}
+
+// per-vertex PBR values: getTextureRGBA, getTextureOccMetRoughValues and
+// occluseColor (PhysicallyBasedMaterial.cpp:27-95, 178-200, 261-276)
+struct PbrParams {
+    float color[4];
+    float metal, alpha;
+    bool transmissive;
+    float omr_metal, omr_rough;  // before the roughness clamp (the validation subjects)
+};
+
+static __device__ __noinline__ PbrParams pbr_params_textured(const DevScene& S, const DevMaterial& M,
+                                                             const Surf& sp)
+{
+    PbrParams P;
+    float4 rgba = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+    tex_slot(S, M, kTexBase, sp, rgba);
+    P.color[0] = rgba.x * M.factor[0];
+    P.color[1] = rgba.y * M.factor[1];
+    P.color[2] = rgba.z * M.factor[2];
+    P.color[3] = M.alpha_mode != OMV_ALPHA_BLEND ? 1.0f : rgba.w * M.factor[3];
+    P.transmissive = M.double_sided || P.color[3] < 1.0f;
+    float o0 = 1.0f, o1 = M.metal, o2 = M.rough;
+    float4 tb;
+    if (tex_slot(S, M, kTexMetRough, sp, tb)) {
+        o0 *= tb.x;
+        o1 *= tb.z;
+        o2 *= tb.y;
+    }
+    if (M.tex[kTexOcclusion].tex != M.tex[kTexMetRough].tex && tex_slot(S, M, kTexOcclusion, sp, tb)) o0 = tb.x;
+    for (int i = 0; i < 3; ++i) P.color[i] = lerpf(P.color[i], o0 * P.color[i], M.occl_strength);
+    P.omr_metal = o1;
+    P.omr_rough = o2;
+    P.metal = o1;
+    const float rough = clampf(o2, 0.00001f, 0.99999f);
+    P.alpha = __fmul_rn(rough, rough);  // std::pow(roughness, 2.0f)
+    return P;
+}
+
+__device__ __forceinline__ PbrParams pbr_params(const DevScene& S, const DevMaterial& M, const Surf& sp)
+{
+    if (M.textured) return pbr_params_textured(S, M, sp);
+    PbrParams P;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) P.color[i] = M.color[i];
+    P.metal = M.metal;
+    P.alpha = M.alpha;
+    P.transmissive = M.transmissive != 0;
+    P.omr_metal = M.metal;
+    P.omr_rough = M.rough;
+    return P;
+}
+
+// PhysicallyBasedMaterial::modifyFrame (:147-167): the normal map's tangent-space
+// normal, or (0, 0, 1) without one
+static __device__ __noinline__ V3 normal_map(const DevScene& S, const DevMaterial& M, const Surf& sp)
+{
+    float4 t;
+    if (!tex_slot(S, M, kTexNormal, sp, t)) return v3(0.0f, 0.0f, 1.0f);
+    if (t.z <= 0.5f) t.z = 0.5f + kEps;
+    V3 tn = v3(2.0f * t.x + -1.0f, 2.0f * t.y + -1.0f, 2.0f * t.z + -1.0f);
+    tn.x = M.normal_scale * tn.x;
+    tn.y = M.normal_scale * tn.y;
+    return normalize(tn);
+}
+
+// PhysicallyBasedMaterial::getEmissivity + Helper::getTextureEmissivity
+// (:96-117, 280-287, 293-299); only called for an emissive material
+static __device__ __noinline__ V3 pbr_emission(const DevScene& S, const DevMaterial& M, const Surf& sp)
+{
+    float2 euv;
+    tex_coords(S, sp, M.tex[kTexEmissive].ch, euv);
+    const float4 t = tex_transformed(S, M.tex[kTexEmissive], euv);
+    return v3(t.x * M.emissive[0], t.y * M.emissive[1], t.z * M.emissive[2]);
+}
 
 __device__ __forceinline__ V3 m33(const float* m, V3 v)
 {
@@ -29,7 +179,7 @@ __device__ __forceinline__ V3 m33(const float* m, V3 v)
 // (RenderMesh.cpp:159-196), then SurfacePoint::applyTextureNormal((0,0,1))
 // (SurfacePoint.cpp:19-34) as every material's modifyFrame without a normal map
 __device__ __forceinline__ Surf surface_point(const DevScene& S, uint32_t inst, uint32_t prim, float u, float v,
-                                              bool frame)
+                                              bool frame, const DevMaterial* M = nullptr)
 {
     const DevInstance* I = S.insts + inst;
     Surf sp;
@@ -38,6 +188,9 @@ __device__ __forceinline__ Surf surface_point(const DevScene& S, uint32_t inst, 
     sp.mat = __ldg(&I->material);
     sp.vert_base = __ldg(&I->vert_base);
     sp.face_base = __ldg(&I->face_base);
+    sp.bu = u;
+    sp.bv = v;
+    sp.uv_mask = __ldg(&I->uv_mask);
     const uint32_t* F = S.faces + 3 * (size_t)(sp.face_base + prim);
     const uint32_t f0 = __ldg(F), f1 = __ldg(F + 1), f2 = __ldg(F + 2);
     const float b0 = 1.0f - u - v, b1 = u, b2 = v;
@@ -68,8 +221,11 @@ __device__ __forceinline__ Surf surface_point(const DevScene& S, uint32_t inst, 
     V3 n = normalize_if_needed(m33(nm, pn));
     V3 t = normalize_if_needed(m33(nm, pt));
     V3 b = normalize_if_needed(m33(nm, pbn));
-    // applyTextureNormal((0,0,1)): nn = 0*t + 0*b + 1*n
-    n = normalize_if_needed(t * 0.0f + b * 0.0f + n * 1.0f);
+    // modifyFrame -> applyTextureNormal(tn): nn = tn.x t + tn.y b + tn.z n, with
+    // tn = (0, 0, 1) unless the material (given) has a normal map
+    const V3 tnm = (M && M->type == kMatPbr && M->tex[kTexNormal].tex >= 0) ? normal_map(S, *M, sp)
+                                                                          : v3(0.0f, 0.0f, 1.0f);
+    n = normalize_if_needed(t * tnm.x + b * tnm.y + n * tnm.z);
     t = normalize_if_needed(cross(b, n));
     b = cross(n, t) * tw;
     sp.nrm = n;
@@ -96,9 +252,11 @@ __device__ __forceinline__ V3 face_normal(const DevScene& S, const Surf& sp)
     return normalize(m33(nm, cross(e1, e2)));
 }
 
-// RenderMaterial::getRayAndBrdf of each material kind; u = the vertex's uniforms
-__device__ __forceinline__ V3 material_sample(const DevScene& S, const DevMaterial& M, const Surf& sp, V3 in, bool inv,
-                                              const Rng4& u, V3& out, SampleInfo* info = nullptr)
+// RenderMaterial::getRayAndBrdf of each material kind; u = the vertex's
+// uniforms, P = the vertex's PBR values (pbr_params)
+__device__ __forceinline__ V3 material_sample(const DevScene& S, const DevMaterial& M, const PbrParams& P,
+                                              const Surf& sp, V3 in, bool inv, const Rng4& u, V3& out,
+                                              SampleInfo* info = nullptr)
 {
     if (M.type == kMatPbr) {  // PhysicallyBasedMaterial::getRayAndBrdf (:248-291)
         BsdfIn d;
@@ -106,11 +264,11 @@ __device__ __forceinline__ V3 material_sample(const DevScene& S, const DevMateri
         d.N = sp.nrm;
         d.T = sp.tan;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) d.color[i] = M.color[i];
-        d.metal = M.metal;
-        d.alpha = M.alpha;
+        for (int i = 0; i < 4; ++i) d.color[i] = P.color[i];
+        d.metal = P.metal;
+        d.alpha = P.alpha;
         d.eta = M.eta;
-        d.transmissive = M.transmissive != 0;
+        d.transmissive = P.transmissive;
         return bsdf_sample_indirect(d, u.u[0], u.u[1], u.u[2], out, info);
     }
     if (M.type == kMatOm) {  // OpenMaterial::defineNextDirection + getRayAndBrdf (:72-93, :165-232)
@@ -130,12 +288,12 @@ __device__ __forceinline__ V3 material_sample(const DevScene& S, const DevMateri
 }
 
 // RenderMaterial::getBrdf (impSmpScale = false) for a connection
-__device__ __forceinline__ V3 material_eval(const DevMaterial& M, const Surf& sp, V3 in, V3 out)
+__device__ __forceinline__ V3 material_eval(const DevMaterial& M, const PbrParams& P, const Surf& sp, V3 in, V3 out)
 {
     if (M.type == kMatPbr) {  // PhysicallyBasedMaterial::getBrdf (:178-245)
         V3 N = sp.nrm;
-        if (dot(in, N) > 0.0f && M.transmissive) N = -N;
-        return bsdf_eval_direct(in, out, N, M.color, M.metal, M.alpha);
+        if (dot(in, N) > 0.0f && P.transmissive) N = -N;
+        return bsdf_eval_direct(in, out, N, P.color, P.metal, P.alpha);
     }
     if (M.type == kMatOm) {  // OpenMaterial::getBrdf (:95-163): mirror directions only
         if (!M.om_valid) return v3(0.0f, 0.0f, 0.0f);
@@ -145,6 +303,43 @@ __device__ __forceinline__ V3 material_eval(const DevMaterial& M, const Surf& sp
                   om_channel(M.om_n[2], M.om_k[2], c));
     }
     return v3(M.color[0], M.color[1], M.color[2]);
+}
+
+// the same without textures (the material's constants)
+__device__ __forceinline__ V3 material_sample(const DevScene& S, const DevMaterial& M, const Surf& sp, V3 in, bool inv,
+                                              const Rng4& u, V3& out, SampleInfo* info = nullptr)
+{
+    return material_sample(S, M, pbr_params(S, M, sp), sp, in, inv, u, out, info);
+}
+__device__ __forceinline__ V3 material_eval(const DevMaterial& M, const Surf& sp, V3 in, V3 out)
+{
+    PbrParams P;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) P.color[i] = M.color[i];
+    P.metal = M.metal;
+    P.alpha = M.alpha;
+    P.transmissive = M.transmissive != 0;
+    return material_eval(M, P, sp, in, out);
+}
+
+// PhysicallyBasedMaterial::isMasked (:301-316) for a MASK material with a base
+// colour texture: factor alpha x the texture's alpha at the untransformed
+// coordinates (1 where the mesh lacks the set, BitmapTexture.cpp:142-156)
+static __device__ __noinline__ bool texture_masked(const DevScene& S, const DevMaterial& M, uint32_t inst,
+                                                   uint32_t prim, float u, float v)
+{
+    const DevInstance* I = S.insts + inst;
+    Surf sp;
+    sp.face = prim;
+    sp.vert_base = __ldg(&I->vert_base);
+    sp.face_base = __ldg(&I->face_base);
+    sp.uv_mask = __ldg(&I->uv_mask);
+    sp.bu = u;
+    sp.bv = v;
+    float2 uv;
+    float a = 1.0f;
+    if (tex_coords(S, sp, M.tex[kTexBase].ch, uv)) a = tex_sample(S, M.tex[kTexBase].tex, uv.x, uv.y).w;
+    return M.factor[3] * a < M.cutoff;
 }
 
 // BDPTRenderer::sceneIntersect (BDPTRenderer.cpp:75-102): closest hit, skipping
@@ -157,7 +352,9 @@ __device__ __forceinline__ bool scene_intersect(const DevScene& S, const uint32_
     for (int itr = 0; itr < 10; ++itr) {
         if (!trace_closest(S, items, o, d, tnear, tfar, h, st, tc)) return false;
         const uint32_t mat = __ldg(&S.insts[h.inst].material);
-        if (!S.mats[mat].masked) return true;
+        const int masked = S.mats[mat].masked;
+        if (!masked) return true;
+        if (masked == 2 && !texture_masked(S, S.mats[mat], h.inst, h.prim, h.u, h.v)) return true;
         V3 org = v3(o.x + h.t * d.x, o.y + h.t * d.y, o.z + h.t * d.z);
         float vv = max_abs(org, 1.0f);
         vv = vv > h.t ? vv : h.t;
