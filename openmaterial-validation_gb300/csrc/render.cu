@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(kShadeThreads, 3) k_camera_shade(WaveArgs A, i
                 const float ct = fabsf(dot(O, sp.nrm));
                 const V3 tpn = v3(tp.x * brdf.x * ct, tp.y * brdf.y * ct, tp.z * brdf.z * ct);
                 if (M.type == kMatPbr && M.emissive_on) {  // Rad += outFactor x emission (:171-173)
-                    const V3 e = pbr_emission(S, M, sp);
+                    const V3 e = pbr_emission(S, M, tex_hit(sp));
                     float4 r = A.R.rad[k];
                     r.x += tpn.x * e.x;
                     r.y += tpn.y * e.y;

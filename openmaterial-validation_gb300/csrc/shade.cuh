@@ -23,6 +23,17 @@ struct Surf {
 
 // ------------------------------------------------------------ textures ---
 
+// what a texture lookup needs of a hit, passed by value to the out-of-line
+// texture helpers (a Surf passed by reference would live in local memory)
+struct TexHit {
+    uint32_t face, vert_base, face_base, uv_mask;
+    float bu, bv;
+};
+__device__ __forceinline__ TexHit tex_hit(const Surf& sp)
+{
+    return TexHit{sp.face, sp.vert_base, sp.face_base, sp.uv_mask, sp.bu, sp.bv};
+}
+
 // BitmapTexture::getPixCoords + texture(u, v, fvec4) (BitmapTexture.cpp:73-125):
 // bilinear over the four wrapped neighbours, texels scaled by 1/255
 __device__ __forceinline__ float4 tex_sample(const DevScene& S, int t, float u, float v)
@@ -62,7 +73,7 @@ __device__ __forceinline__ float2 vertex_uv(const DevScene& S, int ch, uint32_t 
 
 // SurfacePoint::getTexCoords -> RenderMesh::getTexCoord (RenderMesh.cpp:146-157):
 // (0, 0) and false when the mesh lacks the coordinate set
-__device__ __forceinline__ bool tex_coords(const DevScene& S, const Surf& sp, int ch, float2& tc)
+__device__ __forceinline__ bool tex_coords(const DevScene& S, const TexHit& sp, int ch, float2& tc)
 {
     tc = make_float2(0.0f, 0.0f);
     if (ch < 0 || ch > 1 || !(sp.uv_mask & (1u << ch))) return false;
@@ -85,7 +96,7 @@ __device__ __forceinline__ float4 tex_transformed(const DevScene& S, const DevTe
 
 // a slot as PhysicallyBasedMaterial::Helper reads it: only when the image
 // exists and the mesh has the slot's coordinate set
-__device__ __forceinline__ bool tex_slot(const DevScene& S, const DevMaterial& M, int slot, const Surf& sp,
+__device__ __forceinline__ bool tex_slot(const DevScene& S, const DevMaterial& M, int slot, const TexHit& sp,
                                          float4& out)
 {
     const DevTexRef& t = M.tex[slot];
@@ -104,8 +115,7 @@ struct PbrParams {
     float omr_metal, omr_rough;  // before the roughness clamp (the validation subjects)
 };
 
-static __device__ __noinline__ PbrParams pbr_params_textured(const DevScene& S, const DevMaterial& M,
-                                                             const Surf& sp)
+static __device__ __noinline__ PbrParams pbr_params_textured(const DevScene& S, const DevMaterial& M, TexHit sp)
 {
     PbrParams P;
     float4 rgba = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
@@ -134,7 +144,7 @@ static __device__ __noinline__ PbrParams pbr_params_textured(const DevScene& S, 
 
 __device__ __forceinline__ PbrParams pbr_params(const DevScene& S, const DevMaterial& M, const Surf& sp)
 {
-    if (M.textured) return pbr_params_textured(S, M, sp);
+    if (M.textured) return pbr_params_textured(S, M, tex_hit(sp));
     PbrParams P;
 #pragma unroll
     for (int i = 0; i < 4; ++i) P.color[i] = M.color[i];
@@ -148,7 +158,7 @@ __device__ __forceinline__ PbrParams pbr_params(const DevScene& S, const DevMate
 
 // PhysicallyBasedMaterial::modifyFrame (:147-167): the normal map's tangent-space
 // normal, or (0, 0, 1) without one
-static __device__ __noinline__ V3 normal_map(const DevScene& S, const DevMaterial& M, const Surf& sp)
+static __device__ __noinline__ V3 normal_map(const DevScene& S, const DevMaterial& M, TexHit sp)
 {
     float4 t;
     if (!tex_slot(S, M, kTexNormal, sp, t)) return v3(0.0f, 0.0f, 1.0f);
@@ -161,7 +171,7 @@ static __device__ __noinline__ V3 normal_map(const DevScene& S, const DevMateria
 
 // PhysicallyBasedMaterial::getEmissivity + Helper::getTextureEmissivity
 // (:96-117, 280-287, 293-299); only called for an emissive material
-static __device__ __noinline__ V3 pbr_emission(const DevScene& S, const DevMaterial& M, const Surf& sp)
+static __device__ __noinline__ V3 pbr_emission(const DevScene& S, const DevMaterial& M, TexHit sp)
 {
     float2 euv;
     tex_coords(S, sp, M.tex[kTexEmissive].ch, euv);
@@ -223,7 +233,7 @@ __device__ __forceinline__ Surf surface_point(const DevScene& S, uint32_t inst, 
     V3 b = normalize_if_needed(m33(nm, pbn));
     // modifyFrame -> applyTextureNormal(tn): nn = tn.x t + tn.y b + tn.z n, with
     // tn = (0, 0, 1) unless the material (given) has a normal map
-    const V3 tnm = (M && M->type == kMatPbr && M->tex[kTexNormal].tex >= 0) ? normal_map(S, *M, sp)
+    const V3 tnm = (M && M->type == kMatPbr && M->tex[kTexNormal].tex >= 0) ? normal_map(S, *M, tex_hit(sp))
                                                                           : v3(0.0f, 0.0f, 1.0f);
     n = normalize_if_needed(t * tnm.x + b * tnm.y + n * tnm.z);
     t = normalize_if_needed(cross(b, n));
@@ -329,13 +339,7 @@ static __device__ __noinline__ bool texture_masked(const DevScene& S, const DevM
                                                    uint32_t prim, float u, float v)
 {
     const DevInstance* I = S.insts + inst;
-    Surf sp;
-    sp.face = prim;
-    sp.vert_base = __ldg(&I->vert_base);
-    sp.face_base = __ldg(&I->face_base);
-    sp.uv_mask = __ldg(&I->uv_mask);
-    sp.bu = u;
-    sp.bv = v;
+    const TexHit sp{prim, __ldg(&I->vert_base), __ldg(&I->face_base), __ldg(&I->uv_mask), u, v};
     float2 uv;
     float a = 1.0f;
     if (tex_coords(S, sp, M.tex[kTexBase].ch, uv)) a = tex_sample(S, M.tex[kTexBase].tex, uv.x, uv.y).w;
