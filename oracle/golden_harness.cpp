@@ -22,6 +22,8 @@
  *   golden_harness median  W H in out     SimpleDenoiserMedian<1> (Denoiser.h:24); in/out as tonemap
  *   golden_harness rgba8   W H in out     saveImage's conversion (main.cpp:92): unsigned char(255 f),
  *       out: W*H*4 bytes
+ *   golden_harness png     in out        stb_image as tinygltf loads images (4 channels; 16-bit
+ *       files through stbi_load_16), out: int32 W H then W*H*4 uint16 samples
  *   golden_harness texture W H img uv out BitmapTexture::texture(u, v, fvec4) (BitmapTexture.cpp:108-125)
  *       img: W*H*4 bytes; uv: 2 floats/case; out: 4 floats/case
  */
@@ -40,6 +42,7 @@
 #include "ToneMapping.h"
 #include "Denoiser.h"
 #include "BitmapTexture.h"
+#include "stb_image.h"
 #include "materials/AssetMaterial.h"
 #include "materials/AssetMaterialIor.h"
 
@@ -175,6 +178,27 @@ int main(int argc, char** argv)
         long n = std::atol(argv[3]);
         for (long i = 0; i < n; ++i) out.push_back(rs.rand());
         write_floats(argv[4], out);
+    } else if (mode == "png" && argc == 4) {
+        int w = 0, h = 0, c = 0;
+        std::vector<uint16_t> px;
+        if (stbi_is_16_bit(argv[2])) {
+            stbi_us* d = stbi_load_16(argv[2], &w, &h, &c, 4);
+            if (!d) return 2;
+            px.assign(d, d + (size_t)w * h * 4);
+            stbi_image_free(d);
+        } else {
+            stbi_uc* d = stbi_load(argv[2], &w, &h, &c, 4);
+            if (!d) return 2;
+            px.assign(d, d + (size_t)w * h * 4);
+            stbi_image_free(d);
+        }
+        FILE* f = std::fopen(argv[3], "wb");
+        if (!f) return 2;
+        const int32_t wh[2] = {w, h};
+        std::fwrite(wh, sizeof(int32_t), 2, f);
+        std::fwrite(px.data(), sizeof(uint16_t), px.size(), f);
+        std::fclose(f);
+        return 0;
     } else if (mode == "texture" && argc == 7) {
         const int W = std::atoi(argv[2]), H = std::atoi(argv[3]);
         FILE* f = std::fopen(argv[4], "rb");

@@ -24,6 +24,10 @@ Fixtures (numpy .npz):
                     (wrapping, negative, texel-centre and edge cases)
   film_textured_32x8.npz / scene_textured.npz
                     -C 1 film and committed scene of the textured PBR scene
+  png.npz           stb_image's RGBA decode (as tinygltf loads images) of seeded PNG
+                    files of every colour type, depth and row filter
+  assets.npz        digests of the reference's committed scene for each of its own
+                    objects/ and scenes/ assets (pathtracer -L, the OMV_REF_SCENE dump)
   fc.npz            false-colour films (-F pid gid mid mmp rmp md sg mn in, and an
                     unknown name) of the validation scene, before tone mapping
   lightbox.npz      the 8 light-box views (-V) of the mixed scene: cameras
@@ -328,6 +332,150 @@ def gen_textured(tmp):
     np.savez_compressed(os.path.join(HERE, "scene_textured.npz"), **dump)
 
 
+def write_png_variant(path, samples, ctype, depth, filters, palette=None, trns=None):
+    """A PNG file with the given samples (H, W, C), colour type, bit depth and
+    per-row filter types (0-4), for decoder checks."""
+    import struct
+    import zlib
+
+    h, w = samples.shape[:2]
+    if depth == 16:
+        rows = [samples[y].astype(">u2").tobytes() for y in range(h)]
+    elif depth == 8:
+        rows = [samples[y].astype(np.uint8).tobytes() for y in range(h)]
+    else:
+        rows = []
+        per = 8 // depth
+        for y in range(h):
+            b = bytearray((w * depth + 7) // 8)
+            for x in range(w):
+                b[x // per] |= int(samples[y, x, 0]) << (8 - depth * (x % per + 1))
+            rows.append(bytes(b))
+    bpp = max(1, (depth * samples.shape[2]) // 8)
+    raw = bytearray()
+    prev = bytes(len(rows[0]))
+    for y, row in enumerate(rows):
+        f = filters[y % len(filters)]
+        out = bytearray(len(row))
+        for x in range(len(row)):
+            a = row[x - bpp] if x >= bpp else 0
+            b = prev[x]
+            c = prev[x - bpp] if x >= bpp else 0
+            if f == 0:
+                p = 0
+            elif f == 1:
+                p = a
+            elif f == 2:
+                p = b
+            elif f == 3:
+                p = (a + b) >> 1
+            else:
+                q = a + b - c
+                pa, pb, pc = abs(q - a), abs(q - b), abs(q - c)
+                p = a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
+            out[x] = (row[x] - p) & 0xFF
+        raw.append(f)
+        raw += out
+        prev = row
+
+    def chunk(t, d):
+        return struct.pack(">I", len(d)) + t + d + struct.pack(">I", zlib.crc32(t + d) & 0xFFFFFFFF)
+
+    data = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, ctype, 0, 0, 0))
+    if palette is not None:
+        data += chunk(b"PLTE", palette.astype(np.uint8).tobytes())
+    if trns is not None:
+        data += chunk(b"tRNS", trns)
+    data += chunk(b"IDAT", zlib.compress(bytes(raw))) + chunk(b"IEND", b"")
+    with open(path, "wb") as fh:
+        fh.write(data)
+
+
+def gen_png(tmp):
+    import struct
+
+    rng = np.random.default_rng(21)
+    cases = []
+    for ctype, chans in ((0, 1), (2, 3), (4, 2), (6, 4)):
+        for depth in (8, 16):
+            top = 255 if depth == 8 else 65535
+            cases.append((ctype, depth, rng.integers(0, top + 1, (9, 13, chans)), None, None))
+    for depth in (1, 2, 4, 8):
+        pal = rng.integers(0, 256, (1 << depth, 3))
+        trns = bytes(rng.integers(0, 256, max(1, (1 << depth) // 2)).astype(np.uint8))
+        cases.append((3, depth, rng.integers(0, 1 << depth, (7, 11, 1)), pal, trns))
+    for depth in (1, 2, 4):
+        cases.append((0, depth, rng.integers(0, 1 << depth, (6, 10, 1)), None, None))
+    key = struct.pack(">HHH", 10, 20, 30)
+    s = rng.integers(0, 40, (8, 8, 3))
+    s[2, 3] = (10, 20, 30)
+    cases.append((2, 8, s, None, key))
+    out = {}
+    for i, (ct, d, smp, pal, tr) in enumerate(cases):
+        p = os.path.join(tmp, f"v{i}.png")
+        write_png_variant(p, smp, ct, d, [0, 1, 2, 3, 4], pal, tr)
+        o = os.path.join(tmp, f"v{i}.out")
+        harness("png", p, o)
+        wh = np.fromfile(o, dtype=np.int32, count=2)
+        px = np.fromfile(o, dtype=np.uint16, offset=8).reshape(wh[1], wh[0], 4)
+        out[f"file{i}"] = np.frombuffer(open(p, "rb").read(), dtype=np.uint8)
+        out[f"rgba{i}"] = px
+        out[f"bits{i}"] = d
+    out["count"] = len(cases)
+    np.savez_compressed(os.path.join(HERE, "png.npz"), **out)
+
+
+ASSETS = ["objects/" + n for n in (
+    "cone_gold", "cube_aluminium", "cube_gold", "cube_pbr_gold", "cubes_pbr", "icospheres_gold_iron_aluminium",
+    "icospheres_gold_iron_missing", "monkey_gold", "plane_pointlight", "sphere_aluminium", "sphere_gold",
+    "teapot_aluminium", "teapot_gold", "teapot_iron", "torus_aluminium", "torus_gold", "torus_pbr",
+    "truck_example", "vehicle_example")] + ["scenes/multiple_instances"]
+
+
+def scene_digest(meshes_v, meshes_f, mesh_rec, inst_mesh, inst_xf, inst_nrm, lights):
+    """What the asset checks compare: per mesh a hash of its committed vertex
+    block and faces and the record of its material; instances; lights."""
+    import hashlib
+
+    def canon(v):  # one NaN pattern: the payload of a NaN is not part of the contract
+        v = np.array(v, np.float32)
+        v[np.isnan(v)] = np.float32("nan")
+        return v
+
+    mh = np.array([int(hashlib.sha1(canon(v).tobytes() +
+                                    np.ascontiguousarray(f, np.uint32).tobytes()).hexdigest()[:15], 16)
+                   for v, f in zip(meshes_v, meshes_f)], dtype=np.int64)
+    return {"mesh_hash": mh, "mesh_rec": np.asarray(mesh_rec, np.float32).reshape(len(mh), -1),
+            "inst_mesh": np.asarray(inst_mesh, np.int32), "inst_xf": np.asarray(inst_xf, np.float32),
+            "inst_nrm": np.asarray(inst_nrm, np.float32), "lights": np.asarray(lights, np.float32).reshape(-1, 8)}
+
+
+def gen_assets(tmp):
+    out = {}
+    for a in ASSETS:
+        path = os.path.join(REF, a + ".gltf")
+        dump = os.path.join(tmp, "asset.bin")
+        env = dict(os.environ, OMV_REF_SCENE=dump)
+        run([os.path.join(BIN, "pathtracer"), "-i", path, "-r", "4", "-a", "1", "-S", "1", "-B", "1", "-b", "1",
+             "-L", "-C", "1", "-o", os.path.join(tmp, "asset.png")], env=env)
+        d = read_scene_dump(dump)
+        nm = len(d["mesh_material"])
+        recs = []
+        for i in range(nm):
+            mi = int(d["mesh_material"][i])
+            if 0 <= mi < len(d["mat_type"]) and d["mat_type"][mi] != 2:
+                recs.append(np.concatenate([[d["mat_type"][mi]], d["mat_rec"][mi]]).astype(np.float32))
+            else:
+                recs.append(np.concatenate([[2], np.zeros(16)]).astype(np.float32))
+        dg = scene_digest([d[f"verts{i}"] for i in range(nm)], [d[f"faces{i}"] for i in range(nm)], recs,
+                          d["inst_mesh"], d["inst_xf"], d["inst_nrm"], d["lights"])
+        key = a.replace("/", "__")
+        for k, v in dg.items():
+            out[f"{key}.{k}"] = v
+        print(a, nm, len(d["inst_mesh"]), len(d["lights"]))
+    np.savez_compressed(os.path.join(HERE, "assets.npz"), **out)
+
+
 FC_SUBJECTS = ["pid", "gid", "mid", "mmp", "rmp", "md", "sg", "mn", "in", "nosuch"]
 
 
@@ -365,7 +513,7 @@ def gen_lightbox(tmp):
 
 GENS = {"mt": gen_mt, "brdf": gen_brdf, "om": gen_om, "ior": gen_ior, "env": gen_env, "camera": gen_camera,
         "films": gen_films, "ids": gen_ids, "post": gen_post, "fc": gen_fc, "lightbox": gen_lightbox,
-        "textured": gen_textured, "texture": gen_texture}
+        "textured": gen_textured, "texture": gen_texture, "png": gen_png, "assets": gen_assets}
 
 
 def main():
