@@ -9,6 +9,7 @@ so the two agree up to the difference quotient's error.  Roughness also
 moves the GGX-sampled directions under common random numbers, while the
 adjoint keeps them fixed and adds the score of their density: the two agree
 in expectation only."""
+import dataclasses
 import importlib
 import json
 import os
@@ -105,3 +106,50 @@ def test_adjoint_roughness_in_expectation(case):
     pbr = np.array([m.type == 0 for m in sc.materials])
     scale = np.abs(g_fd[pbr]).max()
     assert np.all(np.abs(g_ad[pbr] - g_fd[pbr]) <= 0.2 * np.abs(g_fd[pbr]) + 0.05 * scale), (g_ad, g_fd)
+
+
+def test_adjoint_matches_finite_differences_on_the_reference_renderer(gpu, oracle, scenes):
+    """The GPU path-replay gradient of a linear image loss against central
+    differences of the same loss on the reference CPU renderer (the oracle's
+    reference-exact mode: one mt19937 stream, so both sides of a difference
+    use common random numbers).  The two renderers draw different random
+    numbers, so they agree in expectation: base colours and metallic, whose
+    derivative does not move sampled directions, within 15% of the largest
+    component or 25% relative."""
+    torch = pytest.importorskip("torch")
+    diff = importlib.import_module("openmaterial-validation_gb300.diff")
+    sc = scenes.scene_materials(24, 24, 1, tris=4000, bounces=3, n_materials=4)
+    P0 = diff.params_from_materials(sc.materials)
+    rng = np.random.default_rng(3)
+    H, W = sc.camera.height, sc.camera.width
+    w = rng.uniform(0.0, 1.0, (H, W, 3)) / (H * W)
+    R = diff.MaterialRenderer(sc, spp=4096, seed=5)
+    P = torch.tensor(P0, dtype=torch.float64, requires_grad=True)
+    wt = torch.tensor(w, dtype=torch.float64, device="cuda")
+    (R.image(P) * wt).sum().backward()
+    g_ad = P.grad.detach().cpu().numpy()
+
+    def loss_cpu(Px):
+        s2 = dataclasses.replace(sc, materials=diff.materials_from_params(sc.materials, Px))
+        film, _, _ = oracle.OracleScene(s2).render(params=oracle.capi.params_for(s2, spp=512), mode=0)
+        return float((film[..., :3].astype(np.float64) * w).sum())
+
+    eps = 0.05
+    checked = []
+    for i, m in enumerate(sc.materials):
+        if m.type != 0:
+            continue
+        for k in (0, 1, 2, 4):
+            Pp, Pm = P0.copy(), P0.copy()
+            Pp[i, k] += eps
+            Pm[i, k] -= eps
+            checked.append((i, k, (loss_cpu(Pp) - loss_cpu(Pm)) / (2 * eps)))
+    fd = np.array([c[2] for c in checked])
+    ad = np.array([g_ad[i, k] for i, k, _ in checked])
+    scale = np.abs(fd).max()
+    out = os.environ.get("OMV_ADJOINT_REPORT")
+    if out:
+        with open(out, "w") as fh:
+            json.dump({"ad": ad.tolist(), "fd": fd.tolist()}, fh)
+    assert scale > 0
+    assert np.all(np.abs(ad - fd) <= np.maximum(0.15 * scale, 0.25 * np.abs(fd))), (ad, fd)
