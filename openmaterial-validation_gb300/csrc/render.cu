@@ -38,6 +38,11 @@ namespace omv {
 namespace {
 
 constexpr int kTraceThreads = 128;
+// 6 resident blocks of the trace kernels per SM (80 registers, a few spilled
+// stack words): more warps in flight for the latency-bound traversal than the
+// 5 blocks its unconstrained 96 registers allow (measured 3.18 -> 3.06 ms per
+// extension launch on the 1920x1080x64 frame; 7 and 8 blocks spill more)
+constexpr int kTraceMinBlocks = 6;
 constexpr int kShadeThreads = 256;
 
 // counter slots within RenderScratch::ctr (reset per wave)
@@ -280,7 +285,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_light_gen(WaveArgs A)
 
 // ------------------------------------------------------------ extend ---
 // persistent closest-hit over one ray queue (count at *count)
-__global__ void __launch_bounds__(kTraceThreads) k_extend(DevScene S, const uint32_t* items, float4* rq, uint4* hits,
+__global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_extend(DevScene S, const uint32_t* items, float4* rq, uint4* hits,
                                                           const uint32_t* count, uint32_t* work,
                                                           unsigned long long* stats, int stat_kind)
 {
@@ -493,7 +498,7 @@ __global__ void __launch_bounds__(kShadeThreads, 3) k_camera_shade(WaveArgs A, i
 
 // ------------------------------------------------------------ shadow ---
 // BDPTRenderer::isConnected (BDPTRenderer.cpp:208-235)
-__global__ void __launch_bounds__(kTraceThreads) k_shadow(DevScene S, const uint32_t* items, const float4* sq,
+__global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevScene S, const uint32_t* items, const float4* sq,
                                                           const uint32_t* count, uint32_t* work, float4* rad,
                                                           unsigned long long* stats)
 {
