@@ -191,7 +191,19 @@ typedef struct omv_camera {
 
 /* ----------------------------------------------------------- parameters --- */
 
-enum { OMV_ESTIMATOR_REFERENCE = 0 };
+/* OMV_ESTIMATOR_REFERENCE: BDPTRenderer's estimator (BDPTRenderer.cpp:237-302).
+ * OMV_ESTIMATOR_MIS: the same, plus at every camera vertex on a PBR surface a
+ * direction drawn from the HDRI's 2D alias table (cells weighted by luminance
+ * times solid angle), traced as a sampled ray in that direction would be
+ * (shifted origin, no end point: it reaches the environment when nothing is
+ * hit) and weighted against the vertex's own sampling by the power heuristic;
+ * the background seen by a sampled escape gets the complementary weight.
+ * Both strategies estimate the reference sampler's own integrand, so the
+ * image converges to the reference estimator's with less variance under
+ * bright, small environment features.
+ * No effect without an HDRI; not available in omv_render_device_static or the
+ * adjoint. */
+enum { OMV_ESTIMATOR_REFERENCE = 0, OMV_ESTIMATOR_MIS = 1 };
 
 /* RendererParameters (RendererParameters.h:20-96) plus the build's own keys. */
 typedef struct omv_params {
@@ -204,7 +216,7 @@ typedef struct omv_params {
     float light_min_distance;           /* lightMinDistance, default 0.01 */
     float ray_cut_value;                /* rayCutPixValue, default 0.002 */
     uint64_t seed;                      /* Philox key */
-    int32_t estimator;                  /* OMV_ESTIMATOR_REFERENCE */
+    int32_t estimator;                  /* OMV_ESTIMATOR_REFERENCE or OMV_ESTIMATOR_MIS */
     int32_t sample_offset;              /* first sample index (progressive rendering) */
     int32_t accumulate_variance;        /* also accumulate per-pixel sum of squares */
     int32_t wave_paths;                 /* paths per wavefront wave; 0 = automatic */

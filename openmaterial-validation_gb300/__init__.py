@@ -161,6 +161,10 @@ def check(status: int) -> None:
 
 # ------------------------------------------------------------ parameters --
 
+ESTIMATOR_REFERENCE = 0  # BDPTRenderer's estimator
+ESTIMATOR_MIS = 1  # plus environment connections weighted by the power heuristic
+
+
 @dataclasses.dataclass
 class RendererParameters:
     """RendererParameters (RendererParameters.h:20-96) plus the build's keys."""
@@ -176,13 +180,14 @@ class RendererParameters:
     sample_offset: int = 0
     accumulate_variance: bool = False
     wave_paths: int = 0
+    estimator: int = 0  # OMV_ESTIMATOR_REFERENCE (0) or OMV_ESTIMATOR_MIS (1)
 
     def to_c(self) -> capi.Params:
         return capi.Params(camera_bounces=self.cameraBouncesN, light_bounces=self.lightBouncesN, time_kernels=0,
                            max_path_length=self.maxPathLength, samples_per_pixel=self.samplesPerPixel,
                            light_distance_attenuation=self.lightDistanceAttenuation,
                            light_scale=self.lightScaleValue, light_min_distance=self.lightMinDistance,
-                           ray_cut_value=self.rayCutPixValue, seed=self.seed, estimator=0,
+                           ray_cut_value=self.rayCutPixValue, seed=self.seed, estimator=self.estimator,
                            sample_offset=self.sample_offset, accumulate_variance=1 if self.accumulate_variance else 0,
                            wave_paths=self.wave_paths)
 

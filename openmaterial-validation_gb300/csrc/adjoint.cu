@@ -411,6 +411,7 @@ void adjoint_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, con
     const int nmat = s.num_materials - 1;
     if (nmat > kAdjMaxMaterials) throw ArgError("the adjoint supports at most 16 materials");
     if (!d_adjoint || !d_grad) throw ArgError("adjoint image and gradient buffers are required");
+    if (p.estimator != OMV_ESTIMATOR_REFERENCE) throw ArgError("the adjoint replays the reference estimator only");
     for (const DevMaterial& m : s.h_mats)
         if (m.type == kMatPbr && (m.textured || m.emissive_on))
             throw ArgError("the adjoint differentiates untextured materials only");

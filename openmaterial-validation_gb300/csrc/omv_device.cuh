@@ -433,6 +433,46 @@ __device__ __forceinline__ float om_channel(float n, float k, float cosTheta)
     return lerpf(P, S, 0.5f) / fabsf(cosTheta);
 }
 
+// Density of the reflection branches of bsdf_sample_indirect at direction O and
+// the integrand they estimate: sum over branches b of P_b w_b(O) |N.O| pdf_b(O),
+// w_b the branch's weight (bsdf_evaluate).  A direction another strategy
+// samples then carries the same expected contribution as the sampler's own
+// (the MIS estimator's environment connection).  Diffuse: cosine hemisphere,
+// P = p color.a; specular: GGX half vector with alpha^2 = (alpha)^2 reflected,
+// pdf D(H) (N.H) / (4 |O.H|), P = 1 - p.  Transmission is not covered (zero).
+__device__ __forceinline__ float bsdf_reflection_mix(BsdfIn d, V3 O, float ct, V3& feff)
+{
+    feff = v3(0.0f, 0.0f, 0.0f);
+    const float VdotN = -dot(d.I, d.N);
+    if (VdotN < 0.0f) {
+        if (!d.transmissive) return 0.0f;
+        d.N = -d.N;
+    }
+    const float cosO = dot(d.N, O);
+    if (!(cosO > 0.0f)) return 0.0f;
+    const float p = 0.8f * fabsf(VdotN) + 0.1f;
+    const float Pd = p * d.color[3], Ps = 1.0f - p;
+    const float pdf_d = cosO / kPi;
+    float pdf_s = 0.0f;
+    // the sampler reflects I about H and normalises, so the half vector of O is
+    // taken with the unit incoming direction (camera rays need not be unit)
+    const V3 H = normalize(O - normalize(d.I));
+    const float NdotH = dot(d.N, H);
+    if (NdotH > 0.0f) {
+        const float a2 = d.alpha * d.alpha;
+        const float den = 1.0f + (a2 - 1.0f) * NdotH * NdotH;
+        const float D = a2 / (kPi * den * den);
+        const float OdotH = fabsf(dot(O, H));
+        if (OdotH > 0.0f) pdf_s = D * NdotH / (4.0f * OdotH);
+    }
+    const float pdf = Pd * pdf_d + Ps * pdf_s;
+    if (!(pdf > 0.0f)) return 0.0f;
+    if (Pd > 0.0f) feff = feff + bsdf_evaluate(d.I, O, d.N, d.color, d.metal, d.alpha, 0, O, p) * (Pd * pdf_d);
+    if (pdf_s > 0.0f) feff = feff + bsdf_evaluate(d.I, O, d.N, d.color, d.metal, d.alpha, 1, H, p) * (Ps * pdf_s);
+    feff = feff * ct;
+    return pdf;
+}
+
 // ------------------------------------------------------ environment ---
 // HDRBackground::getRadiance (HdrBackground.cpp:55-97)
 __device__ __forceinline__ V3 env_radiance(const DevEnv& e, V3 dir)
@@ -461,6 +501,56 @@ __device__ __forceinline__ V3 env_radiance(const DevEnv& e, V3 dir)
     V3 val = v3(c0.x * w0 + c1.x * w1 + c2.x * w2 + c3.x * w3, c0.y * w0 + c1.y * w1 + c2.y * w2 + c3.y * w3,
                 c0.z * w0 + c1.z * w1 + c2.z * w2 + c3.z * w3);
     return val * e.scale;
+}
+
+// lookup coordinates of a world direction (the first half of env_radiance)
+__device__ __forceinline__ void env_uv(const DevEnv& e, V3 dir, float& u, float& v)
+{
+    const float* R = e.rot;
+    V3 rd = v3(R[0] * dir.x + R[3] * dir.y + R[6] * dir.z, R[1] * dir.x + R[4] * dir.y + R[7] * dir.z,
+               R[2] * dir.x + R[5] * dir.y + R[8] * dir.z);
+    V3 rxy = normalize(v3(rd.x, rd.y, 0.0f));
+    float xang = acosf(clampf(rxy.x, -1.0f, 1.0f));
+    xang = rxy.y < 0.0f ? 2.0f * kPi - xang : xang;
+    float yang = asinf(clampf(rd.z, -1.0f, 1.0f)) + 0.5f * kPi;
+    u = xang / (2.0f * kPi);
+    v = 1.0f - yang / kPi;
+}
+
+// density per steradian with which env_sample draws `dir`
+__device__ __forceinline__ float env_pdf(const DevEnv& e, V3 dir)
+{
+    if (e.smp.cells <= 0) return 0.0f;
+    float u, v;
+    env_uv(e, dir, u, v);
+    const int i = min(max((int)(u * (float)e.width), 0), e.width - 1);
+    const int j = min(max((int)(v * (float)e.height), 0), e.height - 1);
+    return __ldg(e.smp.pdf + (size_t)j * e.width + i);
+}
+
+// a direction from the environment's alias table (u0: cell, u1: alias
+// choice, u2/u3: position in the cell, uniform in solid angle); returns its
+// density per steradian (0: nothing to sample)
+__device__ __forceinline__ float env_sample(const DevEnv& e, float u0, float u1, float u2, float u3, V3& dir)
+{
+    const int n = e.smp.cells;
+    if (n <= 0) return 0.0f;
+    int c = min((int)(u0 * (float)n), n - 1);
+    if (!(u1 < __ldg(e.smp.prob + c))) c = (int)__ldg(e.smp.alias + c);
+    const float pdf = __ldg(e.smp.pdf + c);
+    if (!(pdf > 0.0f)) return 0.0f;
+    const int i = c % e.width, j = c / e.width;
+    const float u = ((float)i + u2) / (float)e.width;
+    const float c0 = cospif((float)j / (float)e.height), c1 = cospif((float)(j + 1) / (float)e.height);
+    const float z = c0 - u3 * (c0 - c1);  // cos(pi v), uniform in solid angle over the cell's rows
+    const float sxy = sqrtf(fmaxf(0.0f, 1.0f - z * z));
+    float sn, cs;
+    sincospif(2.0f * u, &sn, &cs);
+    const V3 rd = v3(sxy * cs, sxy * sn, z);
+    const float* R = e.rot;  // rd = dir R, R a rotation: dir = R rd
+    dir = normalize(v3(R[0] * rd.x + R[1] * rd.y + R[2] * rd.z, R[3] * rd.x + R[4] * rd.y + R[5] * rd.z,
+                       R[6] * rd.x + R[7] * rd.y + R[8] * rd.z));
+    return pdf;
 }
 
 }  // namespace omv

@@ -97,12 +97,24 @@ struct alignas(16) DevMaterial {
     DevTexRef tex[kTexSlots];
 };
 
+// environment importance sampling (the MIS estimator): one cell per texel
+// square [i, i+1) x [j, j+1) of the lookup's (u, v) grid, weighted by the
+// largest luminance its bilinear lookup can reach times its solid angle;
+// Vose's alias table over the cells, and each cell's density per steradian
+struct DevEnvSampler {
+    const float* prob;       // alias threshold of cell i
+    const uint32_t* alias;   // alias of cell i
+    const float* pdf;        // density per steradian of directions in cell i (0: never sampled)
+    int32_t cells;           // width * height, 0 when not built
+};
+
 struct DevEnv {
     const float4* rgb;
     int32_t width, height;
     float rot[9];
     float scale;
     int32_t present;
+    DevEnvSampler smp;
 };
 
 struct DevScene {

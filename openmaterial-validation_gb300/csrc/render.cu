@@ -11,7 +11,8 @@
 //     k_camera_gen      jittered pinhole rays (PinholeCamera::getRay)
 //     k_extend
 //     k_camera_shade    surface point, BRDF sample, environment on escape,
-//                       light/camera vertex connections -> shadow queue
+//                       light/camera vertex connections (and, with the MIS
+//                       estimator, environment rays) -> shadow queue
 //     k_shadow          isConnected (closest hit + end-point test), add
 //   k_film              per-path radiance into the FP64 film (PinholeCamera::hit)
 // Queues are SoA-packed float4 records appended with warp-aggregated atomics
@@ -391,9 +392,55 @@ __global__ void __launch_bounds__(kShadeThreads) k_light_shade(WaveArgs A, int b
     }
 }
 
+// ------------------------------------------------ environment connection ---
+constexpr uint32_t kDimEnvConnect = 2048u;
+
+// The MIS estimator at camera vertex b of a PBR surface: a direction drawn
+// from the environment's alias table, weighted by the power heuristic against
+// the vertex's own reflection sampling, and queued as an environment ray; the
+// escape of the sampled direction O (next bounce) gets the complementary
+// weight from the density returned here.  Both strategies estimate the
+// sampler's own integrand (bsdf_reflection_mix), and the environment ray is
+// traced exactly as a sampled ray in that direction would be (origin shifted
+// along it, the path's tnear, unbounded, escaping when nothing is hit, so
+// that both see the same self-intersections), so the image's expectation is
+// the reference estimator's.  Only an escape the reference would count is
+// connected: b < camera bounces and b + 1 <= maxPathLength.
+static __device__ __noinline__ float env_connect(const WaveArgs& A, int b, int k, uint64_t seed, uint32_t pixel,
+                                                 uint32_t sample, BsdfIn d, V3 pos, V3 nrm, V3 tp, V3 O, int kind,
+                                                 float tnear)
+{
+    const DevScene& S = A.S;
+    float pdf_o = 0.0f;
+    V3 unused;
+    if (kind == 0 || kind == 1) pdf_o = bsdf_reflection_mix(d, O, 1.0f, unused);
+    if (b >= A.cam_bounces || b + 1 > A.max_len) return pdf_o;
+    const Rng4 r = rng4(seed, pixel, sample, kDimEnvConnect + (uint32_t)b, kStreamCamera);
+    V3 w;
+    const float pe = env_sample(S.env, r.u[0], r.u[1], r.u[2], r.u[3], w);
+    if (!(pe > 0.0f)) return pdf_o;
+    V3 feff;
+    const float pb = bsdf_reflection_mix(d, w, fabsf(dot(w, nrm)), feff);
+    if (!(pb > 0.0f)) return pdf_o;
+    const V3 L = env_radiance(S.env, w);
+    const float m = pe / (pe * pe + pb * pb);  // power heuristic pe^2 / (pe^2 + pb^2), over pe
+    const V3 c = v3(tp.x * feff.x * L.x * m, tp.y * feff.y * L.y * m, tp.z * feff.z * L.z * m);
+    if (!(c.x > 0.0f || c.y > 0.0f || c.z > 0.0f)) return pdf_o;
+    const uint32_t sl = atomicAdd(&A.R.ctr[kCtrShadow + b], 1u);
+    float4* q = A.R.sq + 3 * (size_t)sl;
+    const V3 so = shifted_origin(pos, w, 1.0f);
+    q[0] = make_float4(so.x, so.y, so.z, __int_as_float(k));
+    q[1] = make_float4(w.x, w.y, w.z, tnear);
+    q[2] = make_float4(c.x, c.y, c.z, 1.0f);  // w = 1: an environment ray
+    return pdf_o;
+}
+
 // ------------------------------------------------------ camera shade ---
 // BDPTRenderer::computePath for the camera subpath (inv = true), vertex b, plus
-// the escape term and the connections of computePaths (:251-298) at vertex b
+// the escape term and the connections of computePaths (:251-298) at vertex b.
+// kMis: the MIS estimator's environment connections (a separate instantiation,
+// so the reference estimator's kernel carries none of their registers).
+template <bool kMis>
 __global__ void __launch_bounds__(kShadeThreads, 3) k_camera_shade(WaveArgs A, int b, const float4* rq_in,
                                                                  float4* rq_out)
 {
@@ -418,7 +465,11 @@ __global__ void __launch_bounds__(kShadeThreads, 3) k_camera_shade(WaveArgs A, i
             if (h.x == kInvalid) {
                 // escape: background x throughput when cp_len <= maxPathLength (:251-258)
                 if (S.env.present && b <= A.max_len) {
-                    const V3 bg = env_radiance(S.env, in);
+                    V3 bg = env_radiance(S.env, in);
+                    if (kMis && tp4.w > 0.0f) {  // the sampler's share (power heuristic) against env_connect
+                        const float pe = env_pdf(S.env, in);
+                        bg = bg * (tp4.w * tp4.w / (tp4.w * tp4.w + pe * pe));
+                    }
                     float4 r = first ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : A.R.rad[k];
                     r.x += bg.x * tp.x;
                     r.y += bg.y * tp.y;
@@ -435,9 +486,15 @@ __global__ void __launch_bounds__(kShadeThreads, 3) k_camera_shade(WaveArgs A, i
                 const Surf sp = surface_point(S, h.x, h.y, __uint_as_float(h.z), __uint_as_float(h.w), true, &M);
                 const PbrParams P = pbr_params(S, M, sp);
                 const Rng4 u = rng4(c.seed, pixel, sample, (uint32_t)b, kStreamCamera);
-                const V3 brdf = material_sample(S, M, P, sp, in, true, u, O);
+                SampleInfo info;
+                info.kind = -1;
+                const V3 brdf = material_sample(S, M, P, sp, in, true, u, O, kMis ? &info : nullptr);
                 const float ct = fabsf(dot(O, sp.nrm));
                 const V3 tpn = v3(tp.x * brdf.x * ct, tp.y * brdf.y * ct, tp.z * brdf.z * ct);
+                float mis_pdf = 0.0f;  // density of O for the next escape's MIS weight (0: weight 1)
+                if (kMis && M.type == kMatPbr)
+                    mis_pdf = env_connect(A, b, k, c.seed, pixel, sample, pbr_bsdf_in(M, P, sp, in), sp.pos, sp.nrm,
+                                          tp, O, info.kind, tnear);
                 if (M.type == kMatPbr && M.emissive_on) {  // Rad += outFactor x emission (:171-173)
                     const V3 e = pbr_emission(S, M, tex_hit(sp));
                     float4 r = A.R.rad[k];
@@ -481,7 +538,7 @@ __global__ void __launch_bounds__(kShadeThreads, 3) k_camera_shade(WaveArgs A, i
                         q[2] = make_float4(lc.x, lc.y, lc.z, 0.0f);
                     }
                 }
-                A.R.tp[k] = make_float4(tpn.x, tpn.y, tpn.z, 0.0f);
+                A.R.tp[k] = make_float4(tpn.x, tpn.y, tpn.z, mis_pdf);
                 if (b < A.cam_bounces && (tpn.x != 0.0f || tpn.y != 0.0f || tpn.z != 0.0f)) {
                     push = true;
                     so = shifted_origin(sp.pos, O, 1.0f);
@@ -497,7 +554,12 @@ __global__ void __launch_bounds__(kShadeThreads, 3) k_camera_shade(WaveArgs A, i
 }
 
 // ------------------------------------------------------------ shadow ---
-// BDPTRenderer::isConnected (BDPTRenderer.cpp:208-235)
+// BDPTRenderer::isConnected (BDPTRenderer.cpp:208-235) for vertex connections
+// (record w = 0: end points A, B); environment rays of the MIS estimator
+// (record w = 1: origin, direction and tnear) reach the environment when the
+// closest-hit query finds nothing, as a sampled ray escapes in k_extend
+// (kEnv: the instantiation that reads the record kind).
+template <bool kEnv>
 __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevScene S, const uint32_t* items, const float4* sq,
                                                           const uint32_t* count, uint32_t* work, float4* rad,
                                                           unsigned long long* stats)
@@ -520,22 +582,31 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevSc
         const float4 q0 = sq[3 * (size_t)i], q1 = sq[3 * (size_t)i + 1], q2 = sq[3 * (size_t)i + 2];
         const V3 A = v3(q0.x, q0.y, q0.z), B = v3(q1.x, q1.y, q1.z);
         const int k = __float_as_int(q0.w);
+        const bool env = kEnv && q2.w != 0.0f;  // environment ray: (origin, direction, tnear), reached when nothing is hit
         V3 dir = B - A;
         const float len = sqrtf(dot(dir, dir));
         float maxsz = max_abs(A, 1.0f);
         float safeD = 2.0f * kEpsAcc * kEps * maxsz;
         bool connected = true;
-        if (!(len <= safeD)) {
+        float tnear = safeD, tfar = kFltMax;
+        if (env) {
+            dir = B;
+            tnear = q1.w;
+        } else if (!(len <= safeD)) {
             dir = v3(dir.x / len, dir.y / len, dir.z / len);
-            float tnear = safeD;
-            const float tfar = len + (0.1f * len > safeD ? 0.1f * len : safeD);
+            tfar = len + (0.1f * len > safeD ? 0.1f * len : safeD);
+        }
+        if (env || !(len <= safeD)) {  // one closest-hit call site for both kinds
             RayHit h;
             if (scene_intersect(S, items, A, dir, tnear, tfar, h, st, tc)) {
-                const Surf sp = surface_point(S, h.inst, h.prim, h.u, h.v, false);
-                const V3 dd = sp.pos - B;
-                const float sd = dot(dd, dd);
-                const float sb = 10.0f * kEps * max_abs(B, 1.0f);
-                connected = sd <= sb * sb;
+                connected = false;
+                if (!env) {
+                    const Surf sp = surface_point(S, h.inst, h.prim, h.u, h.v, false);
+                    const V3 dd = sp.pos - B;
+                    const float sd = dot(dd, dd);
+                    const float sb = 10.0f * kEps * max_abs(B, 1.0f);
+                    connected = sd <= sb * sb;
+                }
             }
         }
         if (connected) {
@@ -833,6 +904,15 @@ struct FramePlan {
     bool lights;
 };
 
+// the MIS estimator (environment connections) runs when asked for and the
+// scene has an environment
+bool mis_on(const SceneHost& s, const omv_params& p)
+{
+    if (p.estimator != OMV_ESTIMATOR_REFERENCE && p.estimator != OMV_ESTIMATOR_MIS)
+        throw ArgError("unknown estimator");
+    return p.estimator == OMV_ESTIMATOR_MIS && s.dev.env.present;
+}
+
 // `cap` is the requested wave size (0: `default_cap`), clamped to the frame.
 FramePlan plan_frame(const SceneHost& s, const omv_camera& cam, const omv_params& p, int64_t default_cap)
 {
@@ -848,7 +928,7 @@ FramePlan plan_frame(const SceneHost& s, const omv_camera& cam, const omv_params
     P.cap = std::min<int64_t>(P.cap, std::max<int64_t>(P.total, 1));
     P.lights = s.num_lights > 0;
     P.light_slots = P.lights ? p.light_bounces + 1 : 1;
-    P.shadow_slots = P.lights ? P.light_slots : 1;
+    P.shadow_slots = std::max(1, (P.lights ? P.light_slots : 0) + (mis_on(s, p) ? 1 : 0));
     return P;
 }
 
@@ -882,6 +962,8 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
 {
     const int64_t total = P.total, npix = P.npix, cap = P.cap;
     const bool lights = P.lights;
+    const bool mis = mis_on(s, p);
+    if (mis) ensure_env_sampler(s);
     OMV_CUDA(cudaMemsetAsync(R.stats, 0, 16 * 8, st));
     WaveArgs A;
     A.S = s.dev;
@@ -905,7 +987,8 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
     A.path_job = R.path_job;
     int occ_t = 0, occ_s = 0;
     OMV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, k_extend, kTraceThreads, 0));
-    OMV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_camera_shade, kShadeThreads, 0));
+    OMV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, mis ? k_camera_shade<true> : k_camera_shade<false>,
+                                                           kShadeThreads, 0));
     const int trace_grid = std::max(1, occ_t) * s.num_sms;
     const int shade_grid = std::max(1, occ_s) * s.num_sms;
     int64_t launches = 0;
@@ -968,11 +1051,18 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
             k_extend<<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, in, R.hits, R.ctr + kCtrCam + b,
                                                            R.ctr + kCtrWork + work++, R.stats, kStatExt);
             if (time_kernels) timed(ext_ev);
-            k_camera_shade<<<shade_grid, kShadeThreads, 0, st>>>(A, b, in, out);
+            if (mis)
+                k_camera_shade<true><<<shade_grid, kShadeThreads, 0, st>>>(A, b, in, out);
+            else
+                k_camera_shade<false><<<shade_grid, kShadeThreads, 0, st>>>(A, b, in, out);
             launches += 2;
-            if (lights) {
+            if (lights || mis) {
                 if (time_kernels) timed(sh_ev);
-                k_shadow<<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, R.sq, R.ctr + kCtrShadow + b,
+                if (mis)
+                    k_shadow<true><<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, R.sq, R.ctr + kCtrShadow + b,
+                                                               R.ctr + kCtrWork + work++, R.rad, R.stats);
+                else
+                    k_shadow<false><<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, R.sq, R.ctr + kCtrShadow + b,
                                                                R.ctr + kCtrWork + work++, R.rad, R.stats);
                 if (time_kernels) timed(sh_ev);
                 ++launches;
@@ -1130,7 +1220,7 @@ FramePlan batch_frame_plan(SceneHost& s, const BatchJobs& B, const omv_params& p
     P.total = B.total_paths;
     P.lights = s.num_lights > 0;
     P.light_slots = P.lights ? p.light_bounces + 1 : 1;
-    P.shadow_slots = P.lights ? P.light_slots : 1;
+    P.shadow_slots = std::max(1, (P.lights ? P.light_slots : 0) + (mis_on(s, p) ? 1 : 0));
     int64_t cap = wave_paths;
     if (cap <= 0) {
         size_t free_b = 0, total_b = 0;
@@ -1297,6 +1387,9 @@ void render_frame_static(SceneHost& s, const omv_camera& cam, const omv_params& 
                          uint32_t* d_count, cudaStream_t st)
 {
     if (p.time_kernels) throw ArgError("time_kernels needs CUDA events, which the no-allocation render does not create");
+    if (p.estimator == OMV_ESTIMATOR_MIS)
+        throw ArgError("the MIS estimator builds an environment table on first use; the no-allocation render "
+                       "supports the reference estimator only");
     FramePlan P = plan_frame(s, cam, p, 1);
     const int64_t limit = static_wave_limit(P.light_slots, P.shadow_slots);
     if (p.wave_paths > 0) {

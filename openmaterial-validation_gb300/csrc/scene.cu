@@ -337,6 +337,74 @@ void set_material_sets(SceneHost& s, int num_sets, const omv_material_desc* desc
     s.num_mat_sets = num_sets;
 }
 
+// Environment sampler for the MIS estimator: cell (i, j) of the lookup grid
+// (u in [i, i+1) / W, v in [j, j+1) / H) draws its radiance from texels i, i+1 of
+// rows j, j+1 (wrapping, as HDRBackground::getRadiance's bilinear lookup does),
+// so its weight is the largest of their luminances times the cell's solid
+// angle (2 pi / W)(cos(pi j / H) - cos(pi (j+1) / H)).  Alias table by Vose's
+// method (M. D. Vose, "A linear algorithm for generating random numbers with
+// a given distribution", IEEE TSE 1991).  Built once per scene on first use.
+void ensure_env_sampler(SceneHost& s)
+{
+    DevEnv& e = s.dev.env;
+    if (!e.present || e.smp.cells != 0) return;
+    const int W = e.width, H = e.height;
+    const size_t n = (size_t)W * H;
+    std::vector<float4> tex(n);
+    OMV_CUDA(cudaMemcpyAsync(tex.data(), e.rgb, sizeof(float4) * n, cudaMemcpyDeviceToHost, s.stream));
+    OMV_CUDA(cudaStreamSynchronize(s.stream));
+    std::vector<float> lum(n);
+    for (size_t k = 0; k < n; ++k) {
+        const float4 t = tex[k];
+        lum[k] = std::max(0.0f, 0.2126f * t.x + 0.7152f * t.y + 0.0722f * t.z);
+    }
+    std::vector<double> w(n), omega(H);
+    const double pi = 3.14159265358979323846;
+    for (int j = 0; j < H; ++j)
+        omega[j] = (2.0 * pi / W) * (std::cos(pi * j / H) - std::cos(pi * (j + 1) / H));
+    double total = 0.0;
+    for (int j = 0; j < H; ++j)
+        for (int i = 0; i < W; ++i) {
+            const int i1 = (i + 1) % W, j1 = (j + 1) % H;
+            const float m = std::max(std::max(lum[(size_t)j * W + i], lum[(size_t)j * W + i1]),
+                                     std::max(lum[(size_t)j1 * W + i], lum[(size_t)j1 * W + i1]));
+            const double v = (double)m * omega[j];
+            w[(size_t)j * W + i] = v;
+            total += v;
+        }
+    std::vector<float> prob(n, 1.0f), pdf(n, 0.0f);
+    std::vector<uint32_t> alias(n);
+    for (size_t k = 0; k < n; ++k) alias[k] = (uint32_t)k;
+    if (total > 0.0) {
+        std::vector<double> q(n);
+        std::vector<uint32_t> small, large;
+        for (size_t k = 0; k < n; ++k) {
+            q[k] = w[k] / total * (double)n;
+            (q[k] < 1.0 ? small : large).push_back((uint32_t)k);
+            pdf[k] = (float)(w[k] / total / omega[k / W]);
+        }
+        while (!small.empty() && !large.empty()) {
+            const uint32_t a = small.back(), b = large.back();
+            small.pop_back();
+            prob[a] = (float)q[a];
+            alias[a] = b;
+            q[b] = (q[b] + q[a]) - 1.0;
+            if (q[b] < 1.0) {
+                large.pop_back();
+                small.push_back(b);
+            }
+        }
+        for (uint32_t k : large) prob[k] = 1.0f;
+        for (uint32_t k : small) prob[k] = 1.0f;  // rounding leftovers
+    }
+    e.smp.prob = s.upload(prob);
+    e.smp.alias = s.upload(alias);
+    e.smp.pdf = s.upload(pdf);
+    e.smp.cells = total > 0.0 ? (int32_t)n : 0;
+    if (e.smp.cells == 0) e.smp.cells = -1;  // nothing to sample: built, but empty
+    OMV_CUDA(cudaStreamSynchronize(s.stream));
+}
+
 void set_scene_materials(SceneHost& s, int num, const omv_material_desc* descs)
 {
     if (num != s.num_materials - 1 || (num > 0 && !descs))

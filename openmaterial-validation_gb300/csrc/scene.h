@@ -129,6 +129,8 @@ void render_batch(SceneHost& s, int num_jobs, const omv_job* jobs, const omv_par
 void autotune_batch(SceneHost& s, int num_jobs, const omv_job* jobs, const omv_params& p, cudaStream_t st,
                     int64_t* chosen);
 
+// builds the environment's alias table (the MIS estimator) if not yet built
+void ensure_env_sampler(SceneHost& s);
 // replaces the scene's own materials (same count, same alpha-mask status)
 void set_scene_materials(SceneHost& s, int num, const omv_material_desc* descs);
 // path-replay gradient of an image loss with respect to the material parameters

@@ -315,6 +315,22 @@ __device__ __forceinline__ V3 material_eval(const DevMaterial& M, const PbrParam
     return v3(M.color[0], M.color[1], M.color[2]);
 }
 
+// the BsdfIn material_sample builds for a PBR vertex
+__device__ __forceinline__ BsdfIn pbr_bsdf_in(const DevMaterial& M, const PbrParams& P, const Surf& sp, V3 in)
+{
+    BsdfIn d;
+    d.I = in;
+    d.N = sp.nrm;
+    d.T = sp.tan;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) d.color[i] = P.color[i];
+    d.metal = P.metal;
+    d.alpha = P.alpha;
+    d.eta = M.eta;
+    d.transmissive = P.transmissive;
+    return d;
+}
+
 // the same without textures (the material's constants)
 __device__ __forceinline__ V3 material_sample(const DevScene& S, const DevMaterial& M, const Surf& sp, V3 in, bool inv,
                                               const Rng4& u, V3& out, SampleInfo* info = nullptr)
