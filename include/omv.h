@@ -260,7 +260,8 @@ omv_status omv_render(omv_scene* scene, const omv_camera* camera, const omv_para
 /* Same as omv_render, but the film lives in caller-owned DEVICE memory and is
  * accumulated into (not cleared): d_sum_rgb (3*W*H doubles), d_sumsq_rgb (may
  * be NULL), d_count (W*H uint32).  `stream` is a cudaStream_t (NULL: the
- * scene's stream).  Asynchronous: returns after enqueueing all work. */
+ * legacy default stream, as in CUDA and torch).  Asynchronous: returns after
+ * enqueueing all work. */
 omv_status omv_render_device(omv_scene* scene, const omv_camera* camera, const omv_params* params,
                              double* d_sum_rgb, double* d_sumsq_rgb, uint32_t* d_count,
                              void* stream, omv_stats* stats);
@@ -280,7 +281,7 @@ omv_status omv_render_device(omv_scene* scene, const omv_camera* camera, const o
  *
  *   - Same film contract as omv_render_device: caller-owned device buffers,
  *     accumulated into (zero them before the first call), asynchronous on
- *     `stream` (NULL: the scene's stream).
+ *     `stream` (NULL: the legacy default stream).
  *   - The scratch bounds the wave size: params->wave_paths = 0 picks the
  *     largest wave that fits; a larger explicit wave_paths fails with
  *     OMV_ERR_INVALID_ARGUMENT and a message giving the limit.  The number of
@@ -331,7 +332,9 @@ enum { OMV_BATCH_GRAPH = 1 };  /* capture the batch once as a CUDA graph; replay
  * persistent kernels process, with a device job table giving each path its
  * camera, material set and film.  params->samples_per_pixel, seed,
  * sample_offset and wave_paths are ignored (per job / autotuned).
- * Asynchronous on `stream` (NULL: the scene's stream) unless stats is given. */
+ * Asynchronous on `stream` (NULL: the legacy default stream; a captured graph
+ * then replays on the scene's stream, ordered after and before it by events)
+ * unless stats is given. */
 omv_status omv_render_batch(omv_scene* scene, int32_t num_jobs, const omv_job* jobs, const omv_params* params,
                             void* stream, int32_t flags, omv_stats* stats);
 
@@ -364,7 +367,7 @@ omv_status omv_scene_set_materials(omv_scene* scene, int32_t num_materials, cons
  * half-vector density), so the result estimates the gradient of the expected
  * image; luminance cutoffs are not differentiated.  At most 15 camera and 15
  * light bounces and 16 materials.  Asynchronous on `stream` (NULL: the
- * scene's stream).  The reference has no counterpart (it renders only). */
+ * legacy default stream).  The reference has no counterpart (it renders only). */
 omv_status omv_adjoint(omv_scene* scene, const omv_camera* camera, const omv_params* params,
                        const float* d_adjoint_rgb, float* d_grad, void* stream);
 

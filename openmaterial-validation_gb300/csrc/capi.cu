@@ -172,7 +172,7 @@ omv_status omv_render_device(omv_scene* scene, const omv_camera* camera, const o
         check_camera(camera);
         if (!params || !d_sum_rgb || !d_count) throw omv::ArgError("params, d_sum_rgb and d_count are required");
         if (params->accumulate_variance && !d_sumsq_rgb) throw omv::ArgError("accumulate_variance needs d_sumsq_rgb");
-        cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : scene->h->stream;
+        cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL: the legacy default stream
         omv::render_frame(*scene->h, *camera, *params, d_sum_rgb, params->accumulate_variance ? d_sumsq_rgb : nullptr,
                           d_count, st, stats);
     });
@@ -186,7 +186,7 @@ omv_status omv_render_device_static(omv_scene* scene, const omv_camera* camera, 
         check_camera(camera);
         if (!params || !d_sum_rgb || !d_count) throw omv::ArgError("params, d_sum_rgb and d_count are required");
         if (params->accumulate_variance && !d_sumsq_rgb) throw omv::ArgError("accumulate_variance needs d_sumsq_rgb");
-        cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : scene->h->stream;
+        cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL: the legacy default stream
         omv::render_frame_static(*scene->h, *camera, *params, d_sum_rgb,
                                  params->accumulate_variance ? d_sumsq_rgb : nullptr, d_count, st);
     });
@@ -208,7 +208,7 @@ omv_status omv_render_batch(omv_scene* scene, int32_t num_jobs, const omv_job* j
         if (!params) throw omv::ArgError("params is NULL");
         if (params->time_kernels && (flags & OMV_BATCH_GRAPH))
             throw omv::ArgError("time_kernels cannot be combined with OMV_BATCH_GRAPH");
-        cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : scene->h->stream;
+        cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL: the legacy default stream
         omv::render_batch(*scene->h, num_jobs, jobs, *params, st, stats, (flags & OMV_BATCH_GRAPH) != 0);
     });
 }
@@ -219,7 +219,7 @@ omv_status omv_batch_autotune(omv_scene* scene, int32_t num_jobs, const omv_job*
     return guarded([&] {
         check_scene(scene);
         if (!params) throw omv::ArgError("params is NULL");
-        cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : scene->h->stream;
+        cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL: the legacy default stream
         omv::autotune_batch(*scene->h, num_jobs, jobs, *params, st, chosen_wave_paths);
     });
 }
@@ -239,7 +239,7 @@ omv_status omv_adjoint(omv_scene* scene, const omv_camera* camera, const omv_par
         check_scene(scene);
         check_camera(camera);
         if (!params) throw omv::ArgError("params is NULL");
-        cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : scene->h->stream;
+        cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL: the legacy default stream
         omv::adjoint_frame(*scene->h, *camera, *params, d_adjoint_rgb, d_grad, st);
     });
 }

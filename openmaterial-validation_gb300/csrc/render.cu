@@ -1269,6 +1269,17 @@ void render_batch(SceneHost& s, int n, const omv_job* jobs, const omv_params& p,
         run_waves(s, s.scratch, P, cam0, p, nullptr, nullptr, nullptr, st, stats, stats != nullptr, &plan);
         return;
     }
+    // a default stream cannot be captured: capture and replay on the scene's
+    // stream, ordered after the caller's stream and the caller's stream after it
+    const cudaStream_t caller = st;
+    const bool fork = st == nullptr || st == cudaStreamLegacy || st == cudaStreamPerThread;
+    if (fork) {
+        if (!s.fork_ev) OMV_CUDA(cudaEventCreateWithFlags(&s.fork_ev, cudaEventDisableTiming));
+        if (!s.join_ev) OMV_CUDA(cudaEventCreateWithFlags(&s.join_ev, cudaEventDisableTiming));
+        OMV_CUDA(cudaEventRecord(s.fork_ev, caller));
+        OMV_CUDA(cudaStreamWaitEvent(s.stream, s.fork_ev, 0));
+        st = s.stream;
+    }
     // the captured graph is valid for this job table, these parameters and this wave size
     std::vector<unsigned char> key(sizeof(DevJob) * B.jobs.size() + sizeof(omv_params) + sizeof(int64_t));
     std::memcpy(key.data(), B.jobs.data(), sizeof(DevJob) * B.jobs.size());
@@ -1299,6 +1310,10 @@ void render_batch(SceneHost& s, int n, const omv_job* jobs, const omv_params& p,
         s.batch_key = key;
     }
     OMV_CUDA(cudaGraphLaunch(s.batch_graph, st));
+    if (fork) {
+        OMV_CUDA(cudaEventRecord(s.join_ev, st));
+        OMV_CUDA(cudaStreamWaitEvent(caller, s.join_ev, 0));
+    }
     if (stats) {
         OMV_CUDA(cudaStreamSynchronize(st));
         *stats = omv_stats{};

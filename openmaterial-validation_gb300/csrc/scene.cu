@@ -222,6 +222,8 @@ SceneHost::~SceneHost()
     if (mat_sets) cudaFree(mat_sets);
     if (d_jobs) cudaFree(d_jobs);
     if (batch_graph) cudaGraphExecDestroy(batch_graph);
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    if (join_ev) cudaEventDestroy(join_ev);
     if (stream) cudaStreamDestroy(stream);
 }
 

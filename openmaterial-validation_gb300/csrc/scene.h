@@ -99,6 +99,7 @@ struct SceneHost {
     DevJob* d_jobs = nullptr;                // batch job table
     size_t jobs_cap = 0;
     cudaGraphExec_t batch_graph = nullptr;   // captured batch render, replayed for an identical job list
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;  // order `stream` after / before a caller's default stream
     std::vector<unsigned char> batch_key;    // what batch_graph was captured for
     int64_t batch_wave_paths = 0;            // autotuned wave size for batches (0: automatic)
 
