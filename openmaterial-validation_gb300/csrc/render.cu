@@ -285,7 +285,10 @@ __global__ void __launch_bounds__(kShadeThreads) k_light_gen(WaveArgs A)
 }
 
 // ------------------------------------------------------------ extend ---
-// persistent closest-hit over one ray queue (count at *count)
+// Persistent closest-hit over one ray queue (count at *count): a warp takes 32
+// consecutive rays and the next 32 when all are done (camera rays: the 32
+// samples of one pixel stay together).  Replacing finished rays lane by lane
+// (Aila & Laine 2009) was measured slower on every bounce.
 __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_extend(DevScene S, const uint32_t* items, float4* rq, uint4* hits,
                                                           const uint32_t* count, uint32_t* work,
                                                           unsigned long long* stats, int stat_kind)
@@ -439,9 +442,11 @@ static __device__ __noinline__ float env_connect(const WaveArgs& A, int b, int k
 // BDPTRenderer::computePath for the camera subpath (inv = true), vertex b, plus
 // the escape term and the connections of computePaths (:251-298) at vertex b.
 // kMis: the MIS estimator's environment connections (a separate instantiation,
-// so the reference estimator's kernel carries none of their registers).
+// so the reference estimator's kernel carries none of their registers).  Four
+// resident blocks of 256 (64 registers, 28 B of spills) hide more of the
+// vertex-gather latency than three (72 registers): 37.9 vs 38.5 ms per frame.
 template <bool kMis>
-__global__ void __launch_bounds__(kShadeThreads, 3) k_camera_shade(WaveArgs A, int b, const float4* rq_in,
+__global__ void __launch_bounds__(kShadeThreads, 4) k_camera_shade(WaveArgs A, int b, const float4* rq_in,
                                                                  float4* rq_out)
 {
     __shared__ BinScratch bins;

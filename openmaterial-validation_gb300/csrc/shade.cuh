@@ -362,6 +362,28 @@ static __device__ __noinline__ bool texture_masked(const DevScene& S, const DevM
     return M.factor[3] * a < M.cutoff;
 }
 
+// whether sceneIntersect skips this hit: an alpha-masked material (BLEND or
+// MASK below the cutoff), or a texture-masked one whose texel is transparent
+__device__ __forceinline__ bool hit_masked(const DevScene& S, const RayHit& h)
+{
+    const uint32_t mat = __ldg(&S.insts[h.inst].material);
+    const int masked = S.mats[mat].masked;
+    if (!masked) return false;
+    return masked != 2 || texture_masked(S, S.mats[mat], h.inst, h.prim, h.u, h.v);
+}
+
+// tnear of sceneIntersect's next try after a skipped hit at t
+__device__ __forceinline__ float masked_retry_tnear(V3 o, V3 d, float t)
+{
+    V3 org = v3(o.x + t * d.x, o.y + t * d.y, o.z + t * d.z);
+    float vv = max_abs(org, 1.0f);
+    vv = vv > t ? vv : t;
+    const float delta = kEpsAcc * kEps * vv;
+    return t + delta;
+}
+
+constexpr int kMaskedTries = 10;
+
 // BDPTRenderer::sceneIntersect (BDPTRenderer.cpp:75-102): closest hit, skipping
 // alpha-masked materials up to 10 times; tnear persists like the reference's
 // RTCRayHit does across the bounces of one path
@@ -369,17 +391,10 @@ __device__ __forceinline__ bool scene_intersect(const DevScene& S, const uint32_
                                                 float tfar, RayHit& h, TraceStack& st, TraceCounters& tc)
 {
     const float t1 = tfar;
-    for (int itr = 0; itr < 10; ++itr) {
+    for (int itr = 0; itr < kMaskedTries; ++itr) {
         if (!trace_closest(S, items, o, d, tnear, tfar, h, st, tc)) return false;
-        const uint32_t mat = __ldg(&S.insts[h.inst].material);
-        const int masked = S.mats[mat].masked;
-        if (!masked) return true;
-        if (masked == 2 && !texture_masked(S, S.mats[mat], h.inst, h.prim, h.u, h.v)) return true;
-        V3 org = v3(o.x + h.t * d.x, o.y + h.t * d.y, o.z + h.t * d.z);
-        float vv = max_abs(org, 1.0f);
-        vv = vv > h.t ? vv : h.t;
-        const float delta = kEpsAcc * kEps * vv;
-        tnear = h.t + delta;
+        if (!hit_masked(S, h)) return true;
+        tnear = masked_retry_tnear(o, d, h.t);
         tfar = t1;
         if (tfar <= tnear) return false;
     }
