@@ -51,6 +51,7 @@ constexpr int kCtrLight = 0;     // + bounce (0..light_bounces)
 constexpr int kCtrCam = 64;      // + bounce (0..camera_bounces)
 constexpr int kCtrShadow = 128;  // + bounce
 constexpr int kCtrWork = 192;    // + launch index
+constexpr int kCtrEnv = 448;     // + bounce: MIS environment rays
 enum { kStatExt = 0, kStatShadow = 1, kStatLight = 2, kStatNodes = 3, kStatTris = 4, kStatOverflow = 5 };
 
 __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want)
@@ -136,6 +137,7 @@ struct WaveArgs {
     const DevJob* jobs;       // batch job table (num_jobs == 0: one frame with the fields above)
     int32_t num_jobs;
     uint32_t* path_job;       // batch: job of each path of the wave
+    float4* env_q;  // MIS environment rays (3 float4 each), after the vertex connections' slots
     int32_t cam_bounces, light_bounces, max_len;
     int32_t atten_mode;
     float light_scale, min_dist, cut;
@@ -429,12 +431,12 @@ static __device__ __noinline__ float env_connect(const WaveArgs& A, int b, int k
     const float m = pe / (pe * pe + pb * pb);  // power heuristic pe^2 / (pe^2 + pb^2), over pe
     const V3 c = v3(tp.x * feff.x * L.x * m, tp.y * feff.y * L.y * m, tp.z * feff.z * L.z * m);
     if (!(c.x > 0.0f || c.y > 0.0f || c.z > 0.0f)) return pdf_o;
-    const uint32_t sl = atomicAdd(&A.R.ctr[kCtrShadow + b], 1u);
-    float4* q = A.R.sq + 3 * (size_t)sl;
+    const uint32_t sl = atomicAdd(&A.R.ctr[kCtrEnv + b], 1u);
+    float4* q = A.env_q + 3 * (size_t)sl;
     const V3 so = shifted_origin(pos, w, 1.0f);
     q[0] = make_float4(so.x, so.y, so.z, __int_as_float(k));
     q[1] = make_float4(w.x, w.y, w.z, tnear);
-    q[2] = make_float4(c.x, c.y, c.z, 1.0f);  // w = 1: an environment ray
+    q[2] = make_float4(c.x, c.y, c.z, 0.0f);
     return pdf_o;
 }
 
@@ -445,8 +447,9 @@ static __device__ __noinline__ float env_connect(const WaveArgs& A, int b, int k
 // so the reference estimator's kernel carries none of their registers).  Four
 // resident blocks of 256 (64 registers, 28 B of spills) hide more of the
 // vertex-gather latency than three (72 registers): 37.9 vs 38.5 ms per frame.
+// The MIS instantiation keeps three (it would spill 140 B at four).
 template <bool kMis>
-__global__ void __launch_bounds__(kShadeThreads, 4) k_camera_shade(WaveArgs A, int b, const float4* rq_in,
+__global__ void __launch_bounds__(kShadeThreads, kMis ? 3 : 4) k_camera_shade(WaveArgs A, int b, const float4* rq_in,
                                                                  float4* rq_out)
 {
     __shared__ BinScratch bins;
@@ -559,15 +562,17 @@ __global__ void __launch_bounds__(kShadeThreads, 4) k_camera_shade(WaveArgs A, i
 }
 
 // ------------------------------------------------------------ shadow ---
-// BDPTRenderer::isConnected (BDPTRenderer.cpp:208-235) for vertex connections
-// (record w = 0: end points A, B); environment rays of the MIS estimator
-// (record w = 1: origin, direction and tnear) reach the environment when the
-// closest-hit query finds nothing, as a sampled ray escapes in k_extend
-// (kEnv: the instantiation that reads the record kind).
+// kEnv = false: BDPTRenderer::isConnected (BDPTRenderer.cpp:208-235) for the
+// vertex connections (records: end points A, B and the contribution).
+// kEnv = true: the MIS estimator's environment rays (records: shifted origin,
+// direction and tnear, contribution), which reach the environment when a
+// sampled ray in that direction would escape: no hit at all.  Without
+// alpha-masked materials that is an any-hit query; with them sceneIntersect's
+// closest hit and retries decide, as in k_extend (`masked` != 0).
 template <bool kEnv>
 __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevScene S, const uint32_t* items, const float4* sq,
                                                           const uint32_t* count, uint32_t* work, float4* rad,
-                                                          unsigned long long* stats)
+                                                          unsigned long long* stats, int masked)
 {
     __shared__ uint2 sstack[kStackShared * kTraceThreads];
     TraceStack st;
@@ -587,25 +592,23 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevSc
         const float4 q0 = sq[3 * (size_t)i], q1 = sq[3 * (size_t)i + 1], q2 = sq[3 * (size_t)i + 2];
         const V3 A = v3(q0.x, q0.y, q0.z), B = v3(q1.x, q1.y, q1.z);
         const int k = __float_as_int(q0.w);
-        const bool env = kEnv && q2.w != 0.0f;  // environment ray: (origin, direction, tnear), reached when nothing is hit
-        V3 dir = B - A;
-        const float len = sqrtf(dot(dir, dir));
-        float maxsz = max_abs(A, 1.0f);
-        float safeD = 2.0f * kEpsAcc * kEps * maxsz;
         bool connected = true;
-        float tnear = safeD, tfar = kFltMax;
-        if (env) {
-            dir = B;
-            tnear = q1.w;
-        } else if (!(len <= safeD)) {
-            dir = v3(dir.x / len, dir.y / len, dir.z / len);
-            tfar = len + (0.1f * len > safeD ? 0.1f * len : safeD);
-        }
-        if (env || !(len <= safeD)) {  // one closest-hit call site for both kinds
+        if (kEnv) {
+            float tn = q1.w;
             RayHit h;
-            if (scene_intersect(S, items, A, dir, tnear, tfar, h, st, tc)) {
-                connected = false;
-                if (!env) {
+            connected = masked ? !scene_intersect(S, items, A, B, tn, kFltMax, h, st, tc)
+                               : !trace_any(S, items, A, B, tn, kFltMax, st, tc);
+        } else {
+            V3 dir = B - A;
+            const float len = sqrtf(dot(dir, dir));
+            float maxsz = max_abs(A, 1.0f);
+            float safeD = 2.0f * kEpsAcc * kEps * maxsz;
+            if (!(len <= safeD)) {
+                dir = v3(dir.x / len, dir.y / len, dir.z / len);
+                float tnear = safeD;
+                const float tfar = len + (0.1f * len > safeD ? 0.1f * len : safeD);
+                RayHit h;
+                if (scene_intersect(S, items, A, dir, tnear, tfar, h, st, tc)) {
                     const Surf sp = surface_point(S, h.inst, h.prim, h.u, h.v, false);
                     const V3 dd = sp.pos - B;
                     const float sd = dot(dd, dd);
@@ -969,6 +972,8 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
     const bool lights = P.lights;
     const bool mis = mis_on(s, p);
     if (mis) ensure_env_sampler(s);
+    bool masked = false;  // material sets keep which materials are masked
+    for (const DevMaterial& m : s.h_mats) masked = masked || m.masked != 0;
     OMV_CUDA(cudaMemsetAsync(R.stats, 0, 16 * 8, st));
     WaveArgs A;
     A.S = s.dev;
@@ -987,6 +992,7 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
     A.min_dist = p.light_min_distance;
     A.cut = p.ray_cut_value;
     A.R = R;
+    A.env_q = mis ? R.sq + 3 * (size_t)R.wave_cap * (size_t)(R.shadow_slots - 1) : nullptr;
     A.jobs = batch ? batch->d_jobs : nullptr;
     A.num_jobs = batch ? (int32_t)batch->h_jobs->size() : 0;
     A.path_job = R.path_job;
@@ -1061,14 +1067,18 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
             else
                 k_camera_shade<false><<<shade_grid, kShadeThreads, 0, st>>>(A, b, in, out);
             launches += 2;
-            if (lights || mis) {
+            if (lights) {
                 if (time_kernels) timed(sh_ev);
-                if (mis)
-                    k_shadow<true><<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, R.sq, R.ctr + kCtrShadow + b,
-                                                               R.ctr + kCtrWork + work++, R.rad, R.stats);
-                else
-                    k_shadow<false><<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, R.sq, R.ctr + kCtrShadow + b,
-                                                               R.ctr + kCtrWork + work++, R.rad, R.stats);
+                k_shadow<false><<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, R.sq, R.ctr + kCtrShadow + b,
+                                                                      R.ctr + kCtrWork + work++, R.rad, R.stats, 0);
+                if (time_kernels) timed(sh_ev);
+                ++launches;
+            }
+            if (mis) {
+                if (time_kernels) timed(sh_ev);
+                k_shadow<true><<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, A.env_q, R.ctr + kCtrEnv + b,
+                                                                     R.ctr + kCtrWork + work++, R.rad, R.stats,
+                                                                     masked ? 1 : 0);
                 if (time_kernels) timed(sh_ev);
                 ++launches;
             }
@@ -1266,6 +1276,7 @@ void render_batch(SceneHost& s, int n, const omv_job* jobs, const omv_params& p,
 {
     const BatchJobs B = make_batch(s, n, jobs, p);
     const FramePlan P = batch_frame_plan(s, B, p, s.batch_wave_paths);
+    if (mis_on(s, p)) ensure_env_sampler(s);  // allocates: never inside a graph capture
     ensure_scratch(s, P.cap, P.light_slots, P.shadow_slots);
     upload_jobs(s, B, st);
     const BatchPlan plan{s.d_jobs, &B.jobs, B.min_spp};

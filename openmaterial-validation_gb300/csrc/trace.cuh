@@ -212,7 +212,9 @@ __device__ __forceinline__ bool trace_begin(const DevScene& S, V3 o, V3 d, float
     return true;
 }
 
-// Processes one stack entry (an instance or a node); false when the traversal is over.
+// Processes one stack entry (an instance or a node); false when the traversal is
+// over.  kAny: stop at the first triangle hit (an occlusion query).
+template <bool kAny = false>
 __device__ __forceinline__ bool trace_step(const DevScene& S, const uint32_t* __restrict__ tlas_items, TraceState& T,
                                           TraceStack& st, TraceCounters& tc)
 {
@@ -310,6 +312,7 @@ __device__ __forceinline__ bool trace_step(const DevScene& S, const uint32_t* __
                     T.bv = v;
                     T.best_inst = T.cur_inst;
                     T.best_prim = prim;
+                    if (kAny) return false;
                 }
             }
         }
@@ -346,6 +349,18 @@ __device__ __forceinline__ bool trace_end(const TraceState& T, RayHit& hit)
     hit.u = T.bu;
     hit.v = T.bv;
     return true;
+}
+
+// Whether any triangle is hit in [tnear, tfar] (the closest-hit query's answer
+// to "is there a hit", without finding the closest).
+__device__ __forceinline__ bool trace_any(const DevScene& S, const uint32_t* __restrict__ tlas_items, V3 o, V3 d,
+                                          float tnear, float tfar, TraceStack& st, TraceCounters& tc)
+{
+    TraceState T;
+    if (!trace_begin(S, o, d, tnear, tfar, T, st)) return false;
+    while (trace_step<true>(S, tlas_items, T, st, tc)) {
+    }
+    return T.found;
 }
 
 // Closest hit; returns true and fills `hit` when a triangle is found.

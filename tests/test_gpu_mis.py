@@ -88,6 +88,57 @@ def test_mis_under_suns_matches_and_cuts_variance(gpu, scenes):
     assert v_mis.mean() < 0.1 * v_ref.mean(), (v_mis.mean(), v_ref.mean())
 
 
+def test_mis_with_point_light_matches_the_reference_estimator(gpu, scenes):
+    """Sky and a point light: light-vertex connections and environment rays
+    share the shadow queue."""
+    sc = scenes.scene_materials(32, 32, 1, tris=20_000, bounces=4, sky=True)
+    n = 8192
+    m_mis, v_mis = _render(gpu, sc, n, 5, gpu.ESTIMATOR_MIS)
+    m_ref, v_ref = _render(gpu, sc, n, 6, gpu.ESTIMATOR_REFERENCE)
+    frac3, glob = _zstats(m_mis, n, v_mis, m_ref, n, v_ref)
+    assert frac3 < 0.01, frac3
+    assert abs(glob) < 4, glob
+
+
+def test_mis_batch_matches_separate_renders(gpu, scenes):
+    """A batch under the MIS estimator, captured as a graph on its first call
+    (the environment table is built before the capture), gives each job the
+    film of a separate MIS render: counts exactly, sums to FP32 rounding of the
+    shadow contributions' atomic order."""
+    import ctypes as C
+
+    torch = pytest.importorskip("torch")
+    sc = scenes.scene_materials(32, 32, 1, tris=20_000, bounces=4, sky=True)
+    sets = scenes.material_variants(sc, 2, seed=5)
+    rs = gpu.RenderScene(sc)
+    br = gpu.BatchRenderer(rs, gpu.RendererParameters.for_scene(sc, estimator=gpu.ESTIMATOR_MIS))
+    br.set_material_sets(sets)
+    specs = [(32, 24, 4, 11, -1), (16, 16, 9, 12, 0), (24, 40, 5, 13, 1)]
+    films, jobs = [], []
+    for w, h, spp, seed, ms in specs:
+        f = (torch.zeros((h, w, 3), dtype=torch.float64, device="cuda"), None,
+             torch.zeros((h, w), dtype=torch.int32, device="cuda"))
+        cam = gpu.PinholeCamera.from_spec(sc.camera)
+        cam.width, cam.height = w, h
+        cam.adjust_to_resolution()
+        films.append((f, cam))
+        jobs.append(br.job(cam, spp, f, seed=seed, material_set=ms))
+    br.render(jobs, graph=True)
+    torch.cuda.synchronize()
+    for (w, h, spp, seed, ms), (f, cam) in zip(specs, films):
+        mats = sc.materials if ms < 0 else sets[ms]
+        rs2 = gpu.RenderScene(dataclasses.replace(sc, materials=mats))
+        s = torch.zeros((h, w, 3), dtype=torch.float64, device="cuda")
+        c = torch.zeros((h, w), dtype=torch.int32, device="cuda")
+        p = gpu.RendererParameters.for_scene(sc, samplesPerPixel=spp, seed=seed, estimator=gpu.ESTIMATOR_MIS).to_c()
+        cc = cam.to_c()
+        gpu.check(gpu.lib().omv_render_device(rs2.handle, C.byref(cc), C.byref(p), C.c_void_p(s.data_ptr()), None,
+                                              C.c_void_p(c.data_ptr()), None, None))
+        torch.cuda.synchronize()
+        assert bool((f[2] == c).all())
+        assert float((f[0] - s).abs().max()) <= 1e-5 * float(s.abs().max())
+
+
 def test_mis_scene_without_environment_is_the_reference(gpu, scenes):
     sc = scenes.scene_c1(16, 16, 1)
     a, _ = _render(gpu, sc, 64, 3, gpu.ESTIMATOR_MIS)
