@@ -19,6 +19,7 @@
 // (ballot + popc); the tracing kernels are persistent and fetch 32 rays per
 // warp from an atomic work counter.  Random numbers are Philox4x32-10 keyed by
 // (pixel, sample, vertex) so any partition of the work gives the same image.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -64,6 +65,17 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want)
     if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
     base = __shfl_sync(0xFFFFFFFFu, base, leader);
     return base + __popc(m & ((1u << lane) - 1u));
+}
+
+// Opportunistic warp aggregation (for appends inside divergent code): the
+// threads of a warp that arrive together take consecutive slots with one atomic.
+__device__ __forceinline__ uint32_t coalesced_append(uint32_t* counter)
+{
+    namespace cg = cooperative_groups;
+    const cg::coalesced_group g = cg::coalesced_threads();
+    uint32_t base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(counter, (uint32_t)g.size());
+    return g.shfl(base, 0) + (uint32_t)g.thread_rank();
 }
 
 // Direction bin of a ray: the cube face its direction points to (dominant
@@ -419,24 +431,30 @@ static __device__ __noinline__ float env_connect(const WaveArgs& A, int b, int k
     float pdf_o = 0.0f;
     V3 unused;
     if (kind == 0 || kind == 1) pdf_o = bsdf_reflection_mix(d, O, 1.0f, unused);
-    if (b >= A.cam_bounces || b + 1 > A.max_len) return pdf_o;
-    const Rng4 r = rng4(seed, pixel, sample, kDimEnvConnect + (uint32_t)b, kStreamCamera);
-    V3 w;
-    const float pe = env_sample(S.env, r.u[0], r.u[1], r.u[2], r.u[3], w);
-    if (!(pe > 0.0f)) return pdf_o;
-    V3 feff;
-    const float pb = bsdf_reflection_mix(d, w, fabsf(dot(w, nrm)), feff);
-    if (!(pb > 0.0f)) return pdf_o;
-    const V3 L = env_radiance(S.env, w);
-    const float m = pe / (pe * pe + pb * pb);  // power heuristic pe^2 / (pe^2 + pb^2), over pe
-    const V3 c = v3(tp.x * feff.x * L.x * m, tp.y * feff.y * L.y * m, tp.z * feff.z * L.z * m);
-    if (!(c.x > 0.0f || c.y > 0.0f || c.z > 0.0f)) return pdf_o;
-    const uint32_t sl = atomicAdd(&A.R.ctr[kCtrEnv + b], 1u);
-    float4* q = A.env_q + 3 * (size_t)sl;
-    const V3 so = shifted_origin(pos, w, 1.0f);
-    q[0] = make_float4(so.x, so.y, so.z, __int_as_float(k));
-    q[1] = make_float4(w.x, w.y, w.z, tnear);
-    q[2] = make_float4(c.x, c.y, c.z, 0.0f);
+    bool push = false;
+    V3 w = v3(0.0f, 0.0f, 1.0f), c = v3(0.0f, 0.0f, 0.0f);
+    if (b < A.cam_bounces && b + 1 <= A.max_len) {
+        const Rng4 r = rng4(seed, pixel, sample, kDimEnvConnect + (uint32_t)b, kStreamCamera);
+        const float pe = env_sample(S.env, r.u[0], r.u[1], r.u[2], r.u[3], w);
+        if (pe > 0.0f) {
+            V3 feff;
+            const float pb = bsdf_reflection_mix(d, w, fabsf(dot(w, nrm)), feff);
+            if (pb > 0.0f) {
+                const V3 L = env_radiance(S.env, w);
+                const float m = pe / (pe * pe + pb * pb);  // power heuristic pe^2 / (pe^2 + pb^2), over pe
+                c = v3(tp.x * feff.x * L.x * m, tp.y * feff.y * L.y * m, tp.z * feff.z * L.z * m);
+                push = c.x > 0.0f || c.y > 0.0f || c.z > 0.0f;
+            }
+        }
+    }
+    if (push) {  // the lanes of a warp that connect take consecutive slots: coherent environment rays
+        const uint32_t sl = coalesced_append(&A.R.ctr[kCtrEnv + b]);
+        float4* q = A.env_q + 3 * (size_t)sl;
+        const V3 so = shifted_origin(pos, w, 1.0f);
+        q[0] = make_float4(so.x, so.y, so.z, __int_as_float(k));
+        q[1] = make_float4(w.x, w.y, w.z, tnear);
+        q[2] = make_float4(c.x, c.y, c.z, 0.0f);
+    }
     return pdf_o;
 }
 
@@ -539,7 +557,7 @@ __global__ void __launch_bounds__(kShadeThreads, kMis ? 3 : 4) k_camera_shade(Wa
                         V3 f = material_eval(M, P, sp, LC, outV) * c;
                         lc = v3(f.x * tp.x * lRad.x, f.y * tp.y * lRad.y, f.z * tp.z * lRad.z);
                         if (intensity(lc) < A.cut) continue;
-                        const uint32_t sl = atomicAdd(&A.R.ctr[kCtrShadow + b], 1u);
+                        const uint32_t sl = coalesced_append(&A.R.ctr[kCtrShadow + b]);
                         float4* q = A.R.sq + 3 * (size_t)sl;
                         q[0] = make_float4(lPos.x, lPos.y, lPos.z, __int_as_float(k));
                         q[1] = make_float4(sp.pos.x, sp.pos.y, sp.pos.z, 0.0f);
