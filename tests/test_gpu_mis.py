@@ -100,6 +100,24 @@ def test_mis_with_point_light_matches_the_reference_estimator(gpu, scenes):
     assert abs(glob) < 4, glob
 
 
+def test_mis_with_alpha_masked_textures_matches_the_reference_estimator(gpu, scenes):
+    """Texture-masked and alpha-masked materials under a sky: environment rays
+    then take sceneIntersect's closest hit with masked-material retries, as
+    the sampled rays do; textured PBR vertices connect with their texel values."""
+    import math
+
+    sc = scenes.scene_textured(32, 32, 1)
+    R = np.array([[1, 0, 0], [0, 0, 1], [0, -1, 0]], dtype=np.float32)
+    sky = scenes.make_sky(256, 128, np.random.default_rng(3), suns=False)
+    sc = dataclasses.replace(sc, hdri=scenes.Hdri(sky, R, float(np.float32(math.pi))))
+    n = 8192
+    m_mis, v_mis = _render(gpu, sc, n, 5, gpu.ESTIMATOR_MIS)
+    m_ref, v_ref = _render(gpu, sc, n, 6, gpu.ESTIMATOR_REFERENCE)
+    frac3, glob = _zstats(m_mis, n, v_mis, m_ref, n, v_ref)
+    assert frac3 < 0.01, frac3
+    assert abs(glob) < 4, glob
+
+
 def test_mis_batch_matches_separate_renders(gpu, scenes):
     """A batch under the MIS estimator, captured as a graph on its first call
     (the environment table is built before the capture), gives each job the
