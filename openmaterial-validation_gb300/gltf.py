@@ -27,6 +27,7 @@ from __future__ import annotations
 import base64
 import dataclasses
 import json
+import math
 import os
 import struct
 import zlib
@@ -650,6 +651,18 @@ def _transformation_inverse(M: np.ndarray) -> np.ndarray:
         out[i, 3] = F32(-acc)
     out[3, 3] = F32(1.0)
     return out
+
+
+# backgrounds are z-up and glTF scenes y-up: the rotation main.cpp:400-404 gives
+# every HDR background (applied as dir * R, HdrBackground.cpp:58)
+HDRI_Y_UP = np.array([[1.0, 0.0, 0.0], [0.0, 0.0, 1.0], [0.0, -1.0, 0.0]], dtype=F32)
+
+
+def load_hdri(path: str, scale: float = float(F32(math.pi))) -> scenes.Hdri:
+    """The -H background as main.cpp:397-406 sets it up: the Radiance file
+    decoded as stb_image decodes it (scenes.decode_hdr), the y-up rotation and
+    the radiance scale (RendererParameters::hdrScaleValue, pi)."""
+    return scenes.Hdri(scenes.read_hdr(path), HDRI_Y_UP.copy(), float(F32(scale)))
 
 
 def load_gltf(path: str, use_lights: bool = False, priority: str = "om",

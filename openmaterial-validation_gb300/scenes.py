@@ -38,6 +38,7 @@ import functools
 import json
 import math
 import os
+import re
 import struct
 from typing import List, Optional
 
@@ -696,28 +697,156 @@ def rgbe_quantize(rgb: np.ndarray) -> np.ndarray:
     return rgbe_decode(rgbe_encode(rgb))
 
 
-def write_hdr(path: str, rgb: np.ndarray) -> None:
-    """Flat (uncompressed) RGBE scanlines; the first pixel never starts with
-    the run-length marker bytes 2,2."""
+def _rle_channel(vals: np.ndarray) -> bytes:
+    """One channel of a new-style RLE scanline: runs of 3..127 equal bytes as
+    (128 + n, value), everything else as literal dumps of at most 128 bytes."""
+    out = bytearray()
+    n, i = len(vals), 0
+    lit = []
+    while i < n:
+        r = 1
+        while i + r < n and r < 127 and vals[i + r] == vals[i]:
+            r += 1
+        if r >= 3:
+            while lit:
+                out.append(min(len(lit), 128))
+                out.extend(lit[:128])
+                lit = lit[128:]
+            out += bytes((128 + r, int(vals[i])))
+            i += r
+        else:
+            lit.append(int(vals[i]))
+            i += 1
+    while lit:
+        out.append(min(len(lit), 128))
+        out.extend(lit[:128])
+        lit = lit[128:]
+    return bytes(out)
+
+
+def write_hdr(path: str, rgb: np.ndarray, rle: bool = False) -> None:
+    """Radiance .hdr: flat RGBE scanlines, or (rle, widths 8..32767) new-style
+    run-length scanlines as Radiance writes them.  A flat file's first pixel
+    must not start with the RLE marker bytes 2, 2."""
     h, w, _ = rgb.shape
     data = rgbe_encode(rgb)
-    if data[0, 0, 0] == 2 and data[0, 0, 1] == 2:
-        raise ValueError("first pixel would read as an RLE marker")
     with open(path, "wb") as fh:
         fh.write(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n")
         fh.write(f"-Y {h} +X {w}\n".encode())
-        fh.write(data.tobytes())
+        if rle:
+            if not 8 <= w < 32768:
+                raise ValueError("run-length scanlines need 8 <= width < 32768")
+            for j in range(h):
+                fh.write(bytes((2, 2, w >> 8, w & 255)))
+                for k in range(4):
+                    fh.write(_rle_channel(data[j, :, k]))
+        else:
+            if data[0, 0, 0] == 2 and data[0, 0, 1] == 2:
+                raise ValueError("first pixel would read as an RLE marker")
+            fh.write(data.tobytes())
+
+
+def decode_hdr(raw: bytes) -> np.ndarray:
+    """A Radiance .hdr file as the reference loads it (stbi_loadf with 0
+    requested channels, HdrBackground.cpp:42, through stb_image's HDR loader):
+    signature #?RADIANCE or #?RGBE, header lines up to an empty one (one must
+    be FORMAT=32-bit_rle_rgbe), then "-Y H +X W".  Widths 8..32767 read
+    new-style run-length scanlines; a scanline that does not start with
+    (2, 2, length < 32768) makes stb decode the whole image again as flat
+    pixels from there (that scanline's 4 bytes become pixel 0).  Other widths
+    are flat.  A file that ends inside the pixel data raises ValueError (stb
+    then repeats whatever its 4-byte read buffer last held).
+    Returns (H, W, 3) float32: byte * 2^(e - 136), zero when e == 0."""
+    n = len(raw)
+    pos = 0
+
+    def get8():
+        nonlocal pos
+        if pos >= n:
+            raise ValueError("truncated HDR pixel data")
+        pos += 1
+        return raw[pos - 1]
+
+    def token():
+        nonlocal pos
+        end = raw.find(b"\n", pos)
+        end = n if end < 0 else end
+        t = raw[pos:end][:1023]
+        pos = min(end + 1, n)
+        return t.decode("latin-1")
+
+    if token() not in ("#?RADIANCE", "#?RGBE"):
+        raise ValueError("not a Radiance HDR file")
+    valid = False
+    while True:
+        t = token()
+        if not t:
+            break
+        valid = valid or t == "FORMAT=32-bit_rle_rgbe"
+    if not valid:
+        raise ValueError("unsupported HDR format")
+    def strtol(x):  # C strtol: leading white space, sign, digits; (0, x) when none
+        m = re.match(r"[ \t\n\v\f\r]*([+-]?[0-9]+)", x)
+        return (int(m.group(1)), x[m.end():]) if m else (0, x)
+
+    t = token()
+    if not t.startswith("-Y "):
+        raise ValueError("unsupported HDR data layout")
+    height, rest = strtol(t[3:])
+    rest = rest.lstrip(" ")
+    if not rest.startswith("+X "):
+        raise ValueError("unsupported HDR data layout")
+    width, _ = strtol(rest[3:])
+    if width <= 0 or height <= 0:
+        raise ValueError("bad HDR size")
+    total = width * height
+    px = np.zeros((total, 4), dtype=np.uint8)
+
+    def flat(first: int) -> None:
+        nonlocal pos
+        need = 4 * (total - first)
+        if pos + need > n:
+            raise ValueError("truncated HDR pixel data")
+        px[first:] = np.frombuffer(raw[pos:pos + need], dtype=np.uint8).reshape(-1, 4)
+        pos += need
+
+    if width < 8 or width >= 32768:
+        flat(0)
+    else:
+        line = np.zeros((width, 4), dtype=np.uint8)
+        for j in range(height):
+            c1, c2, ln = get8(), get8(), get8()
+            if c1 != 2 or c2 != 2 or (ln & 0x80):
+                px[0] = (c1, c2, ln, get8())
+                flat(1)
+                break
+            ln = (ln << 8) | get8()
+            if ln != width:
+                raise ValueError("invalid decoded scanline length")
+            for k in range(4):
+                i = 0
+                while i < width:
+                    count = get8()
+                    if count > 128:
+                        count -= 128
+                        if count > width - i:
+                            raise ValueError("bad RLE data in HDR")
+                        line[i:i + count, k] = get8()
+                    else:
+                        if count > width - i:
+                            raise ValueError("bad RLE data in HDR")
+                        if pos + count > n:
+                            raise ValueError("truncated HDR pixel data")
+                        line[i:i + count, k] = np.frombuffer(raw[pos:pos + count], dtype=np.uint8)
+                        pos += count
+                    i += count
+            px[j * width:(j + 1) * width] = line
+    return rgbe_decode(px.reshape(height, width, 4))
 
 
 def read_hdr(path: str) -> np.ndarray:
     with open(path, "rb") as fh:
-        raw = fh.read()
-    end = raw.index(b"\n\n") + 2
-    line_end = raw.index(b"\n", end)
-    parts = raw[end:line_end].split()
-    h, w = int(parts[1]), int(parts[3])
-    data = np.frombuffer(raw[line_end + 1:line_end + 1 + 4 * w * h], dtype=np.uint8).reshape(h, w, 4)
-    return rgbe_decode(data)
+        return decode_hdr(fh.read())
 
 
 # -------------------------------------------------------------- glTF writer --

@@ -24,6 +24,8 @@
  *       out: W*H*4 bytes
  *   golden_harness png     in out        stb_image as tinygltf loads images (4 channels; 16-bit
  *       files through stbi_load_16), out: int32 W H then W*H*4 uint16 samples
+ *   golden_harness hdr     in out        stbi_loadf(in, 0 channels) as HDRBackground loads a .hdr
+ *       (HdrBackground.cpp:42), out: int32 W H channels then W*H*channels floats
  *   golden_harness texture W H img uv out BitmapTexture::texture(u, v, fvec4) (BitmapTexture.cpp:108-125)
  *       img: W*H*4 bytes; uv: 2 floats/case; out: 4 floats/case
  */
@@ -198,6 +200,18 @@ int main(int argc, char** argv)
         std::fwrite(wh, sizeof(int32_t), 2, f);
         std::fwrite(px.data(), sizeof(uint16_t), px.size(), f);
         std::fclose(f);
+        return 0;
+    } else if (mode == "hdr" && argc == 4) {
+        int w = 0, h = 0, c = 0;
+        float* d = stbi_loadf(argv[2], &w, &h, &c, 0);
+        if (!d) return 2;
+        FILE* f = std::fopen(argv[3], "wb");
+        if (!f) return 2;
+        const int32_t whc[3] = {w, h, c};
+        std::fwrite(whc, sizeof(int32_t), 3, f);
+        std::fwrite(d, sizeof(float), (size_t)w * h * 3, f);
+        std::fclose(f);
+        stbi_image_free(d);
         return 0;
     } else if (mode == "texture" && argc == 7) {
         const int W = std::atoi(argv[2]), H = std::atoi(argv[3]);

@@ -425,6 +425,47 @@ def gen_png(tmp):
     np.savez_compressed(os.path.join(HERE, "png.npz"), **out)
 
 
+def gen_hdr(tmp):
+    """Radiance files in every form stb_image's HDR loader takes (flat and
+    run-length scanlines, both signatures, extra header lines, widths at the
+    RLE limits, the mid-file fallback to flat pixels, zero exponents)."""
+    rng = np.random.default_rng(23)
+
+    def sky(h, w):
+        img = np.exp(rng.normal(size=(h, w, 3))).astype(np.float32)
+        img[:, w // 4:w // 2] = img[:, w // 4:w // 4 + 1]  # runs
+        img[0, 0] = (2.0, 1.0, 0.5)                          # not an RLE marker as a flat first pixel
+        return img
+
+    def hdr_bytes(img, rle, head=b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n"):
+        p = os.path.join(tmp, "w.hdr")
+        S.write_hdr(p, img, rle=rle)
+        raw = open(p, "rb").read()
+        return head + raw[raw.index(b"\n\n") + 2:]
+
+    files = [hdr_bytes(sky(3, 5), False), hdr_bytes(sky(7, 40), True), hdr_bytes(sky(2, 8), True),
+             hdr_bytes(sky(3, 300), True,
+                       b"#?RGBE\n# written by a test\nEXPOSURE=1.0\nFORMAT=32-bit_rle_rgbe\nGAMMA=1\n\n"),
+             hdr_bytes(sky(4, 16), False)]
+    a = hdr_bytes(sky(5, 12), True)
+    z = S.rgbe_encode(sky(5, 12)).tobytes()
+    files.append(a[:a.index(b"\x02\x02\x00\x0c", a.index(b"\x02\x02\x00\x0c") + 1)] + z[:4 * 60])
+    dark = sky(2, 9)
+    dark[1, 3] = 0.0
+    files.append(hdr_bytes(dark, True))
+    out = {}
+    for i, raw in enumerate(files):
+        p = os.path.join(tmp, f"h{i}.hdr")
+        open(p, "wb").write(raw)
+        o = os.path.join(tmp, f"h{i}.out")
+        harness("hdr", p, o)
+        whc = np.fromfile(o, dtype=np.int32, count=3)
+        out[f"file{i}"] = np.frombuffer(raw, dtype=np.uint8)
+        out[f"rgb{i}"] = np.fromfile(o, dtype=np.float32, offset=12).reshape(whc[1], whc[0], 3)
+    out["count"] = len(files)
+    np.savez_compressed(os.path.join(HERE, "hdr.npz"), **out)
+
+
 ASSETS = ["objects/" + n for n in (
     "cone_gold", "cube_aluminium", "cube_gold", "cube_pbr_gold", "cubes_pbr", "icospheres_gold_iron_aluminium",
     "icospheres_gold_iron_missing", "monkey_gold", "plane_pointlight", "sphere_aluminium", "sphere_gold",
@@ -513,7 +554,7 @@ def gen_lightbox(tmp):
 
 GENS = {"mt": gen_mt, "brdf": gen_brdf, "om": gen_om, "ior": gen_ior, "env": gen_env, "camera": gen_camera,
         "films": gen_films, "ids": gen_ids, "post": gen_post, "fc": gen_fc, "lightbox": gen_lightbox,
-        "textured": gen_textured, "texture": gen_texture, "png": gen_png, "assets": gen_assets}
+        "textured": gen_textured, "texture": gen_texture, "png": gen_png, "hdr": gen_hdr, "assets": gen_assets}
 
 
 def main():
