@@ -535,6 +535,14 @@ omv_status omv_env_radiance(omv_scene* scene, int64_t n, const float* dirs, floa
 const char* omv_last_error(void);
 const char* omv_version(void);
 
+/* Optional log callback: every failing call also reports its status and
+ * message to `fn` (on the failing call's thread), as the reference collects
+ * Embree's error callback messages in RenderScene::getRunErrors
+ * (RenderScene.cpp:14-18).  Process-wide; NULL removes it.  Set it before
+ * other threads call into the library. */
+typedef void (*omv_log_fn)(void* user, omv_status status, const char* message);
+omv_status omv_set_log_callback(omv_log_fn fn, void* user);
+
 /* sizeof of the public structs in this order: omv_mesh_desc, omv_instance_desc,
  * omv_material_desc, omv_light_desc, omv_hdri_desc, omv_scene_desc,
  * omv_scene_info, omv_camera, omv_params, omv_stats, omv_hit, omv_job,

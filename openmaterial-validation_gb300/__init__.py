@@ -150,8 +150,24 @@ def lib():
               "omv_develop", "omv_tonemap", "omv_denoise_median", "omv_rgba8", "omv_save_image",
               "omv_render_fc", "omv_scene_bounds", "omv_lightbox_cameras", "omv_texture_sample"):
         getattr(L, n).restype = st
+    L.omv_set_log_callback.argtypes = [LogCallback, C.c_void_p]
+    L.omv_set_log_callback.restype = st
     _lib = L
     return L
+
+
+# omv_log_fn: (user, status, message)
+LogCallback = C.CFUNCTYPE(None, C.c_void_p, C.c_int32, C.c_char_p)
+_log_keep = None
+
+
+def set_log_callback(fn) -> None:
+    """fn(status, message) is called for every failing library call (None
+    removes it): omv_set_log_callback."""
+    global _log_keep
+    cb = LogCallback(lambda _user, status, msg: fn(int(status), msg.decode(errors="replace"))) if fn else None
+    check(lib().omv_set_log_callback(cb if cb is not None else LogCallback(), None))
+    _log_keep = cb
 
 
 def check(status: int) -> None:

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -32,10 +33,13 @@ struct omv_scene {
 namespace {
 
 thread_local std::string g_last_error;
+std::atomic<omv_log_fn> g_log_fn{nullptr};
+std::atomic<void*> g_log_user{nullptr};
 
 omv_status fail(omv_status code, const char* msg)
 {
     g_last_error = msg ? msg : "unknown error";
+    if (const omv_log_fn fn = g_log_fn.load()) fn(g_log_user.load(), code, g_last_error.c_str());
     return code;
 }
 
@@ -117,6 +121,13 @@ void omv_params_default(omv_params* p)
 }
 
 const char* omv_last_error(void) { return g_last_error.c_str(); }
+
+omv_status omv_set_log_callback(omv_log_fn fn, void* user)
+{
+    g_log_user.store(user);
+    g_log_fn.store(fn);
+    return OMV_OK;
+}
 
 const char* omv_version(void) { return "omv-gb300 0.1 (sm_103a)"; }
 

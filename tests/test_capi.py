@@ -66,3 +66,19 @@ def test_no_device_is_reported_not_crashed(omv):
     x = np.zeros((1, 17), np.float32)
     st = omv.lib().omv_brdf_eval_direct(1, omv.capi.fptr(x), omv.capi.fptr(out))
     assert st != 0
+
+
+def test_log_callback_sees_every_failure(omv):
+    seen = []
+    omv.set_log_callback(lambda status, msg: seen.append((status, msg)))
+    try:
+        L = omv.lib()
+        assert L.omv_render(None, None, None, None, None, None, None, None) == 1
+        assert L.omv_trace_rays(None, 1, None, None) == 1
+        assert L.omv_scene_destroy(None) == 0  # success: not reported
+    finally:
+        omv.set_log_callback(None)
+    assert [s for s, _ in seen] == [1, 1]
+    assert all(m for _, m in seen)
+    L.omv_render(None, None, None, None, None, None, None, None)
+    assert len(seen) == 2  # removed
