@@ -142,6 +142,24 @@ def test_large_scene_frame_properties(gpu, scenes):
     assert img[..., :3].mean() > 0
 
 
+def test_benchmark_frame_partition_invariance(gpu, scenes):
+    """The benchmark frame at full size (1920x1080, 64 spp, 1,048,576 triangles
+    in 64 instances, 132.7M paths): one wave, waves of 30,000,001 paths (wave
+    boundaries inside pixels) and two calls of 32 samples (sample_offset) give
+    the same film up to FP64 summation order, every pixel with 64 samples."""
+    sc = scenes.scene_c2(1920, 1080, 64)
+    _, a, _, ca, st = _render(gpu, sc, 64, seed=5, variance=False)
+    _, b, _, cb, _ = _render(gpu, sc, 64, seed=5, variance=False, wave_paths=30_000_001)
+    _, c1, _, cc1, _ = _render(gpu, sc, 32, seed=5, variance=False)
+    _, c2, _, cc2, _ = _render(gpu, sc, 32, seed=5, variance=False, sample_offset=32)
+    assert st["paths"] == 1920 * 1080 * 64
+    assert (ca == 64).all() and (cb == 64).all() and ((cc1 + cc2) == 64).all()
+    assert np.isfinite(a).all() and (a >= 0).all()
+    scale = np.abs(a).max()
+    assert np.abs(a - b).max() <= 1e-9 * scale
+    assert np.abs(a - (c1 + c2)).max() <= 1e-9 * scale
+
+
 @pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(__file__), "golden", "film_c1_256x4096.npz")),
                     reason="4096-spp reference film not generated")
 def test_c1_full_resolution_4096spp_rel_rmse(gpu, scenes):
