@@ -111,6 +111,28 @@ def _dist():
     return ws, rank, local
 
 
+def rank_sample_offset(rank: int, spp: int) -> int:
+    """Replicas: rank r renders samples [r spp, (r + 1) spp) of every pixel, so
+    the ranks' films are disjoint sample ranges of one image (no collective)."""
+    return rank * spp
+
+
+def max_over_ranks(x: float, dist, device) -> float:
+    """The slowest rank's time (the job's time): MAX all-reduce, or x alone."""
+    import torch
+
+    if dist is None:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(paths_per_rank: int, ws: int, seconds: float) -> float:
+    """Mpaths/s of the whole job: the paths of all ranks over the slowest rank's time."""
+    return paths_per_rank * ws / seconds / 1e6
+
+
 def cpu_reference(oracle, scene, spp: int, target_s: float, seed: int = 7, threads: int = None):
     """Times the oracle port (all host threads) on a centred band of rows sized to
     about target_s seconds.  Returns (Mpaths/s, Mrays/s, cores, rows, seconds)."""
@@ -478,7 +500,7 @@ def run_ours(args, scene, ws, rank, local):
     npix = W * H
     cam = capi.camera_struct(scene.camera)
     params = capi.params_for(scene, spp=spp, seed=1234)
-    params.sample_offset = rank * spp
+    params.sample_offset = rank_sample_offset(rank, spp)
     params.time_kernels = 1
     dev = torch.device("cuda", local)
     film = torch.zeros(3 * npix, dtype=torch.float64, device=dev)
@@ -522,13 +544,9 @@ def run_ours(args, scene, ws, rank, local):
         dist.barrier()
     clock = clocks.stop()
     dev_ms = sum(a.elapsed_time(b) for a, b in evs)
-    t = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    max_ms = float(t.item())
+    max_ms = max_over_ranks(dev_ms, dist, dev)
     cnt_ok = bool((count == spp).all().item())
-    paths = npix * spp * args.steps * ws
-    value = paths / (max_ms / 1e3) / 1e6
+    value = whole_job_rate(npix * spp * args.steps, ws, max_ms / 1e3)
     rays = (agg["extension_rays"] + agg["shadow_rays"] + agg["light_rays"]) * ws
     # roofline of the closest-hit kernel: algorithmic bytes = nodes x 128 B + triangles x 48 B
     hbm, peak_kind = _peaks()
@@ -545,7 +563,7 @@ def run_ours(args, scene, ws, rank, local):
     if rank == 0 or ws > 1:
         img = torch.empty((H, W, 4), dtype=torch.float32, pin_memory=True).numpy()
         p2 = capi.params_for(scene, spp=spp, seed=99)
-        p2.sample_offset = rank * spp
+        p2.sample_offset = rank_sample_offset(rank, spp)
         for _ in range(args.warmup):
             omv.check(L.omv_render(rs.handle, C.byref(cam), C.byref(p2), capi.fptr(img), None, None, None, None))
         times = []
@@ -553,10 +571,8 @@ def run_ours(args, scene, ws, rank, local):
             t0 = time.perf_counter()
             omv.check(L.omv_render(rs.handle, C.byref(cam), C.byref(p2), capi.fptr(img), None, None, None, None))
             times.append(time.perf_counter() - t0)
-        e2e_t = torch.tensor([sum(times)], dtype=torch.float64, device=dev)
-        if dist:
-            dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
-        e2e = {"value": round(npix * spp * args.steps * ws / float(e2e_t.item()) / 1e6, 4), "unit": "Mpaths/s",
+        e2e_s = max_over_ranks(sum(times), dist, dev)
+        e2e = {"value": round(whole_job_rate(npix * spp * args.steps, ws, e2e_s), 4), "unit": "Mpaths/s",
                "h2d_bytes_per_step": C.sizeof(capi.Camera) + C.sizeof(capi.Params),
                "d2h_bytes_per_step": int(img.nbytes)}
     cpu = None
