@@ -19,14 +19,14 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <stdexcept>
 #include <string>
-#include <vector>
-#include <atomic>
 #include <thread>
+#include <vector>
 
 #include "bvh_build.h"
 #include "omv_types.h"
@@ -73,15 +73,25 @@ __global__ void k_tri_boxes(int n, const float* __restrict__ pos, const uint32_t
             b.lo[a] = 3.0e38f;
             b.hi[a] = -3.0e38f;
         }
+        bool finite = true;
         for (int k = 0; k < 3; ++k) {
             const float* p = pos + 3 * (size_t)faces[3 * (size_t)i + k];
             for (int a = 0; a < 3; ++a) {
+                finite = finite && isfinite(p[a]);
                 b.lo[a] = fminf(b.lo[a], p[a]);
                 b.hi[a] = fmaxf(b.hi[a], p[a]);
             }
         }
+        // a triangle with a NaN or infinite coordinate can never be hit; it gets
+        // an empty box (never entered, no effect on any bound), as an Embree
+        // robust build leaves invalid primitives out
+        if (!finite)
+            for (int a = 0; a < 3; ++a) {
+                b.lo[a] = 3.0e38f;
+                b.hi[a] = -3.0e38f;
+            }
         boxes[i] = b;
-        for (int a = 0; a < 3; ++a) c[a] = 0.5f * (b.lo[a] + b.hi[a]);
+        for (int a = 0; a < 3; ++a) c[a] = finite ? 0.5f * (b.lo[a] + b.hi[a]) : 0.0f;
     }
     for (int a = 0; a < 3; ++a) {
         uint32_t lo = ok ? f2ord(c[a]) : 0xFFFFFFFFu, hi = ok ? f2ord(c[a]) : 0u;
@@ -96,7 +106,7 @@ __global__ void k_tri_boxes(int n, const float* __restrict__ pos, const uint32_t
     }
 }
 
-// World bounds of one instance: every vertex its faces reference, through the
+// World bounds of one instance: every vertex its finite faces reference, through the
 // instance transform (double arithmetic, rounded to float), reduced into six
 // ordered ints (lo xyz, hi xyz).  Tighter than the box of the transformed
 // object box, which a rotation inflates.
@@ -107,13 +117,22 @@ __global__ void k_instance_bounds(int nfaces, const float* __restrict__ pos, con
                                   Xf34 xf, uint32_t* out6)
 {
     float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * nfaces; i += gridDim.x * blockDim.x) {
-        const float* p = pos + 3 * (size_t)faces[i];
-        for (int a = 0; a < 3; ++a) {
-            const double w = (double)xf.m[4 * a] * p[0] + (double)xf.m[4 * a + 1] * p[1] +
-                             (double)xf.m[4 * a + 2] * p[2] + (double)xf.m[4 * a + 3];
-            lo[a] = fminf(lo[a], (float)w);
-            hi[a] = fmaxf(hi[a], (float)w);
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nfaces; f += gridDim.x * blockDim.x) {
+        const float* v[3];
+        bool finite = true;
+        for (int k = 0; k < 3; ++k) {
+            v[k] = pos + 3 * (size_t)faces[3 * (size_t)f + k];
+            finite = finite && isfinite(v[k][0]) && isfinite(v[k][1]) && isfinite(v[k][2]);
+        }
+        if (!finite) continue;  // left out of the tree (k_tri_boxes)
+        for (int k = 0; k < 3; ++k) {
+            const float* p = v[k];
+            for (int a = 0; a < 3; ++a) {
+                const double w = (double)xf.m[4 * a] * p[0] + (double)xf.m[4 * a + 1] * p[1] +
+                                 (double)xf.m[4 * a + 2] * p[2] + (double)xf.m[4 * a + 3];
+                lo[a] = fminf(lo[a], (float)w);
+                hi[a] = fmaxf(hi[a], (float)w);
+            }
         }
     }
     for (int a = 0; a < 3; ++a) {
@@ -841,6 +860,12 @@ void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<Instance
                         b.lo[a] = 3.0e38f;
                         b.hi[a] = -3.0e38f;
                     }
+                    bool finite = true;
+                    for (int k = 0; k < 3; ++k) {
+                        const float* p = m.h_pos + 3 * (size_t)m.h_faces[3 * (size_t)f + k];
+                        for (int a = 0; a < 3; ++a) finite = finite && std::isfinite(p[a]);
+                    }
+                    if (!finite) continue;  // empty box: left out of the tree, as in k_tri_boxes
                     for (int k = 0; k < 3; ++k) {
                         const float* p = m.h_pos + 3 * (size_t)m.h_faces[3 * (size_t)f + k];
                         for (int a = 0; a < 3; ++a) {

@@ -135,3 +135,47 @@ def test_alpha_masked_material_is_skipped_like_reference(gpu, oracle, scenes):
     ok, msg = _hits_equal(a, b)
     assert ok, msg
     assert not np.any(a["material"] == 3)
+
+
+def test_non_finite_triangles_change_no_hit(gpu, scenes):
+    """Triangles with NaN or infinite vertices (appended to a mesh, so every
+    valid triangle keeps its id) are never hit and change no other hit, as an
+    Embree robust build ignores invalid primitives: the closest-hit query on
+    random rays and the camera ID pass are bit-identical with and without them,
+    and the frame renders finite."""
+    import dataclasses
+
+    sc = scenes.scene_c1(64, 64, 1)
+    m = sc.meshes[0]
+    rng = np.random.default_rng(12)
+    bad_v, bad_f = [], []
+    nv = len(m.positions)
+    for k, val in enumerate((np.nan, np.inf, -np.inf, np.nan, np.inf)):
+        tri = m.positions[m.faces[rng.integers(len(m.faces))]].astype(np.float32).copy()
+        if k == 3:
+            tri[:, :] = np.nan                           # all three vertices
+        else:
+            tri[k % 3, k % 3] = val                      # one coordinate
+        bad_v.append(tri)
+        bad_f.append(nv + 3 * k + np.arange(3))
+    pos = np.concatenate([m.positions.astype(np.float32)] + bad_v)
+    faces = np.concatenate([m.faces.astype(np.uint32), np.array(bad_f, np.uint32)])
+    normals = None if m.normals is None else np.concatenate([m.normals, np.tile(m.normals[:1], (len(bad_v) * 3, 1))])
+    sc_bad = dataclasses.replace(sc, meshes=[dataclasses.replace(m, positions=pos, faces=faces, normals=normals)]
+                                 + list(sc.meshes[1:]))
+    a, b = gpu.RenderScene(sc), gpu.RenderScene(sc_bad)
+    rays = _random_rays(rng, 200_000, -3.0, 3.0)
+    ok, msg = _hits_equal(a.trace(rays), b.trace(rays))
+    assert ok, msg
+    ids = []
+    for rs in (a, b):
+        r = gpu.BDPTRenderer()
+        r.set_scene(rs)
+        ids.append(r.render_ids(gpu.PinholeCamera.from_spec(sc.camera), jitter=np.full(2 * 64 * 64, 0.5, np.float32))[0])
+    ok, msg = _hits_equal(ids[0], ids[1])
+    assert ok, msg
+    r = gpu.BDPTRenderer()
+    r.set_scene(b)
+    r.set_parameters(gpu.RendererParameters.for_scene(sc_bad, samplesPerPixel=16))
+    img = r.render(gpu.PinholeCamera.from_spec(sc.camera))
+    assert np.isfinite(img).all()
