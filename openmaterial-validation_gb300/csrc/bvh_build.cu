@@ -33,12 +33,17 @@
 
 namespace omv {
 
+// throws with the runtime's message ("out of memory" for a failed allocation,
+// which the C ABI reports as OMV_ERR_OUT_OF_MEMORY) and clears the runtime's
+// non-sticky error state
 #define OMV_CK(x)                                                                                 \
     do {                                                                                          \
         cudaError_t e_ = (x);                                                                     \
-        if (e_ != cudaSuccess)                                                                    \
+        if (e_ != cudaSuccess) {                                                                  \
+            (void)cudaGetLastError();                                                             \
             throw std::runtime_error(std::string("CUDA error ") + cudaGetErrorString(e_) + " at " \
                                      + __FILE__ + ":" + std::to_string(__LINE__));                \
+        }                                                                                         \
     } while (0)
 
 namespace {

@@ -52,6 +52,8 @@ omv_status guarded(F&& f)
         return OMV_OK;
     } catch (const omv::ArgError& e) {
         return fail(OMV_ERR_INVALID_ARGUMENT, e.what());
+    } catch (const omv::DeviceOutOfMemory& e) {
+        return fail(OMV_ERR_OUT_OF_MEMORY, e.what());
     } catch (const omv::CudaError& e) {
         return fail(OMV_ERR_CUDA, e.what());
     } catch (const std::bad_alloc&) {
@@ -60,6 +62,7 @@ omv_status guarded(F&& f)
         std::string m = e.what();
         if (m.find("no valid instance") != std::string::npos) return fail(OMV_ERR_EMPTY_SCENE, e.what());
         if (m.find("no CUDA device") != std::string::npos) return fail(OMV_ERR_NO_DEVICE, e.what());
+        if (m.find("out of memory") != std::string::npos) return fail(OMV_ERR_OUT_OF_MEMORY, e.what());
         return fail(OMV_ERR_INTERNAL, e.what());
     } catch (...) {
         return fail(OMV_ERR_INTERNAL, "unknown exception");

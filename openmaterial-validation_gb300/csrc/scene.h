@@ -12,17 +12,27 @@
 #include "../../include/omv.h"
 #include "omv_types.h"
 
+// A failed call throws; the runtime's non-sticky error state is cleared so
+// that the next call on the handle starts clean (an allocation that does not
+// fit is reported as out of memory and the handle stays usable).
 #define OMV_CUDA(x)                                                                               \
     do {                                                                                          \
         cudaError_t e_ = (x);                                                                     \
-        if (e_ != cudaSuccess)                                                                    \
+        if (e_ != cudaSuccess) {                                                                  \
+            (void)cudaGetLastError();                                                             \
+            if (e_ == cudaErrorMemoryAllocation)                                                  \
+                throw omv::DeviceOutOfMemory(std::string(#x) + ": " + cudaGetErrorString(e_));    \
             throw omv::CudaError(std::string(#x) + ": " + cudaGetErrorString(e_));                \
+        }                                                                                         \
     } while (0)
 
 namespace omv {
 
 struct CudaError : std::runtime_error {
     using std::runtime_error::runtime_error;
+};
+struct DeviceOutOfMemory : CudaError {
+    using CudaError::CudaError;
 };
 struct ArgError : std::runtime_error {
     using std::runtime_error::runtime_error;

@@ -179,3 +179,23 @@ def test_c1_full_resolution_4096spp_rel_rmse(gpu, scenes):
     fin = np.isfinite(ref)
     rel_rmse = np.sqrt(np.mean((mean - ref)[fin] ** 2)) / ref[fin].mean()
     assert rel_rmse < 0.01, rel_rmse
+
+
+def test_wave_that_does_not_fit_is_out_of_memory_and_the_handle_recovers(gpu, scenes):
+    """A requested wave whose path state exceeds the device memory (2e9 paths,
+    hundreds of GB) fails with OMV_ERR_OUT_OF_MEMORY before any launch; the
+    same renderer then renders normally, identical to a fresh one."""
+    sc = scenes.scene_c1(32, 32, 1)
+    rs = gpu.RenderScene(sc)
+    r = gpu.BDPTRenderer()
+    r.set_scene(rs)
+    huge = scenes.camera_default(1920, 1080)
+    r.set_parameters(gpu.RendererParameters.for_scene(sc, samplesPerPixel=1024, wave_paths=2_000_000_000))
+    with pytest.raises(gpu.OmvError) as e:
+        r.render(gpu.PinholeCamera.from_spec(huge))
+    assert "status 3" in str(e.value)
+    r.set_parameters(gpu.RendererParameters.for_scene(sc, samplesPerPixel=16, seed=4))
+    a = r.render(gpu.PinholeCamera.from_spec(sc.camera))
+    b = _render(gpu, sc, 16, seed=4, variance=False)[0]
+    assert np.isfinite(a).all()
+    assert np.abs(a - b).max() <= 1e-6 * np.abs(b).max()
