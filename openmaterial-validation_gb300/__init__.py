@@ -418,6 +418,63 @@ class BDPTRenderer:
         return hits, gp
 
 
+class ProgressiveFilm:
+    """Checkpoint / resume of a progressive render.  The whole state of a
+    render in progress is its FP64 film (sums, optional sums of squares,
+    sample counts) and the next sample index: samples are keyed by (pixel,
+    sample), so `add` continues the sequence (sample_offset) and the film
+    after 16 + 16 samples, saved and reloaded in between, is the 32-sample
+    film.  The reference has no counterpart (it renders a fixed spp)."""
+
+    def __init__(self, width: int, height: int, variance: bool = False, next_sample: int = 0) -> None:
+        self.sum = np.zeros((height, width, 3), dtype=np.float64)
+        self.sumsq = np.zeros((height, width, 3), dtype=np.float64) if variance else None
+        self.count = np.zeros((height, width), dtype=np.uint32)
+        self.next_sample = int(next_sample)
+
+    def add(self, renderer: BDPTRenderer, camera: PinholeCamera, spp: int) -> None:
+        """Renders `spp` more samples per pixel with `renderer`'s scene and
+        parameters, continuing at next_sample, and accumulates them."""
+        if (camera.height, camera.width) != self.count.shape:
+            raise ValueError("camera resolution differs from the film's")
+        keep = renderer.params
+        p = dataclasses.replace(keep, samplesPerPixel=int(spp), sample_offset=self.next_sample,
+                                accumulate_variance=self.sumsq is not None)
+        renderer.set_parameters(p)
+        try:
+            _, s, q, cnt = renderer.render(camera, sums=True)
+        finally:
+            renderer.set_parameters(keep)
+        self.sum += s
+        if self.sumsq is not None:
+            self.sumsq += q
+        self.count += cnt
+        self.next_sample += int(spp)
+
+    def image(self) -> np.ndarray:
+        """The normalised RGBA image (PinholeCamera::stop)."""
+        img = np.zeros(self.count.shape + (4,), dtype=np.float32)
+        n = np.maximum(self.count, 1)[..., None]
+        img[..., :3] = np.where(self.count[..., None] >= 1, self.sum / n, 0.0)
+        img[..., 3] = 1.0
+        return img
+
+    def save(self, path: str) -> None:
+        extra = {"sumsq": self.sumsq} if self.sumsq is not None else {}
+        np.savez(path, sum=self.sum, count=self.count, next_sample=np.int64(self.next_sample), **extra)
+
+    @classmethod
+    def load(cls, path: str) -> "ProgressiveFilm":
+        with np.load(path) as z:
+            H, W = z["count"].shape
+            f = cls(W, H, variance="sumsq" in z.files, next_sample=int(z["next_sample"]))
+            f.sum[...] = z["sum"]
+            f.count[...] = z["count"]
+            if f.sumsq is not None:
+                f.sumsq[...] = z["sumsq"]
+        return f
+
+
 # --------------------------------------------------- validation (-F / -V) --
 
 FC_SUBJECTS = ("pid", "gid", "mid", "mmp", "rmp", "md", "sg", "mn", "in")

@@ -21,6 +21,7 @@
 // (pixel, sample, vertex) so any partition of the work gives the same image.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cfloat>
@@ -66,6 +67,18 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want)
     base = __shfl_sync(0xFFFFFFFFu, base, leader);
     return base + __popc(m & ((1u << lane) - 1u));
 }
+
+// NVTX range for profilers (a wave, a stage, a bounce); free without a tool attached
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+constexpr const char* kBounceNames[] = {"bounce 0",  "bounce 1",  "bounce 2",  "bounce 3",  "bounce 4",  "bounce 5",
+                                        "bounce 6",  "bounce 7",  "bounce 8",  "bounce 9",  "bounce 10", "bounce 11",
+                                        "bounce 12", "bounce 13", "bounce 14", "bounce 15", "bounce > 15"};
+inline const char* bounce_name(int b) { return kBounceNames[b < 16 ? b : 16]; }
 
 // Opportunistic warp aggregation (for appends inside divergent code): the
 // threads of a warp that arrive together take consecutive slots with one atomic.
@@ -1038,6 +1051,7 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
         OMV_CUDA(cudaEventRecord(e0, st));
     }
     for (int64_t wb = 0; wb < total; wb += cap) {
+        const NvtxRange wave_range("omv wave");
         A.wave_base = wb;
         A.wave_n = (int32_t)std::min<int64_t>(cap, total - wb);
         if (batch) {
@@ -1056,9 +1070,11 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
             ++launches;
         }
         if (lights) {
+            const NvtxRange light_range("omv light subpaths");
             k_light_gen<<<grid_for(A.wave_n, kShadeThreads), kShadeThreads, 0, st>>>(A);
             ++launches;
             for (int b = 1; b <= p.light_bounces; ++b) {
+                const NvtxRange bounce_range(bounce_name(b));
                 float4* in = R.rq[1];
                 float4* out = R.rq[0];
                 if (b % 2 == 0) std::swap(in, out);
@@ -1071,37 +1087,42 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
                 launches += 2;
             }
         }
-        k_camera_gen<<<grid_for(A.wave_n, kShadeThreads), kShadeThreads, 0, st>>>(A);
-        ++launches;
-        for (int b = 1; b <= p.camera_bounces; ++b) {
-            float4* in = R.rq[(b + 1) % 2];
-            float4* out = R.rq[b % 2];
-            if (time_kernels) timed(ext_ev);
-            k_extend<<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, in, R.hits, R.ctr + kCtrCam + b,
-                                                           R.ctr + kCtrWork + work++, R.stats, kStatExt);
-            if (time_kernels) timed(ext_ev);
-            if (mis)
-                k_camera_shade<true><<<shade_grid, kShadeThreads, 0, st>>>(A, b, in, out);
-            else
-                k_camera_shade<false><<<shade_grid, kShadeThreads, 0, st>>>(A, b, in, out);
-            launches += 2;
-            if (lights) {
-                if (time_kernels) timed(sh_ev);
-                k_shadow<false><<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, R.sq, R.ctr + kCtrShadow + b,
-                                                                      R.ctr + kCtrWork + work++, R.rad, R.stats, 0);
-                if (time_kernels) timed(sh_ev);
-                ++launches;
-            }
-            if (mis) {
-                if (time_kernels) timed(sh_ev);
-                k_shadow<true><<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, A.env_q, R.ctr + kCtrEnv + b,
-                                                                     R.ctr + kCtrWork + work++, R.rad, R.stats,
-                                                                     masked ? 1 : 0);
-                if (time_kernels) timed(sh_ev);
-                ++launches;
+        {
+            const NvtxRange camera_range("omv camera subpaths");
+            k_camera_gen<<<grid_for(A.wave_n, kShadeThreads), kShadeThreads, 0, st>>>(A);
+            ++launches;
+            for (int b = 1; b <= p.camera_bounces; ++b) {
+                const NvtxRange bounce_range(bounce_name(b));
+                float4* in = R.rq[(b + 1) % 2];
+                float4* out = R.rq[b % 2];
+                if (time_kernels) timed(ext_ev);
+                k_extend<<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, in, R.hits, R.ctr + kCtrCam + b,
+                                                               R.ctr + kCtrWork + work++, R.stats, kStatExt);
+                if (time_kernels) timed(ext_ev);
+                if (mis)
+                    k_camera_shade<true><<<shade_grid, kShadeThreads, 0, st>>>(A, b, in, out);
+                else
+                    k_camera_shade<false><<<shade_grid, kShadeThreads, 0, st>>>(A, b, in, out);
+                launches += 2;
+                if (lights) {
+                    if (time_kernels) timed(sh_ev);
+                    k_shadow<false><<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, R.sq, R.ctr + kCtrShadow + b,
+                                                                          R.ctr + kCtrWork + work++, R.rad, R.stats, 0);
+                    if (time_kernels) timed(sh_ev);
+                    ++launches;
+                }
+                if (mis) {
+                    if (time_kernels) timed(sh_ev);
+                    k_shadow<true><<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, A.env_q, R.ctr + kCtrEnv + b,
+                                                                         R.ctr + kCtrWork + work++, R.rad, R.stats,
+                                                                         masked ? 1 : 0);
+                    if (time_kernels) timed(sh_ev);
+                    ++launches;
+                }
             }
         }
         {
+            const NvtxRange film_range("omv film");
             // about 8 samples per lane: group = power of two <= spp / 8, in [1, 32]
             const int64_t spp = batch ? batch->min_spp : p.samples_per_pixel;
             int group = 1;
