@@ -364,7 +364,7 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_extend(DevSc
 
 // ------------------------------------------------------- light shade ---
 // BDPTRenderer::computePath for the light subpath (inv = false), vertex b
-__global__ void __launch_bounds__(kShadeThreads) k_light_shade(WaveArgs A, int b, const float4* rq_in,
+__global__ void __launch_bounds__(kShadeThreads, 4) k_light_shade(WaveArgs A, int b, const float4* rq_in,
                                                                 float4* rq_out)
 {
     const uint32_t n = A.R.ctr[kCtrLight + b];
