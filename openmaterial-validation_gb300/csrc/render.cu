@@ -594,16 +594,18 @@ __global__ void __launch_bounds__(kShadeThreads, kMis ? 3 : 4) k_camera_shade(Wa
 
 // ------------------------------------------------------------ shadow ---
 // kEnv = false: BDPTRenderer::isConnected (BDPTRenderer.cpp:208-235) for the
-// vertex connections (records: end points A, B and the contribution).
+// vertex connections (records: end points A, B and the contribution); without
+// alpha-masked materials the closest-hit query stops at a hit well short of B,
+// which already decides "not connected".
 // kEnv = true: the MIS estimator's environment rays (records: shifted origin,
 // direction and tnear, contribution), which reach the environment when a
 // sampled ray in that direction would escape: no hit at all.  Without
 // alpha-masked materials that is an any-hit query; with them sceneIntersect's
 // closest hit and retries decide, as in k_extend (`masked` != 0).
-template <bool kEnv>
+template <bool kEnv, bool kMasked>
 __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevScene S, const uint32_t* items, const float4* sq,
                                                           const uint32_t* count, uint32_t* work, float4* rad,
-                                                          unsigned long long* stats, int masked)
+                                                          unsigned long long* stats)
 {
     __shared__ uint2 sstack[kStackShared * kTraceThreads];
     TraceStack st;
@@ -627,8 +629,8 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevSc
         if (kEnv) {
             float tn = q1.w;
             RayHit h;
-            connected = masked ? !scene_intersect(S, items, A, B, tn, kFltMax, h, st, tc)
-                               : !trace_any(S, items, A, B, tn, kFltMax, st, tc);
+            connected = kMasked ? !scene_intersect(S, items, A, B, tn, kFltMax, h, st, tc)
+                                : !trace_any(S, items, A, B, tn, kFltMax, st, tc);
         } else {
             V3 dir = B - A;
             const float len = sqrtf(dot(dir, dir));
@@ -638,12 +640,27 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevSc
                 dir = v3(dir.x / len, dir.y / len, dir.z / len);
                 float tnear = safeD;
                 const float tfar = len + (0.1f * len > safeD ? 0.1f * len : safeD);
+                const float sb = 10.0f * kEps * max_abs(B, 1.0f);
                 RayHit h;
-                if (scene_intersect(S, items, A, dir, tnear, tfar, h, st, tc)) {
+                bool hit;
+                if (kMasked) {
+                    hit = scene_intersect(S, items, A, dir, tnear, tfar, h, st, tc);
+                } else {
+                    // any hit this far short of B is farther than sb from it (the
+                    // margin is ~800 ulps of the coordinates, far above the error of
+                    // the hit's surface position), so it decides: not connected,
+                    // whichever hit is the closest.  Hits near B get the exact test.
+                    const float margin = 1.0e-4f * fmaxf(maxsz, max_abs(B, 1.0f)) + 2.0f * sb;
+                    hit = trace_closest_or_below(S, items, A, dir, tnear, tfar, len - margin, h, st, tc);
+                    if (hit && h.t < len - margin) {
+                        hit = false;
+                        connected = false;
+                    }
+                }
+                if (hit) {
                     const Surf sp = surface_point(S, h.inst, h.prim, h.u, h.v, false);
                     const V3 dd = sp.pos - B;
                     const float sd = dot(dd, dd);
-                    const float sb = 10.0f * kEps * max_abs(B, 1.0f);
                     connected = sd <= sb * sb;
                 }
             }
@@ -1106,16 +1123,23 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
                 launches += 2;
                 if (lights) {
                     if (time_kernels) timed(sh_ev);
-                    k_shadow<false><<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, R.sq, R.ctr + kCtrShadow + b,
-                                                                          R.ctr + kCtrWork + work++, R.rad, R.stats, 0);
+                    if (masked)
+                        k_shadow<false, true><<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, R.sq, R.ctr + kCtrShadow + b,
+                                                                          R.ctr + kCtrWork + work++, R.rad, R.stats);
+                    else
+                        k_shadow<false, false><<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, R.sq, R.ctr + kCtrShadow + b,
+                                                                          R.ctr + kCtrWork + work++, R.rad, R.stats);
                     if (time_kernels) timed(sh_ev);
                     ++launches;
                 }
                 if (mis) {
                     if (time_kernels) timed(sh_ev);
-                    k_shadow<true><<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, A.env_q, R.ctr + kCtrEnv + b,
-                                                                         R.ctr + kCtrWork + work++, R.rad, R.stats,
-                                                                         masked ? 1 : 0);
+                    if (masked)
+                        k_shadow<true, true><<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, A.env_q, R.ctr + kCtrEnv + b,
+                                                                         R.ctr + kCtrWork + work++, R.rad, R.stats);
+                    else
+                        k_shadow<true, false><<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, A.env_q, R.ctr + kCtrEnv + b,
+                                                                         R.ctr + kCtrWork + work++, R.rad, R.stats);
                     if (time_kernels) timed(sh_ev);
                     ++launches;
                 }

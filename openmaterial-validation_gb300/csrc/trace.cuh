@@ -213,10 +213,11 @@ __device__ __forceinline__ bool trace_begin(const DevScene& S, V3 o, V3 d, float
 }
 
 // Processes one stack entry (an instance or a node); false when the traversal is
-// over.  kAny: stop at the first triangle hit (an occlusion query).
-template <bool kAny = false>
+// over.  kStop: also over as soon as a hit with t < stop_below is taken (an
+// occlusion query stops at any hit: stop_below = infinity).
+template <bool kStop = false>
 __device__ __forceinline__ bool trace_step(const DevScene& S, const uint32_t* __restrict__ tlas_items, TraceState& T,
-                                          TraceStack& st, TraceCounters& tc)
+                                          TraceStack& st, TraceCounters& tc, float stop_below = 0.0f)
 {
     if (T.guard++ > (1u << 22)) {  // a malformed tree can never spin a warp forever
         st.overflow = 1;
@@ -312,7 +313,7 @@ __device__ __forceinline__ bool trace_step(const DevScene& S, const uint32_t* __
                     T.bv = v;
                     T.best_inst = T.cur_inst;
                     T.best_prim = prim;
-                    if (kAny) return false;
+                    if (kStop && t < stop_below) return false;
                 }
             }
         }
@@ -358,9 +359,22 @@ __device__ __forceinline__ bool trace_any(const DevScene& S, const uint32_t* __r
 {
     TraceState T;
     if (!trace_begin(S, o, d, tnear, tfar, T, st)) return false;
-    while (trace_step<true>(S, tlas_items, T, st, tc)) {
+    while (trace_step<true>(S, tlas_items, T, st, tc, __int_as_float(0x7F800000))) {
     }
     return T.found;
+}
+
+// Closest hit, except that the traversal stops at the first hit found with
+// t < stop_below (then `hit` is that hit, not necessarily the closest).
+__device__ __forceinline__ bool trace_closest_or_below(const DevScene& S, const uint32_t* __restrict__ tlas_items, V3 o,
+                                                       V3 d, float tnear, float tfar, float stop_below, RayHit& hit,
+                                                       TraceStack& st, TraceCounters& tc)
+{
+    TraceState T;
+    if (!trace_begin(S, o, d, tnear, tfar, T, st)) return false;
+    while (trace_step<true>(S, tlas_items, T, st, tc, stop_below)) {
+    }
+    return trace_end(T, hit);
 }
 
 // Closest hit; returns true and fills `hit` when a triangle is found.
