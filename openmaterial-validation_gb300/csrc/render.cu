@@ -753,6 +753,9 @@ __global__ void __launch_bounds__(kShadeThreads) k_film(WaveArgs A, int group, d
     FF v[6];
 #pragma unroll
     for (int q = 0; q < 6; ++q) v[q] = FF{0.0f, 0.0f};
+    // squares only for a film with a variance channel (the same for all lanes
+    // of a pixel's group)
+    const bool squares = fsq != nullptr;
     if (live) {
         const int64_t g0 = max(first_path, g_begin), g1 = min(first_path + npp, g_end);
         for (int64_t g = g0 + j; g < g1; g += group) {
@@ -760,16 +763,20 @@ __global__ void __launch_bounds__(kShadeThreads) k_film(WaveArgs A, int group, d
             v[0] = ff_add(v[0], FF{r.x, 0.0f});
             v[1] = ff_add(v[1], FF{r.y, 0.0f});
             v[2] = ff_add(v[2], FF{r.z, 0.0f});
-            v[3] = ff_add(v[3], ff_sqr(r.x));
-            v[4] = ff_add(v[4], ff_sqr(r.y));
-            v[5] = ff_add(v[5], ff_sqr(r.z));
+            if (squares) {
+                v[3] = ff_add(v[3], ff_sqr(r.x));
+                v[4] = ff_add(v[4], ff_sqr(r.y));
+                v[5] = ff_add(v[5], ff_sqr(r.z));
+            }
             ++c;
         }
     }
+    const int nq = __any_sync(0xFFFFFFFFu, squares) ? 6 : 3;
     for (int off = group >> 1; off > 0; off >>= 1) {
         c += __shfl_xor_sync(0xFFFFFFFFu, c, off);
 #pragma unroll
         for (int q = 0; q < 6; ++q) {
+            if (q >= nq) break;
             FF o;
             o.hi = __shfl_xor_sync(0xFFFFFFFFu, v[q].hi, off);
             o.lo = __shfl_xor_sync(0xFFFFFFFFu, v[q].lo, off);
