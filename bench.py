@@ -525,7 +525,7 @@ def run_ours(args, scene, ws, rank, local):
     torch.cuda.synchronize(dev)
     evs = []
     agg = {k: 0 for k in ("extension_rays", "shadow_rays", "light_rays", "kernel_launches", "nodes_visited",
-                          "triangles_tested", "extend_launches")}
+                          "triangles_tested", "extend_launches", "stack_overflows")}
     ext_ms = 0.0
     for _ in range(args.steps):
         flush.zero_()
@@ -595,7 +595,8 @@ def run_ours(args, scene, ws, rank, local):
                            "parallelism": f"replicas x{ws} (disjoint sample ranges)", "film": "FP64 sums"},
                 "mrays_per_s": round(rays / (max_ms / 1e3) / 1e6, 4), "film_counts_ok": cnt_ok,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clock,
-                "gpu_launches": agg["kernel_launches"], "scene_build_ms": round(info["build_ms"], 1)}
+                "gpu_launches": agg["kernel_launches"], "scene_build_ms": round(info["build_ms"], 1),
+                "stack_overflows": agg["stack_overflows"]}
         if ws == 1 and not args.no_post:
             line["post"] = run_post(args, dev, film, count, W, H, flush)
         if ws == 1 and not args.no_mis:

@@ -242,6 +242,8 @@ typedef struct omv_stats {
     int64_t extend_launches;
     double shadow_ms;          /* summed device time of the shadow-ray kernel (time_kernels) */
     int64_t shadow_launches;
+    int64_t stack_overflows;   /* warps whose traversal stack (64 entries) overflowed and dropped
+                                  entries; 0 unless a tree is degenerate */
 } omv_stats;
 
 /* BDPTRenderer::render (BDPTRenderer.cpp:372-393) for one camera.

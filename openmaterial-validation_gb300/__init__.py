@@ -396,7 +396,7 @@ class BDPTRenderer:
                                cnt.ctypes.data_as(C.POINTER(C.c_uint32)) if cnt is not None else None, C.byref(st)))
         self.last_stats = {"paths": st.paths, "extension_rays": st.extension_rays, "shadow_rays": st.shadow_rays,
                            "light_rays": st.light_rays, "render_ms": st.render_ms,
-                           "kernel_launches": st.kernel_launches}
+                           "kernel_launches": st.kernel_launches, "stack_overflows": st.stack_overflows}
         if sums:
             return img, s, q, cnt
         return img

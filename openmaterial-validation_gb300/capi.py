@@ -95,7 +95,8 @@ class Stats(C.Structure):
     _fields_ = [("paths", C.c_int64), ("extension_rays", C.c_int64), ("shadow_rays", C.c_int64),
                 ("light_rays", C.c_int64), ("render_ms", C.c_double), ("kernel_launches", C.c_int64),
                 ("nodes_visited", C.c_int64), ("triangles_tested", C.c_int64), ("extend_ms", C.c_double),
-                ("extend_launches", C.c_int64), ("shadow_ms", C.c_double), ("shadow_launches", C.c_int64)]
+                ("extend_launches", C.c_int64), ("shadow_ms", C.c_double), ("shadow_launches", C.c_int64),
+                ("stack_overflows", C.c_int64)]
 
 
 class Hit(C.Structure):

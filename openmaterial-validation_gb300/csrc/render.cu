@@ -678,9 +678,11 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevSc
         nodes += __shfl_xor_sync(0xFFFFFFFFu, nodes, o);
         tris += __shfl_xor_sync(0xFFFFFFFFu, tris, o);
     }
+    const bool ov = __any_sync(0xFFFFFFFFu, st.overflow);
     if (lane == 0) {
         atomicAdd(&stats[kStatNodes], (unsigned long long)nodes);
         atomicAdd(&stats[kStatTris], (unsigned long long)tris);
+        if (ov) atomicAdd(&stats[kStatOverflow], 1ull);
     }
 }
 
@@ -1185,6 +1187,7 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
         stats->kernel_launches = launches;
         stats->nodes_visited = (int64_t)h[kStatNodes];
         stats->triangles_tested = (int64_t)h[kStatTris];
+        stats->stack_overflows = (int64_t)h[kStatOverflow];
         auto sum_pairs = [](std::vector<cudaEvent_t>& ev) {
             double t = 0.0;
             for (size_t i = 0; i + 1 < ev.size(); i += 2) {

@@ -139,6 +139,7 @@ def test_large_scene_frame_properties(gpu, scenes):
     assert (img[..., 3] == 1).all()
     assert st["paths"] == 192 * 108 * 8
     assert st["extension_rays"] >= st["paths"]
+    assert st["stack_overflows"] == 0
     assert img[..., :3].mean() > 0
 
 
