@@ -40,7 +40,7 @@ enum {
     OMV_ERR_CUDA = 2,
     OMV_ERR_OUT_OF_MEMORY = 3,
     OMV_ERR_EMPTY_SCENE = 4,     /* no valid instance: RenderScene::commitScene returns false */
-    OMV_ERR_TIMEOUT = 5,         /* a bounded device-side wait gave up */
+    OMV_ERR_TIMEOUT = 5,         /* reserved for bounded device-side waits (no kernel waits on another today) */
     OMV_ERR_INTERNAL = 6,
     OMV_ERR_NO_DEVICE = 7
 };

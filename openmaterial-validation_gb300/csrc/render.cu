@@ -896,7 +896,7 @@ namespace {
 // Byte offsets of one wave's arrays inside a single scratch block (each array
 // starts on a 256-byte boundary).
 struct ScratchLayout {
-    size_t tp, rad, ltp, lrad, lmeta, lvp, lvr, rq0, rq1, hits, pjob, sq, ctr, stats, err, bytes;
+    size_t tp, rad, ltp, lrad, lmeta, lvp, lvr, rq0, rq1, hits, pjob, sq, ctr, stats, bytes;
 };
 
 ScratchLayout scratch_layout(int64_t wave_cap, int light_slots, int shadow_slots)
@@ -923,7 +923,6 @@ ScratchLayout scratch_layout(int64_t wave_cap, int light_slots, int shadow_slots
     L.sq = take((size_t)shadow_slots * W * 48 + 48);
     L.ctr = take(kMaxCounters * 4);
     L.stats = take(16 * 8);
-    L.err = take(16 * 4);
     L.bytes = off;
     return L;
 }
@@ -959,7 +958,6 @@ void carve_scratch(RenderScratch& R, void* base, int64_t wave_cap, int light_slo
     R.sq = (float4*)(b + L.sq);
     R.ctr = (uint32_t*)(b + L.ctr);
     R.stats = (unsigned long long*)(b + L.stats);
-    R.err = (uint32_t*)(b + L.err);
 }
 
 // Validated sizes of one frame: paths, wave capacity and vertex slots.
@@ -1481,7 +1479,7 @@ void* static_scratch_address(int device)
 int64_t static_wave_limit(int light_slots, int shadow_slots)
 {
     const size_t per_path = path_scratch_bytes(light_slots, shadow_slots);
-    const size_t fixed = 48 + kMaxCounters * 4 + 16 * 8 + 16 * 4 + 15 * 256;
+    const size_t fixed = 48 + kMaxCounters * 4 + 16 * 8 + 14 * 256;
     int64_t cap = (int64_t)((OMV_STATIC_SCRATCH_BYTES - fixed) / per_path) & ~(int64_t)31;
     while (cap > 0 && scratch_layout(cap, light_slots, shadow_slots).bytes > OMV_STATIC_SCRATCH_BYTES) cap -= 32;
     return cap;

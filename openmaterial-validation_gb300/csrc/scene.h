@@ -58,7 +58,6 @@ struct RenderScratch {
     float4* sq = nullptr;        // shadow queue: 3 float4 per entry
     uint32_t* ctr = nullptr;     // per-wave queue and work counters
     unsigned long long* stats = nullptr;  // cumulative ray counters
-    uint32_t* err = nullptr;     // device error flags
 };
 
 constexpr int kMaxCounters = 512;
