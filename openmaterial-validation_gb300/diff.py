@@ -104,8 +104,9 @@ class MaterialRenderer:
         self.omv.check(self.omv.lib().omv_render_device(self.rs.handle, C.byref(self.cam), C.byref(self.params),
                                                         C.c_void_p(s.data_ptr()), None, C.c_void_p(c.data_ptr()),
                                                         st, None))
-        # a NULL stream (torch's legacy default stream) means the scene's own
-        # non-blocking stream: wait for it before torch reads the film
+        # the render runs on torch's current stream (NULL: the legacy default
+        # stream), so torch reads the film in order; the host waits here so that
+        # a caller's timing brackets the render
         torch.cuda.synchronize()
         return s, c
 
