@@ -178,5 +178,15 @@ def test_mis_rejected_where_unsupported(gpu, scenes):
     assert L.omv_render_device_static(rs.handle, C.byref(cam), C.byref(p), C.c_void_p(s.data_ptr()), None,
                                       C.c_void_p(n.data_ptr()), None) == 1
     assert b"MIS" in L.omv_last_error()
+    # the adjoint replays the reference estimator only (8 materials: within its limits)
+    sm = scenes.scene_materials(8, 8, 1, tris=20_000, bounces=4, sky=True)
+    rm = gpu.RenderScene(sm)
+    cm = gpu.PinholeCamera.from_spec(sm.camera).to_c()
+    pm = gpu.RendererParameters.for_scene(sm, samplesPerPixel=1, estimator=gpu.ESTIMATOR_MIS).to_c()
+    adj = torch.zeros((cm.height, cm.width, 3), dtype=torch.float32, device="cuda")
+    grad = torch.zeros((len(sm.materials), 11), dtype=torch.float32, device="cuda")
+    assert L.omv_adjoint(rm.handle, C.byref(cm), C.byref(pm), C.c_void_p(adj.data_ptr()),
+                         C.c_void_p(grad.data_ptr()), None) == 1
+    assert b"reference estimator" in L.omv_last_error()
     p.estimator = 7
     assert L.omv_render(rs.handle, C.byref(cam), C.byref(p), None, None, None, None, None) == 1
