@@ -436,9 +436,14 @@ constexpr uint32_t kDimEnvConnect = 2048u;
 // that both see the same self-intersections), so the image's expectation is
 // the reference estimator's.  Only an escape the reference would count is
 // connected: b < camera bounces and b + 1 <= maxPathLength.
-static __device__ __noinline__ float env_connect(const WaveArgs& A, int b, int k, uint64_t seed, uint32_t pixel,
+struct EnvRay {
+    V3 so, w, c;  // shifted origin, direction, contribution
+    float tnear;
+    bool push;
+};
+static __device__ __noinline__ float env_connect(const WaveArgs& A, int b, uint64_t seed, uint32_t pixel,
                                                  uint32_t sample, BsdfIn d, V3 pos, V3 nrm, V3 tp, V3 O, int kind,
-                                                 float tnear)
+                                                 float tnear, EnvRay& er)
 {
     const DevScene& S = A.S;
     float pdf_o = 0.0f;
@@ -460,14 +465,11 @@ static __device__ __noinline__ float env_connect(const WaveArgs& A, int b, int k
             }
         }
     }
-    if (push) {  // the lanes of a warp that connect take consecutive slots: coherent environment rays
-        const uint32_t sl = coalesced_append(&A.R.ctr[kCtrEnv + b]);
-        float4* q = A.env_q + 3 * (size_t)sl;
-        const V3 so = shifted_origin(pos, w, 1.0f);
-        q[0] = make_float4(so.x, so.y, so.z, __int_as_float(k));
-        q[1] = make_float4(w.x, w.y, w.z, tnear);
-        q[2] = make_float4(c.x, c.y, c.z, 0.0f);
-    }
+    er.push = push;
+    er.w = w;
+    er.c = c;
+    er.tnear = tnear;
+    er.so = push ? shifted_origin(pos, w, 1.0f) : pos;
     return pdf_o;
 }
 
@@ -492,6 +494,9 @@ __global__ void __launch_bounds__(kShadeThreads, kMis ? 3 : 4) k_camera_shade(Wa
         V3 so = v3(0, 0, 0), O = v3(0, 0, 1);
         float tnear = 0.0f;
         int k = 0;
+        EnvRay er;
+        er.push = false;
+        er.w = v3(0.0f, 0.0f, 1.0f);
         if (i < n) {
             const float4 ra = rq_in[2 * (size_t)i], rb = rq_in[2 * (size_t)i + 1];
             const uint4 h = A.R.hits[i];
@@ -532,8 +537,8 @@ __global__ void __launch_bounds__(kShadeThreads, kMis ? 3 : 4) k_camera_shade(Wa
                 const V3 tpn = v3(tp.x * brdf.x * ct, tp.y * brdf.y * ct, tp.z * brdf.z * ct);
                 float mis_pdf = 0.0f;  // density of O for the next escape's MIS weight (0: weight 1)
                 if (kMis && M.type == kMatPbr)
-                    mis_pdf = env_connect(A, b, k, c.seed, pixel, sample, pbr_bsdf_in(M, P, sp, in), sp.pos, sp.nrm,
-                                          tp, O, info.kind, tnear);
+                    mis_pdf = env_connect(A, b, c.seed, pixel, sample, pbr_bsdf_in(M, P, sp, in), sp.pos, sp.nrm,
+                                          tp, O, info.kind, tnear, er);
                 if (M.type == kMatPbr && M.emissive_on) {  // Rad += outFactor x emission (:171-173)
                     const V3 e = pbr_emission(S, M, tex_hit(sp));
                     float4 r = A.R.rad[k];
@@ -588,6 +593,15 @@ __global__ void __launch_bounds__(kShadeThreads, kMis ? 3 : 4) k_camera_shade(Wa
         if (push) {
             rq_out[2 * (size_t)slot] = make_float4(so.x, so.y, so.z, tnear);
             rq_out[2 * (size_t)slot + 1] = make_float4(O.x, O.y, O.z, __int_as_float(k));
+        }
+        if (kMis) {  // environment rays grouped by direction like the next-bounce rays
+            const uint32_t es = block_append_binned(&A.R.ctr[kCtrEnv + b], er.push, direction_bin(er.w), bins);
+            if (er.push) {
+                float4* q = A.env_q + 3 * (size_t)es;
+                q[0] = make_float4(er.so.x, er.so.y, er.so.z, __int_as_float(k));
+                q[1] = make_float4(er.w.x, er.w.y, er.w.z, er.tnear);
+                q[2] = make_float4(er.c.x, er.c.y, er.c.z, 0.0f);
+            }
         }
     }
 }
