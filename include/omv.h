@@ -291,9 +291,15 @@ omv_status omv_render_device(omv_scene* scene, const omv_camera* camera, const o
  *   - Nothing in the scratch has to be zero on entry: the call clears its queue
  *     and ray counters itself (cudaMemsetAsync on `stream`).
  *   - No stats and no timing (it creates no CUDA events); time_kernels must be 0.
- *   - The first call on each device resolves the scratch address
- *     (cudaGetSymbolAddress, which may load the module on that device); make one
- *     call before any stream capture.
+ *   - The reference estimator only: OMV_ESTIMATOR_MIS on a scene with an HDRI
+ *     fails with OMV_ERR_INVALID_ARGUMENT (its table is allocated on first use);
+ *     on a scene without one it has no effect, as in omv_render_device.
+ *   - Every call looks up the scratch address in the current context
+ *     (cudaGetSymbolAddress) and makes sure every kernel a frame can launch is
+ *     loaded (cudaFuncGetAttributes).  Under lazy module loading the first call
+ *     in a context loads them, which allocates the module's device memory
+ *     (the scratch included) once; later calls allocate nothing, whatever the
+ *     scene (lights, alpha masks).  Make one call before any stream capture.
  *   - One scratch per device for all scenes: calls that overlap on the device
  *     (different streams or threads, any scenes) race on it; keep them ordered
  *     on one stream or serialise them. */
@@ -356,7 +362,10 @@ omv_status omv_batch_autotune(omv_scene* scene, int32_t num_jobs, const omv_job*
 
 /* Replaces the scene's materials (num_materials descriptors, as given to
  * omv_scene_create, whose alpha-mask status may not change).  Geometry and
- * acceleration structure are kept. */
+ * acceleration structure are kept.  Waits for all work queued on the device
+ * (cudaDeviceSynchronize) before the table is replaced, so a render still
+ * queued on any stream uses the old materials throughout and one enqueued
+ * after the call the new ones. */
 omv_status omv_scene_set_materials(omv_scene* scene, int32_t num_materials, const omv_material_desc* materials);
 
 /* Gradient of an image loss with respect to the material parameters by path

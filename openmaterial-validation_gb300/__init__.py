@@ -426,11 +426,22 @@ class ProgressiveFilm:
     after 16 + 16 samples, saved and reloaded in between, is the 32-sample
     film.  The reference has no counterpart (it renders a fixed spp)."""
 
+    # the renderer parameters that define the image: samples rendered with
+    # other values belong to another image (another estimator, seed, bounce
+    # limit or light model) and must not be summed into this film
+    IMAGE_KEYS = ("cameraBouncesN", "lightBouncesN", "maxPathLength", "lightDistanceAttenuation",
+                  "lightScaleValue", "lightMinDistance", "rayCutPixValue", "seed", "estimator")
+
     def __init__(self, width: int, height: int, variance: bool = False, next_sample: int = 0) -> None:
         self.sum = np.zeros((height, width, 3), dtype=np.float64)
         self.sumsq = np.zeros((height, width, 3), dtype=np.float64) if variance else None
         self.count = np.zeros((height, width), dtype=np.uint32)
         self.next_sample = int(next_sample)
+        self.params: Optional[dict] = None  # IMAGE_KEYS of the first add(), then fixed
+
+    @classmethod
+    def _image_params(cls, p: "RendererParameters") -> dict:
+        return {k: getattr(p, k) for k in cls.IMAGE_KEYS}
 
     def add(self, renderer: BDPTRenderer, camera: PinholeCamera, spp: int) -> None:
         """Renders `spp` more samples per pixel with `renderer`'s scene and
@@ -438,6 +449,11 @@ class ProgressiveFilm:
         if (camera.height, camera.width) != self.count.shape:
             raise ValueError("camera resolution differs from the film's")
         keep = renderer.params
+        ip = self._image_params(keep)
+        if self.params is not None and ip != self.params:
+            diff = sorted(k for k in ip if ip[k] != self.params[k])
+            raise ValueError(f"renderer parameters differ from the film's ({', '.join(diff)}): "
+                             "their samples would estimate another image")
         p = dataclasses.replace(keep, samplesPerPixel=int(spp), sample_offset=self.next_sample,
                                 accumulate_variance=self.sumsq is not None)
         renderer.set_parameters(p)
@@ -450,6 +466,7 @@ class ProgressiveFilm:
             self.sumsq += q
         self.count += cnt
         self.next_sample += int(spp)
+        self.params = ip
 
     def image(self) -> np.ndarray:
         """The normalised RGBA image (PinholeCamera::stop)."""
@@ -461,6 +478,8 @@ class ProgressiveFilm:
 
     def save(self, path: str) -> None:
         extra = {"sumsq": self.sumsq} if self.sumsq is not None else {}
+        if self.params is not None:
+            extra["params"] = np.array(json.dumps(self.params))
         np.savez(path, sum=self.sum, count=self.count, next_sample=np.int64(self.next_sample), **extra)
 
     @classmethod
@@ -472,6 +491,8 @@ class ProgressiveFilm:
             f.count[...] = z["count"]
             if f.sumsq is not None:
                 f.sumsq[...] = z["sumsq"]
+            if "params" in z.files:
+                f.params = json.loads(str(z["params"]))
         return f
 
 

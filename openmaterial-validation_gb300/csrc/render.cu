@@ -27,7 +27,6 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
-#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1474,18 +1473,36 @@ namespace {
 
 __device__ __align__(256) unsigned char g_static_scratch[OMV_STATIC_SCRATCH_BYTES];
 
-constexpr int kMaxDevices = 64;
-
-// Device address of g_static_scratch on `device` (current).  Resolved once per
-// device; the first call may load the module on that device.
-void* static_scratch_address(int device)
+// Loads every kernel the wave loop of a reference-estimator frame can launch
+// into the current context.  With lazy module loading (the CUDA default) a
+// kernel is loaded, and its module's device memory allocated, on its first
+// launch; a later frame on a scene with point lights or alpha-masked
+// materials would otherwise load k_light_gen / k_light_shade / the masked
+// shadow kernel then.  Querying a kernel's attributes loads it.
+void load_wave_kernels()
 {
-    static std::mutex mu;
-    static void* addr[kMaxDevices] = {};
-    if (device < 0 || device >= kMaxDevices) throw ArgError("device index out of range for the static scratch");
-    std::lock_guard<std::mutex> lock(mu);
-    if (!addr[device]) OMV_CUDA(cudaGetSymbolAddress(&addr[device], g_static_scratch));
-    return addr[device];
+    cudaFuncAttributes a;
+    OMV_CUDA(cudaFuncGetAttributes(&a, k_job_ids));
+    OMV_CUDA(cudaFuncGetAttributes(&a, k_camera_gen));
+    OMV_CUDA(cudaFuncGetAttributes(&a, k_light_gen));
+    OMV_CUDA(cudaFuncGetAttributes(&a, k_extend));
+    OMV_CUDA(cudaFuncGetAttributes(&a, k_light_shade));
+    OMV_CUDA(cudaFuncGetAttributes(&a, k_camera_shade<false>));
+    OMV_CUDA(cudaFuncGetAttributes(&a, k_shadow<false, false>));
+    OMV_CUDA(cudaFuncGetAttributes(&a, k_shadow<false, true>));
+    OMV_CUDA(cudaFuncGetAttributes(&a, k_film));
+}
+
+// Device address of g_static_scratch in the current context, resolved on
+// every call (a lookup once the module is loaded), so that a context created
+// after a device reset gets its own address.  The first call in a context
+// loads the module and the wave kernels.
+void* static_scratch_address()
+{
+    load_wave_kernels();
+    void* addr = nullptr;
+    OMV_CUDA(cudaGetSymbolAddress(&addr, g_static_scratch));
+    return addr;
 }
 
 }  // namespace
@@ -1503,9 +1520,9 @@ void render_frame_static(SceneHost& s, const omv_camera& cam, const omv_params& 
                          uint32_t* d_count, cudaStream_t st)
 {
     if (p.time_kernels) throw ArgError("time_kernels needs CUDA events, which the no-allocation render does not create");
-    if (p.estimator == OMV_ESTIMATOR_MIS)
+    if (mis_on(s, p))
         throw ArgError("the MIS estimator builds an environment table on first use; the no-allocation render "
-                       "supports the reference estimator only");
+                       "supports the reference estimator only (MIS has no effect on a scene without an HDRI)");
     FramePlan P = plan_frame(s, cam, p, 1);
     const int64_t limit = static_wave_limit(P.light_slots, P.shadow_slots);
     if (p.wave_paths > 0) {
@@ -1519,7 +1536,7 @@ void render_frame_static(SceneHost& s, const omv_camera& cam, const omv_params& 
         P.cap = std::min<int64_t>(limit, std::max<int64_t>(P.total, 1));
     }
     RenderScratch R;
-    carve_scratch(R, static_scratch_address(s.device), P.cap, P.light_slots, P.shadow_slots);
+    carve_scratch(R, static_scratch_address(), P.cap, P.light_slots, P.shadow_slots);
     run_waves(s, R, P, cam, p, d_sum, d_sumsq, d_count, st, nullptr, false);
 }
 

@@ -327,7 +327,8 @@ void set_material_sets(SceneHost& s, int num_sets, const omv_material_desc* desc
         all[(size_t)k * per + per - 1] = missing_material();
     }
     if (s.mat_sets) {
-        OMV_CUDA(cudaStreamSynchronize(s.stream));
+        // batches still queued on any stream read the old sets
+        OMV_CUDA(cudaDeviceSynchronize());
         cudaFree(s.mat_sets);
         s.mat_sets = nullptr;
         s.num_mat_sets = 0;
@@ -418,7 +419,9 @@ void set_scene_materials(SceneHost& s, int num, const omv_material_desc* descs)
             throw ArgError("omv_scene_set_materials cannot change which materials are alpha-masked");
     }
     mats[num] = missing_material();
-    OMV_CUDA(cudaStreamSynchronize(s.stream));
+    // renders still queued on any stream (the caller's may be non-blocking)
+    // read the table: wait for all of the device's work before replacing it
+    OMV_CUDA(cudaDeviceSynchronize());
     OMV_CUDA(cudaMemcpy(const_cast<DevMaterial*>(s.dev.mats), mats.data(), sizeof(DevMaterial) * mats.size(),
                         cudaMemcpyHostToDevice));
     s.h_mats = mats;

@@ -349,6 +349,37 @@ def scene_c1(width: int = 256, height: int = 256, spp: int = 16) -> Scene:
                  RenderSpec(spp, 6, 6, 6), gltf_nodes=[nodes])
 
 
+def gltf_light_intensity(color, intensity) -> tuple:
+    """The RGB intensity the reference gives a KHR_lights_punctual point light:
+    colour x intensity with the green and blue entries exchanged (main.cpp:360-362
+    reads getLightGreen / getLightBlue, which return m_color[2] / m_color[1],
+    PointLight.h:52-56), in float32."""
+    c = np.asarray(color, dtype=F32)
+    i = F32(intensity)
+    return (float(c[0] * i), float(c[2] * i), float(c[1] * i))
+
+
+def scene_lights(width: int = 48, height: int = 48, spp: int = 16) -> Scene:
+    """C1's geometry and materials under three coloured point lights of
+    different power, one with a glTF range: the light pick by the luminance
+    CDF of their power (RenderScene.cpp:274-279, DistanceRandom.h:98-115), the
+    green/blue order of coloured lights and the ranged attenuation branches
+    (BDPTRenderer.cpp:104-126, RenderLightPoint.cpp:20-26)."""
+    base = scene_c1(width, height, spp)
+    root = (0.0, 0.0, -5.0)
+    spec = [{"translation": (2.0, 4.0, 2.0), "color": (1.0, 0.8, 0.55), "intensity": 60.0},
+            {"translation": (-3.0, 2.5, 1.0), "color": (0.2, 0.45, 1.0), "intensity": 25.0, "range": 7.5},
+            {"translation": (0.5, 6.0, -2.0), "color": (0.9, 0.15, 0.35), "intensity": 90.0}]
+    lights = []
+    for lt in spec:
+        pos = tuple(float(F32(F32(root[k]) + F32(lt["translation"][k]))) for k in range(3))
+        lights.append(Light(position=pos, intensity=gltf_light_intensity(lt["color"], lt["intensity"]),
+                            range=float(lt.get("range", 0.0))))
+    nodes = {"root_translation": root, "lights": spec}
+    return Scene("lights", base.meshes, base.instances, base.materials, lights, None, base.camera,
+                 RenderSpec(spp, 6, 6, 6), gltf_nodes=[nodes])
+
+
 def make_sky(width: int, height: int, rng: np.random.Generator, suns: bool = True) -> np.ndarray:
     """Log-normal sky (mu=0, sigma=1 of the log) from a smooth Gaussian field on
     the sphere, plus three Gaussian sun lobes of peak 1e4, in the equirect
@@ -1008,14 +1039,21 @@ def write_gltf(scene: Scene, dirname: str) -> dict:
         # one root node (translated) holding a node per mesh and the light node
         cfg = scene.gltf_nodes[0]
         nm = len(scene.meshes)
+        lights = cfg.get("lights") or [{"translation": cfg["light_translation"], "color": cfg["light_color"],
+                                        "intensity": cfg["light_intensity"]}]
         nodes.append({"name": "root", "translation": list(cfg["root_translation"]),
-                      "children": list(range(1, nm + 2))})
+                      "children": list(range(1, nm + 1 + len(lights)))})
         for i, m in enumerate(scene.meshes):
             nodes.append({"name": m.name, "mesh": i})
-        nodes.append({"name": "light", "translation": list(cfg["light_translation"]),
-                      "extensions": {"KHR_lights_punctual": {"light": 0}}})
-        extensions["KHR_lights_punctual"] = {"lights": [{"type": "point", "color": list(cfg["light_color"]),
-                                                          "intensity": cfg["light_intensity"]}]}
+        gl_lights = []
+        for i, lt in enumerate(lights):
+            nodes.append({"name": f"light{i}" if i else "light", "translation": list(lt["translation"]),
+                          "extensions": {"KHR_lights_punctual": {"light": i}}})
+            rec = {"type": "point", "color": list(lt["color"]), "intensity": lt["intensity"]}
+            if lt.get("range"):
+                rec["range"] = lt["range"]
+            gl_lights.append(rec)
+        extensions["KHR_lights_punctual"] = {"lights": gl_lights}
         used.append("KHR_lights_punctual")
         scene_nodes = [0]
     else:

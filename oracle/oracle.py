@@ -22,7 +22,23 @@ if ROOT not in sys.path:
 capi = importlib.import_module("openmaterial-validation_gb300.capi")
 
 LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_BUILD = os.path.join(HERE, "_ref")
 REFERENCE_SEED = 3254638  # RenderScene.cpp:20
+
+
+def reference_tree():
+    """The reference source tree: $OMV_REFERENCE, else the tree `make ref`
+    last built from (recorded in _ref/REFERENCE_TREE); None when neither
+    exists (then the tests that read the reference's own files skip)."""
+    cands = [os.environ.get("OMV_REFERENCE")]
+    marker = os.path.join(REF_BUILD, "REFERENCE_TREE")
+    if os.path.exists(marker):
+        with open(marker) as f:
+            cands.append(f.read().strip())
+    for c in cands:
+        if c and os.path.isdir(os.path.join(c, "pathtracer", "src")):
+            return c
+    return None
 
 _lib = None
 

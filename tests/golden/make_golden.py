@@ -1,7 +1,8 @@
 """Generates the golden fixtures in this directory by running the reference
 renderer's own code (built from its unmodified sources by oracle/Makefile
-`make ref` against the Embree-API shim).  Needs the reference tree
-(REF=... or /root/reference) and runs on the development host only; the
+`make ref` against the Embree-API shim).  Needs the reference tree where
+the oracle recipe finds it (its REF, or OMV_REFERENCE) and runs on the
+development host only; the
 fixtures it writes are committed and are all the tests need elsewhere.
 
     python tests/golden/make_golden.py [--only name,...] [--big]
@@ -24,6 +25,9 @@ Fixtures (numpy .npz):
                     (wrapping, negative, texel-centre and edge cases)
   film_textured_32x8.npz / scene_textured.npz
                     -C 1 film and committed scene of the textured PBR scene
+  film_lights_32x4_A<a>.npz / scene_lights.npz
+                    -C 1 films at -A 0, 1, 2 and the committed scene of three
+                    coloured point lights (one with a glTF range)
   png.npz           stb_image's RGBA decode (as tinygltf loads images) of seeded PNG
                     files of every colour type, depth and row filter
   assets.npz        digests of the reference's committed scene for each of its own
@@ -48,7 +52,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 S = importlib.import_module("openmaterial-validation_gb300.scenes")
-REF = os.environ.get("REF", "/root/reference")
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import oracle as O  # noqa: E402
+
+REF = None  # the reference tree, set by main() after the recipe has built it
 BIN = os.path.join(ROOT, "oracle", "_ref")
 
 
@@ -250,6 +257,18 @@ def render_reference(sc, tmp, exe="pathtracer", extra=(), log=None):
     hdr = np.fromfile(os.path.join(d, "film.bin"), dtype=np.int32, count=2)
     film = np.fromfile(os.path.join(d, "film.bin"), dtype=np.float32)[2:].reshape(hdr[1], hdr[0], 4)
     return film, float(line[1]), int(line[2]), read_scene_dump(os.path.join(d, "scene.bin"))
+
+
+def gen_lights(tmp):
+    """Three coloured point lights, one ranged, at attenuation modes 0, 1, 2
+    (-A): films and the committed scene (light positions, G/B-ordered
+    intensities, ranges, powers)."""
+    sc = S.scene_lights(32, 32, 4)
+    for A in (0, 1, 2):
+        film, secs, rays, dump = render_reference(sc, tmp, extra=["-A", str(A)])
+        np.savez_compressed(os.path.join(HERE, f"film_lights_32x4_A{A}.npz"), film=film, seconds=secs, rays=rays,
+                            width=32, height=32, spp=4, attenuation=A)
+    np.savez_compressed(os.path.join(HERE, "scene_lights.npz"), **dump)
 
 
 def gen_films(tmp, big=False):
@@ -554,7 +573,8 @@ def gen_lightbox(tmp):
 
 GENS = {"mt": gen_mt, "brdf": gen_brdf, "om": gen_om, "ior": gen_ior, "env": gen_env, "camera": gen_camera,
         "films": gen_films, "ids": gen_ids, "post": gen_post, "fc": gen_fc, "lightbox": gen_lightbox,
-        "textured": gen_textured, "texture": gen_texture, "png": gen_png, "hdr": gen_hdr, "assets": gen_assets}
+        "textured": gen_textured, "texture": gen_texture, "png": gen_png, "hdr": gen_hdr, "assets": gen_assets,
+        "lights": gen_lights}
 
 
 def main():
@@ -562,9 +582,11 @@ def main():
     ap.add_argument("--only", default="")
     ap.add_argument("--big", action="store_true", help="also the 256x256 4096-spp C1 reference film")
     a = ap.parse_args()
-    if not os.path.isdir(REF):
-        sys.exit(f"reference tree not found at {REF}")
-    run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "-j8", "ref", f"REF={REF}"])
+    global REF
+    run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "-j8", "ref"])
+    REF = O.reference_tree()
+    if REF is None:
+        sys.exit("reference tree not found: set OMV_REFERENCE")
     names = [n for n in a.only.split(",") if n] or list(GENS)
     with tempfile.TemporaryDirectory() as tmp:
         for n in names:

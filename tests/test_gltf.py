@@ -12,7 +12,10 @@ import numpy as np
 import pytest
 from conftest import ROOT, golden
 
-REF_TREE = os.environ.get("REF", "/root/reference")
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import oracle as _oracle  # noqa: E402
+
+REF_TREE = _oracle.reference_tree()
 
 
 @pytest.fixture(scope="module")
@@ -135,7 +138,8 @@ def _assets():
     return M.ASSETS
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF_TREE, "objects")), reason="reference assets not present")
+@pytest.mark.skipif(REF_TREE is None or not os.path.isdir(os.path.join(REF_TREE, "objects")),
+                    reason="reference assets not present")
 @pytest.mark.parametrize("asset", _assets())
 def test_loader_matches_reference_on_its_assets(gl, oracle, scenes, asset):
     g = golden("assets")

@@ -73,7 +73,7 @@ def test_camera_properties_and_rays(oracle, scenes):
     assert np.array_equal(rays.view(np.uint32), g["rays"].view(np.uint32))
 
 
-@pytest.mark.parametrize("name", ["c1", "mixed", "textured"])
+@pytest.mark.parametrize("name", ["c1", "mixed", "textured", "lights"])
 def test_committed_scene_matches_reference(oracle, scenes, name):
     """Flattening + commit (normals, tangents, normal matrices, missing
     material, light power) equal the reference's RenderScene after commitScene."""
@@ -119,6 +119,20 @@ def test_port_reproduces_reference_film(oracle, scenes, name, scene_fn):
     g = golden(name)
     sc = getattr(scenes, scene_fn)(int(g["width"]), int(g["height"]), int(g["spp"]))
     film, _, rays = oracle.OracleScene(sc).render(mode=0)
+    assert rays == int(g["rays"])
+    assert np.array_equal(film.view(np.uint32), g["film"].view(np.uint32))
+
+
+@pytest.mark.parametrize("attenuation", [0, 1, 2])
+def test_port_reproduces_reference_lights(oracle, scenes, attenuation):
+    """Three coloured point lights (one with a range) at -A 0, 1, 2: the light
+    pick by power, the green/blue order and every attenuation branch, bit for
+    bit with the reference at -C 1."""
+    g = golden(f"film_lights_32x4_A{attenuation}")
+    sc = scenes.scene_lights(int(g["width"]), int(g["height"]), int(g["spp"]))
+    p = oracle.capi.params_for(sc)
+    p.light_distance_attenuation = attenuation
+    film, _, rays = oracle.OracleScene(sc).render(params=p, mode=0)
     assert rays == int(g["rays"])
     assert np.array_equal(film.view(np.uint32), g["film"].view(np.uint32))
 

@@ -19,6 +19,32 @@ def test_save_and_load_round_trip(omv, tmp_path):
     assert np.allclose(g.image()[..., :3], f.sum / 48)
 
 
+def test_checkpoint_keeps_the_image_parameters_and_refuses_others(omv, tmp_path):
+    """The parameters that define the image (seed, bounces, estimator, light
+    model, cut-off) are saved with the film; resuming with different ones
+    raises before anything is rendered."""
+    f = omv.ProgressiveFilm(4, 3)
+    p0 = omv.RendererParameters(seed=3, estimator=0)
+    f.params = omv.ProgressiveFilm._image_params(p0)
+    path = str(tmp_path / "film.npz")
+    f.save(path)
+    g = omv.ProgressiveFilm.load(path)
+    assert g.params == f.params
+
+    class Stub:  # only the parameters are read before a mismatch raises
+        def __init__(self, params):
+            self.params = params
+
+    cam = omv.PinholeCamera(4, 3)
+    for change in ({"seed": 4}, {"estimator": 1}, {"cameraBouncesN": 3}, {"lightDistanceAttenuation": 2},
+                   {"rayCutPixValue": 0.0}):
+        bad = omv.RendererParameters(seed=3, estimator=0)
+        for k, v in change.items():
+            setattr(bad, k, v)
+        with pytest.raises(ValueError, match=next(iter(change))):
+            g.add(Stub(bad), cam, 4)
+
+
 @pytest.mark.gpu
 def test_resumed_render_equals_one_render(gpu, scenes, tmp_path):
     sc = scenes.scene_c1(24, 24, 1)

@@ -8,6 +8,9 @@ order of the FP64 atomic additions (the static scratch may split the frame into
 more waves), so sums agree to 1e-9 of the film's largest value and sample counts
 exactly."""
 import ctypes as C
+import os
+import subprocess
+import sys
 
 import pytest
 
@@ -93,3 +96,54 @@ def test_static_render_rejects_a_wave_beyond_the_scratch(gpu, scenes):
     params.wave_paths = 0
     params.time_kernels = 1
     assert _render(gpu, torch, "static", scene, cam, params, film) == OMV_ERR_INVALID_ARGUMENT
+
+
+_FRESH = r"""
+import ctypes as C, importlib, sys
+import torch
+sys.path.insert(0, sys.argv[1])
+omv = importlib.import_module("openmaterial-validation_gb300")
+S = omv.scenes
+L = omv.lib()
+
+def setup(sc):
+    scene = omv.RenderScene(sc)
+    cam = omv.PinholeCamera.from_spec(sc.camera).to_c()
+    params = omv.RendererParameters.for_scene(sc, samplesPerPixel=8, seed=2).to_c()
+    n = cam.width * cam.height
+    film = [torch.zeros(3 * n, dtype=torch.float64, device="cuda"), None,
+            torch.zeros(n, dtype=torch.int32, device="cuda")]
+    return scene, cam, params, film
+
+def static(scene, cam, params, film):
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    omv.check(L.omv_render_device_static(scene.handle, C.byref(cam), C.byref(params),
+                                         C.c_void_p(film[0].data_ptr()), None, C.c_void_p(film[2].data_ptr()),
+                                         stream))
+    torch.cuda.synchronize()
+
+lit = setup(S.scene_c1(32, 32, 1))       # point light, opaque materials
+masked = setup(S.scene_mixed(32, 32, 1))  # point light, an alpha-blended material
+assert any(m.alpha_mode != 0 for m in masked[0].spec.materials)
+torch.cuda.synchronize()
+static(*lit)  # the first call in this process: loads the module and the wave kernels
+free0 = torch.cuda.mem_get_info()[0]
+static(*masked)  # masked shadow rays: a kernel the first frame did not launch
+static(*lit)
+free1 = torch.cuda.mem_get_info()[0]
+assert int(lit[3][2].min()) == 16 and int(masked[3][2].min()) == 8, "film counts"
+print("FREE", free0, free1)
+"""
+
+
+def test_static_render_first_in_a_fresh_process_allocates_nothing_later(gpu, scenes):
+    """In a process whose first render is the static one (lazy module loading
+    has loaded nothing yet), a later frame on a scene with alpha-masked
+    materials, which launches kernels the first frame did not, still leaves
+    free device memory unchanged."""
+    pytest.importorskip("torch")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", _FRESH, root], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    line = [x for x in r.stdout.splitlines() if x.startswith("FREE")][-1].split()
+    assert int(line[1]) == int(line[2]), line
