@@ -474,6 +474,49 @@ def run_mis(args, dev, rs, scene, flush):
             "timing": "CUDA events, median of 3 frames, L2 flushed, per-pixel variance accumulated on both sides"}
 
 
+def run_builders(args, dev, scene, flush):
+    """The three acceleration-structure builders on the benchmark scene: the
+    scene creation time (omv_scene_create, which the build dominates) and the
+    frame's device time on each tree (CUDA events, median of 3 frames, L2
+    flushed), with the nodes each extension ray fetched."""
+    import torch
+
+    omv = importlib.import_module("openmaterial-validation_gb300")
+    L, capi = omv.lib(), omv.capi
+    W, H = scene.camera.width, scene.camera.height
+    spp, npix = scene.render.samples_per_pixel, W * H
+    cam = capi.camera_struct(scene.camera)
+    s = torch.zeros(3 * npix, dtype=torch.float64, device=dev)
+    n = torch.zeros(npix, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    out = {}
+    for name, b in (("ploc", capi.BVH_PLOC), ("lbvh", capi.BVH_LBVH), ("host_sah", capi.BVH_HOST_SAH)):
+        rs = omv.RenderScene(scene, dev.index or 0, bvh_builder=b)
+        info = rs.info()
+        p = capi.params_for(scene, spp=spp, seed=77)
+        times, st = [], capi.Stats()
+        for it in range(4):
+            s.zero_()
+            n.zero_()
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            omv.check(L.omv_render_device(rs.handle, C.byref(cam), C.byref(p), C.c_void_p(s.data_ptr()), None,
+                                          C.c_void_p(n.data_ptr()), C.c_void_p(stream.cuda_stream), C.byref(st)))
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            if it:
+                times.append(e0.elapsed_time(e1))
+        ms = sorted(times)[1]
+        out[name] = {"build_ms": round(info["build_ms"], 1), "frame_ms": round(ms, 3),
+                     "mpaths_per_s": round(npix * spp / (ms / 1e3) / 1e6, 1),
+                     "nodes_per_ray": round(st.nodes_visited / max(1, st.extension_rays), 2),
+                     "bvh8_nodes": info["blas_nodes"]}
+        rs.close()
+    out["build_ms_note"] = "omv_scene_create wall time: geometry upload, normals, the BVH build and its validation"
+    return out
+
+
 def run_ours(args, scene, ws, rank, local):
     import numpy as np
     import torch
@@ -593,6 +636,8 @@ def run_ours(args, scene, ws, rank, local):
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clock,
                 "gpu_launches": agg["kernel_launches"], "scene_build_ms": round(info["build_ms"], 1),
                 "stack_overflows": agg["stack_overflows"]}
+        if ws == 1 and not args.no_builders:
+            line["builders"] = run_builders(args, dev, scene, flush)
         if ws == 1 and not args.no_post:
             line["post"] = run_post(args, dev, film, count, W, H, flush)
         if ws == 1 and not args.no_mis:
@@ -620,6 +665,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched material sweep")
     ap.add_argument("--no-post", action="store_true", help="skip the image development leg")
+    ap.add_argument("--no-builders", action="store_true", help="skip the BVH builder comparison leg")
     ap.add_argument("--no-mis", action="store_true", help="skip the MIS-vs-reference estimator leg")
     ap.add_argument("--batch-jobs", type=int, default=256)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-vs-finite-difference leg")

@@ -156,12 +156,24 @@ typedef struct omv_scene_desc {
     const omv_hdri_desc* hdri;      /* NULL: no background */
     int32_t num_textures;
     const omv_texture_desc* textures;
+    int32_t bvh_builder;            /* OMV_BVH_*: how the binary trees are built (0: PLOC) */
 } omv_scene_desc;
+
+/* Builders of the acceleration structure (Embree's build, RenderScene.cpp:225-272).
+ * Each builds a binary tree per mesh and one over the instances, which the
+ * device collapses into 8-wide nodes with 16-bit quantized child boxes.
+ *   OMV_BVH_PLOC      on the device: Morton codes, radix sort, parallel
+ *                     locally-ordered clustering of all meshes at once (default)
+ *   OMV_BVH_LBVH      on the device: Morton codes, radix sort, Karras LBVH
+ *   OMV_BVH_HOST_SAH  binned surface-area-heuristic trees on host threads
+ * Hits do not depend on the builder; build time and traversal speed do. */
+enum { OMV_BVH_PLOC = 0, OMV_BVH_LBVH = 1, OMV_BVH_HOST_SAH = 2 };
 
 typedef struct omv_scene omv_scene;
 
-/* RenderScene::allocate + set* + commitScene.  Builds the GPU acceleration
- * structure (Morton codes -> radix sort -> LBVH -> 8-wide quantized BVH). */
+/* RenderScene::allocate + set* + commitScene.  Builds the acceleration
+ * structure with desc->bvh_builder (omv_scene_info.build_ms times the whole
+ * call). */
 omv_status omv_scene_create(const omv_scene_desc* desc, int32_t device, omv_scene** out);
 omv_status omv_scene_destroy(omv_scene* scene);
 
@@ -222,7 +234,15 @@ typedef struct omv_params {
     int32_t wave_paths;                 /* paths per wavefront wave; 0 = automatic */
     int32_t time_kernels;               /* record CUDA events around every closest-hit
                                            kernel launch (omv_stats.extend_ms) */
+    int32_t traversal;                  /* OMV_TRAVERSAL_*: how camera rays are traced */
 } omv_params;
+
+/* OMV_TRAVERSAL_AUTO: the first camera bounce is traced warp-coherently (the
+ * 32 lanes of a warp, 32 samples of one pixel, share one traversal stack;
+ * each lane still tests its own ray), except on scenes with alpha-masked
+ * materials; every other ray is traced on its own.  OMV_TRAVERSAL_PER_RAY:
+ * every ray on its own.  Both give the same hits, so the same image. */
+enum { OMV_TRAVERSAL_AUTO = 0, OMV_TRAVERSAL_PER_RAY = 1 };
 
 /* Fills `p` with the reference defaults (RendererParameters.h:56-89). */
 void omv_params_default(omv_params* p);

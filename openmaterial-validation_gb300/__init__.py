@@ -32,7 +32,7 @@ CSRC = os.path.join(PKG_DIR, "csrc")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "libomv.so")
 SOURCES = ["bvh_build.cu", "scene.cu", "render.cu", "adjoint.cu", "fc.cu", "post.cu", "capi.cu"]
-HEADERS = ["bvh_build.h", "omv_device.cuh", "omv_types.h", "scene.h", "trace.cuh", "shade.cuh", "dual.cuh"]
+HEADERS = ["bvh_build.h", "omv_device.cuh", "omv_types.h", "scene.h", "trace.cuh", "shade.cuh", "dual.cuh", "crmath.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
 # translation units whose device float math must round like the reference
@@ -197,6 +197,7 @@ class RendererParameters:
     accumulate_variance: bool = False
     wave_paths: int = 0
     estimator: int = 0  # OMV_ESTIMATOR_REFERENCE (0) or OMV_ESTIMATOR_MIS (1)
+    traversal: int = 0  # OMV_TRAVERSAL_AUTO (0) or OMV_TRAVERSAL_PER_RAY (1): same hits either way
 
     def to_c(self) -> capi.Params:
         return capi.Params(camera_bounces=self.cameraBouncesN, light_bounces=self.lightBouncesN, time_kernels=0,
@@ -205,7 +206,7 @@ class RendererParameters:
                            light_scale=self.lightScaleValue, light_min_distance=self.lightMinDistance,
                            ray_cut_value=self.rayCutPixValue, seed=self.seed, estimator=self.estimator,
                            sample_offset=self.sample_offset, accumulate_variance=1 if self.accumulate_variance else 0,
-                           wave_paths=self.wave_paths)
+                           wave_paths=self.wave_paths, traversal=self.traversal)
 
     @classmethod
     def for_scene(cls, scene: scenes.Scene, **kw) -> "RendererParameters":
@@ -271,9 +272,11 @@ class RenderScene:
     """Device scene behind omv_scene_create (RenderScene::commitScene plus the
     GPU acceleration build)."""
 
-    def __init__(self, scene: scenes.Scene, device: int = 0) -> None:
+    def __init__(self, scene: scenes.Scene, device: int = 0, bvh_builder: int = capi.BVH_PLOC) -> None:
+        """bvh_builder: capi.BVH_PLOC (device, default), BVH_LBVH (device) or
+        BVH_HOST_SAH (host threads); hits do not depend on it."""
         self.spec = scene
-        self._holder = capi.DescHolder(scene)
+        self._holder = capi.DescHolder(scene, bvh_builder)
         h = C.c_void_p()
         check(lib().omv_scene_create(C.byref(self._holder.desc), device, C.byref(h)))
         self.handle = h
@@ -396,7 +399,8 @@ class BDPTRenderer:
                                cnt.ctypes.data_as(C.POINTER(C.c_uint32)) if cnt is not None else None, C.byref(st)))
         self.last_stats = {"paths": st.paths, "extension_rays": st.extension_rays, "shadow_rays": st.shadow_rays,
                            "light_rays": st.light_rays, "render_ms": st.render_ms,
-                           "kernel_launches": st.kernel_launches, "stack_overflows": st.stack_overflows}
+                           "kernel_launches": st.kernel_launches, "stack_overflows": st.stack_overflows,
+                           "nodes_visited": st.nodes_visited, "triangles_tested": st.triangles_tested}
         if sums:
             return img, s, q, cnt
         return img

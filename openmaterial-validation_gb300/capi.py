@@ -69,7 +69,10 @@ class SceneDesc(C.Structure):
                 ("num_materials", C.c_int32), ("materials", C.POINTER(MaterialDesc)),
                 ("num_lights", C.c_int32), ("lights", C.POINTER(LightDesc)),
                 ("hdri", C.POINTER(HdriDesc)), ("num_textures", C.c_int32),
-                ("textures", C.POINTER(TextureDesc))]
+                ("textures", C.POINTER(TextureDesc)), ("bvh_builder", C.c_int32)]
+
+
+BVH_PLOC, BVH_LBVH, BVH_HOST_SAH = 0, 1, 2
 
 
 class SceneInfo(C.Structure):
@@ -88,7 +91,11 @@ class Params(C.Structure):
                 ("samples_per_pixel", C.c_int32), ("light_distance_attenuation", C.c_int32),
                 ("light_scale", C.c_float), ("light_min_distance", C.c_float), ("ray_cut_value", C.c_float),
                 ("seed", C.c_uint64), ("estimator", C.c_int32), ("sample_offset", C.c_int32),
-                ("accumulate_variance", C.c_int32), ("wave_paths", C.c_int32), ("time_kernels", C.c_int32)]
+                ("accumulate_variance", C.c_int32), ("wave_paths", C.c_int32), ("time_kernels", C.c_int32),
+                ("traversal", C.c_int32)]
+
+
+TRAVERSAL_AUTO, TRAVERSAL_PER_RAY = 0, 1
 
 
 class Stats(C.Structure):
@@ -202,7 +209,7 @@ def material_set_descs(sets, keep: List[Any]):
 class DescHolder:
     """Keeps every numpy buffer referenced by an omv_scene_desc alive."""
 
-    def __init__(self, scene) -> None:
+    def __init__(self, scene, bvh_builder: int = BVH_PLOC) -> None:
         self.keep: List[Any] = []
         meshes = (MeshDesc * max(1, len(scene.meshes)))()
         for i, m in enumerate(scene.meshes):
@@ -277,4 +284,5 @@ class DescHolder:
                 tds[i].rgba = a.ctypes.data_as(C.POINTER(C.c_uint8))
             self.keep.append(tds)
             d.num_textures, d.textures = len(texs), tds
+        d.bvh_builder = int(bvh_builder)
         self.desc = d

@@ -3,19 +3,23 @@
 // tree per mesh (Embree: one scene per mesh) and one top-level tree over the
 // instances (Embree: instance geometries in the top scene).
 //
-// Pipeline per tree (all on the device):
-//   1. item boxes + centroid bounds (block reduction, atomics on ordered ints)
-//   2. 30-bit Morton codes of the centroids
-//   3. LSD radix sort of (code, item) pairs, 8-bit digits, stable block ranks
-//      from warp match_any + per-warp digit counts
-//   4. Karras LBVH ("Maximizing parallelism in the construction of BVHs,
-//      octrees, and k-d trees", HPG 2012): one thread per internal node
-//   5. bottom-up boxes with arrival counters
-//   6. top-down collapse into 8-wide nodes (greedy: expand the child of largest
-//      surface area; children placed in octant slots), leaves of at most
-//      kLeafMax triangles, child boxes
-//      quantised to 16 bits per bound against the node box, rounded outward and
-//      verified in float so the decoded box always contains the true box.
+// Three builders of the binary tree, one collapse:
+//   OMV_BVH_PLOC (default, on the device): item boxes and per-mesh centroid
+//     bounds; 30-bit Morton codes; LSD radix sort by (mesh, code); parallel
+//     locally-ordered clustering over all meshes at once (Meister and
+//     Bittner 2018), one tree per mesh; leaf counts bottom-up, leaf order and
+//     node ranges by a walk to the root.
+//   OMV_BVH_LBVH (on the device): Morton codes, radix sort, Karras LBVH
+//     ("Maximizing parallelism in the construction of BVHs, octrees, and k-d
+//     trees", HPG 2012), one thread per internal node, boxes bottom-up with
+//     arrival counters; one mesh after another.
+//   OMV_BVH_HOST_SAH: binned surface-area-heuristic trees on host threads.
+// Collapse (device, level by level): top-down into 8-wide nodes (greedy:
+// expand the child of largest surface area; children placed in octant
+// slots), leaves of at most kLeafMax triangles, child boxes quantised to 16
+// bits per bound against the node box, rounded outward and verified in float
+// so the decoded box always contains the true box.  Every box test of the
+// traversal is conservative, so hits do not depend on the builder.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -387,11 +391,33 @@ __device__ __forceinline__ uint32_t quant_exponent(float ext)
     return e;
 }
 
+// The meshes of a bottom-level forest: mesh s owns the items (triangles)
+// [base, base + its face count) of the forest's item numbering.
+struct SegPtr {
+    const float* pos;
+    const uint32_t* faces;
+    uint32_t base;
+};
+
+// segment of item g: the last s with segs[s].base <= g
+__device__ __forceinline__ int segment_of(const SegPtr* segs, int nseg, uint32_t g)
+{
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (segs[mid].base <= g)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
 template <bool kTlas>
 __global__ void k_collapse(int nwork, const Work* __restrict__ work, const Node2* nodes, const uint32_t* vals,
                            const Box* item_boxes, Bvh8Node* out_nodes, uint32_t* node_counter, Work* next_work,
                            uint32_t* next_count, float4* out_tris, uint32_t* out_items, uint32_t* prim_counter,
-                           const float* pos, const uint32_t* faces, uint32_t node_cap, uint32_t* overflow)
+                           const SegPtr* segs, int nseg, uint32_t node_cap, uint32_t* overflow)
 {
     int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nwork) return;
@@ -545,11 +571,13 @@ __global__ void k_collapse(int nwork, const Work* __restrict__ work, const Node2
                 if (kTlas) {
                     out_items[dst] = item;
                 } else {
-                    const uint32_t* f = faces + 3 * (size_t)item;
-                    const float* a0 = pos + 3 * (size_t)f[0];
-                    const float* a1 = pos + 3 * (size_t)f[1];
-                    const float* a2 = pos + 3 * (size_t)f[2];
-                    out_tris[3 * (size_t)dst + 0] = make_float4(a0[0], a0[1], a0[2], __uint_as_float(item));
+                    const SegPtr& sg = segs[segment_of(segs, nseg, item)];
+                    const uint32_t prim = item - sg.base;  // face index within its mesh
+                    const uint32_t* f = sg.faces + 3 * (size_t)prim;
+                    const float* a0 = sg.pos + 3 * (size_t)f[0];
+                    const float* a1 = sg.pos + 3 * (size_t)f[1];
+                    const float* a2 = sg.pos + 3 * (size_t)f[2];
+                    out_tris[3 * (size_t)dst + 0] = make_float4(a0[0], a0[1], a0[2], __uint_as_float(prim));
                     out_tris[3 * (size_t)dst + 1] = make_float4(a1[0], a1[1], a1[2], 0.0f);
                     out_tris[3 * (size_t)dst + 2] = make_float4(a2[0], a2[1], a2[2], 0.0f);
                 }
@@ -580,13 +608,14 @@ struct DBuf {
 
 inline int blocks(size_t n, int t) { return (int)((n + t - 1) / t); }
 
-// sorts (keys, vals) in place; tmp buffers provided
-void radix_sort(int n, uint32_t* keys, uint32_t* vals, uint32_t* k2, uint32_t* v2, cudaStream_t st)
+// sorts (keys, vals) in place by the low 8 * passes key bits (stable, LSD);
+// tmp buffers provided; passes even, so the result ends in (keys, vals)
+void radix_sort(int n, uint32_t* keys, uint32_t* vals, uint32_t* k2, uint32_t* v2, cudaStream_t st, int passes = 4)
 {
     int nb = blocks(n, kSortTile);
     DBuf<uint32_t> hist((size_t)nb * 256);
     uint32_t *ki = keys, *vi = vals, *ko = k2, *vo = v2;
-    for (int shift = 0; shift < 32; shift += 8) {
+    for (int shift = 0; shift < 8 * passes; shift += 8) {
         k_sort_hist<<<nb, 256, 0, st>>>(n, shift, ki, hist.p, nb);
         k_scan<<<1, 1024, 0, st>>>(nb * 256, hist.p);
         k_sort_scatter<<<nb, kSortThreads, 0, st>>>(n, shift, ki, vi, ko, vo, hist.p, nb);
@@ -594,27 +623,297 @@ void radix_sort(int n, uint32_t* keys, uint32_t* vals, uint32_t* k2, uint32_t* v
         std::swap(vi, vo);
     }
     OMV_CK(cudaGetLastError());
-    // four passes: the result is back in (keys, vals)
+}
+
+// ------------------------------------------------------------- PLOC ---
+// Parallel locally-ordered clustering (D. Meister and J. Bittner, "Parallel
+// Locally-Ordered Clustering for Bounding Volume Hierarchy Construction",
+// IEEE TVCG 24(3), 2018): the items of every segment (one mesh, or the
+// instances) start as clusters in Morton order; each round, every cluster
+// finds the cluster within kPlocRadius positions (same segment) whose union
+// box has the smallest surface area, mutual nearest neighbours merge into a
+// new node at the lower position, and the survivors are compacted in order.
+// The globally cheapest pair (ties to the lowest indices) is always mutual,
+// so every round merges at least one pair per segment with two clusters.
+constexpr int kPlocRadius = 16;
+constexpr int kPlocThreads = 256;
+constexpr int kScanBlock = 1024;
+
+__global__ void k_morton_seg(int n, const Box* boxes, const uint32_t* seg_base, int nseg, const uint32_t* cbounds,
+                             uint32_t* keys, uint32_t* vals, uint32_t* segs)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (seg_base[mid] <= (uint32_t)i)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    const uint32_t* cb = cbounds + 6 * lo;
+    uint32_t q[3];
+    for (int a = 0; a < 3; ++a) {
+        const float l = ord2f(cb[a]), h = ord2f(cb[3 + a]);
+        const float c = 0.5f * (boxes[i].lo[a] + boxes[i].hi[a]);
+        const float ext = h - l;
+        const float t = ext > 0.f ? (c - l) / ext : 0.5f;
+        q[a] = (uint32_t)fminf(fmaxf(t * 1024.0f, 0.0f), 1023.0f);
+    }
+    keys[i] = (expand_bits(q[0]) << 2) | (expand_bits(q[1]) << 1) | expand_bits(q[2]);
+    vals[i] = (uint32_t)i;
+    segs[i] = (uint32_t)lo;
+}
+
+// segment of every sorted item (the key of the second, segment-major sort)
+__global__ void k_gather_u32(int n, const uint32_t* idx, const uint32_t* src, uint32_t* dst)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[idx[i]];
+}
+
+// centroid bounds of n boxes into one segment's six ordered ints
+__global__ void k_box_cbounds(int n, const Box* boxes, uint32_t* cbounds)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool ok = i < n;
+    for (int a = 0; a < 3; ++a) {
+        const float c = ok ? 0.5f * (boxes[i].lo[a] + boxes[i].hi[a]) : 0.0f;
+        uint32_t lo = ok ? f2ord(c) : 0xFFFFFFFFu, hi = ok ? f2ord(c) : 0u;
+        for (int o = 16; o; o >>= 1) {
+            lo = min(lo, __shfl_xor_sync(0xFFFFFFFFu, lo, o));
+            hi = max(hi, __shfl_xor_sync(0xFFFFFFFFu, hi, o));
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicMin(&cbounds[a], lo);
+            atomicMax(&cbounds[3 + a], hi);
+        }
+    }
+}
+
+// clusters from the sorted items: leaf i (sorted position) is the reference ~i
+__global__ void k_ploc_init(int n, const uint32_t* vals, const uint32_t* segs, const Box* item_boxes, int* ref,
+                            Box* box, uint32_t* seg, int* leaf_parent)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    ref[i] = ~i;
+    box[i] = item_boxes[vals[i]];
+    seg[i] = segs[i];
+    leaf_parent[i] = -1;
+}
+
+__global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(int c, const Box* __restrict__ box,
+                                                          const uint32_t* __restrict__ seg, int* nn)
+{
+    constexpr int W = kPlocThreads + 2 * kPlocRadius;
+    __shared__ Box sb[W];
+    __shared__ uint32_t ss[W];
+    const int base = blockIdx.x * kPlocThreads - kPlocRadius;
+    for (int t = threadIdx.x; t < W; t += blockDim.x) {
+        const int g = base + t;
+        const bool in = g >= 0 && g < c;
+        ss[t] = in ? seg[g] : 0xFFFFFFFFu;
+        if (in) sb[t] = box[g];
+    }
+    __syncthreads();
+    const int i = blockIdx.x * kPlocThreads + threadIdx.x;
+    if (i >= c) return;
+    const int li = threadIdx.x + kPlocRadius;
+    const Box bi = sb[li];
+    const uint32_t si = ss[li];
+    float best = 3.4e38f;
+    int bj = -1;
+    for (int d = -kPlocRadius; d <= kPlocRadius; ++d) {  // ascending positions: ties keep the lower one
+        if (d == 0 || ss[li + d] != si) continue;
+        const float a = half_area(box_union(bi, sb[li + d]));
+        if (a < best || bj < 0) {
+            best = a;
+            bj = i + d;
+        }
+    }
+    nn[i] = bj;
+}
+
+__device__ __forceinline__ void set_parent(int ref, int p, int* node_parent, int* leaf_parent)
+{
+    if (ref >= 0)
+        node_parent[ref] = p;
+    else
+        leaf_parent[~ref] = p;
+}
+
+__global__ void k_ploc_merge(int c, const int* __restrict__ nn, int* ref, Box* box, uint32_t* keep, uint32_t* counter,
+                             int2* child, Box* node_box, int* node_parent, int* leaf_parent, uint32_t cap,
+                             uint32_t* overflow)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c) return;
+    const int j = nn[i];
+    uint32_t k_ = 1u;
+    if (j >= 0 && nn[j] == i) {
+        if (i < j) {  // this position takes the new node; position j is dropped
+            const uint32_t k = atomicAdd(counter, 1u);
+            if (k >= cap) {
+                atomicAdd(overflow, 1u);
+            } else {
+                const int a = ref[i], b = ref[j];
+                const Box u = box_union(box[i], box[j]);
+                child[k] = make_int2(a, b);
+                node_box[k] = u;
+                node_parent[k] = -1;
+                set_parent(a, (int)k, node_parent, leaf_parent);
+                set_parent(b, (int)k, node_parent, leaf_parent);
+                ref[i] = (int)k;
+                box[i] = u;
+            }
+        } else {
+            k_ = 0u;
+        }
+    }
+    keep[i] = k_;
+}
+
+// kept clusters per block of kScanBlock positions (and in total)
+__global__ void __launch_bounds__(kScanBlock) k_count_kept(int c, const uint32_t* keep, uint32_t* bsum, uint32_t* total)
+{
+    __shared__ uint32_t w[kScanBlock / 32];
+    const int i = blockIdx.x * kScanBlock + threadIdx.x;
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, i < c && keep[i]);
+    if ((threadIdx.x & 31) == 0) w[threadIdx.x >> 5] = __popc(m);
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        uint32_t v = w[threadIdx.x];
+        for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+        if (threadIdx.x == 0) {
+            bsum[blockIdx.x] = v;
+            atomicAdd(total, v);
+        }
+    }
+}
+
+// order-preserving compaction of the kept clusters (block offsets: the
+// exclusive scan of k_count_kept's sums)
+__global__ void __launch_bounds__(kScanBlock) k_compact(int c, const uint32_t* keep, const uint32_t* boff,
+                                                        const int* ref, const Box* box, const uint32_t* seg,
+                                                        int* ref_out, Box* box_out, uint32_t* seg_out)
+{
+    __shared__ uint32_t w[kScanBlock / 32];
+    const int i = blockIdx.x * kScanBlock + threadIdx.x;
+    const bool k = i < c && keep[i];
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, k);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) w[warp] = __popc(m);
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const uint32_t v = w[threadIdx.x];
+        uint32_t x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+            if (lane >= o) x += y;
+        }
+        w[threadIdx.x] = x - v;
+    }
+    __syncthreads();
+    if (!k) return;
+    const uint32_t dst = boff[blockIdx.x] + w[warp] + __popc(m & ((1u << lane) - 1u));
+    ref_out[dst] = ref[i];
+    box_out[dst] = box[i];
+    seg_out[dst] = seg[i];
+}
+
+// roots get the parent code -2 - segment
+__global__ void k_mark_roots(int nseg, const int* ref, int* node_parent, int* leaf_parent)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nseg) set_parent(ref[s], -2 - s, node_parent, leaf_parent);
+}
+
+// leaf counts of the internal nodes, bottom-up with arrival counters
+__global__ void k_ploc_counts(int n, const int* __restrict__ leaf_parent, const int* node_parent, const int2* child,
+                              uint32_t* cnt, uint32_t* arrivals, uint32_t* overflow)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int p = leaf_parent[i];
+    for (int guard = 0; p >= 0; ++guard) {
+        if (guard > 4096) {
+            atomicAdd(overflow, 1u);
+            return;
+        }
+        __threadfence();
+        if (atomicAdd(&arrivals[p], 1u) == 0) return;
+        __threadfence();
+        const int2 ch = child[p];
+        const volatile uint32_t* vc = cnt;
+        const uint32_t a = ch.x >= 0 ? vc[ch.x] : 1u, b = ch.y >= 0 ? vc[ch.y] : 1u;
+        ((volatile uint32_t*)cnt)[p] = a + b;
+        p = node_parent[p];
+    }
+}
+
+// First position of every node's leaves in the final item order (each tree
+// in left-to-right leaf order, segment by segment): the walk to the root adds
+// the leaf count of every left sibling on the way.  Threads [0, n) are the
+// leaves (sorted positions), [n, n + ni) the internal nodes.
+__global__ void k_ploc_place(int n, int ni, const int* leaf_parent, const int* node_parent, const int2* child,
+                             const uint32_t* cnt, const uint32_t* seg_start, const uint32_t* vals, uint32_t* vals_out,
+                             uint32_t* leaf_pos, uint32_t* node_first, uint32_t* overflow)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n + ni) return;
+    int x = t < n ? ~t : t - n;
+    int p = t < n ? leaf_parent[t] : node_parent[t - n];
+    uint32_t off = 0;
+    for (int guard = 0; p >= 0; ++guard) {
+        if (guard > 4096) {
+            atomicAdd(overflow, 1u);
+            return;
+        }
+        const int2 ch = child[p];
+        if (ch.y == x) off += ch.x >= 0 ? cnt[ch.x] : 1u;
+        x = p;
+        p = node_parent[p];
+    }
+    const uint32_t first = seg_start[-2 - p] + off;
+    if (first >= (uint32_t)n) {  // inconsistent counts: reported, never written
+        atomicAdd(overflow, 1u);
+        return;
+    }
+    if (t < n) {
+        leaf_pos[t] = first;
+        vals_out[first] = vals[t];
+    } else {
+        node_first[t - n] = first;
+    }
+}
+
+__global__ void k_ploc_nodes(int ni, const int2* child, const Box* node_box, const int* node_parent,
+                             const uint32_t* cnt, const uint32_t* node_first, const uint32_t* leaf_pos, Node2* out)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ni) return;
+    const int2 ch = child[k];
+    Node2 nd;
+    nd.left = ch.x >= 0 ? ch.x : ~(int)leaf_pos[~ch.x];
+    nd.right = ch.y >= 0 ? ch.y : ~(int)leaf_pos[~ch.y];
+    nd.first = (int)node_first[k];
+    nd.last = (int)(node_first[k] + cnt[k]) - 1;
+    nd.parent = node_parent[k];
+    nd.box = node_box[k];
+    out[k] = nd;
 }
 
 }  // namespace
-
-// Builds one tree over n items whose boxes are in `item_boxes` (device).
-// Appends nodes at node_base... of `out_nodes`, primitives at prim_base... .
-static uint32_t collapse_tree(bool tlas, int n, const Node2* nodes, const uint32_t* vals, const Box* item_boxes,
-                              const float* pos, const uint32_t* faces, Bvh8Node* out_nodes, uint32_t* node_counter,
-                              uint32_t node_cap, float4* out_tris, uint32_t* out_items, uint32_t* prim_counter,
-                              uint32_t* overflow, cudaStream_t st);
 
 // Binary tree by the surface area heuristic, leaves of one item: binned
 // (kSahBins bins per axis over the centroid bounds) on ranges of more than
 // kSweepMax items, a full sweep over every split position below.  nodes[0] is
 // the root; `order` receives the item order the node ranges refer to.  Runs on
-// the host: for the top-level tree and for bottom-level trees of up to
-// kHostSahMaxTris triangles (one thread per mesh).
+// the host (the OMV_BVH_HOST_SAH builder, one thread per mesh).
 constexpr int kSahBins = 32;
 constexpr int kSweepMax = 32;
-constexpr int kHostSahMaxTris = 1 << 21;
 
 static void host_sah_tree(const std::vector<Box>& boxes, std::vector<Node2>& nodes, std::vector<uint32_t>& order)
 {
@@ -764,57 +1063,184 @@ static void host_sah_tree(const std::vector<Box>& boxes, std::vector<Node2>& nod
     }
 }
 
-static uint32_t build_tree(bool tlas, int n, Box* item_boxes, uint32_t* cbounds, const float* pos,
-                           const uint32_t* faces, Bvh8Node* out_nodes, uint32_t* node_counter, uint32_t node_cap,
-                           float4* out_tris, uint32_t* out_items, uint32_t* prim_counter, uint32_t* overflow,
-                           cudaStream_t st)
-{
-    DBuf<uint32_t> keys(n), vals(n), k2(n), v2(n);
-    k_morton<<<blocks(n, 256), 256, 0, st>>>(n, item_boxes, cbounds, keys.p, vals.p);
-    radix_sort(n, keys.p, vals.p, k2.p, v2.p, st);
-    int ni = n > 1 ? n - 1 : 1;
-    DBuf<Node2> nodes(ni);
-    DBuf<int> leaf_parent(n), arrivals(ni);
-    OMV_CK(cudaMemsetAsync(arrivals.p, 0, sizeof(int) * ni, st));
-    if (n > 1) {
-        k_karras<<<blocks(n - 1, 256), 256, 0, st>>>(n, keys.p, nodes.p, leaf_parent.p);
-        k_bottom_up<<<blocks(n, 256), 256, 0, st>>>(n, vals.p, item_boxes, nodes.p, leaf_parent.p, arrivals.p);
+
+// A binary forest ready for the 8-wide collapse: internal nodes, the item
+// order their ranges refer to, and one root reference per tree (an internal
+// node, or ~position for a tree of one item).
+struct Forest {
+    Node2* nodes = nullptr;    // device
+    uint32_t* vals = nullptr;  // device, items in tree order
+    std::vector<int> roots;
+    Forest() = default;
+    Forest(const Forest&) = delete;
+    Forest& operator=(const Forest&) = delete;
+    ~Forest()
+    {
+        cudaFree(nodes);
+        cudaFree(vals);
     }
-    return collapse_tree(tlas, n, nodes.p, vals.p, item_boxes, pos, faces, out_nodes, node_counter, node_cap, out_tris,
-                         out_items, prim_counter, overflow, st);
+    void alloc(int n)
+    {
+        OMV_CK(cudaMalloc(&nodes, sizeof(Node2) * (size_t)std::max(1, n - 1)));
+        OMV_CK(cudaMalloc(&vals, sizeof(uint32_t) * (size_t)std::max(1, n)));
+    }
+};
+
+// Karras LBVH over n items (one tree): 30-bit Morton codes of the centroids
+// against `cbounds`, radix sort, one thread per internal node, boxes bottom-up.
+static void lbvh_tree(int n, const Box* item_boxes, const uint32_t* cbounds, Forest& f, cudaStream_t st)
+{
+    f.alloc(n);
+    DBuf<uint32_t> keys(n), k2(n), v2(n);
+    k_morton<<<blocks(n, 256), 256, 0, st>>>(n, item_boxes, cbounds, keys.p, f.vals);
+    radix_sort(n, keys.p, f.vals, k2.p, v2.p, st);
+    if (n > 1) {
+        DBuf<int> leaf_parent(n), arrivals(n - 1);
+        OMV_CK(cudaMemsetAsync(arrivals.p, 0, sizeof(int) * (n - 1), st));
+        k_karras<<<blocks(n - 1, 256), 256, 0, st>>>(n, keys.p, f.nodes, leaf_parent.p);
+        k_bottom_up<<<blocks(n, 256), 256, 0, st>>>(n, f.vals, item_boxes, f.nodes, leaf_parent.p, arrivals.p);
+        OMV_CK(cudaGetLastError());
+        OMV_CK(cudaStreamSynchronize(st));  // before the temporaries are freed
+    }
+    f.roots = {n > 1 ? 0 : ~0};
 }
 
-// Top-down collapse of a binary tree (nodes[0] the root when n > 1) into 8-wide
-// nodes appended to out_nodes; returns the root's index.
-static uint32_t collapse_tree(bool tlas, int n, const Node2* nodes, const uint32_t* vals, const Box* item_boxes,
-                              const float* pos, const uint32_t* faces, Bvh8Node* out_nodes, uint32_t* node_counter,
-                              uint32_t node_cap, float4* out_tris, uint32_t* out_items, uint32_t* prim_counter,
-                              uint32_t* overflow, cudaStream_t st)
+// PLOC forest: one tree per segment (items [seg_base[s], seg_base[s + 1]),
+// all non-empty), Morton codes against each segment's centroid bounds
+// (cbounds + 6 s), items sorted by (segment, code).
+static void ploc_forest(int n, const std::vector<uint32_t>& seg_base, const Box* item_boxes, const uint32_t* cbounds,
+                        Forest& f, cudaStream_t st)
 {
-    Work root{};
-    root.node2 = n > 1 ? 0 : ~0;
-    uint32_t root_index = 0;
-    OMV_CK(cudaMemcpyAsync(&root_index, node_counter, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    const int nseg = (int)seg_base.size();
+    const int ni = n - nseg;  // internal nodes of the forest
+    f.alloc(n);
+    DBuf<uint32_t> d_seg_base(nseg), keys(n), segs(n), k2(n), v2(n);
+    OMV_CK(cudaMemcpyAsync(d_seg_base.p, seg_base.data(), sizeof(uint32_t) * nseg, cudaMemcpyHostToDevice, st));
+    k_morton_seg<<<blocks(n, 256), 256, 0, st>>>(n, item_boxes, d_seg_base.p, nseg, cbounds, keys.p, f.vals, segs.p);
+    radix_sort(n, keys.p, f.vals, k2.p, v2.p, st);
+    if (nseg > 1) {  // stable second pass by segment: (segment, code) order
+        k_gather_u32<<<blocks(n, 256), 256, 0, st>>>(n, f.vals, segs.p, keys.p);
+        radix_sort(n, keys.p, f.vals, k2.p, v2.p, st, nseg <= 256 ? 2 : 4);
+    } else {
+        OMV_CK(cudaMemsetAsync(keys.p, 0, sizeof(uint32_t) * n, st));
+    }
+    // clusters (ping-pong), nodes, parents
+    DBuf<int> ref0(n), ref1(n), nn(n), leaf_parent(n), node_parent(std::max(1, ni));
+    DBuf<Box> box0(n), box1(n), node_box(std::max(1, ni));
+    DBuf<uint32_t> seg0(n), seg1(n), keep(n), bsum(blocks(n, kScanBlock)), ctr(3);  // nodes, kept, overflow
+    DBuf<int2> child(std::max(1, ni));
+    OMV_CK(cudaMemsetAsync(ctr.p, 0, sizeof(uint32_t) * 3, st));
+    k_ploc_init<<<blocks(n, 256), 256, 0, st>>>(n, f.vals, keys.p, item_boxes, ref0.p, box0.p, seg0.p, leaf_parent.p);
+    int c = n;
+    int* ref = ref0.p;
+    Box* box = box0.p;
+    uint32_t* seg = seg0.p;
+    int* ref_o = ref1.p;
+    Box* box_o = box1.p;
+    uint32_t* seg_o = seg1.p;
+    for (int round = 0; c > nseg; ++round) {
+        if (round > 10000) throw std::runtime_error("PLOC build did not converge");
+        k_ploc_nn<<<blocks(c, kPlocThreads), kPlocThreads, 0, st>>>(c, box, seg, nn.p);
+        k_ploc_merge<<<blocks(c, 256), 256, 0, st>>>(c, nn.p, ref, box, keep.p, ctr.p, child.p, node_box.p,
+                                                     node_parent.p, leaf_parent.p, (uint32_t)std::max(0, ni), ctr.p + 2);
+        const int nb = blocks(c, kScanBlock);
+        OMV_CK(cudaMemsetAsync(ctr.p + 1, 0, sizeof(uint32_t), st));
+        k_count_kept<<<nb, kScanBlock, 0, st>>>(c, keep.p, bsum.p, ctr.p + 1);
+        k_scan<<<1, 1024, 0, st>>>(nb, bsum.p);
+        k_compact<<<nb, kScanBlock, 0, st>>>(c, keep.p, bsum.p, ref, box, seg, ref_o, box_o, seg_o);
+        OMV_CK(cudaGetLastError());
+        uint32_t h[3];
+        OMV_CK(cudaMemcpyAsync(h, ctr.p, sizeof(h), cudaMemcpyDeviceToHost, st));
+        OMV_CK(cudaStreamSynchronize(st));
+        if (h[2]) throw std::runtime_error("PLOC build: node capacity exceeded");
+        if ((int)h[1] >= c) throw std::runtime_error("PLOC build made no progress");
+        c = (int)h[1];
+        std::swap(ref, ref_o);
+        std::swap(box, box_o);
+        std::swap(seg, seg_o);
+    }
+    // final item order and Node2 records (ranges of consecutive positions)
+    DBuf<uint32_t> cnt(std::max(1, ni)), arrivals(std::max(1, ni)), node_first(std::max(1, ni)), leaf_pos(n),
+        d_seg_start(nseg), vals_out(n);
+    OMV_CK(cudaMemcpyAsync(d_seg_start.p, seg_base.data(), sizeof(uint32_t) * nseg, cudaMemcpyHostToDevice, st));
+    OMV_CK(cudaMemsetAsync(arrivals.p, 0, sizeof(uint32_t) * std::max(1, ni), st));
+    k_mark_roots<<<blocks(nseg, 256), 256, 0, st>>>(nseg, ref, node_parent.p, leaf_parent.p);
+    k_ploc_counts<<<blocks(n, 256), 256, 0, st>>>(n, leaf_parent.p, node_parent.p, child.p, cnt.p, arrivals.p,
+                                                  ctr.p + 2);
+    k_ploc_place<<<blocks(n + ni, 256), 256, 0, st>>>(n, ni, leaf_parent.p, node_parent.p, child.p, cnt.p,
+                                                      d_seg_start.p, f.vals, vals_out.p, leaf_pos.p, node_first.p,
+                                                      ctr.p + 2);
+    if (ni > 0)
+        k_ploc_nodes<<<blocks(ni, 256), 256, 0, st>>>(ni, child.p, node_box.p, node_parent.p, cnt.p, node_first.p,
+                                                      leaf_pos.p, f.nodes);
+    OMV_CK(cudaMemcpyAsync(f.vals, vals_out.p, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st));
+    OMV_CK(cudaGetLastError());
+    std::vector<int> roots(nseg);
+    uint32_t ov = 0;
+    OMV_CK(cudaMemcpyAsync(roots.data(), ref, sizeof(int) * nseg, cudaMemcpyDeviceToHost, st));
+    OMV_CK(cudaMemcpyAsync(&ov, ctr.p + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     OMV_CK(cudaStreamSynchronize(st));
-    root.node8 = root_index;
-    uint32_t one = root_index + 1;
-    OMV_CK(cudaMemcpyAsync(node_counter, &one, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-    DBuf<Work> wa(n + 1), wb(n + 1);
+    if (ov) throw std::runtime_error("PLOC build: inconsistent tree (deeper than 4096 levels or bad leaf counts)");
+    for (int s = 0; s < nseg; ++s) {
+        if (roots[s] < 0) {  // a one-item tree: its item's final position
+            uint32_t pos = 0;
+            OMV_CK(cudaMemcpy(&pos, leaf_pos.p + ~roots[s], sizeof(uint32_t), cudaMemcpyDeviceToHost));
+            roots[s] = ~(int)pos;
+        }
+    }
+    f.roots = roots;
+}
+
+// host SAH tree over n boxes (one tree)
+static void host_sah_forest(const std::vector<Box>& boxes, Forest& f, cudaStream_t st)
+{
+    const int n = (int)boxes.size();
+    std::vector<Node2> nodes;
+    std::vector<uint32_t> order;
+    host_sah_tree(boxes, nodes, order);
+    f.alloc(n);
+    if (!nodes.empty())
+        OMV_CK(cudaMemcpyAsync(f.nodes, nodes.data(), sizeof(Node2) * nodes.size(), cudaMemcpyHostToDevice, st));
+    OMV_CK(cudaMemcpyAsync(f.vals, order.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, st));
+    OMV_CK(cudaStreamSynchronize(st));  // the host vectors go out of scope
+    f.roots = {n > 1 ? 0 : ~0};
+}
+
+// Top-down collapse of a binary forest into 8-wide nodes appended to
+// out_nodes (counters: nodes, primitives, overflow); returns each tree's root.
+static std::vector<uint32_t> collapse_forest(bool tlas, const Forest& f, int nitems, const Box* item_boxes,
+                                             const SegPtr* segs, int nseg, Bvh8Node* out_nodes, uint32_t* counters,
+                                             uint32_t node_cap, float4* out_tris, uint32_t* out_items,
+                                             cudaStream_t st)
+{
+    const int nroots = (int)f.roots.size();
+    uint32_t root_index = 0;
+    OMV_CK(cudaMemcpyAsync(&root_index, counters, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    OMV_CK(cudaStreamSynchronize(st));
+    std::vector<Work> roots(nroots);
+    std::vector<uint32_t> out(nroots);
+    for (int r = 0; r < nroots; ++r) {
+        roots[r] = Work{f.roots[r], root_index + (uint32_t)r};
+        out[r] = root_index + (uint32_t)r;
+    }
+    const uint32_t next = root_index + (uint32_t)nroots;
+    OMV_CK(cudaMemcpyAsync(counters, &next, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    DBuf<Work> wa(nitems + nroots), wb(nitems + nroots);
     DBuf<uint32_t> cnt(1);
-    OMV_CK(cudaMemcpyAsync(wa.p, &root, sizeof(Work), cudaMemcpyHostToDevice, st));
-    int nwork = 1;
+    OMV_CK(cudaMemcpyAsync(wa.p, roots.data(), sizeof(Work) * nroots, cudaMemcpyHostToDevice, st));
+    int nwork = nroots;
     Work *cur = wa.p, *nxt = wb.p;
     for (int level = 0; nwork > 0; ++level) {
         if (level > 200) throw std::runtime_error("BVH collapse did not terminate");
         OMV_CK(cudaMemsetAsync(cnt.p, 0, sizeof(uint32_t), st));
         if (tlas)
-            k_collapse<true><<<blocks(nwork, 128), 128, 0, st>>>(nwork, cur, nodes, vals, item_boxes, out_nodes,
-                                                                 node_counter, nxt, cnt.p, out_tris, out_items,
-                                                                 prim_counter, pos, faces, node_cap, overflow);
+            k_collapse<true><<<blocks(nwork, 128), 128, 0, st>>>(nwork, cur, f.nodes, f.vals, item_boxes, out_nodes,
+                                                                 counters, nxt, cnt.p, out_tris, out_items,
+                                                                 counters + 1, segs, nseg, node_cap, counters + 2);
         else
-            k_collapse<false><<<blocks(nwork, 128), 128, 0, st>>>(nwork, cur, nodes, vals, item_boxes, out_nodes,
-                                                                  node_counter, nxt, cnt.p, out_tris, out_items,
-                                                                  prim_counter, pos, faces, node_cap, overflow);
+            k_collapse<false><<<blocks(nwork, 128), 128, 0, st>>>(nwork, cur, f.nodes, f.vals, item_boxes, out_nodes,
+                                                                  counters, nxt, cnt.p, out_tris, out_items,
+                                                                  counters + 1, segs, nseg, node_cap, counters + 2);
         OMV_CK(cudaGetLastError());
         uint32_t h = 0;
         OMV_CK(cudaMemcpyAsync(&h, cnt.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
@@ -822,45 +1248,89 @@ static uint32_t collapse_tree(bool tlas, int n, const Node2* nodes, const uint32
         nwork = (int)h;
         std::swap(cur, nxt);
     }
-    return root_index;
+    return out;
 }
 
 void validate_accel(const AccelResult& a, const std::vector<MeshGeom>& meshes, cudaStream_t st);
 
-void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<InstanceGeom>& insts, AccelResult& out,
-                 cudaStream_t st)
+void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<InstanceGeom>& insts, BvhBuilder builder,
+                 AccelResult& out, cudaStream_t st)
 {
     size_t total_tri = 0;
-    for (const auto& m : meshes) total_tri += m.num_faces;
+    for (const auto& m : meshes) total_tri += m.valid ? m.num_faces : 0;
     const uint32_t node_cap = (uint32_t)(total_tri + 2 * meshes.size() + 2 * insts.size() + 16);
     OMV_CK(cudaMalloc(&out.nodes, sizeof(Bvh8Node) * node_cap));
     OMV_CK(cudaMalloc(&out.tris, sizeof(float4) * 3 * (total_tri ? total_tri : 1)));
     OMV_CK(cudaMalloc(&out.tlas_items, sizeof(uint32_t) * (insts.size() ? insts.size() : 1)));
     DBuf<uint32_t> counters(3);  // nodes, prims, overflow
     OMV_CK(cudaMemsetAsync(counters.p, 0, sizeof(uint32_t) * 3, st));
-    DBuf<uint32_t> cb(6);
     out.blas_root.assign(meshes.size(), 0xFFFFFFFFu);
-    // host SAH trees for the meshes that are small enough, one thread per mesh
-    struct HostTree {
-        std::vector<Box> boxes;
-        std::vector<Node2> nodes;
-        std::vector<uint32_t> order;
-    };
-    std::vector<HostTree> ht(meshes.size());
-    {
-        std::vector<size_t> todo;
-        for (size_t mi = 0; mi < meshes.size(); ++mi)
-            if (meshes[mi].valid && meshes[mi].num_faces > 0 && meshes[mi].num_faces <= kHostSahMaxTris &&
-                meshes[mi].h_pos && meshes[mi].h_faces)
-                todo.push_back(mi);
+    std::vector<size_t> todo;  // meshes with triangles
+    for (size_t mi = 0; mi < meshes.size(); ++mi)
+        if (meshes[mi].valid && meshes[mi].num_faces > 0) todo.push_back(mi);
+
+    // ---- bottom level: one tree per mesh
+    if (builder == BvhBuilder::Ploc && !todo.empty()) {
+        // every mesh in one PLOC forest: one launch sequence for all of them
+        std::vector<uint32_t> seg_base(todo.size());
+        std::vector<SegPtr> segs(todo.size());
+        uint32_t n = 0;
+        for (size_t s = 0; s < todo.size(); ++s) {
+            const MeshGeom& m = meshes[todo[s]];
+            seg_base[s] = n;
+            segs[s] = SegPtr{m.d_pos, m.d_faces, n};
+            n += (uint32_t)m.num_faces;
+        }
+        DBuf<Box> boxes(n);
+        DBuf<uint32_t> cb(6 * todo.size());
+        DBuf<SegPtr> d_segs(todo.size());
+        std::vector<uint32_t> init(6 * todo.size());
+        for (size_t s = 0; s < todo.size(); ++s)
+            for (int a = 0; a < 3; ++a) {
+                init[6 * s + a] = 0xFFFFFFFFu;
+                init[6 * s + 3 + a] = 0u;
+            }
+        OMV_CK(cudaMemcpyAsync(cb.p, init.data(), sizeof(uint32_t) * init.size(), cudaMemcpyHostToDevice, st));
+        OMV_CK(cudaMemcpyAsync(d_segs.p, segs.data(), sizeof(SegPtr) * segs.size(), cudaMemcpyHostToDevice, st));
+        for (size_t s = 0; s < todo.size(); ++s) {
+            const MeshGeom& m = meshes[todo[s]];
+            k_tri_boxes<<<blocks(m.num_faces, 256), 256, 0, st>>>(m.num_faces, m.d_pos, m.d_faces,
+                                                                  boxes.p + seg_base[s], cb.p + 6 * s);
+        }
+        OMV_CK(cudaGetLastError());
+        Forest f;
+        ploc_forest((int)n, seg_base, boxes.p, cb.p, f, st);
+        const std::vector<uint32_t> roots = collapse_forest(false, f, (int)n, boxes.p, d_segs.p, (int)todo.size(),
+                                                            out.nodes, counters.p, node_cap, out.tris, nullptr, st);
+        for (size_t s = 0; s < todo.size(); ++s) out.blas_root[todo[s]] = roots[s];
+    } else if (builder == BvhBuilder::Lbvh) {
+        DBuf<uint32_t> cb(6);
+        DBuf<SegPtr> d_seg(1);
+        for (size_t mi : todo) {
+            const MeshGeom& m = meshes[mi];
+            DBuf<Box> boxes(m.num_faces);
+            const uint32_t init[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
+            const SegPtr sp{m.d_pos, m.d_faces, 0u};
+            OMV_CK(cudaMemcpyAsync(cb.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
+            OMV_CK(cudaMemcpyAsync(d_seg.p, &sp, sizeof(sp), cudaMemcpyHostToDevice, st));
+            k_tri_boxes<<<blocks(m.num_faces, 256), 256, 0, st>>>(m.num_faces, m.d_pos, m.d_faces, boxes.p, cb.p);
+            OMV_CK(cudaGetLastError());
+            Forest f;
+            lbvh_tree(m.num_faces, boxes.p, cb.p, f, st);
+            out.blas_root[mi] = collapse_forest(false, f, m.num_faces, boxes.p, d_seg.p, 1, out.nodes, counters.p,
+                                                node_cap, out.tris, nullptr, st)[0];
+        }
+    } else if (builder == BvhBuilder::HostSah) {
+        // binned-SAH trees on the host, one thread per mesh
+        std::vector<std::vector<Box>> hb(meshes.size());
         std::atomic<size_t> next{0};
         auto worker = [&]() {
             for (size_t j; (j = next.fetch_add(1)) < todo.size();) {
                 const MeshGeom& m = meshes[todo[j]];
-                HostTree& t = ht[todo[j]];
-                t.boxes.resize(m.num_faces);
+                std::vector<Box>& bx = hb[todo[j]];
+                bx.resize(m.num_faces);
                 for (int f = 0; f < m.num_faces; ++f) {
-                    Box& b = t.boxes[f];
+                    Box& b = bx[f];
                     for (int a = 0; a < 3; ++a) {
                         b.lo[a] = 3.0e38f;
                         b.hi[a] = -3.0e38f;
@@ -870,7 +1340,7 @@ void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<Instance
                         const float* p = m.h_pos + 3 * (size_t)m.h_faces[3 * (size_t)f + k];
                         for (int a = 0; a < 3; ++a) finite = finite && std::isfinite(p[a]);
                     }
-                    if (!finite) continue;  // empty box: left out of the tree, as in k_tri_boxes
+                    if (!finite) continue;  // empty box: no effect on any bound, as in k_tri_boxes
                     for (int k = 0; k < 3; ++k) {
                         const float* p = m.h_pos + 3 * (size_t)m.h_faces[3 * (size_t)f + k];
                         for (int a = 0; a < 3; ++a) {
@@ -879,7 +1349,6 @@ void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<Instance
                         }
                     }
                 }
-                host_sah_tree(t.boxes, t.nodes, t.order);
             }
         };
         const unsigned nt = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), (unsigned)todo.size()));
@@ -887,38 +1356,22 @@ void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<Instance
         for (unsigned k = 1; k < nt; ++k) pool.emplace_back(worker);
         worker();
         for (auto& th : pool) th.join();
-    }
-    for (size_t mi = 0; mi < meshes.size(); ++mi) {
-        const MeshGeom& m = meshes[mi];
-        if (!m.valid || m.num_faces <= 0) continue;
-        const HostTree& t = ht[mi];
-        if (!t.boxes.empty()) {
-            const int n = m.num_faces;
-            DBuf<Box> boxes(n);
-            DBuf<uint32_t> vals(n);
-            DBuf<Node2> d_nodes(std::max<size_t>(1, t.nodes.size()));
-            OMV_CK(cudaMemcpyAsync(boxes.p, t.boxes.data(), sizeof(Box) * n, cudaMemcpyHostToDevice, st));
-            OMV_CK(cudaMemcpyAsync(vals.p, t.order.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, st));
-            if (!t.nodes.empty())
-                OMV_CK(cudaMemcpyAsync(d_nodes.p, t.nodes.data(), sizeof(Node2) * t.nodes.size(),
-                                       cudaMemcpyHostToDevice, st));
-            out.blas_root[mi] = collapse_tree(false, n, d_nodes.p, vals.p, boxes.p, m.d_pos, m.d_faces, out.nodes,
-                                              counters.p, node_cap, out.tris, nullptr, counters.p + 1, counters.p + 2,
-                                              st);
-            continue;
+        DBuf<SegPtr> d_seg(1);
+        for (size_t mi : todo) {
+            const MeshGeom& m = meshes[mi];
+            DBuf<Box> boxes(m.num_faces);
+            const SegPtr sp{m.d_pos, m.d_faces, 0u};
+            OMV_CK(cudaMemcpyAsync(boxes.p, hb[mi].data(), sizeof(Box) * m.num_faces, cudaMemcpyHostToDevice, st));
+            OMV_CK(cudaMemcpyAsync(d_seg.p, &sp, sizeof(sp), cudaMemcpyHostToDevice, st));
+            Forest f;
+            host_sah_forest(hb[mi], f, st);
+            out.blas_root[mi] = collapse_forest(false, f, m.num_faces, boxes.p, d_seg.p, 1, out.nodes, counters.p,
+                                                node_cap, out.tris, nullptr, st)[0];
         }
-        // very large meshes: device LBVH
-        DBuf<Box> boxes(m.num_faces);
-        uint32_t init[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
-        OMV_CK(cudaMemcpyAsync(cb.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
-        k_tri_boxes<<<blocks(m.num_faces, 256), 256, 0, st>>>(m.num_faces, m.d_pos, m.d_faces, boxes.p, cb.p);
-        OMV_CK(cudaGetLastError());
-        out.blas_root[mi] = build_tree(false, m.num_faces, boxes.p, cb.p, m.d_pos, m.d_faces, out.nodes, counters.p,
-                                       node_cap, out.tris, nullptr, counters.p + 1, counters.p + 2, st);
     }
-    // top level: world boxes of the valid instances (their referenced vertices
-    // through the instance transform), widened so that no object-space hit is
-    // ever culled by world-space rounding
+    // ---- top level: world boxes of the valid instances (their referenced
+    // vertices through the instance transform), widened so that no
+    // object-space hit is ever culled by world-space rounding
     std::vector<uint32_t> ids;
     for (size_t i = 0; i < insts.size(); ++i)
         if (insts[i].valid) ids.push_back((uint32_t)i);
@@ -964,20 +1417,25 @@ void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<Instance
     out.num_valid_instances = (uint32_t)ib.size();
     if (!ib.empty()) {
         const int n = (int)ib.size();
-        std::vector<Node2> h_nodes;
-        std::vector<uint32_t> h_order;
-        host_sah_tree(ib, h_nodes, h_order);
         DBuf<Box> boxes(n);
-        DBuf<uint32_t> vals(n);
-        DBuf<Node2> d_nodes(std::max<size_t>(1, h_nodes.size()));
         OMV_CK(cudaMemcpyAsync(boxes.p, ib.data(), sizeof(Box) * n, cudaMemcpyHostToDevice, st));
-        OMV_CK(cudaMemcpyAsync(vals.p, h_order.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, st));
-        if (!h_nodes.empty())
-            OMV_CK(cudaMemcpyAsync(d_nodes.p, h_nodes.data(), sizeof(Node2) * h_nodes.size(), cudaMemcpyHostToDevice,
-                                   st));
+        Forest f;
+        if (builder == BvhBuilder::HostSah) {
+            host_sah_forest(ib, f, st);
+        } else {
+            DBuf<uint32_t> cb(6);
+            const uint32_t init[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
+            OMV_CK(cudaMemcpyAsync(cb.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
+            k_box_cbounds<<<blocks(n, 256), 256, 0, st>>>(n, boxes.p, cb.p);
+            OMV_CK(cudaGetLastError());
+            if (builder == BvhBuilder::Lbvh)
+                lbvh_tree(n, boxes.p, cb.p, f, st);
+            else
+                ploc_forest(n, std::vector<uint32_t>{0u}, boxes.p, cb.p, f, st);
+        }
         OMV_CK(cudaMemsetAsync(counters.p + 1, 0, sizeof(uint32_t), st));
-        out.tlas_root = collapse_tree(true, n, d_nodes.p, vals.p, boxes.p, nullptr, nullptr, out.nodes, counters.p,
-                                      node_cap, nullptr, out.tlas_items, counters.p + 1, counters.p + 2, st);
+        out.tlas_root = collapse_forest(true, f, n, boxes.p, nullptr, 0, out.nodes, counters.p, node_cap, nullptr,
+                                        out.tlas_items, st)[0];
         // TLAS items are positions in `ids`; translate to instance indices
         std::vector<uint32_t> items(n);
         OMV_CK(cudaMemcpyAsync(items.data(), out.tlas_items, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, st));

@@ -38,8 +38,10 @@ struct AccelResult {
     uint32_t num_valid_instances = 0;
 };
 
+enum class BvhBuilder { Ploc = 0, Lbvh = 1, HostSah = 2 };  // OMV_BVH_PLOC / _LBVH / _HOST_SAH
+
 // Builds every BLAS and the TLAS; throws std::runtime_error on CUDA errors.
-void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<InstanceGeom>& insts, AccelResult& out,
-                 cudaStream_t stream);
+void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<InstanceGeom>& insts, BvhBuilder builder,
+                 AccelResult& out, cudaStream_t stream);
 
 }  // namespace omv

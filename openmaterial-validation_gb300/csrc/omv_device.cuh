@@ -5,12 +5,15 @@
 // setup, camera rays, instance transforms, the triangle test) use explicit
 // round-to-nearest intrinsics (__fmul_rn/__fadd_rn/...), which the compiler
 // never fuses into FMAs.  Everything else may be contracted; it is checked
-// against the oracle within 1e-5 relative.
+// against the oracle within 1e-5 relative.  The reference's float library
+// calls on that path (sin, cos, pow, acos, asin) are evaluated correctly
+// rounded (crmath.cuh).
 #pragma once
 
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "crmath.cuh"
 #include "omv_types.h"
 
 namespace omv {
@@ -207,7 +210,8 @@ __device__ __forceinline__ float ggx_pdf(float c, float alpha)
     float l = lerpf(1.0f, a2, c2);
     return a2 / (kPi * (l * l));
 }
-__device__ __forceinline__ float ggx_lambda(float a) { return 0.5f * (sqrtf(1.0f + 1.0f / (a * a)) - 1.0f); }
+// std::pow(a, -2.0f) (BRDFModel.h:55) correctly rounded
+__device__ __forceinline__ float ggx_lambda(float a) { return 0.5f * (sqrtf(1.0f + cr::rcp_sq_cr(a)) - 1.0f); }
 __device__ __forceinline__ float smith_g1(float c, float alpha)
 {
     float a = c / (alpha * sqrtf(1.0f - c * c));
@@ -218,11 +222,9 @@ __device__ __forceinline__ float smith_g2(float s, float m)
     float p = s * m;
     return p / (s + m - p);
 }
-__device__ __forceinline__ float pow5(float x)
-{
-    float x2 = x * x;
-    return x2 * x2 * x;
-}
+// std::pow(x, 5.0f) (BRDFModel.h:180, 231) correctly rounded for x >= 2^-20
+// (below, x^5 < 2^-100 and the Schlick term it feeds does not see it)
+__device__ __forceinline__ float pow5(float x) { return cr::pow5_cr(x); }
 
 struct BsdfIn {
     V3 I, N, T;
@@ -298,7 +300,7 @@ __device__ __forceinline__ V3 ggx_hemisphere(float alpha2, float uphi, float rnd
     float cth = sqrtf((1.f - rnd) / (1.f - (1.0f - alpha2) * rnd));
     float sth = sqrtf(fmaxf(1.0f - cth * cth, 0.0f));
     float s, c;
-    sincosf(phi, &s, &c);
+    cr::sincos_cr(phi, s, c);
     return v3(sth * c, sth * s, cth);
 }
 __device__ __forceinline__ V3 cosine_hemisphere(float uphi, float rnd)
@@ -306,7 +308,7 @@ __device__ __forceinline__ V3 cosine_hemisphere(float uphi, float rnd)
     float phi = (2.0f * kPi) * uphi;
     float sth = sqrtf(rnd);
     float s, c;
-    sincosf(phi, &s, &c);
+    cr::sincos_cr(phi, s, c);
     return v3(sth * c, sth * s, sqrtf(1.0f - rnd));
 }
 __device__ __forceinline__ V3 uniform_hemisphere(float uphi, float cth)
@@ -314,7 +316,7 @@ __device__ __forceinline__ V3 uniform_hemisphere(float uphi, float cth)
     float phi = (2.0f * kPi) * uphi;
     float sth = sqrtf(fmaxf(1.0f - cth * cth, 0.0f));
     float s, c;
-    sincosf(phi, &s, &c);
+    cr::sincos_cr(phi, s, c);
     return v3(sth * c, sth * s, cth);
 }
 // transformToNormalSpace (BRDFModel.h:25-34)
@@ -481,9 +483,9 @@ __device__ __forceinline__ V3 env_radiance(const DevEnv& e, V3 dir)
     V3 rd = v3(R[0] * dir.x + R[3] * dir.y + R[6] * dir.z, R[1] * dir.x + R[4] * dir.y + R[7] * dir.z,
                R[2] * dir.x + R[5] * dir.y + R[8] * dir.z);
     V3 rxy = normalize(v3(rd.x, rd.y, 0.0f));
-    float xang = acosf(clampf(rxy.x, -1.0f, 1.0f));
+    float xang = cr::acos_cr(clampf(rxy.x, -1.0f, 1.0f));
     xang = rxy.y < 0.0f ? 2.0f * kPi - xang : xang;
-    float yang = asinf(clampf(rd.z, -1.0f, 1.0f)) + 0.5f * kPi;
+    float yang = cr::asin_cr(clampf(rd.z, -1.0f, 1.0f)) + 0.5f * kPi;
     float u = xang / (2.0f * kPi);
     float v = 1.0f - yang / kPi;
     const int W = e.width, H = e.height;
@@ -510,9 +512,9 @@ __device__ __forceinline__ void env_uv(const DevEnv& e, V3 dir, float& u, float&
     V3 rd = v3(R[0] * dir.x + R[3] * dir.y + R[6] * dir.z, R[1] * dir.x + R[4] * dir.y + R[7] * dir.z,
                R[2] * dir.x + R[5] * dir.y + R[8] * dir.z);
     V3 rxy = normalize(v3(rd.x, rd.y, 0.0f));
-    float xang = acosf(clampf(rxy.x, -1.0f, 1.0f));
+    float xang = cr::acos_cr(clampf(rxy.x, -1.0f, 1.0f));
     xang = rxy.y < 0.0f ? 2.0f * kPi - xang : xang;
-    float yang = asinf(clampf(rd.z, -1.0f, 1.0f)) + 0.5f * kPi;
+    float yang = cr::asin_cr(clampf(rd.z, -1.0f, 1.0f)) + 0.5f * kPi;
     u = xang / (2.0f * kPi);
     v = 1.0f - yang / kPi;
 }

@@ -33,12 +33,11 @@ def test_sample_indirect_matches_reference(gpu, oracle):
         x[i, 17:20] = oracle.mt_uniforms(int(s), 3)
     y = gpu.brdf_sample_indirect(x)
     ref = g["y"]
-    ok = _close(y, ref, rtol=1e-4).all(1)
-    # a branch decision (u < p, dot(N,O) > 0) taken on a value within an ulp of
-    # its threshold may go the other way; such cases must stay rare
-    assert ok.mean() > 0.995, ok.mean()
-    dirs_ok = _close(y[:, :3], ref[:, :3], rtol=1e-4).all(1)
-    assert dirs_ok.mean() > 0.995
+    # directions and weights within 1e-5 on every case: the device evaluates the
+    # reference's std::sin / std::cos / std::pow correctly rounded (crmath.cuh),
+    # and the reference's float order otherwise
+    ok = _close(y, ref).all(1)
+    assert ok.all(), (np.flatnonzero(~ok)[:10], y[~ok][:3], ref[~ok][:3])
 
 
 def test_openmaterial_fresnel_matches_reference(gpu):
@@ -65,8 +64,6 @@ def test_background_lookup_matches_reference(gpu, scenes):
     sc.hdri = scenes.Hdri(g["image"], g["rotation"], float(g["scale"]))
     rs = gpu.RenderScene(sc)
     y = rs.env_radiance(g["dirs"])
-    # acos/asin of the device libm differ in the last bits: the texel weights
-    # move by ~1e-7, so the radiance agrees to the same relative order
-    ok = _close(y, g["y"], rtol=1e-4, atol_frac=1e-5)
-    assert ok.all(1).mean() > 0.999
-    assert np.abs(y.sum() / g["y"].sum() - 1) < 1e-5
+    # every direction within 1e-5 (acos / asin correctly rounded on the device)
+    ok = _close(y, g["y"]).all(1)
+    assert ok.all(), (np.flatnonzero(~ok)[:10], y[~ok][:3], g["y"][~ok][:3])

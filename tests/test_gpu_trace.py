@@ -9,6 +9,11 @@ pytestmark = pytest.mark.gpu
 
 FLT_MAX = np.float32(3.402823466e38)
 
+# every acceleration-structure builder must give the same hits: the box tests
+# are conservative and the hit contract (closest t, then lowest instance and
+# primitive) does not depend on the tree
+BUILDERS = pytest.mark.parametrize("builder", [0, 1, 2], ids=["ploc", "lbvh", "host_sah"])
+
 
 def _hits_equal(a, b):
     for k in ("inst", "geom", "prim", "material"):
@@ -36,14 +41,15 @@ def test_reference_rays_give_reference_ids(gpu, scenes):
         assert np.array_equal(hits[k][hit].view(np.uint32), g[k][hit].view(np.uint32)), k
 
 
-def test_id_pass_with_reference_jitter_full_c1(gpu, oracle, scenes):
+@BUILDERS
+def test_id_pass_with_reference_jitter_full_c1(gpu, oracle, scenes, builder):
     """C1 material-ID pass at 256x256: GPU raygen + trace with the reference's
     jitter stream equals the oracle replay (itself pinned bit-exact to the
     reference binary) for every pixel."""
     sc = scenes.scene_c1(256, 256, 1)
     _, ref = oracle.OracleScene(sc).render_ids()
     jitter = oracle.mt_uniforms(oracle.REFERENCE_SEED, 2 * 256 * 256)
-    rs = gpu.RenderScene(sc)
+    rs = gpu.RenderScene(sc, bvh_builder=builder)
     r = gpu.BDPTRenderer()
     r.set_scene(rs)
     hits, gprim = r.render_ids(gpu.PinholeCamera.from_spec(sc.camera), jitter=jitter)
@@ -67,11 +73,12 @@ def _random_rays(rng, n, lo, hi, spread=1.0):
     return r
 
 
-def test_large_instanced_scene_matches_oracle(gpu, oracle, scenes):
+@BUILDERS
+def test_large_instanced_scene_matches_oracle(gpu, oracle, scenes, builder):
     """1M-triangle scene, 64 rotated/scaled instances: GPU hits equal the
     oracle's on camera rays and on random rays (bit-exact)."""
     sc = scenes.scene_c2(160, 90, 1)
-    rs = gpu.RenderScene(sc)
+    rs = gpu.RenderScene(sc, bvh_builder=builder)
     os_ = oracle.OracleScene(sc)
     rng = np.random.default_rng(5)
     cam = rays_from_camera(oracle, sc)
@@ -93,11 +100,12 @@ def rays_from_camera(oracle, sc):
     return r
 
 
-def test_edge_cases_match_oracle(gpu, oracle, scenes):
+@BUILDERS
+def test_edge_cases_match_oracle(gpu, oracle, scenes, builder):
     """Shared edges (ties between the two ground triangles), vertices, grazing
     rays, zero/NaN directions, empty intervals, origins on surfaces."""
     sc = scenes.scene_mixed(8, 8, 1)
-    rs = gpu.RenderScene(sc)
+    rs = gpu.RenderScene(sc, bvh_builder=builder)
     os_ = oracle.OracleScene(sc)
     rows = []
     # rays through the ground quad's diagonal (shared edge) and its corners
@@ -124,11 +132,12 @@ def test_edge_cases_match_oracle(gpu, oracle, scenes):
     assert ok, msg
 
 
-def test_alpha_masked_material_is_skipped_like_reference(gpu, oracle, scenes):
+@BUILDERS
+def test_alpha_masked_material_is_skipped_like_reference(gpu, oracle, scenes, builder):
     sc = scenes.scene_mixed(8, 8, 1)
     sc.materials[3].alpha_mode = 1  # MASK with base alpha 0.5 < cutoff 0.75
     sc.materials[3].alpha_cutoff = 0.75
-    rs = gpu.RenderScene(sc)
+    rs = gpu.RenderScene(sc, bvh_builder=builder)
     os_ = oracle.OracleScene(sc)
     rays = rays_from_camera(oracle, scenes.scene_mixed(96, 96, 1))
     a, b = rs.trace(rays), os_.trace(rays)
@@ -137,7 +146,8 @@ def test_alpha_masked_material_is_skipped_like_reference(gpu, oracle, scenes):
     assert not np.any(a["material"] == 3)
 
 
-def test_non_finite_triangles_change_no_hit(gpu, scenes):
+@BUILDERS
+def test_non_finite_triangles_change_no_hit(gpu, scenes, builder):
     """Triangles with NaN or infinite vertices (appended to a mesh, so every
     valid triangle keeps its id) are never hit and change no other hit, as an
     Embree robust build ignores invalid primitives: the closest-hit query on
@@ -163,7 +173,7 @@ def test_non_finite_triangles_change_no_hit(gpu, scenes):
     normals = None if m.normals is None else np.concatenate([m.normals, np.tile(m.normals[:1], (len(bad_v) * 3, 1))])
     sc_bad = dataclasses.replace(sc, meshes=[dataclasses.replace(m, positions=pos, faces=faces, normals=normals)]
                                  + list(sc.meshes[1:]))
-    a, b = gpu.RenderScene(sc), gpu.RenderScene(sc_bad)
+    a, b = gpu.RenderScene(sc, bvh_builder=builder), gpu.RenderScene(sc_bad, bvh_builder=builder)
     rays = _random_rays(rng, 200_000, -3.0, 3.0)
     ok, msg = _hits_equal(a.trace(rays), b.trace(rays))
     assert ok, msg
@@ -179,3 +189,34 @@ def test_non_finite_triangles_change_no_hit(gpu, scenes):
     r.set_parameters(gpu.RendererParameters.for_scene(sc_bad, samplesPerPixel=16))
     img = r.render(gpu.PinholeCamera.from_spec(sc.camera))
     assert np.isfinite(img).all()
+
+
+@BUILDERS
+def test_many_meshes_of_every_size_match_oracle(gpu, oracle, scenes, builder):
+    """Meshes of 1, 2, 3, 5 ... triangles beside large ones, coincident
+    triangles (equal boxes: every clustering distance ties) and meshes shared
+    by several instances: one device forest over all meshes, hits bit-exact
+    against the oracle."""
+    import dataclasses
+
+    rng = np.random.default_rng(21)
+    base = scenes.scene_mixed(8, 8, 1)
+    meshes, insts = [], []
+    for k, nt in enumerate([1, 2, 3, 5, 8, 17, 64, 257, 1000, 4099]):
+        c = rng.uniform(-3, 3, 3).astype(np.float32)
+        v = (c + rng.normal(size=(3 * nt, 3)) * 0.3).astype(np.float32)
+        f = np.arange(3 * nt, dtype=np.uint32).reshape(nt, 3)
+        if k == 6:  # 64 copies of one triangle
+            v = np.tile(v[:3], (nt, 1))
+        meshes.append(scenes.Mesh(positions=v, normals=None, faces=f, material=k % len(base.materials), name=f"m{k}"))
+        for r in range(1 + k % 3):
+            t = np.eye(4, dtype=np.float32)
+            t[:3, 3] = rng.uniform(-2, 2, 3) - np.array([0, 0, 8], np.float32)
+            insts.append(scenes.Instance(t, k))
+    sc = dataclasses.replace(base, meshes=meshes, instances=insts)
+    rs = gpu.RenderScene(sc, bvh_builder=builder)
+    os_ = oracle.OracleScene(sc)
+    rays = _random_rays(rng, 50_000, [-6, -6, -14], [6, 6, -2])
+    ok, msg = _hits_equal(rs.trace(rays), os_.trace(rays))
+    assert ok, msg
+    assert np.count_nonzero(rs.trace(rays)["inst"] != 0xFFFFFFFF) > 1000
