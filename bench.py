@@ -474,8 +474,78 @@ def run_mis(args, dev, rs, scene, flush):
             "timing": "CUDA events, median of 3 frames, L2 flushed, per-pixel variance accumulated on both sides"}
 
 
+def run_lights(args, dev, flush):
+    """The point-light path (light subpaths, vertex connections and their
+    closest-hit shadow rays, BDPTRenderer.cpp:260-298, 208-235): C1 (256x256,
+    16 spp, max path length 6, one point light, 5,122 triangles) and the same
+    scene at 1920x1080, 64 spp, which fills the GPU.  Device time per frame
+    (CUDA events, median of 3, L2 flushed, per-kernel events on), rays of every
+    kind, the shadow kernel's roofline (nodes x 128 B + triangles x 48 B per
+    launch over its event time) and the oracle port on the machine's cores beside
+    it (C1: the whole frame; full HD: a centred band of rows)."""
+    import torch
+
+    omv = importlib.import_module("openmaterial-validation_gb300")
+    S = importlib.import_module("openmaterial-validation_gb300.scenes")
+    L, capi = omv.lib(), omv.capi
+    hbm, peak_kind = _peaks()
+    stream = torch.cuda.current_stream(dev)
+    out = {}
+    for name, sc in (("c1_256x256x16", S.scene_c1(256, 256, 16)), ("c1_1920x1080x64", S.scene_c1(1920, 1080, 64))):
+        rs = omv.RenderScene(sc, dev.index or 0)
+        W, H = sc.camera.width, sc.camera.height
+        spp, npix = sc.render.samples_per_pixel, W * H
+        cam = capi.camera_struct(sc.camera)
+        p = capi.params_for(sc, spp=spp, seed=31)
+        p.time_kernels = 1
+        s = torch.zeros(3 * npix, dtype=torch.float64, device=dev)
+        n = torch.zeros(npix, dtype=torch.int32, device=dev)
+        runs = []
+        for it in range(4):
+            s.zero_()
+            n.zero_()
+            flush.zero_()
+            st = capi.Stats()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            omv.check(L.omv_render_device(rs.handle, C.byref(cam), C.byref(p), C.c_void_p(s.data_ptr()), None,
+                                          C.c_void_p(n.data_ptr()), C.c_void_p(stream.cuda_stream), C.byref(st)))
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            if it:
+                runs.append((e0.elapsed_time(e1), st))
+        runs.sort(key=lambda r: r[0])
+        ms, st = runs[1]
+        rays = st.extension_rays + st.shadow_rays + st.light_rays
+        sl = max(1, st.shadow_launches)
+        sh_bytes = (st.shadow_nodes_visited * 128 + st.shadow_triangles_tested * 48) / sl
+        sh_ms = st.shadow_ms / sl
+        sh_gbs = sh_bytes / (sh_ms / 1e3) / 1e9 if sh_ms > 0 else 0.0
+        rec = {"frame_ms": round(ms, 3), "mpaths_per_s": round(npix * spp / (ms / 1e3) / 1e6, 1),
+               "mrays_per_s": round(rays / (ms / 1e3) / 1e6, 1), "extension_rays": st.extension_rays,
+               "light_rays": st.light_rays, "shadow_rays": st.shadow_rays, "launches": st.kernel_launches,
+               "extend_ms": round(st.extend_ms, 3), "shadow_ms": round(st.shadow_ms, 3),
+               "shadow_roofline": {"kernel": "k_shadow (vertex connections)", "bound": "hbm",
+                                   "achieved": round(sh_gbs, 1), "peak": hbm, "unit": "GB/s",
+                                   "frac": round(sh_gbs / hbm, 4), "peak_source": peak_kind,
+                                   "bytes_per_launch": round(sh_bytes), "ms_per_launch": round(sh_ms, 4)}}
+        if not args.no_cpu_baseline:
+            import oracle
+
+            oracle.build()
+            v, rv, cores, rows, dt = cpu_reference(oracle, sc, spp, target_s=min(4.0, args.cpu_seconds))
+            rec["cpu_baseline"] = {"value": round(v, 4), "unit": "Mpaths/s", "cores": cores, "kind": "port",
+                                   "mrays_per_s": round(rv, 4),
+                                   "sample": f"rows {H // 2 - rows // 2}..+{rows} of the {W}x{H} frame at {spp} spp"}
+            rec["gpu_over_cpu"] = round(rec["mpaths_per_s"] / max(v, 1e-9), 1)
+        out[name] = rec
+        rs.close()
+        del s, n
+    return out
+
+
 def run_builders(args, dev, scene, flush):
-    """The three acceleration-structure builders on the benchmark scene: the
+    """The four acceleration-structure builders on the benchmark scene: the
     scene creation time (omv_scene_create, which the build dominates) and the
     frame's device time on each tree (CUDA events, median of 3 frames, L2
     flushed), with the nodes each extension ray fetched."""
@@ -490,7 +560,8 @@ def run_builders(args, dev, scene, flush):
     n = torch.zeros(npix, dtype=torch.int32, device=dev)
     stream = torch.cuda.current_stream(dev)
     out = {}
-    for name, b in (("ploc", capi.BVH_PLOC), ("lbvh", capi.BVH_LBVH), ("host_sah", capi.BVH_HOST_SAH)):
+    for name, b in (("sah", capi.BVH_SAH), ("ploc", capi.BVH_PLOC), ("lbvh", capi.BVH_LBVH),
+                    ("host_sah", capi.BVH_HOST_SAH)):
         rs = omv.RenderScene(scene, dev.index or 0, bvh_builder=b)
         info = rs.info()
         p = capi.params_for(scene, spp=spp, seed=77)
@@ -636,6 +707,8 @@ def run_ours(args, scene, ws, rank, local):
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clock,
                 "gpu_launches": agg["kernel_launches"], "scene_build_ms": round(info["build_ms"], 1),
                 "stack_overflows": agg["stack_overflows"]}
+        if ws == 1 and not args.no_lights:
+            line["lights"] = run_lights(args, dev, flush)
         if ws == 1 and not args.no_builders:
             line["builders"] = run_builders(args, dev, scene, flush)
         if ws == 1 and not args.no_post:
@@ -666,6 +739,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched material sweep")
     ap.add_argument("--no-post", action="store_true", help="skip the image development leg")
     ap.add_argument("--no-builders", action="store_true", help="skip the BVH builder comparison leg")
+    ap.add_argument("--no-lights", action="store_true", help="skip the point-light leg")
     ap.add_argument("--no-mis", action="store_true", help="skip the MIS-vs-reference estimator leg")
     ap.add_argument("--batch-jobs", type=int, default=256)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-vs-finite-difference leg")

@@ -156,18 +156,20 @@ typedef struct omv_scene_desc {
     const omv_hdri_desc* hdri;      /* NULL: no background */
     int32_t num_textures;
     const omv_texture_desc* textures;
-    int32_t bvh_builder;            /* OMV_BVH_*: how the binary trees are built (0: PLOC) */
+    int32_t bvh_builder;            /* OMV_BVH_*: how the binary trees are built (0: device SAH) */
 } omv_scene_desc;
 
 /* Builders of the acceleration structure (Embree's build, RenderScene.cpp:225-272).
  * Each builds a binary tree per mesh and one over the instances, which the
  * device collapses into 8-wide nodes with 16-bit quantized child boxes.
+ *   OMV_BVH_SAH       on the device (default): top-down surface area heuristic,
+ *                     binned above 32 items, full sweep below, all meshes at once
  *   OMV_BVH_PLOC      on the device: Morton codes, radix sort, parallel
- *                     locally-ordered clustering of all meshes at once (default)
+ *                     locally-ordered clustering of all meshes at once
  *   OMV_BVH_LBVH      on the device: Morton codes, radix sort, Karras LBVH
- *   OMV_BVH_HOST_SAH  binned surface-area-heuristic trees on host threads
+ *   OMV_BVH_HOST_SAH  the SAH build of OMV_BVH_SAH on host threads
  * Hits do not depend on the builder; build time and traversal speed do. */
-enum { OMV_BVH_PLOC = 0, OMV_BVH_LBVH = 1, OMV_BVH_HOST_SAH = 2 };
+enum { OMV_BVH_SAH = 0, OMV_BVH_PLOC = 1, OMV_BVH_LBVH = 2, OMV_BVH_HOST_SAH = 3 };
 
 typedef struct omv_scene omv_scene;
 
@@ -234,15 +236,7 @@ typedef struct omv_params {
     int32_t wave_paths;                 /* paths per wavefront wave; 0 = automatic */
     int32_t time_kernels;               /* record CUDA events around every closest-hit
                                            kernel launch (omv_stats.extend_ms) */
-    int32_t traversal;                  /* OMV_TRAVERSAL_*: how camera rays are traced */
 } omv_params;
-
-/* OMV_TRAVERSAL_AUTO: the first camera bounce is traced warp-coherently (the
- * 32 lanes of a warp, 32 samples of one pixel, share one traversal stack;
- * each lane still tests its own ray), except on scenes with alpha-masked
- * materials; every other ray is traced on its own.  OMV_TRAVERSAL_PER_RAY:
- * every ray on its own.  Both give the same hits, so the same image. */
-enum { OMV_TRAVERSAL_AUTO = 0, OMV_TRAVERSAL_PER_RAY = 1 };
 
 /* Fills `p` with the reference defaults (RendererParameters.h:56-89). */
 void omv_params_default(omv_params* p);
@@ -256,14 +250,17 @@ typedef struct omv_stats {
     int64_t light_rays;
     double render_ms;
     int64_t kernel_launches;
-    int64_t nodes_visited;     /* 8-wide BVH nodes fetched by all closest-hit queries */
-    int64_t triangles_tested;  /* triangle records fetched by all closest-hit queries */
+    int64_t nodes_visited;     /* 8-wide BVH nodes fetched by the extension-ray kernels (camera and light
+                                  subpaths) */
+    int64_t triangles_tested;  /* triangle records fetched by the extension-ray kernels */
     double extend_ms;          /* summed device time of the extension-ray kernel (time_kernels) */
     int64_t extend_launches;
     double shadow_ms;          /* summed device time of the shadow-ray kernel (time_kernels) */
     int64_t shadow_launches;
     int64_t stack_overflows;   /* warps whose traversal stack (64 entries) overflowed and dropped
                                   entries; 0 unless a tree is degenerate */
+    int64_t shadow_nodes_visited;     /* nodes fetched by the shadow-ray kernel */
+    int64_t shadow_triangles_tested;  /* triangle records fetched by the shadow-ray kernel */
 } omv_stats;
 
 /* BDPTRenderer::render (BDPTRenderer.cpp:372-393) for one camera.

@@ -197,7 +197,6 @@ class RendererParameters:
     accumulate_variance: bool = False
     wave_paths: int = 0
     estimator: int = 0  # OMV_ESTIMATOR_REFERENCE (0) or OMV_ESTIMATOR_MIS (1)
-    traversal: int = 0  # OMV_TRAVERSAL_AUTO (0) or OMV_TRAVERSAL_PER_RAY (1): same hits either way
 
     def to_c(self) -> capi.Params:
         return capi.Params(camera_bounces=self.cameraBouncesN, light_bounces=self.lightBouncesN, time_kernels=0,
@@ -206,7 +205,7 @@ class RendererParameters:
                            light_scale=self.lightScaleValue, light_min_distance=self.lightMinDistance,
                            ray_cut_value=self.rayCutPixValue, seed=self.seed, estimator=self.estimator,
                            sample_offset=self.sample_offset, accumulate_variance=1 if self.accumulate_variance else 0,
-                           wave_paths=self.wave_paths, traversal=self.traversal)
+                           wave_paths=self.wave_paths)
 
     @classmethod
     def for_scene(cls, scene: scenes.Scene, **kw) -> "RendererParameters":
@@ -272,9 +271,9 @@ class RenderScene:
     """Device scene behind omv_scene_create (RenderScene::commitScene plus the
     GPU acceleration build)."""
 
-    def __init__(self, scene: scenes.Scene, device: int = 0, bvh_builder: int = capi.BVH_PLOC) -> None:
-        """bvh_builder: capi.BVH_PLOC (device, default), BVH_LBVH (device) or
-        BVH_HOST_SAH (host threads); hits do not depend on it."""
+    def __init__(self, scene: scenes.Scene, device: int = 0, bvh_builder: int = capi.BVH_SAH) -> None:
+        """bvh_builder: capi.BVH_SAH (device, default), BVH_PLOC (device),
+        BVH_LBVH (device) or BVH_HOST_SAH (host threads); hits do not depend on it."""
         self.spec = scene
         self._holder = capi.DescHolder(scene, bvh_builder)
         h = C.c_void_p()

@@ -72,7 +72,7 @@ class SceneDesc(C.Structure):
                 ("textures", C.POINTER(TextureDesc)), ("bvh_builder", C.c_int32)]
 
 
-BVH_PLOC, BVH_LBVH, BVH_HOST_SAH = 0, 1, 2
+BVH_SAH, BVH_PLOC, BVH_LBVH, BVH_HOST_SAH = 0, 1, 2, 3
 
 
 class SceneInfo(C.Structure):
@@ -91,11 +91,7 @@ class Params(C.Structure):
                 ("samples_per_pixel", C.c_int32), ("light_distance_attenuation", C.c_int32),
                 ("light_scale", C.c_float), ("light_min_distance", C.c_float), ("ray_cut_value", C.c_float),
                 ("seed", C.c_uint64), ("estimator", C.c_int32), ("sample_offset", C.c_int32),
-                ("accumulate_variance", C.c_int32), ("wave_paths", C.c_int32), ("time_kernels", C.c_int32),
-                ("traversal", C.c_int32)]
-
-
-TRAVERSAL_AUTO, TRAVERSAL_PER_RAY = 0, 1
+                ("accumulate_variance", C.c_int32), ("wave_paths", C.c_int32), ("time_kernels", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -103,7 +99,8 @@ class Stats(C.Structure):
                 ("light_rays", C.c_int64), ("render_ms", C.c_double), ("kernel_launches", C.c_int64),
                 ("nodes_visited", C.c_int64), ("triangles_tested", C.c_int64), ("extend_ms", C.c_double),
                 ("extend_launches", C.c_int64), ("shadow_ms", C.c_double), ("shadow_launches", C.c_int64),
-                ("stack_overflows", C.c_int64)]
+                ("stack_overflows", C.c_int64), ("shadow_nodes_visited", C.c_int64),
+                ("shadow_triangles_tested", C.c_int64)]
 
 
 class Hit(C.Structure):
@@ -209,7 +206,7 @@ def material_set_descs(sets, keep: List[Any]):
 class DescHolder:
     """Keeps every numpy buffer referenced by an omv_scene_desc alive."""
 
-    def __init__(self, scene, bvh_builder: int = BVH_PLOC) -> None:
+    def __init__(self, scene, bvh_builder: int = BVH_SAH) -> None:
         self.keep: List[Any] = []
         meshes = (MeshDesc * max(1, len(scene.meshes)))()
         for i, m in enumerate(scene.meshes):

@@ -3,8 +3,12 @@
 // tree per mesh (Embree: one scene per mesh) and one top-level tree over the
 // instances (Embree: instance geometries in the top scene).
 //
-// Three builders of the binary tree, one collapse:
-//   OMV_BVH_PLOC (default, on the device): item boxes and per-mesh centroid
+// Four builders of the binary tree, one collapse:
+//   OMV_BVH_SAH (default, on the device): top-down surface area heuristic
+//     over all meshes at once, level by level: binned (32 bins per axis) on
+//     ranges of more than 32 items, a full sweep below (Wald 2007); the
+//     algorithm of the host build, so the same trace speed.
+//   OMV_BVH_PLOC (on the device): item boxes and per-mesh centroid
 //     bounds; 30-bit Morton codes; LSD radix sort by (mesh, code); parallel
 //     locally-ordered clustering over all meshes at once (Meister and
 //     Bittner 2018), one tree per mesh; leaf counts bottom-up, leaf order and
@@ -905,13 +909,388 @@ __global__ void k_ploc_nodes(int ni, const int2* child, const Box* node_box, con
     out[k] = nd;
 }
 
+// ------------------------------------------------------- device SAH ---
+// Top-down binary trees by the surface area heuristic, leaves of one item,
+// the host SAH build's algorithm on the device (I. Wald, "On fast
+// Construction of SAH-based Bounding Volume Hierarchies", IEEE RT 2007):
+// ranges of more than kSweepMax items are split at the best of kSahBins
+// centroid bins per axis (one block per range: bounds, binning in shared
+// memory, one warp scans the bins, a stable block-wide partition), smaller
+// ranges at the best position of a full sweep over the items sorted along
+// each axis (one warp per range: bitonic sort, prefix and suffix box
+// unions).  Every range of a level is processed in the same launch, across
+// all meshes; a range's items stay contiguous, so node ranges need no
+// placement pass.
+constexpr int kSahBinsDev = 32;
+constexpr int kSweepMaxDev = 32;
+constexpr int kSahLargeThreads = 256;
+
+struct SahTask {
+    int first, last, node, parent;
+};
+
+__device__ __forceinline__ Box empty_box()
+{
+    Box b;
+    for (int a = 0; a < 3; ++a) {
+        b.lo[a] = 3.0e38f;
+        b.hi[a] = -3.0e38f;
+    }
+    return b;
+}
+
+// a child range: a leaf reference (~position), or a new internal node and its task
+__device__ __forceinline__ int sah_child(int first, int last, int parent, uint32_t* node_counter, SahTask* next_large,
+                                         uint32_t* n_large, SahTask* next_small, uint32_t* n_small)
+{
+    if (first == last) return ~first;
+    const int id = (int)atomicAdd(node_counter, 1u);
+    const SahTask t{first, last, id, parent};
+    if (last - first + 1 > kSweepMaxDev)
+        next_large[atomicAdd(n_large, 1u)] = t;
+    else
+        next_small[atomicAdd(n_small, 1u)] = t;
+    return id;
+}
+
+__device__ __forceinline__ int sah_bin(float c2, float cmin, float scale)
+{
+    return (int)fminf((float)(kSahBinsDev - 1), (c2 - cmin) * scale);
+}
+
+__global__ void __launch_bounds__(kSahLargeThreads) k_sah_large(const SahTask* __restrict__ tasks,
+                                                                const Box* __restrict__ item_boxes, uint32_t* order,
+                                                                uint32_t* tmp, Node2* nodes, uint32_t* node_counter,
+                                                                SahTask* next_large, uint32_t* n_large,
+                                                                SahTask* next_small, uint32_t* n_small)
+{
+    constexpr int NW = kSahLargeThreads / 32;
+    __shared__ uint32_t sbox[6], scen[6];
+    __shared__ uint32_t bcnt[3][kSahBinsDev];
+    __shared__ uint32_t bbox[3][kSahBinsDev][6];
+    __shared__ int s_axis, s_bin, s_nl;
+    __shared__ uint32_t wl[NW], wr[NW];
+    const SahTask t = tasks[blockIdx.x];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int k = tid; k < 3 * kSahBinsDev; k += blockDim.x) {
+        (&bcnt[0][0])[k] = 0u;
+        for (int c = 0; c < 3; ++c) {
+            bbox[k / kSahBinsDev][k % kSahBinsDev][c] = 0xFFFFFFFFu;
+            bbox[k / kSahBinsDev][k % kSahBinsDev][3 + c] = 0u;
+        }
+    }
+    if (tid < 3) {
+        sbox[tid] = scen[tid] = 0xFFFFFFFFu;
+        sbox[3 + tid] = scen[3 + tid] = 0u;
+    }
+    __syncthreads();
+    // bounds of the boxes and of the doubled centroids
+    uint32_t lo[3], hi[3], clo[3], chi[3];
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = clo[a] = 0xFFFFFFFFu;
+        hi[a] = chi[a] = 0u;
+    }
+    for (int i = t.first + tid; i <= t.last; i += blockDim.x) {
+        const Box b = item_boxes[order[i]];
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = min(lo[a], f2ord(b.lo[a]));
+            hi[a] = max(hi[a], f2ord(b.hi[a]));
+            const uint32_t c = f2ord(b.lo[a] + b.hi[a]);
+            clo[a] = min(clo[a], c);
+            chi[a] = max(chi[a], c);
+        }
+    }
+    for (int a = 0; a < 3; ++a) {
+        for (int o = 16; o; o >>= 1) {
+            lo[a] = min(lo[a], __shfl_xor_sync(0xFFFFFFFFu, lo[a], o));
+            hi[a] = max(hi[a], __shfl_xor_sync(0xFFFFFFFFu, hi[a], o));
+            clo[a] = min(clo[a], __shfl_xor_sync(0xFFFFFFFFu, clo[a], o));
+            chi[a] = max(chi[a], __shfl_xor_sync(0xFFFFFFFFu, chi[a], o));
+        }
+        if (lane == 0) {
+            atomicMin(&sbox[a], lo[a]);
+            atomicMax(&sbox[3 + a], hi[a]);
+            atomicMin(&scen[a], clo[a]);
+            atomicMax(&scen[3 + a], chi[a]);
+        }
+    }
+    __syncthreads();
+    float cmin[3], scale[3];
+    bool on[3];
+    for (int a = 0; a < 3; ++a) {
+        cmin[a] = ord2f(scen[a]);
+        const float ext = ord2f(scen[3 + a]) - cmin[a];
+        on[a] = ext > 0.0f;
+        scale[a] = on[a] ? (float)kSahBinsDev / ext : 0.0f;
+    }
+    // binning
+    for (int i = t.first + tid; i <= t.last; i += blockDim.x) {
+        const Box b = item_boxes[order[i]];
+        for (int a = 0; a < 3; ++a) {
+            if (!on[a]) continue;
+            const int q = sah_bin(b.lo[a] + b.hi[a], cmin[a], scale[a]);
+            atomicAdd(&bcnt[a][q], 1u);
+            for (int c = 0; c < 3; ++c) {
+                atomicMin(&bbox[a][q][c], f2ord(b.lo[c]));
+                atomicMax(&bbox[a][q][3 + c], f2ord(b.hi[c]));
+            }
+        }
+    }
+    __syncthreads();
+    // one warp: the best boundary between bins q and q + 1 (lane q)
+    if (warp == 0) {
+        float best = 3.0e38f;
+        int best_axis = -1, best_bin = 0;
+        for (int a = 0; a < 3; ++a) {
+            if (!on[a]) continue;
+            const uint32_t c = bcnt[a][lane];
+            Box b = empty_box();
+            if (c)
+                for (int k = 0; k < 3; ++k) {
+                    b.lo[k] = ord2f(bbox[a][lane][k]);
+                    b.hi[k] = ord2f(bbox[a][lane][3 + k]);
+                }
+            // prefix (bins 0..lane) and suffix (bins lane..31) unions and counts
+            Box pre = b, suf = b;
+            uint32_t pc = c, sc = c;
+            for (int o = 1; o < 32; o <<= 1) {
+                Box x, y;
+                for (int k = 0; k < 3; ++k) {
+                    x.lo[k] = __shfl_up_sync(0xFFFFFFFFu, pre.lo[k], o);
+                    x.hi[k] = __shfl_up_sync(0xFFFFFFFFu, pre.hi[k], o);
+                    y.lo[k] = __shfl_down_sync(0xFFFFFFFFu, suf.lo[k], o);
+                    y.hi[k] = __shfl_down_sync(0xFFFFFFFFu, suf.hi[k], o);
+                }
+                const uint32_t xc = __shfl_up_sync(0xFFFFFFFFu, pc, o), yc = __shfl_down_sync(0xFFFFFFFFu, sc, o);
+                if (lane >= o) {
+                    pre = box_union(x, pre);
+                    pc += xc;
+                }
+                if (lane + o < 32) {
+                    suf = box_union(suf, y);
+                    sc += yc;
+                }
+            }
+            // right side of boundary `lane`: the suffix from lane + 1
+            Box r;
+            for (int k = 0; k < 3; ++k) {
+                r.lo[k] = __shfl_down_sync(0xFFFFFFFFu, suf.lo[k], 1);
+                r.hi[k] = __shfl_down_sync(0xFFFFFFFFu, suf.hi[k], 1);
+            }
+            const uint32_t rc = __shfl_down_sync(0xFFFFFFFFu, sc, 1);
+            float cost = 3.4e38f;
+            if (lane < kSahBinsDev - 1 && pc > 0 && rc > 0)
+                cost = half_area(pre) * (float)pc + half_area(r) * (float)rc;
+            // the first minimum in bin order (ties: the lowest boundary)
+            float mc = cost;
+            int mq = lane;
+            for (int o = 16; o; o >>= 1) {
+                const float oc = __shfl_xor_sync(0xFFFFFFFFu, mc, o);
+                const int oq = __shfl_xor_sync(0xFFFFFFFFu, mq, o);
+                if (oc < mc || (oc == mc && oq < mq)) {
+                    mc = oc;
+                    mq = oq;
+                }
+            }
+            if (mc < best) {
+                best = mc;
+                best_axis = a;
+                best_bin = mq;
+            }
+        }
+        if (lane == 0) {
+            s_axis = best_axis;
+            s_bin = best_bin;
+            int nl = 0;
+            if (best_axis >= 0)
+                for (int q = 0; q <= best_bin; ++q) nl += (int)bcnt[best_axis][q];
+            s_nl = nl;
+        }
+    }
+    __syncthreads();
+    const int cnt = t.last - t.first + 1;
+    int split;
+    if (s_axis < 0) {
+        split = t.first + cnt / 2 - 1;  // no split: halves in the current order
+    } else {
+        // stable partition into tmp, then back into order
+        const int a = s_axis, qb = s_bin, nl = s_nl;
+        int lbase = 0, rbase = 0;
+        for (int c0 = t.first; c0 <= t.last; c0 += blockDim.x) {
+            const int i = c0 + tid;
+            const bool ok = i <= t.last;
+            const uint32_t item = ok ? order[i] : 0u;
+            bool left = false;
+            if (ok) {
+                const Box b = item_boxes[item];
+                left = sah_bin(b.lo[a] + b.hi[a], cmin[a], scale[a]) <= qb;
+            }
+            const uint32_t ml = __ballot_sync(0xFFFFFFFFu, ok && left), mr = __ballot_sync(0xFFFFFFFFu, ok && !left);
+            if (lane == 0) {
+                wl[warp] = __popc(ml);
+                wr[warp] = __popc(mr);
+            }
+            __syncthreads();
+            int pl = 0, pr = 0, tl = 0, tr = 0;
+            for (int w = 0; w < NW; ++w) {
+                if (w < warp) {
+                    pl += (int)wl[w];
+                    pr += (int)wr[w];
+                }
+                tl += (int)wl[w];
+                tr += (int)wr[w];
+            }
+            const uint32_t below = (1u << lane) - 1u;
+            if (ok) {  // positions stay inside the range even if the counts disagreed
+                const int dst = left ? t.first + lbase + pl + __popc(ml & below)
+                                     : t.first + nl + rbase + pr + __popc(mr & below);
+                if (dst >= t.first && dst <= t.last) tmp[dst] = item;
+            }
+            lbase += tl;
+            rbase += tr;
+            __syncthreads();
+        }
+        for (int i = t.first + tid; i <= t.last; i += blockDim.x) order[i] = tmp[i];
+        split = t.first + nl - 1;
+    }
+    if (tid == 0) {
+        Node2 nd;
+        nd.first = t.first;
+        nd.last = t.last;
+        nd.parent = t.parent;
+        for (int k = 0; k < 3; ++k) {
+            nd.box.lo[k] = ord2f(sbox[k]);
+            nd.box.hi[k] = ord2f(sbox[3 + k]);
+        }
+        nd.left = sah_child(t.first, split, t.node, node_counter, next_large, n_large, next_small, n_small);
+        nd.right = sah_child(split + 1, t.last, t.node, node_counter, next_large, n_large, next_small, n_small);
+        nodes[t.node] = nd;
+    }
+}
+
+// warp-wide bitonic sort of one 64-bit key per lane, ascending
+__device__ __forceinline__ uint64_t warp_sort64(uint64_t key)
+{
+    const int lane = threadIdx.x & 31;
+    for (int k = 2; k <= 32; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const uint32_t lo = __shfl_xor_sync(0xFFFFFFFFu, (uint32_t)key, j);
+            const uint32_t hi = __shfl_xor_sync(0xFFFFFFFFu, (uint32_t)(key >> 32), j);
+            const uint64_t other = ((uint64_t)hi << 32) | lo;
+            const bool up = (lane & k) == 0;
+            const bool lower = (lane & j) == 0;
+            const uint64_t mn = key < other ? key : other, mx = key < other ? other : key;
+            key = (lower == up) ? mn : mx;
+        }
+    return key;
+}
+
+// ranges of 2..kSweepMaxDev items: one warp each, full sweep on every axis
+__global__ void k_sah_small(int ntasks, const SahTask* __restrict__ tasks, const Box* __restrict__ item_boxes,
+                            uint32_t* order, Node2* nodes, uint32_t* node_counter, SahTask* next_large,
+                            uint32_t* n_large, SahTask* next_small, uint32_t* n_small)
+{
+    const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (w >= ntasks) return;  // whole warps leave together
+    const int lane = threadIdx.x & 31;
+    const SahTask t = tasks[w];
+    const int cnt = t.last - t.first + 1;
+    const bool valid = lane < cnt;
+    const uint32_t item = valid ? order[t.first + lane] : 0u;
+    const Box b = valid ? item_boxes[item] : empty_box();
+    // node box
+    Box nb = b;
+    for (int o = 16; o; o >>= 1)
+        for (int k = 0; k < 3; ++k) {
+            nb.lo[k] = fminf(nb.lo[k], __shfl_xor_sync(0xFFFFFFFFu, nb.lo[k], o));
+            nb.hi[k] = fmaxf(nb.hi[k], __shfl_xor_sync(0xFFFFFFFFu, nb.hi[k], o));
+        }
+    float best = 3.0e38f;
+    int best_axis = -1, best_k = 0;
+    for (int a = 0; a < 3; ++a) {
+        // stable order along the axis: key = (doubled centroid, position)
+        const uint64_t key = valid ? (((uint64_t)f2ord(b.lo[a] + b.hi[a]) << 32) | (uint32_t)lane) : ~0ull;
+        const uint64_t sk = warp_sort64(key);
+        const int src = (int)(sk & 31u);
+        Box sb;
+        for (int k = 0; k < 3; ++k) {
+            sb.lo[k] = __shfl_sync(0xFFFFFFFFu, b.lo[k], src);
+            sb.hi[k] = __shfl_sync(0xFFFFFFFFu, b.hi[k], src);
+        }
+        if (lane >= cnt) sb = empty_box();
+        Box pre = sb, suf = sb;
+        for (int o = 1; o < 32; o <<= 1) {
+            Box x, y;
+            for (int k = 0; k < 3; ++k) {
+                x.lo[k] = __shfl_up_sync(0xFFFFFFFFu, pre.lo[k], o);
+                x.hi[k] = __shfl_up_sync(0xFFFFFFFFu, pre.hi[k], o);
+                y.lo[k] = __shfl_down_sync(0xFFFFFFFFu, suf.lo[k], o);
+                y.hi[k] = __shfl_down_sync(0xFFFFFFFFu, suf.hi[k], o);
+            }
+            if (lane >= o) pre = box_union(x, pre);
+            if (lane + o < 32) suf = box_union(suf, y);
+        }
+        Box r;
+        for (int k = 0; k < 3; ++k) {
+            r.lo[k] = __shfl_down_sync(0xFFFFFFFFu, suf.lo[k], 1);
+            r.hi[k] = __shfl_down_sync(0xFFFFFFFFu, suf.hi[k], 1);
+        }
+        float cost = 3.4e38f;
+        if (lane < cnt - 1)
+            cost = half_area(pre) * (float)(lane + 1) + half_area(r) * (float)(cnt - 1 - lane);
+        float mc = cost;
+        int mk = lane;
+        for (int o = 16; o; o >>= 1) {
+            const float oc = __shfl_xor_sync(0xFFFFFFFFu, mc, o);
+            const int ok_ = __shfl_xor_sync(0xFFFFFFFFu, mk, o);
+            if (oc < mc || (oc == mc && ok_ < mk)) {
+                mc = oc;
+                mk = ok_;
+            }
+        }
+        if (mc < best) {
+            best = mc;
+            best_axis = a;
+            best_k = mk;
+        }
+    }
+    int split;
+    if (best_axis >= 0) {
+        const uint64_t key = valid ? (((uint64_t)f2ord(b.lo[best_axis] + b.hi[best_axis]) << 32) | (uint32_t)lane)
+                                   : ~0ull;
+        const uint64_t sk = warp_sort64(key);
+        const uint32_t it = __shfl_sync(0xFFFFFFFFu, item, (int)(sk & 31u));
+        if (valid) order[t.first + lane] = it;
+        split = t.first + best_k;
+    } else {
+        split = t.first + cnt / 2 - 1;
+    }
+    if (lane == 0) {
+        Node2 nd;
+        nd.first = t.first;
+        nd.last = t.last;
+        nd.parent = t.parent;
+        nd.box = nb;
+        nd.left = sah_child(t.first, split, t.node, node_counter, next_large, n_large, next_small, n_small);
+        nd.right = sah_child(split + 1, t.last, t.node, node_counter, next_large, n_large, next_small, n_small);
+        nodes[t.node] = nd;
+    }
+}
+
+__global__ void k_iota(int n, uint32_t* v)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = (uint32_t)i;
+}
+
 }  // namespace
 
 // Binary tree by the surface area heuristic, leaves of one item: binned
 // (kSahBins bins per axis over the centroid bounds) on ranges of more than
 // kSweepMax items, a full sweep over every split position below.  nodes[0] is
 // the root; `order` receives the item order the node ranges refer to.  Runs on
-// the host (the OMV_BVH_HOST_SAH builder, one thread per mesh).
+// the host (the OMV_BVH_HOST_SAH builder, one thread per mesh); k_sah_large /
+// k_sah_small run the same algorithm on the device.
 constexpr int kSahBins = 32;
 constexpr int kSweepMax = 32;
 
@@ -1191,6 +1570,55 @@ static void ploc_forest(int n, const std::vector<uint32_t>& seg_base, const Box*
     f.roots = roots;
 }
 
+// Device SAH forest: one tree per segment (items [seg_base[s], seg_base[s + 1])).
+static void sah_forest(int n, const std::vector<uint32_t>& seg_base, const Box* item_boxes, Forest& f,
+                       cudaStream_t st)
+{
+    const int nseg = (int)seg_base.size();
+    f.alloc(n);
+    k_iota<<<blocks(n, 256), 256, 0, st>>>(n, f.vals);
+    DBuf<uint32_t> tmp(n), ctr(3);  // nodes, large tasks, small tasks
+    DBuf<SahTask> la(n), lb(n), sa(n), sb(n);
+    std::vector<SahTask> large, small;
+    std::vector<int> roots(nseg);
+    int next_id = 0;
+    for (int s = 0; s < nseg; ++s) {
+        const int first = (int)seg_base[s], last = (s + 1 < nseg ? (int)seg_base[s + 1] : n) - 1;
+        if (first == last) {
+            roots[s] = ~first;
+            continue;
+        }
+        const SahTask t{first, last, next_id, -2 - s};
+        roots[s] = next_id++;
+        (last - first + 1 > kSweepMaxDev ? large : small).push_back(t);
+    }
+    uint32_t h[3] = {(uint32_t)next_id, (uint32_t)large.size(), (uint32_t)small.size()};
+    if (!large.empty())
+        OMV_CK(cudaMemcpyAsync(la.p, large.data(), sizeof(SahTask) * large.size(), cudaMemcpyHostToDevice, st));
+    if (!small.empty())
+        OMV_CK(cudaMemcpyAsync(sa.p, small.data(), sizeof(SahTask) * small.size(), cudaMemcpyHostToDevice, st));
+    OMV_CK(cudaMemcpyAsync(ctr.p, h, sizeof(h), cudaMemcpyHostToDevice, st));
+    SahTask *cl = la.p, *nl = lb.p, *cs = sa.p, *ns = sb.p;
+    for (int level = 0; h[1] + h[2] > 0; ++level) {
+        if (level > 4096) throw std::runtime_error("device SAH build did not terminate");
+        const int nlarge = (int)h[1], nsmall = (int)h[2];
+        OMV_CK(cudaMemsetAsync(ctr.p + 1, 0, 2 * sizeof(uint32_t), st));
+        if (nlarge)
+            k_sah_large<<<nlarge, kSahLargeThreads, 0, st>>>(cl, item_boxes, f.vals, tmp.p, f.nodes, ctr.p, nl,
+                                                             ctr.p + 1, ns, ctr.p + 2);
+        if (nsmall)
+            k_sah_small<<<blocks((size_t)nsmall * 32, 128), 128, 0, st>>>(nsmall, cs, item_boxes, f.vals, f.nodes,
+                                                                          ctr.p, nl, ctr.p + 1, ns, ctr.p + 2);
+        OMV_CK(cudaGetLastError());
+        OMV_CK(cudaMemcpyAsync(h, ctr.p, sizeof(h), cudaMemcpyDeviceToHost, st));
+        OMV_CK(cudaStreamSynchronize(st));
+        if ((int)h[0] > std::max(1, n - nseg)) throw std::runtime_error("device SAH build: node capacity exceeded");
+        std::swap(cl, nl);
+        std::swap(cs, ns);
+    }
+    f.roots = roots;
+}
+
 // host SAH tree over n boxes (one tree)
 static void host_sah_forest(const std::vector<Box>& boxes, Forest& f, cudaStream_t st)
 {
@@ -1270,8 +1698,8 @@ void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<Instance
         if (meshes[mi].valid && meshes[mi].num_faces > 0) todo.push_back(mi);
 
     // ---- bottom level: one tree per mesh
-    if (builder == BvhBuilder::Ploc && !todo.empty()) {
-        // every mesh in one PLOC forest: one launch sequence for all of them
+    if ((builder == BvhBuilder::Sah || builder == BvhBuilder::Ploc) && !todo.empty()) {
+        // every mesh in one forest: one launch sequence for all of them
         std::vector<uint32_t> seg_base(todo.size());
         std::vector<SegPtr> segs(todo.size());
         uint32_t n = 0;
@@ -1299,7 +1727,10 @@ void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<Instance
         }
         OMV_CK(cudaGetLastError());
         Forest f;
-        ploc_forest((int)n, seg_base, boxes.p, cb.p, f, st);
+        if (builder == BvhBuilder::Sah)
+            sah_forest((int)n, seg_base, boxes.p, f, st);
+        else
+            ploc_forest((int)n, seg_base, boxes.p, cb.p, f, st);
         const std::vector<uint32_t> roots = collapse_forest(false, f, (int)n, boxes.p, d_segs.p, (int)todo.size(),
                                                             out.nodes, counters.p, node_cap, out.tris, nullptr, st);
         for (size_t s = 0; s < todo.size(); ++s) out.blas_root[todo[s]] = roots[s];
@@ -1430,6 +1861,8 @@ void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<Instance
             OMV_CK(cudaGetLastError());
             if (builder == BvhBuilder::Lbvh)
                 lbvh_tree(n, boxes.p, cb.p, f, st);
+            else if (builder == BvhBuilder::Sah)
+                sah_forest(n, std::vector<uint32_t>{0u}, boxes.p, f, st);
             else
                 ploc_forest(n, std::vector<uint32_t>{0u}, boxes.p, cb.p, f, st);
         }

@@ -38,7 +38,7 @@ struct AccelResult {
     uint32_t num_valid_instances = 0;
 };
 
-enum class BvhBuilder { Ploc = 0, Lbvh = 1, HostSah = 2 };  // OMV_BVH_PLOC / _LBVH / _HOST_SAH
+enum class BvhBuilder { Sah = 0, Ploc = 1, Lbvh = 2, HostSah = 3 };  // OMV_BVH_SAH / _PLOC / _LBVH / _HOST_SAH
 
 // Builds every BLAS and the TLAS; throws std::runtime_error on CUDA errors.
 void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<InstanceGeom>& insts, BvhBuilder builder,

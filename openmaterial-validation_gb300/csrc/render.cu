@@ -53,7 +53,10 @@ constexpr int kCtrCam = 64;      // + bounce (0..camera_bounces)
 constexpr int kCtrShadow = 128;  // + bounce
 constexpr int kCtrWork = 192;    // + launch index
 constexpr int kCtrEnv = 448;     // + bounce: MIS environment rays
-enum { kStatExt = 0, kStatShadow = 1, kStatLight = 2, kStatNodes = 3, kStatTris = 4, kStatOverflow = 5 };
+enum {
+    kStatExt = 0, kStatShadow = 1, kStatLight = 2, kStatNodes = 3, kStatTris = 4, kStatOverflow = 5,
+    kStatShadowNodes = 6, kStatShadowTris = 7
+};
 
 __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want)
 {
@@ -357,48 +360,6 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_extend(DevSc
     if (lane == 0) {
         atomicAdd(&stats[kStatNodes], (unsigned long long)nodes);
         atomicAdd(&stats[kStatTris], (unsigned long long)tris);
-        if (ov) atomicAdd(&stats[kStatOverflow], 1ull);
-    }
-}
-
-// Closest hit of camera rays by warp-coherent traversal (trace_packet): a
-// warp takes 32 consecutive queue entries, which for the first bounce are 32
-// samples of one pixel.  Scenes without alpha-masked materials only (no
-// retries).  Node and triangle counts are per warp fetch.
-__global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks)
-    k_extend_packet(DevScene S, const uint32_t* items, const float4* rq, uint4* hits, const uint32_t* count,
-                    uint32_t* work, unsigned long long* stats, int stat_kind)
-{
-    __shared__ PacketEntry pstack[(kTraceThreads / 32) * kPacketStack];
-    PacketEntry* stk = pstack + (threadIdx.x >> 5) * kPacketStack;
-    TraceCounters tc{0u, 0u};
-    int overflow = 0;
-    const uint32_t n = *count;
-    const int lane = threadIdx.x & 31;
-    while (true) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(work, 32u);
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if (base >= n) break;
-        const uint32_t i = base + lane;
-        const bool active = i < n;
-        float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f), b = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
-        if (active) {
-            a = rq[2 * (size_t)i];
-            b = rq[2 * (size_t)i + 1];
-        }
-        RayHit h;
-        const bool hit = trace_packet(S, items, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), a.w, kFltMax, active, h, stk, tc,
-                                      overflow);
-        if (active)
-            hits[i] = hit ? make_uint4(h.inst, h.prim, __float_as_uint(h.u), __float_as_uint(h.v))
-                          : make_uint4(kInvalid, kInvalid, 0u, 0u);
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&stats[stat_kind], (unsigned long long)n);
-    const bool ov = __any_sync(0xFFFFFFFFu, overflow);
-    if (lane == 0) {
-        atomicAdd(&stats[kStatNodes], (unsigned long long)tc.nodes);
-        atomicAdd(&stats[kStatTris], (unsigned long long)tc.tris);
         if (ov) atomicAdd(&stats[kStatOverflow], 1ull);
     }
 }
@@ -735,8 +696,8 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevSc
     }
     const bool ov = __any_sync(0xFFFFFFFFu, st.overflow);
     if (lane == 0) {
-        atomicAdd(&stats[kStatNodes], (unsigned long long)nodes);
-        atomicAdd(&stats[kStatTris], (unsigned long long)tris);
+        atomicAdd(&stats[kStatShadowNodes], (unsigned long long)nodes);
+        atomicAdd(&stats[kStatShadowTris], (unsigned long long)tris);
         if (ov) atomicAdd(&stats[kStatOverflow], 1ull);
     }
 }
@@ -1111,13 +1072,6 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
     OMV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, mis ? k_camera_shade<true> : k_camera_shade<false>,
                                                            kShadeThreads, 0));
     const int trace_grid = std::max(1, occ_t) * s.num_sms;
-    // warp-coherent traversal of the first camera bounce (not with alpha-masked
-    // materials, whose hits are retried ray by ray)
-    if (p.traversal != OMV_TRAVERSAL_AUTO && p.traversal != OMV_TRAVERSAL_PER_RAY) throw ArgError("unknown traversal");
-    const bool packets = p.traversal == OMV_TRAVERSAL_AUTO && !masked;
-    int occ_p = 0;
-    if (packets) OMV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_extend_packet, kTraceThreads, 0));
-    const int packet_grid = std::max(1, occ_p) * s.num_sms;
     const int shade_grid = std::max(1, occ_s) * s.num_sms;
     int64_t launches = 0;
     // optional per-launch events around the closest-hit kernels
@@ -1182,15 +1136,8 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
                 float4* in = R.rq[(b + 1) % 2];
                 float4* out = R.rq[b % 2];
                 if (time_kernels) timed(ext_ev);
-                if (b == 1 && packets)  // 32 samples of one pixel per warp
-                    k_extend_packet<<<packet_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, in, R.hits,
-                                                                           R.ctr + kCtrCam + b,
-                                                                           R.ctr + kCtrWork + work++, R.stats,
-                                                                           kStatExt);
-                else
-                    k_extend<<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, in, R.hits,
-                                                                   R.ctr + kCtrCam + b, R.ctr + kCtrWork + work++,
-                                                                   R.stats, kStatExt);
+                k_extend<<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, in, R.hits, R.ctr + kCtrCam + b,
+                                                               R.ctr + kCtrWork + work++, R.stats, kStatExt);
                 if (time_kernels) timed(ext_ev);
                 if (mis)
                     k_camera_shade<true><<<shade_grid, kShadeThreads, 0, st>>>(A, b, in, out);
@@ -1255,6 +1202,8 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
         stats->nodes_visited = (int64_t)h[kStatNodes];
         stats->triangles_tested = (int64_t)h[kStatTris];
         stats->stack_overflows = (int64_t)h[kStatOverflow];
+        stats->shadow_nodes_visited = (int64_t)h[kStatShadowNodes];
+        stats->shadow_triangles_tested = (int64_t)h[kStatShadowTris];
         auto sum_pairs = [](std::vector<cudaEvent_t>& ev) {
             double t = 0.0;
             for (size_t i = 0; i + 1 < ev.size(); i += 2) {
@@ -1542,7 +1491,6 @@ void load_wave_kernels()
     OMV_CUDA(cudaFuncGetAttributes(&a, k_camera_gen));
     OMV_CUDA(cudaFuncGetAttributes(&a, k_light_gen));
     OMV_CUDA(cudaFuncGetAttributes(&a, k_extend));
-    OMV_CUDA(cudaFuncGetAttributes(&a, k_extend_packet));
     OMV_CUDA(cudaFuncGetAttributes(&a, k_light_shade));
     OMV_CUDA(cudaFuncGetAttributes(&a, k_camera_shade<false>));
     OMV_CUDA(cudaFuncGetAttributes(&a, k_shadow<false, false>));

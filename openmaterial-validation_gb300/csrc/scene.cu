@@ -593,7 +593,7 @@ SceneHost* scene_create(const omv_scene_desc& d, int device)
         geo[i].h_pos = pos3[i].data();
         geo[i].h_faces = d.meshes[i].faces;
     }
-    if (d.bvh_builder < OMV_BVH_PLOC || d.bvh_builder > OMV_BVH_HOST_SAH) throw ArgError("unknown bvh_builder");
+    if (d.bvh_builder < OMV_BVH_SAH || d.bvh_builder > OMV_BVH_HOST_SAH) throw ArgError("unknown bvh_builder");
     AccelResult acc;
     build_accel(geo, igeo, static_cast<BvhBuilder>(d.bvh_builder), acc, s->stream);
     s->allocs.push_back(acc.nodes);

@@ -377,201 +377,6 @@ __device__ __forceinline__ bool trace_closest_or_below(const DevScene& S, const 
     return trace_end(T, hit);
 }
 
-// ------------------------------------------------ warp-coherent traversal ---
-// The 32 lanes of a warp traverse one shared stack (packet traversal, I. Wald,
-// P. Slusallek, C. Benthin, M. Wagner, "Interactive Rendering with Coherent
-// Ray Tracing", Eurographics 2001, here over the 8-wide tree): a node is
-// fetched once for the warp (every lane reads the same address), every lane
-// tests its own ray against the node's 8 child boxes, and a child is pushed
-// with the mask of the lanes whose ray enters it and the smallest entry
-// distance among them.  A popped entry is skipped by the lanes that already
-// hold a closer hit.  Leaf triangles are tested by the lanes of their mask,
-// each with its own ray and closest distance.  The box tests are the
-// single-ray traversal's conservative tests and the hit rule (closest t, then
-// lowest instance and primitive) does not depend on the order, so every lane
-// finds exactly the single-ray hit.  For the camera rays of a frame a warp
-// holds 32 samples of one pixel: the lanes' node sets nearly coincide, and the
-// warp visits their union once instead of each lane walking it alone.
-constexpr int kPacketStack = 64;  // entries per warp
-
-struct PacketEntry {
-    uint32_t node;  // node index, or kInstTag | instance
-    uint32_t mask;  // lanes whose ray entered it
-    float tmin;     // smallest entry distance among them
-    uint32_t pad;
-};
-
-// All 32 lanes of the warp must call it together; `active` lanes have a ray.
-// `stk` is the warp's kPacketStack entries (shared memory).  Returns whether
-// this lane's ray hit; `overflow` is set when entries had to be dropped.
-__device__ __forceinline__ bool trace_packet(const DevScene& S, const uint32_t* __restrict__ tlas_items, V3 o, V3 d,
-                                             float tnear, float tfar, bool active, RayHit& hit, PacketEntry* stk,
-                                             TraceCounters& tc, int& overflow)
-{
-    constexpr uint32_t kAll = 0xFFFFFFFFu;
-    const int lane = threadIdx.x & 31;
-    Shear rs;
-    const bool ok = active && tnear <= tfar && S.num_instances > 0 && shear_setup(d, rs);
-    const uint32_t live = __ballot_sync(kAll, ok);
-    if (!live) return false;
-    const V3 idw = v3(box_rcp(d.x), box_rcp(d.y), box_rcp(d.z));
-    V3 ro = o, rid = idw;
-    float best_t = tfar, bu = 0.0f, bv = 0.0f;
-    uint32_t best_inst = kInvalid, best_prim = kInvalid, cur_inst = 0;
-    bool found = false;
-    int sp = 0, blas_base = -1;
-    const uint32_t t0 = __reduce_min_sync(kAll, ok ? __float_as_uint(fmaxf(tnear, 0.0f)) : 0x7F800000u);
-    if (lane == 0) stk[0] = PacketEntry{S.tlas_root, live, __uint_as_float(t0), 0u};
-    sp = 1;
-    __syncwarp();
-    for (uint32_t guard = 0; sp > 0; ++guard) {
-        if (guard > (1u << 22)) {  // a malformed tree can never spin a warp forever
-            overflow = 1;
-            break;
-        }
-        if (blas_base >= 0 && sp == blas_base) {  // the instance's tree is done: back to world space
-            blas_base = -1;
-            ro = o;
-            rid = idw;
-        }
-        --sp;
-        const PacketEntry e = stk[sp];
-        __syncwarp();  // every lane has read the entry before a push overwrites it
-        const bool mine = ((e.mask >> lane) & 1u) && !(e.tmin > best_t);
-        const uint32_t need = __ballot_sync(kAll, mine);
-        if (!need) continue;
-        if (e.node & kInstTag) {
-            const uint32_t ii = e.node & ~kInstTag;
-            const DevInstance* I = S.insts + ii;
-            float m[12];
-#pragma unroll
-            for (int k = 0; k < 12; ++k) m[k] = __ldg(&I->inv[k]);
-            V3 rd;
-            to_object(m, o, d, ro, rd);
-            const bool sok = shear_setup(rd, rs);
-            rid = v3(box_rcp(rd.x), box_rcp(rd.y), box_rcp(rd.z));
-            const uint32_t mk = __ballot_sync(kAll, mine && sok);
-            if (mk) {
-                blas_base = sp;
-                cur_inst = ii;
-                if (lane == 0) stk[sp] = PacketEntry{__ldg(&I->blas_root), mk, e.tmin, 0u};
-                ++sp;
-            } else {
-                ro = o;
-                rid = idw;
-            }
-            __syncwarp();
-            continue;
-        }
-        if (lane == 0) ++tc.nodes;
-        const bool in_blas = blas_base >= 0;
-        const uint4* N = S.nodes + 8 * (size_t)e.node;
-        const uint4 w0 = __ldg(N + 0), w1 = __ldg(N + 1);
-        const uint4 qlx = __ldg(N + 2), qly = __ldg(N + 3), qlz = __ldg(N + 4);
-        const uint4 qhx = __ldg(N + 5), qhy = __ldg(N + 6), qhz = __ldg(N + 7);
-        const float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
-        const uint32_t exps = w0.w;
-        const uint32_t imask = exps >> 24;
-        const uint32_t child_base = w1.x, prim_base = w1.y, meta_lo = w1.z, meta_hi = w1.w;
-        const float sx = __uint_as_float((exps & 0xFFu) << 23);
-        const float sy = __uint_as_float(((exps >> 8) & 0xFFu) << 23);
-        const float sz = __uint_as_float(((exps >> 16) & 0xFFu) << 23);
-        const float ax = sx * rid.x, ay = sy * rid.y, az = sz * rid.z;
-        const float bx = (px - ro.x) * rid.x, by = (py - ro.y) * rid.y, bz = (pz - ro.z) * rid.z;
-        const uint4 nx = rid.x >= 0.0f ? qlx : qhx, fx = rid.x >= 0.0f ? qhx : qlx;
-        const uint4 ny = rid.y >= 0.0f ? qly : qhy, fy = rid.y >= 0.0f ? qhy : qly;
-        const uint4 nz = rid.z >= 0.0f ? qlz : qhz, fz = rid.z >= 0.0f ? qhz : qlz;
-        uint32_t key[8];
-        uint32_t cmask[8];
-        uint32_t leafslots = 0;
-#pragma unroll
-        for (int s = 0; s < 8; ++s) {
-            const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> (8 * (s & 3))) & 0xFFu;
-            const bool internal = (imask >> s) & 1u;
-            const bool valid = internal || meta != 0u;
-            const float tnx = fmaf(qword(nx, s), ax, bx), tfx = fmaf(qword(fx, s), ax, bx);
-            const float tny = fmaf(qword(ny, s), ay, by), tfy = fmaf(qword(fy, s), ay, by);
-            const float tnz = fmaf(qword(nz, s), az, bz), tfz = fmaf(qword(fz, s), az, bz);
-            const float tin = fmaxf(fmaxf(fmaxf(tnx, tny), tnz) * 0.99999952f, tnear);
-            const float tout = fminf(fminf(fminf(tfx, tfy), tfz) * 1.00000048f, best_t);
-            const bool h = mine && valid && tin <= tout;
-            const bool leaf = !internal && in_blas;
-            cmask[s] = __ballot_sync(kAll, h);
-            key[s] = 0xFFFFFFFFu;
-            if (cmask[s]) {
-                if (leaf) {
-                    leafslots |= 1u << s;
-                } else {  // smallest entry distance of the lanes, rounded down to 8 ulp | slot
-                    const uint32_t tb = __reduce_min_sync(kAll, h ? __float_as_uint(fmaxf(tin, 0.0f)) : 0x7F800000u);
-                    key[s] = (tb & ~7u) | (uint32_t)s;
-                }
-            }
-        }
-        // leaf triangles first (they can shrink best_t before the children are pushed)
-        for (uint32_t lm = leafslots; lm; lm &= lm - 1u) {
-            const int s = __ffs(lm) - 1;
-            const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> (8 * (s & 3))) & 0xFFu;
-            const uint32_t cnt = meta >> 5, off = meta & 31u;
-            const bool mine_s = (cmask[s] >> lane) & 1u;
-            for (uint32_t k = 0; k < cnt; ++k) {
-                const float4* Tp = S.tris + 3 * (size_t)(prim_base + off + k);
-                const float4 a = __ldg(Tp), b = __ldg(Tp + 1), c = __ldg(Tp + 2);
-                if (lane == 0) ++tc.tris;
-                float t, u, v;
-                if (mine_s && tri_hit(rs, ro, a, b, c, tnear, best_t, t, u, v)) {
-                    const uint32_t prim = __float_as_uint(a.w);
-                    const bool take = !found || t < best_t ||
-                                      (t == best_t && (cur_inst < best_inst ||
-                                                       (cur_inst == best_inst && prim < best_prim)));
-                    if (take) {
-                        found = true;
-                        best_t = t;
-                        bu = u;
-                        bv = v;
-                        best_inst = cur_inst;
-                        best_prim = prim;
-                    }
-                }
-            }
-        }
-        // 19-comparator sorting network on the warp-uniform keys, ascending entry t
-        cswap(key[0], key[2]); cswap(key[1], key[3]); cswap(key[4], key[6]); cswap(key[5], key[7]);
-        cswap(key[0], key[4]); cswap(key[1], key[5]); cswap(key[2], key[6]); cswap(key[3], key[7]);
-        cswap(key[0], key[1]); cswap(key[2], key[3]); cswap(key[4], key[5]); cswap(key[6], key[7]);
-        cswap(key[2], key[4]); cswap(key[3], key[5]);
-        cswap(key[1], key[4]); cswap(key[3], key[6]);
-        cswap(key[1], key[2]); cswap(key[3], key[4]); cswap(key[5], key[6]);
-        // push far to near: lane j writes the j-th pushed entry
-        int npush = 0;
-#pragma unroll
-        for (int j = 7; j >= 0; --j) {
-            const uint32_t k = key[j];
-            if (k == 0xFFFFFFFFu) continue;
-            if (sp + npush >= kPacketStack) {  // full: the farthest entries are dropped (counted)
-                overflow = 1;
-                continue;
-            }
-            if (lane == npush) {
-                const uint32_t s = k & 7u;
-                const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> (8 * (s & 3))) & 0xFFu;
-                const uint32_t id = ((imask >> s) & 1u) ? child_base + meta
-                                                        : kInstTag | __ldg(tlas_items + prim_base + (meta & 31u));
-                stk[sp + npush] = PacketEntry{id, cmask[s], __uint_as_float(k & ~7u), 0u};
-            }
-            ++npush;
-        }
-        sp += npush;
-        __syncwarp();
-    }
-    if (!found) return false;
-    hit.inst = best_inst;
-    hit.prim = best_prim;
-    hit.t = best_t;
-    hit.u = bu;
-    hit.v = bv;
-    return true;
-}
-
 // Closest hit; returns true and fills `hit` when a triangle is found.
 __device__ __forceinline__ bool trace_closest(const DevScene& S, const uint32_t* __restrict__ tlas_items, V3 o, V3 d,
                                            float tnear, float tfar, RayHit& hit, TraceStack& st, TraceCounters& tc)

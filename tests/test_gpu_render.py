@@ -134,22 +134,6 @@ def test_benchmark_scene_with_sun_lobes_statistically_matches_oracle(gpu, oracle
     assert abs(glob) < 4, glob
 
 
-def test_warp_coherent_camera_rays_give_the_per_ray_image(gpu, scenes):
-    """The first camera bounce traced warp-coherently (the default) and ray by
-    ray give the same hits, so the same film: bit for bit on the benchmark
-    scene (no point light, no atomics), to FP32 summation order with a light."""
-    sc = scenes.scene_c2(192, 108, 1)
-    _, a, _, ca, sa = _render(gpu, sc, 8, seed=21, variance=False)
-    _, b, _, cb, sb = _render(gpu, sc, 8, seed=21, variance=False, traversal=1)
-    assert np.array_equal(ca, cb) and np.array_equal(a, b)
-    assert sa["extension_rays"] == sb["extension_rays"]
-    assert sa["nodes_visited"] < sb["nodes_visited"]  # per warp fetch on the first bounce
-    sc = scenes.scene_c1(64, 64, 1)
-    _, a, _, _, _ = _render(gpu, sc, 32, seed=22, variance=False)
-    _, b, _, _, _ = _render(gpu, sc, 32, seed=22, variance=False, traversal=1)
-    assert np.abs(a - b).max() <= 1e-6 * np.abs(a).max()
-
-
 def test_same_seed_same_image_and_partition_invariance(gpu, scenes):
     sc = scenes.scene_c1(64, 64, 1)
     _, a, _, _, _ = _render(gpu, sc, 64, seed=9, variance=False)

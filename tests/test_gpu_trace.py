@@ -12,7 +12,7 @@ FLT_MAX = np.float32(3.402823466e38)
 # every acceleration-structure builder must give the same hits: the box tests
 # are conservative and the hit contract (closest t, then lowest instance and
 # primitive) does not depend on the tree
-BUILDERS = pytest.mark.parametrize("builder", [0, 1, 2], ids=["ploc", "lbvh", "host_sah"])
+BUILDERS = pytest.mark.parametrize("builder", [0, 1, 2, 3], ids=["sah", "ploc", "lbvh", "host_sah"])
 
 
 def _hits_equal(a, b):
