@@ -256,7 +256,8 @@ def run_batched(args, dev):
     return {"jobs": n, "paths": paths, "plain_jobs_per_s": round(n / t_plain, 3),
             "batched_jobs_per_s": round(n / t_batch, 3), "speedup": round(t_plain / t_batch, 3),
             "plain_mpaths_per_s": round(paths / t_plain / 1e6, 2), "batched_mpaths_per_s": round(paths / t_batch / 1e6, 2),
-            "wave_paths": chosen, "graph": True, "films_match": match, "counts_match": counts_match,
+            "wave_paths": chosen, "shade_block_threads": br.block_threads, "graph": True, "films_match": match,
+            "counts_match": counts_match,
             "films_max_rel_diff": rel,
             "timing": "host wall clock with device synchronisation, one pass over all jobs",
             "equal_rmse": "same estimator, jobs and spp: identical films up to summation order",
@@ -544,6 +545,31 @@ def run_lights(args, dev, flush):
     return out
 
 
+def run_c5(args, dev):
+    """Batched inverse material fit (32 scenes x 50k triangles x 4 materials,
+    256x256, targets at 1024 spp, 200 Adam steps at lr 1e-2, 16 spp forward
+    and adjoint): all scenes in one group, a step being one batch render and
+    one batch of adjoint jobs, against the same fit with one scene after
+    another through their own handles (timed over its first steps; both
+    forms do the same work per step).  Parameter errors against the hidden
+    values."""
+    inv = importlib.import_module("openmaterial-validation_gb300.inverse")
+    g = inv.fit(n_scenes=args.c5_scenes, tris=50_000, res=256, spp=16, target_spp=1024, steps=args.c5_steps,
+                lr=1e-2, seed=0)
+    seq_steps = max(1, min(10, args.c5_steps))
+    q = inv.fit_sequential(n_scenes=args.c5_scenes, tris=50_000, res=256, spp=16, target_spp=1024,
+                           steps=seq_steps, lr=1e-2, seed=0)
+    per_g, per_q = g.seconds / g.steps, q.seconds / q.steps
+    return {"scenes": args.c5_scenes, "steps": g.steps, "group_seconds": round(g.seconds, 2),
+            "group_seconds_per_step": round(per_g, 4), "sequential_seconds_per_step": round(per_q, 4),
+            "sequential_steps_timed": q.steps, "speedup_per_step": round(per_q / per_g, 2),
+            "roughness_error": [round(g.initial_roughness_error, 4), round(g.final_roughness_error, 4)],
+            "conductor_nk_error": [round(g.initial_ior_error, 4), round(g.final_ior_error, 4)],
+            "parameter_error": [round(g.initial_error, 4), round(g.final_error, 4)],
+            "loss": [g.initial_loss, g.final_loss],
+            "timing": "host wall clock of the optimisation loop (targets excluded), device synchronised each step"}
+
+
 def run_builders(args, dev, scene, flush):
     """The four acceleration-structure builders on the benchmark scene: the
     scene creation time (omv_scene_create, which the build dominates) and the
@@ -719,6 +745,8 @@ def run_ours(args, scene, ws, rank, local):
             line["batched"] = run_batched(args, dev)
         if ws == 1 and not args.no_adjoint:
             line["adjoint"] = run_adjoint(args, dev)
+        if ws == 1 and not args.no_c5:
+            line["c5"] = run_c5(args, dev)
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -744,6 +772,9 @@ def main():
     ap.add_argument("--batch-jobs", type=int, default=256)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-vs-finite-difference leg")
     ap.add_argument("--adjoint-spp", type=int, default=32)
+    ap.add_argument("--no-c5", action="store_true", help="skip the batched inverse-fit leg")
+    ap.add_argument("--c5-scenes", type=int, default=32)
+    ap.add_argument("--c5-steps", type=int, default=200)
     args = ap.parse_args()
     ws, rank, local = _dist()
     if args.impl == "reference" and rank != 0:

@@ -179,6 +179,23 @@ typedef struct omv_scene omv_scene;
 omv_status omv_scene_create(const omv_scene_desc* desc, int32_t device, omv_scene** out);
 omv_status omv_scene_destroy(omv_scene* scene);
 
+/* Several independent scenes in one handle (a group); the reference has no
+ * counterpart (one RenderScene per process).  Each scene keeps its meshes,
+ * instances, materials, lights and textures and gets its own top-level tree;
+ * all geometry lives in one device copy and the bottom-level trees of every
+ * mesh are built in one pass.  Batch jobs (omv_job.part) and adjoint jobs
+ * choose their scene, so one wave pipeline renders many scenes at once.
+ *   - Scene p's materials are numbered after those of scenes 0..p-1 (the
+ *     group's material order), followed by the one missing material;
+ *     omv_batch_set_materials and omv_scene_set_materials take the group's
+ *     order.  Each scene's light pick uses its own lights only.
+ *   - Either every scene has point lights or none has; the scenes share one
+ *     HDRI background (the same image, rotation and scale) or none has one.
+ *     descs[0].bvh_builder builds all of them.
+ *   - The single-frame calls (omv_render, omv_render_device, omv_render_ids,
+ *     omv_trace_rays, omv_adjoint, ...) render scene 0. */
+omv_status omv_scene_create_group(int32_t num_scenes, const omv_scene_desc* descs, int32_t device, omv_scene** out);
+
 typedef struct omv_scene_info {
     int64_t num_triangles;
     int64_t num_blas_nodes;
@@ -338,7 +355,7 @@ typedef struct omv_job {
     int32_t sample_offset;
     uint64_t seed;
     int32_t material_set;   /* index into omv_batch_set_materials' sets; -1: the scene's materials */
-    int32_t pad;
+    int32_t part;           /* scene of a group (omv_scene_create_group); 0 for a single scene */
     double* d_sum_rgb;      /* 3 * width * height */
     double* d_sumsq_rgb;    /* may be NULL (required when params->accumulate_variance) */
     uint32_t* d_count;      /* width * height */
@@ -363,11 +380,13 @@ enum { OMV_BATCH_GRAPH = 1 };  /* capture the batch once as a CUDA graph; replay
 omv_status omv_render_batch(omv_scene* scene, int32_t num_jobs, const omv_job* jobs, const omv_params* params,
                             void* stream, int32_t flags, omv_stats* stats);
 
-/* Times a few wave sizes on this job list (renders it several times into the
- * jobs' films: clear them afterwards) and keeps the fastest for the scene's
- * later batches; *chosen_wave_paths (may be NULL) receives it. */
+/* Times wave sizes (the ray and shadow queue capacities follow them) and the
+ * threads per block of the shading kernels (128, 256) on this job list
+ * (renders it several times into the jobs' films: clear them afterwards) and
+ * keeps the fastest pair for the scene's later batches; *chosen_wave_paths
+ * and *chosen_block_threads (either may be NULL) receive it. */
 omv_status omv_batch_autotune(omv_scene* scene, int32_t num_jobs, const omv_job* jobs, const omv_params* params,
-                              void* stream, int64_t* chosen_wave_paths);
+                              void* stream, int64_t* chosen_wave_paths, int32_t* chosen_block_threads);
 
 /* ------------------------------------------------------- differentiation --- */
 
@@ -398,6 +417,23 @@ omv_status omv_scene_set_materials(omv_scene* scene, int32_t num_materials, cons
  * legacy default stream).  The reference has no counterpart (it renders only). */
 omv_status omv_adjoint(omv_scene* scene, const omv_camera* camera, const omv_params* params,
                        const float* d_adjoint_rgb, float* d_grad, void* stream);
+
+/* One replay of a batch of adjoints: the job's scene (job.part), material set,
+ * camera, samples, sample offset and seed, as the forward batch job rendered
+ * them (films are not used).  d_grad (DEVICE) receives the gradient with
+ * respect to the parameters of that scene's materials only, in their order
+ * within the scene (num materials of the scene x OMV_MATERIAL_PARAMS). */
+typedef struct omv_adjoint_job {
+    omv_job job;
+    const float* d_adjoint_rgb;  /* DEVICE, width * height * 3: dLoss / dImage */
+    float* d_grad;               /* DEVICE, accumulated into */
+} omv_adjoint_job;
+
+/* The adjoints of all jobs, enqueued back to back on `stream` (NULL: the
+ * legacy default stream); params->samples_per_pixel, seed and sample_offset
+ * are taken from each job.  The reference has no counterpart. */
+omv_status omv_adjoint_batch(omv_scene* scene, int32_t num_jobs, const omv_adjoint_job* jobs,
+                             const omv_params* params, void* stream);
 
 /* ----------------------------------------------------- rays / ID buffers --- */
 
@@ -574,7 +610,7 @@ omv_status omv_set_log_callback(omv_log_fn fn, void* user);
 /* sizeof of the public structs in this order: omv_mesh_desc, omv_instance_desc,
  * omv_material_desc, omv_light_desc, omv_hdri_desc, omv_scene_desc,
  * omv_scene_info, omv_camera, omv_params, omv_stats, omv_hit, omv_job,
- * omv_texture_desc, omv_texture_ref -- for binding
+ * omv_texture_desc, omv_texture_ref, omv_adjoint_job -- for binding
  * layout checks (no reference counterpart).  With out == NULL returns the
  * count; otherwise writes min(n, count) sizes and returns that number. */
 int32_t omv_struct_sizes(int64_t* out, int32_t n);

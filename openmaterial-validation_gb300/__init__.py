@@ -114,9 +114,11 @@ def lib():
     L.omv_render_batch.argtypes = [vp, C.c_int32, C.POINTER(capi.Job), C.POINTER(capi.Params), vp, C.c_int32,
                                    C.POINTER(capi.Stats)]
     L.omv_batch_autotune.argtypes = [vp, C.c_int32, C.POINTER(capi.Job), C.POINTER(capi.Params), vp,
-                                     C.POINTER(C.c_int64)]
+                                     C.POINTER(C.c_int64), C.POINTER(C.c_int32)]
     L.omv_scene_set_materials.argtypes = [vp, C.c_int32, C.POINTER(capi.MaterialDesc)]
     L.omv_adjoint.argtypes = [vp, C.POINTER(capi.Camera), C.POINTER(capi.Params), vp, vp, vp]
+    L.omv_scene_create_group.argtypes = [C.c_int32, C.POINTER(capi.SceneDesc), C.c_int32, C.POINTER(vp)]
+    L.omv_adjoint_batch.argtypes = [vp, C.c_int32, C.POINTER(capi.AdjointJob), C.POINTER(capi.Params), vp]
     L.omv_trace_rays.argtypes = [vp, C.c_int64, capi.f32p, C.POINTER(capi.Hit)]
     L.omv_render_ids.argtypes = [vp, C.POINTER(capi.Camera), capi.f32p, C.c_uint64, C.POINTER(capi.Hit),
                                  C.POINTER(C.c_uint32)]
@@ -280,6 +282,32 @@ class RenderScene:
         check(lib().omv_scene_create(C.byref(self._holder.desc), device, C.byref(h)))
         self.handle = h
 
+    @classmethod
+    def group(cls, scenes_: list, device: int = 0, bvh_builder: int = capi.BVH_SAH) -> "RenderScene":
+        """Several scenes in one handle (omv_scene_create_group): batch and
+        adjoint jobs pick one by `part`; materials are numbered scene after
+        scene (material_offsets)."""
+        self = cls.__new__(cls)
+        self.spec = scenes_[0]
+        self.parts = list(scenes_)
+        self._holders = [capi.DescHolder(sc, bvh_builder) for sc in scenes_]
+        arr = (capi.SceneDesc * len(scenes_))(*[h.desc for h in self._holders])
+        self._arr = arr
+        h = C.c_void_p()
+        check(lib().omv_scene_create_group(len(scenes_), arr, device, C.byref(h)))
+        self.handle = h
+        return self
+
+    @property
+    def material_offsets(self) -> list:
+        """First material of each scene in the group's material order."""
+        parts = getattr(self, "parts", [self.spec])
+        out, k = [], 0
+        for sc in parts:
+            out.append(k)
+            k += len(sc.materials)
+        return out
+
     def info(self) -> dict:
         i = capi.SceneInfo()
         check(lib().omv_scene_get_info(self.handle, C.byref(i)))
@@ -338,10 +366,11 @@ class BatchRenderer:
 
     @staticmethod
     def job(camera: "PinholeCamera", spp: int, film, seed: int = 0, material_set: int = -1,
-            sample_offset: int = 0) -> "capi.Job":
+            sample_offset: int = 0, part: int = 0) -> "capi.Job":
         j = capi.Job()
         j.camera = camera.to_c() if hasattr(camera, "to_c") else camera
         j.samples_per_pixel, j.sample_offset, j.seed, j.material_set = spp, sample_offset, seed, material_set
+        j.part = part
         j.d_sum_rgb = film[0].data_ptr()
         j.d_sumsq_rgb = film[1].data_ptr() if film[1] is not None else None
         j.d_count = film[2].data_ptr()
@@ -355,11 +384,27 @@ class BatchRenderer:
                                      capi.OMV_BATCH_GRAPH if graph else 0, C.byref(st) if st else None))
         return st
 
+    def adjoint(self, jobs, adjoints, grads, stream=None) -> None:
+        """omv_adjoint_batch: for every job its adjoint image (H, W, 3) float32
+        and its gradient buffer (scene materials, 11) float32, device tensors."""
+        arr = (capi.AdjointJob * len(jobs))()
+        for i, (j, a, g) in enumerate(zip(jobs, adjoints, grads)):
+            arr[i].job = j
+            arr[i].d_adjoint_rgb = a.data_ptr()
+            arr[i].d_grad = g.data_ptr()
+        p = self.params.to_c()
+        check(lib().omv_adjoint_batch(self.scene.handle, len(jobs), arr, C.byref(p), stream))
+
     def autotune(self, jobs, stream=None) -> int:
+        """Picks the wave size and shading block size for these jobs; returns
+        the wave size (the block size is in self.block_threads)."""
         arr = (capi.Job * len(jobs))(*jobs)
         p = self.params.to_c()
         chosen = C.c_int64(0)
-        check(lib().omv_batch_autotune(self.scene.handle, len(jobs), arr, C.byref(p), stream, C.byref(chosen)))
+        threads = C.c_int32(0)
+        check(lib().omv_batch_autotune(self.scene.handle, len(jobs), arr, C.byref(p), stream, C.byref(chosen),
+                                       C.byref(threads)))
+        self.block_threads = threads.value
         return chosen.value
 
 

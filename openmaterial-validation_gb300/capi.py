@@ -114,8 +114,12 @@ HIT_DTYPE = np.dtype([("inst", "<u4"), ("geom", "<u4"), ("prim", "<u4"), ("mater
 
 class Job(C.Structure):
     _fields_ = [("camera", Camera), ("samples_per_pixel", C.c_int32), ("sample_offset", C.c_int32),
-                ("seed", C.c_uint64), ("material_set", C.c_int32), ("pad", C.c_int32),
+                ("seed", C.c_uint64), ("material_set", C.c_int32), ("part", C.c_int32),
                 ("d_sum_rgb", C.c_void_p), ("d_sumsq_rgb", C.c_void_p), ("d_count", C.c_void_p)]
+
+
+class AdjointJob(C.Structure):
+    _fields_ = [("job", Job), ("d_adjoint_rgb", C.c_void_p), ("d_grad", C.c_void_p)]
 
 
 OMV_BATCH_GRAPH = 1

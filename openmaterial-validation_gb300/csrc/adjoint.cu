@@ -45,6 +45,7 @@ struct AdjArgs {
     const float* adj;  // W*H*3 adjoint image
     float* grad;       // num_user_materials * kSlots
     int32_t num_user_materials;
+    uint32_t mat_base;  // first material of the scene (a scene of a group)
 };
 
 // derivatives of a vertex weight (or evaluation) with respect to the
@@ -129,11 +130,12 @@ __device__ __forceinline__ void add_finite(float& slot, float t)
     if (fabsf(t) <= kFltMax) slot += t;
 }
 
-// adds sum_c a[c] * g.d[c][i] to the material's parameter slots
+// adds sum_c a[c] * g.d[c][i] to the material's parameter slots (`mat`:
+// the material's number within the rendered scene)
 __device__ __forceinline__ void accumulate(float* acc, const DevMaterial& M, uint32_t mat, int nmat, V3 a,
                                            const LocalGrad& g)
 {
-    if ((int)mat >= nmat) return;  // the missing material has no parameters
+    if (mat >= (uint32_t)nmat) return;  // the missing material has no parameters
     const float av[3] = {a.x, a.y, a.z};
     float* o = acc + mat * kSlots;
     if (M.type == kMatPbr) {
@@ -373,8 +375,8 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint(AdjArgs A)
                 const DevMaterial M = S.mats[cv.mat];
                 // d/dparams of tp_b * (G_b + w_b * R_{b+1})
                 const V3 a = mul(delta, cv.tp);
-                accumulate(acc, M, cv.mat, nmat, a, cv.gG);
-                if (cv.has_w) accumulate(acc, M, cv.mat, nmat, mul(a, Rs), cv.gw);
+                accumulate(acc, M, cv.mat - A.mat_base, nmat, a, cv.gG);
+                if (cv.has_w) accumulate(acc, M, cv.mat - A.mat_base, nmat, mul(a, Rs), cv.gw);
             }
             Rs = cv.has_w ? cv.G + mul(cv.w, Rs) : cv.G;
         }
@@ -383,7 +385,7 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint(AdjArgs A)
         for (int j = nl; j >= 1; --j) {
             const LightVert& lv = L[j];
             Ss = (j == nl) ? lv.q : lv.q + mul(L[j + 1].w, Ss);
-            accumulate(acc, S.mats[lv.mat], lv.mat, nmat, mul(lv.pre, Ss), lv.g);
+            accumulate(acc, S.mats[lv.mat], lv.mat - A.mat_base, nmat, mul(lv.pre, Ss), lv.g);
         }
     }
     // ---- reduce: warp shuffles, block shared memory, one atomic per block and slot
@@ -401,15 +403,17 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint(AdjArgs A)
 }  // namespace
 
 void adjoint_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, const float* d_adjoint, float* d_grad,
-                   cudaStream_t st)
+                   cudaStream_t st, int part, const DevMaterial* mats)
 {
+    if (part < 0 || part >= (int)s.parts.size()) throw ArgError("adjoint scene (part) out of range");
+    const ScenePart& P = s.parts[part];
     if (cam.width <= 0 || cam.height <= 0) throw ArgError("camera resolution must be positive");
     if (p.samples_per_pixel <= 0) throw ArgError("the adjoint needs at least one sample per pixel");
     if (p.camera_bounces < 0 || p.light_bounces < 0) throw ArgError("negative bounce count");
     if (p.camera_bounces >= kAdjMaxVerts || p.light_bounces >= kAdjMaxVerts)
         throw ArgError("the adjoint supports at most 15 camera and 15 light bounces");
-    const int nmat = s.num_materials - 1;
-    if (nmat > kAdjMaxMaterials) throw ArgError("the adjoint supports at most 16 materials");
+    const int nmat = P.mat_count;
+    if (nmat > kAdjMaxMaterials) throw ArgError("the adjoint supports at most 16 materials per scene");
     if (!d_adjoint || !d_grad) throw ArgError("adjoint image and gradient buffers are required");
     if (p.estimator != OMV_ESTIMATOR_REFERENCE) throw ArgError("the adjoint replays the reference estimator only");
     for (const DevMaterial& m : s.h_mats)
@@ -417,6 +421,15 @@ void adjoint_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, con
             throw ArgError("the adjoint differentiates untextured materials only");
     AdjArgs A;
     A.S = s.dev;
+    // the scene of the group: its top-level tree, its lights, the job's materials
+    A.S.tlas_root = P.tlas_root;
+    A.S.light_pos += P.light_base;
+    A.S.light_int += P.light_base;
+    A.S.light_cdf += P.light_base;
+    A.S.num_lights = P.light_count;
+    A.S.light_max = P.light_max;
+    if (mats) A.S.mats = mats;
+    A.mat_base = (uint32_t)P.mat_base;
     A.items = s.tlas_items;
     A.cam = cam;
     A.seed = p.seed;
@@ -439,6 +452,28 @@ void adjoint_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, con
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)std::max(1, occ) * s.num_sms * 4));
     k_adjoint<<<grid, kAdjThreads, 0, st>>>(A);
     OMV_CUDA(cudaGetLastError());
+}
+
+void adjoint_batch(SceneHost& s, int n, const omv_adjoint_job* jobs, const omv_params& p, cudaStream_t st)
+{
+    for (int i = 0; i < n; ++i) {  // checked before anything is enqueued
+        const omv_job& j = jobs[i].job;
+        if (j.material_set < -1 || j.material_set >= s.num_mat_sets)
+            throw ArgError("adjoint job material set out of range");
+        if (j.part < 0 || j.part >= (int)s.parts.size()) throw ArgError("adjoint job scene (part) out of range");
+        if (j.samples_per_pixel <= 0 || j.camera.width <= 0 || j.camera.height <= 0)
+            throw ArgError("adjoint job without samples or pixels");
+        if (!jobs[i].d_adjoint_rgb || !jobs[i].d_grad) throw ArgError("adjoint job without adjoint image or gradient");
+    }
+    for (int i = 0; i < n; ++i) {
+        const omv_job& j = jobs[i].job;
+        omv_params q = p;
+        q.samples_per_pixel = j.samples_per_pixel;
+        q.sample_offset = j.sample_offset;
+        q.seed = j.seed;
+        const DevMaterial* mats = j.material_set < 0 ? nullptr : s.mat_sets + (size_t)j.material_set * s.num_materials;
+        adjoint_frame(s, j.camera, q, jobs[i].d_adjoint_rgb, jobs[i].d_grad, st, j.part, mats);
+    }
 }
 
 }  // namespace omv

@@ -1283,6 +1283,12 @@ __global__ void k_iota(int n, uint32_t* v)
     if (i < n) v[i] = (uint32_t)i;
 }
 
+__global__ void k_add_u32(int n, uint32_t* v, uint32_t add)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] += add;
+}
+
 }  // namespace
 
 // Binary tree by the surface area heuristic, leaves of one item: binned
@@ -1682,7 +1688,7 @@ static std::vector<uint32_t> collapse_forest(bool tlas, const Forest& f, int nit
 void validate_accel(const AccelResult& a, const std::vector<MeshGeom>& meshes, cudaStream_t st);
 
 void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<InstanceGeom>& insts, BvhBuilder builder,
-                 AccelResult& out, cudaStream_t st)
+                 AccelResult& out, cudaStream_t st, int nparts)
 {
     size_t total_tri = 0;
     for (const auto& m : meshes) total_tri += m.valid ? m.num_faces : 0;
@@ -1803,9 +1809,15 @@ void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<Instance
     // ---- top level: world boxes of the valid instances (their referenced
     // vertices through the instance transform), widened so that no
     // object-space hit is ever culled by world-space rounding
-    std::vector<uint32_t> ids;
-    for (size_t i = 0; i < insts.size(); ++i)
-        if (insts[i].valid) ids.push_back((uint32_t)i);
+    // valid instances grouped by scene (one top-level tree each), in order
+    std::vector<uint32_t> ids, part_base(nparts, 0);
+    for (int p = 0; p < nparts; ++p) {
+        part_base[p] = (uint32_t)ids.size();
+        for (size_t i = 0; i < insts.size(); ++i)
+            if (insts[i].valid && insts[i].part == p) ids.push_back((uint32_t)i);
+        if (ids.size() == part_base[p] && nparts > 1)
+            throw std::runtime_error("scene " + std::to_string(p) + " of the group has no valid instance");
+    }
     std::vector<Box> ib(ids.size());
     if (!ids.empty()) {
         DBuf<uint32_t> ob(6 * ids.size());
@@ -1846,29 +1858,58 @@ void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<Instance
         }
     }
     out.num_valid_instances = (uint32_t)ib.size();
+    out.tlas_roots.assign(nparts, 0xFFFFFFFFu);
     if (!ib.empty()) {
         const int n = (int)ib.size();
         DBuf<Box> boxes(n);
         OMV_CK(cudaMemcpyAsync(boxes.p, ib.data(), sizeof(Box) * n, cudaMemcpyHostToDevice, st));
-        Forest f;
-        if (builder == BvhBuilder::HostSah) {
-            host_sah_forest(ib, f, st);
-        } else {
-            DBuf<uint32_t> cb(6);
-            const uint32_t init[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
-            OMV_CK(cudaMemcpyAsync(cb.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
-            k_box_cbounds<<<blocks(n, 256), 256, 0, st>>>(n, boxes.p, cb.p);
-            OMV_CK(cudaGetLastError());
-            if (builder == BvhBuilder::Lbvh)
-                lbvh_tree(n, boxes.p, cb.p, f, st);
-            else if (builder == BvhBuilder::Sah)
-                sah_forest(n, std::vector<uint32_t>{0u}, boxes.p, f, st);
-            else
-                ploc_forest(n, std::vector<uint32_t>{0u}, boxes.p, cb.p, f, st);
-        }
         OMV_CK(cudaMemsetAsync(counters.p + 1, 0, sizeof(uint32_t), st));
-        out.tlas_root = collapse_forest(true, f, n, boxes.p, nullptr, 0, out.nodes, counters.p, node_cap, nullptr,
-                                        out.tlas_items, st)[0];
+        auto count_of = [&](int p) { return (int)((p + 1 < nparts ? part_base[p + 1] : (uint32_t)n) - part_base[p]); };
+        if (builder == BvhBuilder::Sah || builder == BvhBuilder::Ploc) {
+            // all scenes' top-level trees in one forest
+            Forest f;
+            if (builder == BvhBuilder::Sah) {
+                sah_forest(n, part_base, boxes.p, f, st);
+            } else {
+                DBuf<uint32_t> cb(6 * (size_t)nparts);
+                std::vector<uint32_t> init(6 * (size_t)nparts);
+                for (int p = 0; p < nparts; ++p)
+                    for (int a = 0; a < 3; ++a) {
+                        init[6 * p + a] = 0xFFFFFFFFu;
+                        init[6 * p + 3 + a] = 0u;
+                    }
+                OMV_CK(cudaMemcpyAsync(cb.p, init.data(), sizeof(uint32_t) * init.size(), cudaMemcpyHostToDevice, st));
+                for (int p = 0; p < nparts; ++p)
+                    k_box_cbounds<<<blocks(count_of(p), 256), 256, 0, st>>>(count_of(p), boxes.p + part_base[p],
+                                                                            cb.p + 6 * p);
+                OMV_CK(cudaGetLastError());
+                ploc_forest(n, part_base, boxes.p, cb.p, f, st);
+            }
+            out.tlas_roots = collapse_forest(true, f, n, boxes.p, nullptr, 0, out.nodes, counters.p, node_cap, nullptr,
+                                             out.tlas_items, st);
+        } else {
+            // one tree per scene; item numbers made global before the collapse
+            for (int p = 0; p < nparts; ++p) {
+                const int cnt = count_of(p);
+                Forest f;
+                if (builder == BvhBuilder::HostSah) {
+                    host_sah_forest(std::vector<Box>(ib.begin() + part_base[p], ib.begin() + part_base[p] + cnt), f,
+                                    st);
+                } else {
+                    DBuf<uint32_t> cb(6);
+                    const uint32_t init[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
+                    OMV_CK(cudaMemcpyAsync(cb.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
+                    k_box_cbounds<<<blocks(cnt, 256), 256, 0, st>>>(cnt, boxes.p + part_base[p], cb.p);
+                    OMV_CK(cudaGetLastError());
+                    lbvh_tree(cnt, boxes.p + part_base[p], cb.p, f, st);
+                }
+                k_add_u32<<<blocks(cnt, 256), 256, 0, st>>>(cnt, f.vals, part_base[p]);
+                OMV_CK(cudaGetLastError());
+                out.tlas_roots[p] = collapse_forest(true, f, cnt, boxes.p, nullptr, 0, out.nodes, counters.p, node_cap,
+                                                    nullptr, out.tlas_items, st)[0];
+            }
+        }
+        out.tlas_root = out.tlas_roots[0];
         // TLAS items are positions in `ids`; translate to instance indices
         std::vector<uint32_t> items(n);
         OMV_CK(cudaMemcpyAsync(items.data(), out.tlas_items, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, st));
@@ -1935,7 +1976,8 @@ void validate_accel(const AccelResult& a, const std::vector<MeshGeom>& meshes, c
     };
     for (size_t i = 0; i < meshes.size(); ++i)
         if (a.blas_root[i] != 0xFFFFFFFFu) walk(a.blas_root[i], false, (uint32_t)a.num_tris, (uint32_t)meshes[i].num_faces);
-    if (a.num_valid_instances) walk(a.tlas_root, true, a.num_valid_instances, 0xFFFFFFFFu);
+    if (a.num_valid_instances)
+        for (uint32_t r : a.tlas_roots) walk(r, true, a.num_valid_instances, 0xFFFFFFFFu);
 }
 
 }  // namespace omv

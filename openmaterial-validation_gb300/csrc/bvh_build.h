@@ -24,6 +24,7 @@ struct MeshGeom {
 struct InstanceGeom {
     bool valid = false;
     int mesh = -1;
+    int part = 0;  // scene of a group (one top-level tree per scene)
     float xf[3][4] = {};
 };
 
@@ -34,7 +35,8 @@ struct AccelResult {
     uint32_t num_nodes = 0;
     size_t num_tris = 0;
     std::vector<uint32_t> blas_root;  // per mesh, 0xFFFFFFFF when the mesh is invalid
-    uint32_t tlas_root = 0xFFFFFFFFu;
+    uint32_t tlas_root = 0xFFFFFFFFu;    // scene 0's
+    std::vector<uint32_t> tlas_roots;    // per scene of a group
     uint32_t num_valid_instances = 0;
 };
 
@@ -42,6 +44,6 @@ enum class BvhBuilder { Sah = 0, Ploc = 1, Lbvh = 2, HostSah = 3 };  // OMV_BVH_
 
 // Builds every BLAS and the TLAS; throws std::runtime_error on CUDA errors.
 void build_accel(const std::vector<MeshGeom>& meshes, const std::vector<InstanceGeom>& insts, BvhBuilder builder,
-                 AccelResult& out, cudaStream_t stream);
+                 AccelResult& out, cudaStream_t stream, int nparts = 1);
 
 }  // namespace omv

@@ -142,7 +142,8 @@ int32_t omv_struct_sizes(int64_t* out, int32_t n)
                              (int64_t)sizeof(omv_scene_info), (int64_t)sizeof(omv_camera),
                              (int64_t)sizeof(omv_params),     (int64_t)sizeof(omv_stats),
                              (int64_t)sizeof(omv_hit),        (int64_t)sizeof(omv_job),
-                             (int64_t)sizeof(omv_texture_desc), (int64_t)sizeof(omv_texture_ref)};
+                             (int64_t)sizeof(omv_texture_desc), (int64_t)sizeof(omv_texture_ref),
+                             (int64_t)sizeof(omv_adjoint_job)};
     const int32_t m = (int32_t)(sizeof(sizes) / sizeof(sizes[0]));
     if (!out) return m;
     const int32_t k = std::min(n, m);
@@ -228,13 +229,13 @@ omv_status omv_render_batch(omv_scene* scene, int32_t num_jobs, const omv_job* j
 }
 
 omv_status omv_batch_autotune(omv_scene* scene, int32_t num_jobs, const omv_job* jobs, const omv_params* params,
-                              void* stream, int64_t* chosen_wave_paths)
+                              void* stream, int64_t* chosen_wave_paths, int32_t* chosen_block_threads)
 {
     return guarded([&] {
         check_scene(scene);
         if (!params) throw omv::ArgError("params is NULL");
         cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL: the legacy default stream
-        omv::autotune_batch(*scene->h, num_jobs, jobs, *params, st, chosen_wave_paths);
+        omv::autotune_batch(*scene->h, num_jobs, jobs, *params, st, chosen_wave_paths, chosen_block_threads);
     });
 }
 
@@ -243,6 +244,30 @@ omv_status omv_scene_set_materials(omv_scene* scene, int32_t num_materials, cons
     return guarded([&] {
         check_scene(scene);
         omv::set_scene_materials(*scene->h, num_materials, materials);
+    });
+}
+
+omv_status omv_scene_create_group(int32_t num_scenes, const omv_scene_desc* descs, int32_t device, omv_scene** out)
+{
+    return guarded([&] {
+        if (!descs || !out) throw omv::ArgError("descs and out must not be NULL");
+        if (num_scenes <= 0) throw omv::ArgError("a group needs at least one scene");
+        *out = nullptr;
+        std::unique_ptr<omv_scene> s(new omv_scene);
+        s->h.reset(omv::scene_create_group(num_scenes, descs, device));
+        *out = s.release();
+    });
+}
+
+omv_status omv_adjoint_batch(omv_scene* scene, int32_t num_jobs, const omv_adjoint_job* jobs,
+                             const omv_params* params, void* stream)
+{
+    return guarded([&] {
+        check_scene(scene);
+        if (!params) throw omv::ArgError("params is NULL");
+        if (num_jobs < 0 || (num_jobs > 0 && !jobs)) throw omv::ArgError("invalid adjoint job list");
+        cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL: the legacy default stream
+        omv::adjoint_batch(*scene->h, num_jobs, jobs, *params, st);
     });
 }
 

@@ -136,18 +136,17 @@ OMV_CR_HD void ff_sincos_kernel(FF r, FF& s, FF& c)
     c = ff_add(FF{1.0f, 0.0f}, ff_mul(z, u));
 }
 
-// sin(r) alone (asin's Newton step)
-OMV_CR_HD FF ff_sin_kernel(FF r)
+// sin(y) for a float |y| <= 0.53 (asin's Newton step): y^2 is exact as a
+// double-float, and on this range the terms from y^9 on need float accuracy only
+OMV_CR_HD FF ff_sin_small(float y)
 {
-    FF z = two_prod(r.hi, r.hi);
-    z = fast_two_sum(z.hi, z.lo + 2.0f * r.hi * r.lo);
+    const FF z = two_prod(y, y);
     const float zh = z.hi;
-    float ts = kS5 + zh * (kS6 + zh * (kS7 + zh * kS8));
-    FF t = ff_add(FF{kS4h, kS4l}, ff_mul_f(z, ts));
-    t = ff_add(FF{kS3h, kS3l}, ff_mul(z, t));
+    const float ts = kS4h + zh * (kS5 + zh * (kS6 + zh * kS7));
+    FF t = ff_add(FF{kS3h, kS3l}, ff_mul_f(z, ts));
     t = ff_add(FF{kS2h, kS2l}, ff_mul(z, t));
     t = ff_add(FF{kS1h, kS1l}, ff_mul(z, t));
-    return ff_add(r, ff_mul(r, ff_mul(z, t)));
+    return ff_add(FF{y, 0.0f}, ff_mul_f(ff_mul(z, t), y));
 }
 
 // Correctly rounded sinf / cosf of x in [0, 8] (the sampling angles 2 pi u).
@@ -166,15 +165,25 @@ OMV_CR_HD void sincos_cr(float x, float& s_out, float& c_out)
     c_out = qi == 0 ? cv : qi == 1 ? -sv : qi == 2 ? -cv : sv;
 }
 
-// asin of a double-float t with |t| <= 1/2, as a double-float (one Newton
-// step on sin(y) = t from the float approximation y0)
+// cos(y) and a quotient to about 2^-21 (the Newton correction needs no more)
+OMV_CR_HD float cos_rough(float y)
+{
+#ifdef __CUDA_ARCH__
+    return __cosf(y);
+#else
+    return cosf(y);
+#endif
+}
+
+// asin of a double-float t with 0 <= t <= 1/2, as a double-float: one Newton
+// step on sin(y) = t from the float approximation y0 (the step's own error
+// is of the order of (y - y0)^2, far below the rounding of the result)
 OMV_CR_HD FF asin_ff_small(FF t)
 {
     const float y0 = asinf(t.hi);
-    const FF s = ff_sin_kernel(FF{y0, 0.0f});
+    const FF s = ff_sin_small(y0);
     const float res = (t.hi - s.hi) + (t.lo - s.lo);  // t.hi - s.hi is exact (Sterbenz)
-    const float d = res / cosf(y0);
-    return two_sum(y0, d);
+    return two_sum(y0, res / cos_rough(y0));
 }
 
 // sqrt of a float as a double-float (the residual a - h^2 is exact by FMA)
@@ -185,33 +194,38 @@ OMV_CR_HD FF sqrt_ff(float a)
     return FF{h, fmaf(-h, h, a) / (2.0f * h)};
 }
 
+// The asin of |x| reduced to an argument in [0, 1/2]: |x| itself, or
+// sqrt((1 - |x|) / 2) above 1/2 (asin|x| = pi/2 - 2 asin of that); without a
+// branch, so that the lanes of a warp take one path
+OMV_CR_HD FF asin_reduced(float ax, bool& big)
+{
+    big = ax > 0.5f;
+    const FF r = sqrt_ff((1.0f - ax) * 0.5f);  // 1 - ax exact for ax in [1/2, 1]
+    return asin_ff_small(big ? r : FF{ax, 0.0f});
+}
+
 // correctly rounded asinf for x in [-1, 1]
 OMV_CR_HD float asin_cr(float x)
 {
-    const float ax = fabsf(x);
-    if (ax <= 0.5f) {
-        const FF a = asin_ff_small(FF{x, 0.0f});
-        return a.hi + a.lo;
-    }
-    const FF s = sqrt_ff((1.0f - ax) * 0.5f);  // 1 - ax exact for ax in [1/2, 1]
-    const FF a = asin_ff_small(s);
-    const FF v = ff_add(FF{kPiHalfHi, kPiHalfLo}, FF{-2.0f * a.hi, -2.0f * a.lo});
-    return x < 0.0f ? -v.hi : v.hi;
+    bool big;
+    const FF a = asin_reduced(fabsf(x), big);
+    const FF v = big ? ff_add(FF{kPiHalfHi, kPiHalfLo}, FF{-2.0f * a.hi, -2.0f * a.lo}) : a;
+    const float r = v.hi + v.lo;
+    return x < 0.0f ? -r : r;
 }
 
 // correctly rounded acosf for x in [-1, 1]
 OMV_CR_HD float acos_cr(float x)
 {
-    const float ax = fabsf(x);
-    if (ax <= 0.5f) {
-        const FF a = asin_ff_small(FF{x, 0.0f});
-        return ff_add(FF{kPiHalfHi, kPiHalfLo}, ff_neg(a)).hi;
-    }
-    const FF s = sqrt_ff((1.0f - ax) * 0.5f);
-    const FF a = asin_ff_small(s);
-    const FF b{2.0f * a.hi, 2.0f * a.lo};
-    if (x > 0.0f) return b.hi + b.lo;
-    return ff_add(FF{kPiHi, kPiLo}, ff_neg(b)).hi;
+    bool big;
+    const FF a = asin_reduced(fabsf(x), big);  // asin|x|, or (pi/2 - asin|x|) / 2 when big
+    const bool neg = x < 0.0f;
+    FF v;
+    if (big)  // acos|x| = 2a; acos(-|x|) = pi - 2a
+        v = neg ? ff_add(FF{kPiHi, kPiLo}, FF{-2.0f * a.hi, -2.0f * a.lo}) : FF{2.0f * a.hi, 2.0f * a.lo};
+    else  // acos(x) = pi/2 - asin(x)
+        v = ff_add(FF{kPiHalfHi, kPiHalfLo}, neg ? a : ff_neg(a));
+    return v.hi + v.lo;
 }
 
 // correctly rounded x^5 (std::pow(x, 5.0f) of a float)

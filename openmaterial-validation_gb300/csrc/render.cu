@@ -262,20 +262,29 @@ __global__ void __launch_bounds__(kShadeThreads) k_light_gen(WaveArgs A)
         const PathCtx c = path_ctx(A, k);
         const uint32_t pixel = c.pixel, sample = c.sample;
         const DevScene& S = A.S;
+        // the path's scene's lights (a batch job's; one frame: the scene's)
+        int lbase = 0, N = S.num_lights;
+        float lmax = S.light_max;
+        if (A.num_jobs) {
+            const DevJob& J = A.jobs[A.path_job[k]];
+            lbase = J.light_base;
+            N = J.light_count;
+            lmax = J.light_max;
+        }
+        const float* cdf = S.light_cdf + lbase;
         // DistanceRandom::getValue (DistanceRandom.h:98-115)
-        const float d = rng4(c.seed, pixel, sample, 0u, kStreamLight).u[0] * S.light_max;
+        const float d = rng4(c.seed, pixel, sample, 0u, kStreamLight).u[0] * lmax;
         int li = 0;
-        const int N = S.num_lights;
         if (N > 1) {
-            if (d <= S.light_cdf[0])
+            if (d <= cdf[0])
                 li = 0;
-            else if (d >= S.light_cdf[N - 2])
+            else if (d >= cdf[N - 2])
                 li = N - 1;
             else {
                 int L = 0, Rr = N - 1;
                 while (L < Rr) {
                     int C = (L + Rr) / 2;
-                    if (d <= S.light_cdf[C])
+                    if (d <= cdf[C])
                         Rr = C;
                     else
                         L = C + 1;
@@ -283,6 +292,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_light_gen(WaveArgs A)
                 li = (L + Rr) / 2;
             }
         }
+        li += lbase;
         // RandomSampler::uniformSphere: rejection in the [0,1)^3 cube
         V3 v = v3(1.0f, 0.0f, 0.0f);
         float sl = 1.0f;
@@ -318,9 +328,17 @@ __global__ void __launch_bounds__(kShadeThreads) k_light_gen(WaveArgs A)
 // consecutive rays and the next 32 when all are done (camera rays: the 32
 // samples of one pixel stay together).  Replacing finished rays lane by lane
 // (Aila & Laine 2009) was measured slower on every bounce.
+// `jobs` (batches over a group of scenes, else null): the top-level tree of
+// the path's scene (the path index travels in the ray's last word)
+__device__ __forceinline__ uint32_t path_root(const DevJob* jobs, const uint32_t* path_job, int k)
+{
+    return jobs ? jobs[path_job[k]].tlas_root : kInvalid;
+}
+
 __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_extend(DevScene S, const uint32_t* items, float4* rq, uint4* hits,
                                                           const uint32_t* count, uint32_t* work,
-                                                          unsigned long long* stats, int stat_kind)
+                                                          unsigned long long* stats, int stat_kind,
+                                                          const DevJob* jobs, const uint32_t* path_job)
 {
     __shared__ uint2 sstack[kStackShared * kTraceThreads];
     TraceStack st;
@@ -342,7 +360,8 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_extend(DevSc
             float tnear = a.w;
             RayHit h;
             uint4 out;
-            if (scene_intersect(S, items, o, d, tnear, kFltMax, h, st, tc))
+            if (scene_intersect(S, items, o, d, tnear, kFltMax, h, st, tc,
+                                path_root(jobs, path_job, __float_as_int(b.w))))
                 out = make_uint4(h.inst, h.prim, __float_as_uint(h.u), __float_as_uint(h.v));
             else
                 out = make_uint4(kInvalid, kInvalid, 0u, 0u);
@@ -621,7 +640,8 @@ __global__ void __launch_bounds__(kShadeThreads, kMis ? 3 : 4) k_camera_shade(Wa
 template <bool kEnv, bool kMasked>
 __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevScene S, const uint32_t* items, const float4* sq,
                                                           const uint32_t* count, uint32_t* work, float4* rad,
-                                                          unsigned long long* stats)
+                                                          unsigned long long* stats, const DevJob* jobs,
+                                                          const uint32_t* path_job)
 {
     __shared__ uint2 sstack[kStackShared * kTraceThreads];
     TraceStack st;
@@ -641,12 +661,13 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevSc
         const float4 q0 = sq[3 * (size_t)i], q1 = sq[3 * (size_t)i + 1], q2 = sq[3 * (size_t)i + 2];
         const V3 A = v3(q0.x, q0.y, q0.z), B = v3(q1.x, q1.y, q1.z);
         const int k = __float_as_int(q0.w);
+        const uint32_t root = path_root(jobs, path_job, k);
         bool connected = true;
         if (kEnv) {
             float tn = q1.w;
             RayHit h;
-            connected = kMasked ? !scene_intersect(S, items, A, B, tn, kFltMax, h, st, tc)
-                                : !trace_any(S, items, A, B, tn, kFltMax, st, tc);
+            connected = kMasked ? !scene_intersect(S, items, A, B, tn, kFltMax, h, st, tc, root)
+                                : !trace_any(S, items, A, B, tn, kFltMax, st, tc, root);
         } else {
             V3 dir = B - A;
             const float len = sqrtf(dot(dir, dir));
@@ -660,14 +681,14 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevSc
                 RayHit h;
                 bool hit;
                 if (kMasked) {
-                    hit = scene_intersect(S, items, A, dir, tnear, tfar, h, st, tc);
+                    hit = scene_intersect(S, items, A, dir, tnear, tfar, h, st, tc, root);
                 } else {
                     // any hit this far short of B is farther than sb from it (the
                     // margin is ~800 ulps of the coordinates, far above the error of
                     // the hit's surface position), so it decides: not connected,
                     // whichever hit is the closest.  Hits near B get the exact test.
                     const float margin = 1.0e-4f * fmaxf(maxsz, max_abs(B, 1.0f)) + 2.0f * sb;
-                    hit = trace_closest_or_below(S, items, A, dir, tnear, tfar, len - margin, h, st, tc);
+                    hit = trace_closest_or_below(S, items, A, dir, tnear, tfar, len - margin, h, st, tc, root);
                     if (hit && h.t < len - margin) {
                         hit = false;
                         connected = false;
@@ -1069,9 +1090,14 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
     A.path_job = R.path_job;
     int occ_t = 0, occ_s = 0;
     OMV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, k_extend, kTraceThreads, 0));
+    // threads per block of the shading-side kernels: 256, or a batch's
+    // autotuned choice (a multiple of 32 up to 256)
+    const int sth = batch && s.batch_shade_threads > 0 ? s.batch_shade_threads : kShadeThreads;
     OMV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, mis ? k_camera_shade<true> : k_camera_shade<false>,
-                                                           kShadeThreads, 0));
+                                                           sth, 0));
     const int trace_grid = std::max(1, occ_t) * s.num_sms;
+    // a batch over a group of scenes: every ray starts at its own scene's top-level tree
+    const DevJob* gjobs = batch && s.parts.size() > 1 ? batch->d_jobs : nullptr;
     const int shade_grid = std::max(1, occ_s) * s.num_sms;
     int64_t launches = 0;
     // optional per-launch events around the closest-hit kernels
@@ -1106,12 +1132,12 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
         OMV_CUDA(cudaMemsetAsync(R.ctr, 0, kMaxCounters * 4, st));
         int work = 0;
         if (batch) {
-            k_job_ids<<<grid_for(A.wave_n, kShadeThreads), kShadeThreads, 0, st>>>(A);
+            k_job_ids<<<grid_for(A.wave_n, sth), sth, 0, st>>>(A);
             ++launches;
         }
         if (lights) {
             const NvtxRange light_range("omv light subpaths");
-            k_light_gen<<<grid_for(A.wave_n, kShadeThreads), kShadeThreads, 0, st>>>(A);
+            k_light_gen<<<grid_for(A.wave_n, sth), sth, 0, st>>>(A);
             ++launches;
             for (int b = 1; b <= p.light_bounces; ++b) {
                 const NvtxRange bounce_range(bounce_name(b));
@@ -1121,15 +1147,15 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
                 if (time_kernels) timed(ext_ev);
                 k_extend<<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, in, R.hits,
                                                                R.ctr + kCtrLight + b, R.ctr + kCtrWork + work++,
-                                                               R.stats, kStatLight);
+                                                               R.stats, kStatLight, gjobs, R.path_job);
                 if (time_kernels) timed(ext_ev);
-                k_light_shade<<<shade_grid, kShadeThreads, 0, st>>>(A, b, in, out);
+                k_light_shade<<<shade_grid, sth, 0, st>>>(A, b, in, out);
                 launches += 2;
             }
         }
         {
             const NvtxRange camera_range("omv camera subpaths");
-            k_camera_gen<<<grid_for(A.wave_n, kShadeThreads), kShadeThreads, 0, st>>>(A);
+            k_camera_gen<<<grid_for(A.wave_n, sth), sth, 0, st>>>(A);
             ++launches;
             for (int b = 1; b <= p.camera_bounces; ++b) {
                 const NvtxRange bounce_range(bounce_name(b));
@@ -1137,21 +1163,22 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
                 float4* out = R.rq[b % 2];
                 if (time_kernels) timed(ext_ev);
                 k_extend<<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, in, R.hits, R.ctr + kCtrCam + b,
-                                                               R.ctr + kCtrWork + work++, R.stats, kStatExt);
+                                                               R.ctr + kCtrWork + work++, R.stats, kStatExt, gjobs,
+                                                               R.path_job);
                 if (time_kernels) timed(ext_ev);
                 if (mis)
-                    k_camera_shade<true><<<shade_grid, kShadeThreads, 0, st>>>(A, b, in, out);
+                    k_camera_shade<true><<<shade_grid, sth, 0, st>>>(A, b, in, out);
                 else
-                    k_camera_shade<false><<<shade_grid, kShadeThreads, 0, st>>>(A, b, in, out);
+                    k_camera_shade<false><<<shade_grid, sth, 0, st>>>(A, b, in, out);
                 launches += 2;
                 if (lights) {
                     if (time_kernels) timed(sh_ev);
                     if (masked)
                         k_shadow<false, true><<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, R.sq, R.ctr + kCtrShadow + b,
-                                                                          R.ctr + kCtrWork + work++, R.rad, R.stats);
+                                                                          R.ctr + kCtrWork + work++, R.rad, R.stats, gjobs, R.path_job);
                     else
                         k_shadow<false, false><<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, R.sq, R.ctr + kCtrShadow + b,
-                                                                          R.ctr + kCtrWork + work++, R.rad, R.stats);
+                                                                          R.ctr + kCtrWork + work++, R.rad, R.stats, gjobs, R.path_job);
                     if (time_kernels) timed(sh_ev);
                     ++launches;
                 }
@@ -1159,10 +1186,10 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
                     if (time_kernels) timed(sh_ev);
                     if (masked)
                         k_shadow<true, true><<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, A.env_q, R.ctr + kCtrEnv + b,
-                                                                         R.ctr + kCtrWork + work++, R.rad, R.stats);
+                                                                         R.ctr + kCtrWork + work++, R.rad, R.stats, gjobs, R.path_job);
                     else
                         k_shadow<true, false><<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, A.env_q, R.ctr + kCtrEnv + b,
-                                                                         R.ctr + kCtrWork + work++, R.rad, R.stats);
+                                                                         R.ctr + kCtrWork + work++, R.rad, R.stats, gjobs, R.path_job);
                     if (time_kernels) timed(sh_ev);
                     ++launches;
                 }
@@ -1175,7 +1202,7 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
             int group = 1;
             while (group < 32 && group * 16 <= spp) group *= 2;
             const int64_t pixels = (int64_t)A.last_pixel - (int64_t)A.base_q + 1;
-            k_film<<<grid_for(pixels * group, kShadeThreads), kShadeThreads, 0, st>>>(A, group, d_sum, d_sumsq,
+            k_film<<<grid_for(pixels * group, sth), sth, 0, st>>>(A, group, d_sum, d_sumsq,
                                                                                      d_count);
             ++launches;
         }
@@ -1294,6 +1321,7 @@ BatchJobs make_batch(const SceneHost& s, int n, const omv_job* jobs, const omv_p
         if (!j.d_sum_rgb || !j.d_count) throw ArgError("batch job without a film");
         if (p.accumulate_variance && !j.d_sumsq_rgb) throw ArgError("accumulate_variance needs every job's d_sumsq_rgb");
         if (j.material_set < -1 || j.material_set >= s.num_mat_sets) throw ArgError("batch job material set out of range");
+        if (j.part < 0 || j.part >= (int)s.parts.size()) throw ArgError("batch job scene (part) out of range");
         const int64_t npix = (int64_t)j.camera.width * j.camera.height;
         if (npix * j.samples_per_pixel > (int64_t)0x7FFFFFFF) throw ArgError("batch job too large");
         DevJob& d = B.jobs[i];
@@ -1305,6 +1333,12 @@ BatchJobs make_batch(const SceneHost& s, int n, const omv_job* jobs, const omv_p
         d.sample_offset = j.sample_offset;
         d.seed = j.seed;
         d.mats = j.material_set < 0 ? s.dev.mats : s.mat_sets + (size_t)j.material_set * s.num_materials;
+        const ScenePart& part = s.parts[j.part];
+        d.part = j.part;
+        d.tlas_root = part.tlas_root;
+        d.light_base = part.light_base;
+        d.light_count = part.light_count;
+        d.light_max = part.light_max;
         d.sum = j.d_sum_rgb;
         d.sumsq = p.accumulate_variance ? j.d_sumsq_rgb : nullptr;
         d.count = j.d_count;
@@ -1353,9 +1387,11 @@ void upload_jobs(SceneHost& s, const BatchJobs& B, cudaStream_t st)
         OMV_CUDA(cudaMalloc(&s.d_jobs, sizeof(DevJob) * cap));
         s.jobs_cap = cap;
     }
-    // synchronous: the table must be in place before a captured batch replays
-    OMV_CUDA(cudaStreamSynchronize(st));
-    OMV_CUDA(cudaMemcpy(s.d_jobs, B.jobs.data(), sizeof(DevJob) * B.jobs.size(), cudaMemcpyHostToDevice));
+    // ordered on the caller's stream: after the batches still reading the old
+    // table (a replay on the scene's stream is joined back into it) and before
+    // this batch's kernels or graph, which start after it; the host vector is
+    // pageable, so the call returns once the runtime has staged it
+    OMV_CUDA(cudaMemcpyAsync(s.d_jobs, B.jobs.data(), sizeof(DevJob) * B.jobs.size(), cudaMemcpyHostToDevice, st));
 }
 
 }  // namespace
@@ -1427,36 +1463,46 @@ void render_batch(SceneHost& s, int n, const omv_job* jobs, const omv_params& p,
 }
 
 void autotune_batch(SceneHost& s, int n, const omv_job* jobs, const omv_params& p, cudaStream_t st,
-                    int64_t* chosen)
+                    int64_t* chosen, int32_t* chosen_threads)
 {
     const BatchJobs B = make_batch(s, n, jobs, p);
     const FramePlan Pmax = batch_frame_plan(s, B, p, 0);
+    // candidates: wave sizes 4M x 4^k up to the largest that fits (the queue
+    // capacities follow the wave size), each with 128 and 256 threads per
+    // block of the shading kernels
     std::vector<int64_t> cand;
     for (int64_t c = (int64_t)1 << 22; c < Pmax.cap; c *= 4) cand.push_back(c);
     cand.push_back(Pmax.cap);
+    const int threads[] = {128, 256};
     cudaEvent_t e0, e1;
     OMV_CUDA(cudaEventCreate(&e0));
     OMV_CUDA(cudaEventCreate(&e1));
     int64_t best = Pmax.cap;
+    int best_t = kShadeThreads;
     float best_ms = 3.0e38f;
     const int64_t saved = s.batch_wave_paths;
+    const int saved_t = s.batch_shade_threads;
     try {
-        for (int64_t c : cand) {
-            s.batch_wave_paths = c;
-            render_batch(s, n, jobs, p, st, nullptr, false);  // warm-up (and scratch)
-            OMV_CUDA(cudaEventRecord(e0, st));
-            render_batch(s, n, jobs, p, st, nullptr, false);
-            OMV_CUDA(cudaEventRecord(e1, st));
-            OMV_CUDA(cudaEventSynchronize(e1));
-            float ms = 0.0f;
-            OMV_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-            if (ms < best_ms) {
-                best_ms = ms;
-                best = c;
+        for (int64_t c : cand)
+            for (int t : threads) {
+                s.batch_wave_paths = c;
+                s.batch_shade_threads = t;
+                render_batch(s, n, jobs, p, st, nullptr, false);  // warm-up (and scratch)
+                OMV_CUDA(cudaEventRecord(e0, st));
+                render_batch(s, n, jobs, p, st, nullptr, false);
+                OMV_CUDA(cudaEventRecord(e1, st));
+                OMV_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.0f;
+                OMV_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best = c;
+                    best_t = t;
+                }
             }
-        }
     } catch (...) {
         s.batch_wave_paths = saved;
+        s.batch_shade_threads = saved_t;
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         throw;
@@ -1464,7 +1510,9 @@ void autotune_batch(SceneHost& s, int n, const omv_job* jobs, const omv_params& 
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     s.batch_wave_paths = best;
+    s.batch_shade_threads = best_t;
     if (chosen) *chosen = best;
+    if (chosen_threads) *chosen_threads = best_t;
 }
 
 // ------------------------------------------ render without allocation ---

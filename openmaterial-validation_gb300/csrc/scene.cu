@@ -427,8 +427,15 @@ void set_scene_materials(SceneHost& s, int num, const omv_material_desc* descs)
     s.h_mats = mats;
 }
 
-SceneHost* scene_create(const omv_scene_desc& d, int device)
+SceneHost* scene_create(const omv_scene_desc& d, int device, const std::vector<int>* inst_part,
+                        const std::vector<ScenePart>* parts_in)
 {
+    std::vector<ScenePart> parts = parts_in ? *parts_in : std::vector<ScenePart>(1);
+    if (!parts_in) {
+        parts[0].light_count = std::max(0, d.num_lights);
+        parts[0].mat_count = std::max(0, d.num_materials);
+    }
+    const int nparts = (int)parts.size();
     if (d.num_meshes < 0 || d.num_instances < 0 || d.num_materials < 0 || d.num_lights < 0)
         throw ArgError("negative element count in omv_scene_desc");
     if ((d.num_meshes && !d.meshes) || (d.num_instances && !d.instances) || (d.num_materials && !d.materials) ||
@@ -571,6 +578,7 @@ SceneHost* scene_create(const omv_scene_desc& d, int device)
         I.uv_mask = valid ? mesh_uv_mask[id.mesh] : 0u;
         igeo[i].valid = valid;
         igeo[i].mesh = valid ? id.mesh : -1;
+        igeo[i].part = inst_part ? (*inst_part)[i] : 0;
         std::memcpy(igeo[i].xf, xf, sizeof(xf));
         if (valid) {
             ++nvalid;
@@ -595,7 +603,8 @@ SceneHost* scene_create(const omv_scene_desc& d, int device)
     }
     if (d.bvh_builder < OMV_BVH_SAH || d.bvh_builder > OMV_BVH_HOST_SAH) throw ArgError("unknown bvh_builder");
     AccelResult acc;
-    build_accel(geo, igeo, static_cast<BvhBuilder>(d.bvh_builder), acc, s->stream);
+    build_accel(geo, igeo, static_cast<BvhBuilder>(d.bvh_builder), acc, s->stream, nparts);
+    for (int p = 0; p < nparts; ++p) parts[p].tlas_root = acc.tlas_roots[p];
     s->allocs.push_back(acc.nodes);
     s->allocs.push_back(acc.tris);
     s->allocs.push_back(acc.tlas_items);
@@ -649,26 +658,31 @@ SceneHost* scene_create(const omv_scene_desc& d, int device)
     s->h_mats = mats;
     s->d_face_prefix = s->upload(s->mesh_face_prefix);
 
-    // ---- lights (RenderLightPoint::set, DistanceRandom CDF)
+    // ---- lights (RenderLightPoint::set, DistanceRandom CDF per scene of a group)
     s->num_lights = d.num_lights;
-    D.num_lights = d.num_lights;
     {
         std::vector<float4> lp(std::max(1, d.num_lights)), li(std::max(1, d.num_lights));
         std::vector<float> cdf(std::max(1, d.num_lights));
-        float acc_p = 0.0f;
-        for (int i = 0; i < d.num_lights; ++i) {
-            const omv_light_desc& l = d.lights[i];
-            lp[i] = make_float4(l.position[0], l.position[1], l.position[2], l.range > 0.0f ? l.range : kFltMax);
-            li[i] = make_float4(l.intensity[0], l.intensity[1], l.intensity[2], 0.0f);
-            float power = 0.2126f * l.intensity[0] + 0.7152f * l.intensity[1] + 0.0722f * l.intensity[2];
-            acc_p = acc_p + power;
-            cdf[i] = acc_p;
+        for (ScenePart& P : parts) {
+            float acc_p = 0.0f;
+            for (int i = P.light_base; i < P.light_base + P.light_count; ++i) {
+                const omv_light_desc& l = d.lights[i];
+                lp[i] = make_float4(l.position[0], l.position[1], l.position[2], l.range > 0.0f ? l.range : kFltMax);
+                li[i] = make_float4(l.intensity[0], l.intensity[1], l.intensity[2], 0.0f);
+                float power = 0.2126f * l.intensity[0] + 0.7152f * l.intensity[1] + 0.0722f * l.intensity[2];
+                acc_p = acc_p + power;
+                cdf[i] = acc_p;
+            }
+            P.light_max = P.light_count > 0 ? cdf[P.light_base + P.light_count - 1] : 0.0f;
         }
         D.light_pos = s->upload(lp);
         D.light_int = s->upload(li);
         D.light_cdf = s->upload(cdf);
-        D.light_max = d.num_lights > 0 ? cdf[d.num_lights - 1] : 0.0f;
+        // the single-frame calls render scene 0
+        D.num_lights = parts[0].light_count;
+        D.light_max = parts[0].light_max;
     }
+    s->parts = parts;
 
     // ---- environment
     D.env.present = 0;
@@ -689,6 +703,78 @@ SceneHost* scene_create(const omv_scene_desc& d, int device)
     OMV_CUDA(cudaStreamSynchronize(s->stream));
     s->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return s.release();
+}
+
+SceneHost* scene_create_group(int num, const omv_scene_desc* descs, int device)
+{
+    if (num == 1) return scene_create(descs[0], device);
+    std::vector<omv_mesh_desc> meshes;
+    std::vector<omv_instance_desc> insts;
+    std::vector<omv_material_desc> mats;
+    std::vector<omv_light_desc> lights;
+    std::vector<omv_texture_desc> texs;
+    std::vector<int> inst_part;
+    std::vector<ScenePart> parts(num);
+    for (int p = 0; p < num; ++p) {
+        const omv_scene_desc& d = descs[p];
+        if (d.num_meshes < 0 || d.num_instances < 0 || d.num_materials < 0 || d.num_lights < 0 ||
+            d.num_textures < 0)
+            throw ArgError("negative element count in scene " + std::to_string(p) + " of the group");
+        if ((d.num_meshes && !d.meshes) || (d.num_instances && !d.instances) || (d.num_materials && !d.materials) ||
+            (d.num_lights && !d.lights) || (d.num_textures && !d.textures))
+            throw ArgError("NULL array for a non-zero count in scene " + std::to_string(p) + " of the group");
+        const omv_hdri_desc* h0 = descs[0].hdri;
+        if ((d.hdri != nullptr) != (h0 != nullptr))
+            throw ArgError("the scenes of a group share one HDRI background or none has one");
+        if (h0 && d.hdri != h0) {
+            const omv_hdri_desc& h = *d.hdri;
+            bool same = h.width == h0->width && h.height == h0->height && h.scale == h0->scale && h.rgb && h0->rgb &&
+                        std::memcmp(h.rotation, h0->rotation, sizeof(h.rotation)) == 0;
+            same = same && std::memcmp(h.rgb, h0->rgb, sizeof(float) * 3 * (size_t)h.width * h.height) == 0;
+            if (!same) throw ArgError("the scenes of a group share one HDRI background or none has one");
+        }
+        if ((d.num_lights > 0) != (descs[0].num_lights > 0))
+            throw ArgError("either every scene of a group has point lights or none has");
+        const int mesh_base = (int)meshes.size(), mat_base = (int)mats.size(), tex_base = (int)texs.size();
+        parts[p].mat_base = mat_base;
+        parts[p].mat_count = d.num_materials;
+        parts[p].light_base = (int)lights.size();
+        parts[p].light_count = d.num_lights;
+        for (int i = 0; i < d.num_meshes; ++i) {
+            omv_mesh_desc m = d.meshes[i];
+            m.material = (m.material >= 0 && m.material < d.num_materials) ? mat_base + m.material : -1;
+            meshes.push_back(m);
+        }
+        for (int i = 0; i < d.num_instances; ++i) {
+            omv_instance_desc in = d.instances[i];
+            in.mesh = (in.mesh >= 0 && in.mesh < d.num_meshes) ? mesh_base + in.mesh : -1;
+            insts.push_back(in);
+            inst_part.push_back(p);
+        }
+        for (int i = 0; i < d.num_materials; ++i) {
+            omv_material_desc m = d.materials[i];
+            for (omv_texture_ref* r : {&m.base_color_texture, &m.metallic_roughness_texture, &m.normal_texture,
+                                       &m.occlusion_texture, &m.emissive_texture})
+                if (r->texture > 0) r->texture += tex_base;
+            mats.push_back(m);
+        }
+        lights.insert(lights.end(), d.lights, d.lights + d.num_lights);
+        texs.insert(texs.end(), d.textures, d.textures + d.num_textures);
+    }
+    omv_scene_desc g{};
+    g.num_meshes = (int32_t)meshes.size();
+    g.meshes = meshes.data();
+    g.num_instances = (int32_t)insts.size();
+    g.instances = insts.data();
+    g.num_materials = (int32_t)mats.size();
+    g.materials = mats.data();
+    g.num_lights = (int32_t)lights.size();
+    g.lights = lights.data();
+    g.hdri = descs[0].hdri;
+    g.num_textures = (int32_t)texs.size();
+    g.textures = texs.data();
+    g.bvh_builder = descs[0].bvh_builder;
+    return scene_create(g, device, &inst_part, &parts);
 }
 
 // ------------------------------------------------------- kernel hooks ---

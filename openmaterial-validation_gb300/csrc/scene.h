@@ -71,12 +71,26 @@ struct DevJob {
     uint32_t pixel_base;
     int32_t spp;
     int32_t sample_offset;
-    int32_t pad;
+    int32_t part;             // scene of a group
     uint64_t seed;
     const DevMaterial* mats;
     double* sum;
     double* sumsq;
     uint32_t* count;
+    uint32_t tlas_root;       // the scene's top-level tree
+    int32_t light_base;       // the scene's lights: [light_base, light_base + light_count)
+    int32_t light_count;
+    float light_max;          // their total power (the light-pick CDF's last value)
+};
+
+// One scene of a group (omv_scene_create_group) within the group's arrays:
+// its top-level tree, lights (a light-pick CDF of their own) and materials.
+// A single scene is a group of one.
+struct ScenePart {
+    uint32_t tlas_root = 0xFFFFFFFFu;
+    int32_t light_base = 0, light_count = 0;
+    float light_max = 0.0f;
+    int32_t mat_base = 0, mat_count = 0;  // without the shared missing material
 };
 
 struct SceneHost {
@@ -111,6 +125,8 @@ struct SceneHost {
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;  // order `stream` after / before a caller's default stream
     std::vector<unsigned char> batch_key;    // what batch_graph was captured for
     int64_t batch_wave_paths = 0;            // autotuned wave size for batches (0: automatic)
+    int batch_shade_threads = 0;             // autotuned threads per shading block for batches (0: 256)
+    std::vector<ScenePart> parts;            // the scenes of a group (one for a single scene)
 
     ~SceneHost();
     void* alloc(size_t bytes);
@@ -123,7 +139,13 @@ struct SceneHost {
     }
 };
 
-SceneHost* scene_create(const omv_scene_desc& desc, int device);
+// `parts` (optional): the scenes a merged description holds (instances of
+// scene p have inst_part[i] == p; light and material ranges per scene)
+SceneHost* scene_create(const omv_scene_desc& desc, int device, const std::vector<int>* inst_part = nullptr,
+                        const std::vector<ScenePart>* parts = nullptr);
+// several scenes in one handle: one device copy of all geometry, one
+// top-level tree per scene; batch jobs pick their scene
+SceneHost* scene_create_group(int num, const omv_scene_desc* descs, int device);
 
 void render_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, double* d_sum, double* d_sumsq,
                   uint32_t* d_count, cudaStream_t st, omv_stats* stats);
@@ -137,7 +159,7 @@ void render_batch(SceneHost& s, int num_jobs, const omv_job* jobs, const omv_par
                   omv_stats* stats, bool use_graph);
 // times candidate wave sizes on the job list and keeps the fastest for batches
 void autotune_batch(SceneHost& s, int num_jobs, const omv_job* jobs, const omv_params& p, cudaStream_t st,
-                    int64_t* chosen);
+                    int64_t* chosen, int32_t* chosen_threads);
 
 // builds the environment's alias table (the MIS estimator) if not yet built
 void ensure_env_sampler(SceneHost& s);
@@ -145,7 +167,9 @@ void ensure_env_sampler(SceneHost& s);
 void set_scene_materials(SceneHost& s, int num, const omv_material_desc* descs);
 // path-replay gradient of an image loss with respect to the material parameters
 void adjoint_frame(SceneHost& s, const omv_camera& cam, const omv_params& p, const float* d_adjoint, float* d_grad,
-                   cudaStream_t st);
+                   cudaStream_t st, int part = 0, const DevMaterial* mats = nullptr);
+// the adjoint of every job of a list (each job's scene, material set, camera and samples)
+void adjoint_batch(SceneHost& s, int n, const omv_adjoint_job* jobs, const omv_params& p, cudaStream_t st);
 
 // render_frame on the fixed scratch array; makes no device allocation
 void render_frame_static(SceneHost& s, const omv_camera& cam, const omv_params& p, double* d_sum, double* d_sumsq,

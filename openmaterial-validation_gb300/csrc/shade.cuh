@@ -388,11 +388,12 @@ constexpr int kMaskedTries = 10;
 // alpha-masked materials up to 10 times; tnear persists like the reference's
 // RTCRayHit does across the bounces of one path
 __device__ __forceinline__ bool scene_intersect(const DevScene& S, const uint32_t* items, V3 o, V3 d, float& tnear,
-                                                float tfar, RayHit& h, TraceStack& st, TraceCounters& tc)
+                                                float tfar, RayHit& h, TraceStack& st, TraceCounters& tc,
+                                                uint32_t root = kInvalid)
 {
     const float t1 = tfar;
     for (int itr = 0; itr < kMaskedTries; ++itr) {
-        if (!trace_closest(S, items, o, d, tnear, tfar, h, st, tc)) return false;
+        if (!trace_closest(S, items, o, d, tnear, tfar, h, st, tc, root)) return false;
         if (!hit_masked(S, h)) return true;
         tnear = masked_retry_tnear(o, d, h.t);
         tfar = t1;

@@ -189,7 +189,7 @@ struct TraceState {
 
 // false when the ray cannot hit anything (empty interval, zero or non-finite direction)
 __device__ __forceinline__ bool trace_begin(const DevScene& S, V3 o, V3 d, float tnear, float tfar, TraceState& T,
-                                           TraceStack& st)
+                                           TraceStack& st, uint32_t root = kInvalid)
 {
     if (!(tnear <= tfar) || S.num_instances == 0) return false;
     if (!shear_setup(d, T.rs)) return false;
@@ -208,7 +208,7 @@ __device__ __forceinline__ bool trace_begin(const DevScene& S, V3 o, V3 d, float
     T.in_blas = false;
     T.found = false;
     st.sp = 0;
-    st.push(S.tlas_root, tnear);
+    st.push(root == kInvalid ? S.tlas_root : root, tnear);  // root: one scene of a group
     return true;
 }
 
@@ -355,10 +355,11 @@ __device__ __forceinline__ bool trace_end(const TraceState& T, RayHit& hit)
 // Whether any triangle is hit in [tnear, tfar] (the closest-hit query's answer
 // to "is there a hit", without finding the closest).
 __device__ __forceinline__ bool trace_any(const DevScene& S, const uint32_t* __restrict__ tlas_items, V3 o, V3 d,
-                                          float tnear, float tfar, TraceStack& st, TraceCounters& tc)
+                                          float tnear, float tfar, TraceStack& st, TraceCounters& tc,
+                                          uint32_t root = kInvalid)
 {
     TraceState T;
-    if (!trace_begin(S, o, d, tnear, tfar, T, st)) return false;
+    if (!trace_begin(S, o, d, tnear, tfar, T, st, root)) return false;
     while (trace_step<true>(S, tlas_items, T, st, tc, __int_as_float(0x7F800000))) {
     }
     return T.found;
@@ -368,10 +369,10 @@ __device__ __forceinline__ bool trace_any(const DevScene& S, const uint32_t* __r
 // t < stop_below (then `hit` is that hit, not necessarily the closest).
 __device__ __forceinline__ bool trace_closest_or_below(const DevScene& S, const uint32_t* __restrict__ tlas_items, V3 o,
                                                        V3 d, float tnear, float tfar, float stop_below, RayHit& hit,
-                                                       TraceStack& st, TraceCounters& tc)
+                                                       TraceStack& st, TraceCounters& tc, uint32_t root = kInvalid)
 {
     TraceState T;
-    if (!trace_begin(S, o, d, tnear, tfar, T, st)) return false;
+    if (!trace_begin(S, o, d, tnear, tfar, T, st, root)) return false;
     while (trace_step<true>(S, tlas_items, T, st, tc, stop_below)) {
     }
     return trace_end(T, hit);
@@ -379,10 +380,11 @@ __device__ __forceinline__ bool trace_closest_or_below(const DevScene& S, const 
 
 // Closest hit; returns true and fills `hit` when a triangle is found.
 __device__ __forceinline__ bool trace_closest(const DevScene& S, const uint32_t* __restrict__ tlas_items, V3 o, V3 d,
-                                           float tnear, float tfar, RayHit& hit, TraceStack& st, TraceCounters& tc)
+                                           float tnear, float tfar, RayHit& hit, TraceStack& st, TraceCounters& tc,
+                                           uint32_t root = kInvalid)
 {
     TraceState T;
-    if (!trace_begin(S, o, d, tnear, tfar, T, st)) return false;
+    if (!trace_begin(S, o, d, tnear, tfar, T, st, root)) return false;
     while (trace_step(S, tlas_items, T, st, tc)) {
     }
     return trace_end(T, hit);

@@ -32,7 +32,7 @@ def test_struct_layouts_match_binding(omv):
     assert L.omv_struct_sizes(sizes, n) == n
     py = [capi.MeshDesc, capi.InstanceDesc, capi.MaterialDesc, capi.LightDesc, capi.HdriDesc, capi.SceneDesc,
           capi.SceneInfo, capi.Camera, capi.Params, capi.Stats, capi.Hit, capi.Job, capi.TextureDesc,
-          capi.TextureRef]
+          capi.TextureRef, capi.AdjointJob]
     assert [C.sizeof(t) for t in py] == list(sizes)
     assert capi.HIT_DTYPE.itemsize == C.sizeof(capi.Hit)
 
