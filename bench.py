@@ -48,7 +48,8 @@ def _peaks():
 
 def frame_config(scene, parallelism: str) -> dict:
     """The workload keys both arms report (the same scene on both sides)."""
-    return {"workload": WORKLOAD, "width": scene.camera.width, "height": scene.camera.height,
+    workload = WORKLOAD if scene.name != "c1" else "plain BDPT, point-light scene (C1 geometry and light)"
+    return {"workload": workload, "width": scene.camera.width, "height": scene.camera.height,
             "spp": scene.render.samples_per_pixel, "max_path_length": scene.render.max_path_length,
             "triangles": scene.num_triangles, "instances": len(scene.instances),
             "l2": "flushed by a 256 MiB write between timed frames", "parallelism": parallelism,
@@ -761,6 +762,8 @@ def main():
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--spp", type=int, default=64)
+    ap.add_argument("--scene", choices=["c2", "c1"], default="c2",
+                    help="c2: the benchmark scene; c1: the point-light scene (for profiling the light path)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -780,7 +783,10 @@ def main():
     if args.impl == "reference" and rank != 0:
         return
     S = importlib.import_module("openmaterial-validation_gb300.scenes")
-    scene = S.scene_c2(args.width, args.height, args.spp)
+    if args.scene == "c1":  # the point-light scene (profiling of the light path), not the benchmark frame
+        scene = S.scene_c1(args.width, args.height, args.spp)
+    else:
+        scene = S.scene_c2(args.width, args.height, args.spp)
     if args.impl == "reference":
         run_reference(args, scene, rank)
     else:

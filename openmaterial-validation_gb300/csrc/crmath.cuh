@@ -19,8 +19,10 @@
 //     error from one fused multiply-add;
 //   * sin / cos: additive range reduction by pi/2 split into three 20-bit
 //     parts and a remainder (W. J. Cody and W. Waite, "Software Manual for the
-//     Elementary Functions", 1980), then the Taylor series of sin and cos on
-//     |r| <= pi/4 evaluated by Horner's rule, the first terms in double-float;
+//     Elementary Functions", 1980), a second one by pi/32 against a table of
+//     sin and cos of j pi/32 (the angle-sum method of table-driven
+//     evaluation, P. T. P. Tang, ACM TOMS 1989), and Taylor series of sin and
+//     cos on |r| <= pi/64, their first terms in double-float;
 //   * asin / acos: one Newton step on sin(y) = t from a float starting value,
 //     with sin evaluated in double-float; |t| > 1/2 through
 //     asin(t) = pi/2 - 2 asin(sqrt((1 - t) / 2));
@@ -114,28 +116,6 @@ constexpr float kK4h = 2.4801587642286904e-05f, kK4l = -3.40699609366682e-13f;
 constexpr float kK5 = -2.755731998149713e-07f, kK6 = 2.0876755879584152e-09f, kK7 = -1.147074536050896e-11f,
                 kK8 = 4.7794772561329454e-14f;
 
-// sin(r) and cos(r) for a double-float r with |r| <= pi/4 (plus rounding)
-OMV_CR_HD void ff_sincos_kernel(FF r, FF& s, FF& c)
-{
-    FF z = two_prod(r.hi, r.hi);
-    z = fast_two_sum(z.hi, z.lo + 2.0f * r.hi * r.lo);
-    const float zh = z.hi;
-    // sin: r + r z (S1 + z (S2 + z (S3 + z (S4 + z S5..))))
-    float ts = kS5 + zh * (kS6 + zh * (kS7 + zh * kS8));
-    FF t = ff_add(FF{kS4h, kS4l}, ff_mul_f(z, ts));
-    t = ff_add(FF{kS3h, kS3l}, ff_mul(z, t));
-    t = ff_add(FF{kS2h, kS2l}, ff_mul(z, t));
-    t = ff_add(FF{kS1h, kS1l}, ff_mul(z, t));
-    s = ff_add(r, ff_mul(r, ff_mul(z, t)));
-    // cos: 1 + z (K1 + z (K2 + z (K3 + z (K4 + z K5..))))
-    float tc = kK5 + zh * (kK6 + zh * (kK7 + zh * kK8));
-    FF u = ff_add(FF{kK4h, kK4l}, ff_mul_f(z, tc));
-    u = ff_add(FF{kK3h, kK3l}, ff_mul(z, u));
-    u = ff_add(FF{kK2h, kK2l}, ff_mul(z, u));
-    u = ff_add(FF{kK1h, kK1l}, ff_mul(z, u));
-    c = ff_add(FF{1.0f, 0.0f}, ff_mul(z, u));
-}
-
 // sin(y) for a float |y| <= 0.53 (asin's Newton step): y^2 is exact as a
 // double-float, and on this range the terms from y^9 on need float accuracy only
 OMV_CR_HD FF ff_sin_small(float y)
@@ -149,7 +129,34 @@ OMV_CR_HD FF ff_sin_small(float y)
     return ff_add(FF{y, 0.0f}, ff_mul_f(ff_mul(z, t), y));
 }
 
-// Correctly rounded sinf / cosf of x in [0, 8] (the sampling angles 2 pi u).
+// sin and cos of j pi / 32, j = 0..8, as double-floats (sin hi, lo, cos hi, lo)
+#ifdef __CUDACC__
+__device__
+#endif
+constexpr float kSinCosTable[9][4] = {
+    {0.0f, 0.0f, 1.0f, 0.0f},
+    {0.0980171412229538f, -8.933931927579408e-10f, 0.9951847195625305f, 7.109666189109021e-09f},
+    {0.19509032368659973f, -1.670471427850373e-09f, 0.9807852506637573f, 2.9739473106360492e-08f},
+    {0.290284663438797f, 1.3815665056426951e-08f, 0.9569403529167175f, -1.7184508038781132e-08f},
+    {0.3826834261417389f, 6.2233507236442165e-09f, 0.9238795042037964f, 2.830748968563057e-08f},
+    {0.4713967442512512f, -7.425253745196869e-09f, 0.8819212913513184f, -2.7002963420841297e-08f},
+    {0.5555702447891235f, -1.1769521357507529e-08f, 0.8314695954322815f, 1.687026340846387e-08f},
+    {0.6343932747840881f, 9.37955757507325e-09f, 0.7730104327201843f, 2.0642552556182636e-08f},
+    {0.7071067690849304f, 1.2101617485882343e-08f, 0.7071067690849304f, 1.2101617485882343e-08f},
+};
+
+OMV_CR_HD float table_at(int j, int k)
+{
+#ifdef __CUDA_ARCH__
+    return __ldg(&kSinCosTable[j][k]);
+#else
+    return kSinCosTable[j][k];
+#endif
+}
+
+// Correctly rounded sinf / cosf of x in [0, 8] (the sampling angles 2 pi u):
+// x = q pi/2 + j pi/32 + r with |r| <= pi/64, sin and cos of r by short
+// series, combined with the table's values of j pi / 32 by the angle sums.
 OMV_CR_HD void sincos_cr(float x, float& s_out, float& c_out)
 {
     // quadrant q = nearest integer to x / (pi/2); x - q pi/2 as a double-float
@@ -157,10 +164,27 @@ OMV_CR_HD void sincos_cr(float x, float& s_out, float& c_out)
     FF r = two_sum(x - q * kC1, -(q * kC2));  // x - q kC1 is exact (Sterbenz, or q = 0)
     FF r2 = two_sum(r.hi, -(q * kC3));
     r = fast_two_sum(r2.hi, r2.lo + (r.lo - q * kC4));
-    FF s, c;
-    ff_sincos_kernel(r, s, c);
+    // j = nearest integer to r / (pi/32); pi/32 = (kC1 + kC2 + kC3 + kC4) / 16 and
+    // j kCi / 16 is exact for |j| <= 8; r.hi - j kC1 / 16 is exact (Sterbenz)
+    const float j = rintf(r.hi * (16.0f * kTwoOverPi));
+    FF t = two_sum(r.hi - j * (kC1 * 0.0625f), -(j * (kC2 * 0.0625f)));
+    FF t2 = two_sum(t.hi, -(j * (kC3 * 0.0625f)));
+    t = fast_two_sum(t2.hi, t2.lo + (t.lo + (r.lo - j * (kC4 * 0.0625f))));
+    // sin t = t (1 + z (S1 + z (S2 + z S3))), cos t = 1 + z (K1 + z (K2 + z K3)), z = t^2 <= 0.0025
+    FF z = two_prod(t.hi, t.hi);
+    z = fast_two_sum(z.hi, z.lo + 2.0f * t.hi * t.lo);
+    const float zh = z.hi;
+    const FF ps = ff_add(FF{kS1h, kS1l}, FF{zh * (kS2h + zh * kS3h), 0.0f});
+    const FF st = ff_add(t, ff_mul(t, ff_mul(z, ps)));
+    const FF pc = ff_add(FF{kK1h, kK1l}, ff_mul_f(z, kK2h + zh * kK3h));
+    const FF ct = ff_add(FF{1.0f, 0.0f}, ff_mul(z, pc));
+    // the angle sums with sin / cos of |j| pi / 32 (odd / even in j)
+    const int ja = (int)fabsf(j);
+    const float sg = j < 0.0f ? -1.0f : 1.0f;
+    const FF sj{sg * table_at(ja, 0), sg * table_at(ja, 1)}, cj{table_at(ja, 2), table_at(ja, 3)};
+    const float sv = ff_add(ff_mul(sj, ct), ff_mul(cj, st)).hi;
+    const float cv = ff_add(ff_mul(cj, ct), ff_neg(ff_mul(sj, st))).hi;
     const int qi = (int)q & 3;
-    const float sv = s.hi, cv = c.hi;
     s_out = qi == 0 ? sv : qi == 1 ? cv : qi == 2 ? -sv : -cv;
     c_out = qi == 0 ? cv : qi == 1 ? -sv : qi == 2 ? -cv : sv;
 }
