@@ -8,9 +8,8 @@
 //     k_extend          closest hit of every queued ray
 //     k_light_shade     surface point, BRDF sample, light-vertex store, cut-off
 //   camera stage
-//     k_extend_camera   jittered pinhole rays (PinholeCamera::getRay), generated
-//                       in the kernel, and their closest hits (bounce 1)
-//     k_extend          closest hits of the later bounces
+//     k_camera_gen      jittered pinhole rays (PinholeCamera::getRay)
+//     k_extend
 //     k_camera_shade    surface point, BRDF sample, environment on escape,
 //                       light/camera vertex connections (and, with the MIS
 //                       estimator, environment rays) -> shadow queue
@@ -166,8 +165,6 @@ struct WaveArgs {
     int32_t num_jobs;
     uint32_t* path_job;       // batch: job of each path of the wave
     float4* env_q;  // MIS environment rays (3 float4 each), after the vertex connections' slots
-    int32_t group;   // a batch over a group of scenes: rays start at their scene's top-level tree
-    int32_t masked;  // the scene has alpha-masked materials (hits may be retried, moving tnear)
     int32_t cam_bounces, light_bounces, max_len;
     int32_t atten_mode;
     float light_scale, min_dist, cut;
@@ -228,25 +225,31 @@ __global__ void __launch_bounds__(kShadeThreads) k_job_ids(WaveArgs A)
 }
 
 // ------------------------------------------------------------ raygen ---
-// PinholeCamera::getRay for path k of the wave: origin (before the shift)
-// and direction
-__device__ __forceinline__ void path_camera_ray(const WaveArgs& A, int k, V3& O, V3& R)
-{
-    const PathCtx c = path_ctx(A, k);
-    const omv_camera& cam = A.num_jobs ? A.jobs[A.path_job[k]].cam : A.cam;
-    Rng4 r = rng4(c.seed, c.pixel, c.sample, 0u, kStreamCamera);
-    camera_ray(cam, (int)(c.pixel % (uint32_t)cam.width), (int)(c.pixel / (uint32_t)cam.width), r.u[0], r.u[1], O, R);
-}
-
-// Frames without camera bounces only: the radiance starts at 0.  With camera
-// bounces the first extension and shade kernels (k_extend_camera,
-// k_camera_shade at b = 1) generate the camera rays themselves instead of a
-// queue of 32 bytes per path written here and read back twice; the first
-// camera shade then starts from throughput 1 and radiance 0 without loading them.
 __global__ void __launch_bounds__(kShadeThreads) k_camera_gen(WaveArgs A)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < A.wave_n) A.R.rad[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const bool ok = k < A.wave_n;
+    uint32_t pixel = 0, sample = 0;
+    V3 O = v3(0, 0, 0), R = v3(0, 0, 1);
+    if (ok) {
+        const PathCtx c = path_ctx(A, k);
+        pixel = c.pixel;
+        sample = c.sample;
+        const omv_camera& cam = A.num_jobs ? A.jobs[A.path_job[k]].cam : A.cam;
+        Rng4 r = rng4(c.seed, pixel, sample, 0u, kStreamCamera);
+        camera_ray(cam, (int)(pixel % (uint32_t)cam.width), (int)(pixel / (uint32_t)cam.width), r.u[0], r.u[1], O, R);
+        // throughput starts at 1 and radiance at 0: the first camera shade uses
+        // the constants and writes both, so only a frame without camera
+        // bounces needs the radiance cleared here
+        if (A.cam_bounces == 0) A.R.rad[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    // every path emits a camera ray: queue slot = path index, no append
+    if (k == 0) A.R.ctr[kCtrCam + 1] = (uint32_t)A.wave_n;
+    if (ok) {
+        V3 so = shifted_origin(O, R, 1.0f);
+        A.R.rq[0][2 * (size_t)k] = make_float4(so.x, so.y, so.z, 0.0f);
+        A.R.rq[0][2 * (size_t)k + 1] = make_float4(R.x, R.y, R.z, __int_as_float(k));
+    }
 }
 
 // tryComputeLightPath (BDPTRenderer.cpp:194-206): sampleLight + getRandomRay
@@ -367,56 +370,6 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_extend(DevSc
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&stats[stat_kind], (unsigned long long)n);
-    uint32_t nodes = tc.nodes, tris = tc.tris;
-    for (int o = 16; o; o >>= 1) {
-        nodes += __shfl_xor_sync(0xFFFFFFFFu, nodes, o);
-        tris += __shfl_xor_sync(0xFFFFFFFFu, tris, o);
-    }
-    const bool ov = __any_sync(0xFFFFFFFFu, st.overflow);
-    if (lane == 0) {
-        atomicAdd(&stats[kStatNodes], (unsigned long long)nodes);
-        atomicAdd(&stats[kStatTris], (unsigned long long)tris);
-        if (ov) atomicAdd(&stats[kStatOverflow], 1ull);
-    }
-}
-
-// Closest hit of the wave's camera rays (the first camera bounce): ray k is
-// generated here from path k's keys (path_camera_ray, the same arithmetic as
-// a queued ray), so no ray queue is read; queue slot = path index.
-__global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_extend_camera(WaveArgs A, uint32_t* work)
-{
-    __shared__ uint2 sstack[kStackShared * kTraceThreads];
-    TraceStack st;
-    st.sh = sstack + threadIdx.x;
-    st.stride = kTraceThreads;
-    st.overflow = 0;
-    TraceCounters tc{0u, 0u};
-    const uint32_t n = (uint32_t)A.wave_n;
-    const int lane = threadIdx.x & 31;
-    const DevJob* gjobs = A.group ? A.jobs : nullptr;
-    while (true) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(work, 32u);
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if (base >= n) break;
-        const uint32_t i = base + lane;
-        if (i < n) {
-            V3 O, d;
-            path_camera_ray(A, (int)i, O, d);
-            const V3 o = shifted_origin(O, d, 1.0f);
-            float tnear = 0.0f;
-            RayHit h;
-            uint4 out;
-            if (scene_intersect(A.S, A.items, o, d, tnear, kFltMax, h, st, tc, path_root(gjobs, A.path_job, (int)i)))
-                out = make_uint4(h.inst, h.prim, __float_as_uint(h.u), __float_as_uint(h.v));
-            else
-                out = make_uint4(kInvalid, kInvalid, 0u, 0u);
-            A.R.hits[i] = out;
-            if (A.masked) A.R.cam_tnear[i] = tnear;  // an alpha-masked retry may have moved it
-        }
-    }
-    unsigned long long* stats = A.R.stats;
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&stats[kStatExt], (unsigned long long)n);
     uint32_t nodes = tc.nodes, tris = tc.tris;
     for (int o = 16; o; o >>= 1) {
         nodes += __shfl_xor_sync(0xFFFFFFFFu, nodes, o);
@@ -554,8 +507,7 @@ __global__ void __launch_bounds__(kShadeThreads, kMis ? 3 : 4) k_camera_shade(Wa
                                                                  float4* rq_out)
 {
     __shared__ BinScratch bins;
-    const bool first = b == 1;  // camera rays: generated here again, throughput 1, radiance 0 (not stored yet)
-    const uint32_t n = first ? (uint32_t)A.wave_n : A.R.ctr[kCtrCam + b];
+    const uint32_t n = A.R.ctr[kCtrCam + b];
     const DevScene& S = A.S;
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
         const uint32_t i = i0 + threadIdx.x;
@@ -567,19 +519,12 @@ __global__ void __launch_bounds__(kShadeThreads, kMis ? 3 : 4) k_camera_shade(Wa
         er.push = false;
         er.w = v3(0.0f, 0.0f, 1.0f);
         if (i < n) {
-            V3 in;
-            if (first) {  // queue slot = path index
-                V3 org;
-                path_camera_ray(A, (int)i, org, in);
-                k = (int)i;
-                tnear = A.masked ? A.R.cam_tnear[i] : 0.0f;
-            } else {
-                const float4 ra = rq_in[2 * (size_t)i], rb = rq_in[2 * (size_t)i + 1];
-                k = __float_as_int(rb.w);
-                tnear = ra.w;
-                in = v3(rb.x, rb.y, rb.z);
-            }
+            const float4 ra = rq_in[2 * (size_t)i], rb = rq_in[2 * (size_t)i + 1];
             const uint4 h = A.R.hits[i];
+            k = __float_as_int(rb.w);
+            tnear = ra.w;
+            const V3 in = v3(rb.x, rb.y, rb.z);
+            const bool first = b == 1;  // throughput 1, radiance 0 (not stored yet)
             const float4 tp4 = first ? make_float4(1.0f, 1.0f, 1.0f, 0.0f) : A.R.tp[k];
             const V3 tp = v3(tp4.x, tp4.y, tp4.z);
             if (h.x == kInvalid) {
@@ -988,7 +933,7 @@ namespace {
 // Byte offsets of one wave's arrays inside a single scratch block (each array
 // starts on a 256-byte boundary).
 struct ScratchLayout {
-    size_t tp, rad, ltp, lrad, lmeta, lvp, lvr, rq0, rq1, hits, pjob, ctn, sq, ctr, stats, bytes;
+    size_t tp, rad, ltp, lrad, lmeta, lvp, lvr, rq0, rq1, hits, pjob, sq, ctr, stats, bytes;
 };
 
 ScratchLayout scratch_layout(int64_t wave_cap, int light_slots, int shadow_slots)
@@ -1012,7 +957,6 @@ ScratchLayout scratch_layout(int64_t wave_cap, int light_slots, int shadow_slots
     L.rq1 = take(W * 32);
     L.hits = take(W * 16);
     L.pjob = take(W * 4);
-    L.ctn = take(W * 4);
     L.sq = take((size_t)shadow_slots * W * 48 + 48);
     L.ctr = take(kMaxCounters * 4);
     L.stats = take(16 * 8);
@@ -1021,12 +965,11 @@ ScratchLayout scratch_layout(int64_t wave_cap, int light_slots, int shadow_slots
 }
 
 // Scratch bytes of one path: tp rad ltp lrad (16 B each), lmeta 4, light
-// vertices 32 per slot, two ray-queue entries 64, hit 16, batch job 4, camera
-// tnear 4, shadow entries 48 per slot (each array is further rounded up to
-// 256 bytes).
+// vertices 32 per slot, two ray-queue entries 64, hit 16, batch job 4, shadow
+// entries 48 per slot (each array is further rounded up to 256 bytes).
 size_t path_scratch_bytes(int light_slots, int shadow_slots)
 {
-    return 68 + 32 * (size_t)light_slots + 88 + 48 * (size_t)shadow_slots;
+    return 68 + 32 * (size_t)light_slots + 84 + 48 * (size_t)shadow_slots;
 }
 
 void carve_scratch(RenderScratch& R, void* base, int64_t wave_cap, int light_slots, int shadow_slots)
@@ -1049,7 +992,6 @@ void carve_scratch(RenderScratch& R, void* base, int64_t wave_cap, int light_slo
     R.rq[1] = (float4*)(b + L.rq1);
     R.hits = (uint4*)(b + L.hits);
     R.path_job = (uint32_t*)(b + L.pjob);
-    R.cam_tnear = (float*)(b + L.ctn);
     R.sq = (float4*)(b + L.sq);
     R.ctr = (uint32_t*)(b + L.ctr);
     R.stats = (unsigned long long*)(b + L.stats);
@@ -1145,8 +1087,6 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
     A.env_q = mis ? R.sq + 3 * (size_t)R.wave_cap * (size_t)(R.shadow_slots - 1) : nullptr;
     A.jobs = batch ? batch->d_jobs : nullptr;
     A.num_jobs = batch ? (int32_t)batch->h_jobs->size() : 0;
-    A.group = batch && s.parts.size() > 1 ? 1 : 0;
-    A.masked = masked ? 1 : 0;
     A.path_job = R.path_job;
     int occ_t = 0, occ_s = 0;
     OMV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, k_extend, kTraceThreads, 0));
@@ -1215,21 +1155,16 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
         }
         {
             const NvtxRange camera_range("omv camera subpaths");
-            if (p.camera_bounces == 0) {  // the radiance is cleared there; no camera ray is traced
-                k_camera_gen<<<grid_for(A.wave_n, sth), sth, 0, st>>>(A);
-                ++launches;
-            }
+            k_camera_gen<<<grid_for(A.wave_n, sth), sth, 0, st>>>(A);
+            ++launches;
             for (int b = 1; b <= p.camera_bounces; ++b) {
                 const NvtxRange bounce_range(bounce_name(b));
                 float4* in = R.rq[(b + 1) % 2];
                 float4* out = R.rq[b % 2];
                 if (time_kernels) timed(ext_ev);
-                if (b == 1)  // the camera rays, generated in the kernel
-                    k_extend_camera<<<trace_grid, kTraceThreads, 0, st>>>(A, R.ctr + kCtrWork + work++);
-                else
-                    k_extend<<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, in, R.hits,
-                                                                   R.ctr + kCtrCam + b, R.ctr + kCtrWork + work++,
-                                                                   R.stats, kStatExt, gjobs, R.path_job);
+                k_extend<<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, in, R.hits, R.ctr + kCtrCam + b,
+                                                               R.ctr + kCtrWork + work++, R.stats, kStatExt, gjobs,
+                                                               R.path_job);
                 if (time_kernels) timed(ext_ev);
                 if (mis)
                     k_camera_shade<true><<<shade_grid, sth, 0, st>>>(A, b, in, out);
@@ -1604,7 +1539,6 @@ void load_wave_kernels()
     OMV_CUDA(cudaFuncGetAttributes(&a, k_camera_gen));
     OMV_CUDA(cudaFuncGetAttributes(&a, k_light_gen));
     OMV_CUDA(cudaFuncGetAttributes(&a, k_extend));
-    OMV_CUDA(cudaFuncGetAttributes(&a, k_extend_camera));
     OMV_CUDA(cudaFuncGetAttributes(&a, k_light_shade));
     OMV_CUDA(cudaFuncGetAttributes(&a, k_camera_shade<false>));
     OMV_CUDA(cudaFuncGetAttributes(&a, k_shadow<false, false>));
@@ -1629,7 +1563,7 @@ void* static_scratch_address()
 int64_t static_wave_limit(int light_slots, int shadow_slots)
 {
     const size_t per_path = path_scratch_bytes(light_slots, shadow_slots);
-    const size_t fixed = 48 + kMaxCounters * 4 + 16 * 8 + 15 * 256;
+    const size_t fixed = 48 + kMaxCounters * 4 + 16 * 8 + 14 * 256;
     int64_t cap = (int64_t)((OMV_STATIC_SCRATCH_BYTES - fixed) / per_path) & ~(int64_t)31;
     while (cap > 0 && scratch_layout(cap, light_slots, shadow_slots).bytes > OMV_STATIC_SCRATCH_BYTES) cap -= 32;
     return cap;

@@ -55,7 +55,6 @@ struct RenderScratch {
     float4* rq[2] = {nullptr, nullptr};  // ray queues: 2 float4 per entry
     uint4* hits = nullptr;       // per queue entry
     uint32_t* path_job = nullptr;  // batch: job of each path
-    float* cam_tnear = nullptr;    // camera ray tnear after alpha-masked retries (masked scenes only)
     float4* sq = nullptr;        // shadow queue: 3 float4 per entry
     uint32_t* ctr = nullptr;     // per-wave queue and work counters
     unsigned long long* stats = nullptr;  // cumulative ray counters
