@@ -382,16 +382,17 @@ __device__ __forceinline__ void child_info(const Node2* nodes, const uint32_t* v
     }
 }
 
-// exponent byte e such that 2^(e-127) * 65532 >= extent
+// exponent byte e such that 2^(e-127) * 32764 >= extent (at most 239, so
+// that the traversal's 2^(e-127+15) stays a finite float)
 __device__ __forceinline__ uint32_t quant_exponent(float ext)
 {
     if (!(ext > 0.0f)) return 1u;
-    float s = ext / 65532.0f;
+    float s = ext / 32764.0f;
     uint32_t bits = __float_as_uint(s);
     uint32_t e = (bits >> 23) & 0xFF;
     if (bits & 0x7FFFFFu) e += 1;  // round up to a power of two
     if (e < 1) e = 1;
-    if (e > 254) e = 254;
+    if (e > 239) e = 239;
     return e;
 }
 
@@ -535,11 +536,11 @@ __global__ void k_collapse(int nwork, const Work* __restrict__ work, const Node2
     }
     uint32_t imask = 0, meta[8];
     int rank = 0, off = 0;
-    for (int s = 0; s < 8; ++s) {
+    for (int s = 0; s < 8; ++s) {  // empty slots: inverted boxes
         meta[s] = 0;
         for (int a = 0; a < 3; ++a) {
-            o.qlo[a][s] = 0xFFFF;
-            o.qhi[a][s] = 0;
+            o.qlo[a][s] = kQuantFlag | kQuantMax;
+            o.qhi[a][s] = kQuantFlag;
         }
     }
     // internal children are stored in slot order: child(s) = child_base + popc(imask & ((1<<s)-1));
@@ -552,14 +553,14 @@ __global__ void k_collapse(int nwork, const Work* __restrict__ work, const Node2
             float lo = sb[c].lo[a], hi = sb[c].hi[a];
             int ql = (int)floorf(__fdiv_rn(__fsub_rn(lo, p[a]), sc[a]));
             int qh = (int)ceilf(__fdiv_rn(__fsub_rn(hi, p[a]), sc[a]));
-            ql = max(0, min(65535, ql));
-            qh = max(0, min(65535, qh));
+            ql = max(0, min((int)kQuantMax, ql));
+            qh = max(0, min((int)kQuantMax, qh));
             while (ql > 0 && __fadd_rn(p[a], __fmul_rn((float)ql, sc[a])) > lo) --ql;
-            while (qh < 65535 && __fadd_rn(p[a], __fmul_rn((float)qh, sc[a])) < hi) ++qh;
+            while (qh < (int)kQuantMax && __fadd_rn(p[a], __fmul_rn((float)qh, sc[a])) < hi) ++qh;
             ql = ql > 0 ? ql - 1 : 0;          // one quantum of slack each side
-            qh = qh < 65535 ? qh + 1 : 65535;
-            o.qlo[a][s] = (uint16_t)ql;
-            o.qhi[a][s] = (uint16_t)qh;
+            qh = qh < (int)kQuantMax ? qh + 1 : (int)kQuantMax;
+            o.qlo[a][s] = (uint16_t)(kQuantFlag | ql);
+            o.qhi[a][s] = (uint16_t)(kQuantFlag | qh);
         }
         if (cnt > leaf_max) {
             imask |= 1u << s;

@@ -21,10 +21,15 @@ namespace omv {
 //   w0 = (px, py, pz, ex | ey<<8 | ez<<16 | imask<<24)
 //   w1 = (child_base, prim_base, meta[0..3], meta[4..7])
 //   w2..w4 = qlo x/y/z as 8 x u16;  w5..w7 = qhi x/y/z as 8 x u16
-// child slot i box: lo = p + qlo[i] * 2^(e-127), hi = p + qhi[i] * 2^(e-127).
+// each u16 plane is 0x8000 | q with a 15-bit q (the flag is the exponent bit
+// that makes the plane's bytes, shifted up by one byte under 0x3F, the float
+// 1 + q * 2^-15); child slot i box: lo = p + q(qlo[i]) * 2^(e-127),
+// hi = p + q(qhi[i]) * 2^(e-127).
 // imask bit i: slot i is an internal node, at child_base + meta[i].
 // leaf slot: meta = (count << 5) | offset, primitives prim_base + offset ...
 // empty slot: imask bit clear and meta = 0.
+constexpr uint32_t kQuantFlag = 0x8000u;  // set in every stored plane
+constexpr uint32_t kQuantMax = 0x7FFFu;   // largest quantised plane q
 struct alignas(16) Bvh8Node {
     float px, py, pz;
     uint32_t exps;

@@ -152,13 +152,28 @@ __device__ __forceinline__ void to_object(const float* m, V3 o, V3 d, V3& ro, V3
             __fadd_rn(__fadd_rn(__fmul_rn(m[8], d.x), __fmul_rn(m[9], d.y)), __fmul_rn(m[10], d.z)));
 }
 
-// 16-bit quantised plane of slot s (two slots per word) as a float: the bits
-// 0x4B00_0000 | q are the float 2^23 + q, so one byte permute and one exact
-// subtraction give float(q)
-__device__ __forceinline__ float qword(uint4 w, int s)
+// Quantised plane of slot s (two 16-bit planes per word, each 0x8000 | q) as
+// the float Q = 1 + q * 2^-15: one byte permute places the plane under the
+// byte 0x3F and above a zero byte, and the flag bit completes the exponent 127.
+// A plane's slab distance (p + q s - o) / d is then Q A + (b - A) with
+// A = 2^15 s / d and b = (p - o) / d: one fused multiply-add per plane.
+__device__ __forceinline__ float qplane(uint4 w, int s)
 {
     const uint32_t x = (s >> 1) == 0 ? w.x : (s >> 1) == 1 ? w.y : (s >> 1) == 2 ? w.z : w.w;
-    return __uint_as_float(__byte_perm(x, 0x4B000000u, (s & 1) ? 0x7632u : 0x7610u)) - 8388608.0f;
+    return __uint_as_float(__byte_perm(x, 0x3F000000u, (s & 1) ? 0x7324u : 0x7104u));
+}
+
+// Offset b - k A of the near (kNear) or far plane distances of one axis.  The
+// rounding of b - A is at most 2^-24 (|b| + |A|): the |b| part is of the size
+// of b's own rounding, which the relative margins of the box test cover, and
+// the |A| part (2^-9 of a quantum's distance) is covered by moving the near
+// planes 2^-21 |A| (2^-6 of a quantum) closer and the far planes as much
+// farther (k = 1 -+ 2^-21, exact; A has the sign of 1/d).
+template <bool kNear>
+__device__ __forceinline__ float plane_offset(float b, float A)
+{
+    const float up = 1.0f + 0x1p-21f, down = 1.0f - 0x1p-21f;
+    return fmaf(-((A >= 0.0f) == kNear ? up : down), A, b);
 }
 
 __device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b)
@@ -259,12 +274,16 @@ __device__ __forceinline__ bool trace_step(const DevScene& S, const uint32_t* __
     const uint32_t exps = w0.w;
     const uint32_t imask = exps >> 24;
     const uint32_t child_base = w1.x, prim_base = w1.y, meta_lo = w1.z, meta_hi = w1.w;
-    const float sx = __uint_as_float((exps & 0xFFu) << 23);
-    const float sy = __uint_as_float(((exps >> 8) & 0xFFu) << 23);
-    const float sz = __uint_as_float(((exps >> 16) & 0xFFu) << 23);
+    // 2^15 times the quantum 2^(e-127) of each axis (e <= 239)
+    const float sx = __uint_as_float(((exps & 0xFFu) + 15u) << 23);
+    const float sy = __uint_as_float((((exps >> 8) & 0xFFu) + 15u) << 23);
+    const float sz = __uint_as_float((((exps >> 16) & 0xFFu) + 15u) << 23);
     const V3 rid = T.rid, ro = T.ro;
     const float ax = sx * rid.x, ay = sy * rid.y, az = sz * rid.z;
     const float bx = (px - ro.x) * rid.x, by = (py - ro.y) * rid.y, bz = (pz - ro.z) * rid.z;
+    const float bnx = plane_offset<true>(bx, ax), bfx = plane_offset<false>(bx, ax);
+    const float bny = plane_offset<true>(by, ay), bfy = plane_offset<false>(by, ay);
+    const float bnz = plane_offset<true>(bz, az), bfz = plane_offset<false>(bz, az);
     // entry and exit planes per axis from the ray direction: for a child with
     // qlo <= qhi these are exactly min() and max() of the two slab distances
     const uint4 nx = rid.x >= 0.0f ? qlx : qhx, fx = rid.x >= 0.0f ? qhx : qlx;
@@ -278,9 +297,9 @@ __device__ __forceinline__ bool trace_step(const DevScene& S, const uint32_t* __
         const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> (8 * (s & 3))) & 0xFFu;
         const bool internal = (imask >> s) & 1u;
         const bool valid = internal || meta != 0u;
-        const float tnx = fmaf(qword(nx, s), ax, bx), tfx = fmaf(qword(fx, s), ax, bx);
-        const float tny = fmaf(qword(ny, s), ay, by), tfy = fmaf(qword(fy, s), ay, by);
-        const float tnz = fmaf(qword(nz, s), az, bz), tfz = fmaf(qword(fz, s), az, bz);
+        const float tnx = fmaf(qplane(nx, s), ax, bnx), tfx = fmaf(qplane(fx, s), ax, bfx);
+        const float tny = fmaf(qplane(ny, s), ay, bny), tfy = fmaf(qplane(fy, s), ay, bfy);
+        const float tnz = fmaf(qplane(nz, s), az, bnz), tfz = fmaf(qplane(fz, s), az, bfz);
         const float tin = fmaxf(fmaxf(fmaxf(tnx, tny), tnz) * 0.99999952f, tnear);
         const float tout = fminf(fminf(fminf(tfx, tfy), tfz) * 1.00000048f, lim);
         key[s] = 0xFFFFFFFFu;

@@ -86,7 +86,12 @@ def test_large_instanced_scene_matches_oracle(gpu, oracle, scenes, builder):
     axis = _random_rays(rng, 3000, [-25, -25, -65], [25, 25, -15])
     axis[:, 4:7] = np.eye(3, dtype=np.float32)[rng.integers(0, 3, 3000)] * np.where(
         rng.uniform(size=(3000, 1)) < 0.5, -1, 1)
-    rays = np.concatenate([cam, rnd, axis])
+    # nearly axis-parallel: the other two components tiny (reciprocals up to
+    # the box test's 1e20 clamp), where the slab distances are largest
+    tilt = axis.copy()
+    tiny = rng.choice(np.array([1e-30, 1e-21, 1e-12, 1e-6, 1e-3], np.float32), (3000, 3))
+    tilt[:, 4:7] += tiny * np.where(rng.uniform(size=(3000, 3)) < 0.5, -1, 1) * (tilt[:, 4:7] == 0)
+    rays = np.concatenate([cam, rnd, axis, tilt])
     ok, msg = _hits_equal(rs.trace(rays), os_.trace(rays))
     assert ok, msg
 
