@@ -232,6 +232,27 @@ def run_batched(args, dev):
         for jb in jobs:
             br.render([jb])
 
+    # one job per call through the single-frame API, as a caller without the
+    # batch entry point would do it: the job's materials, then its frame
+    L, capi = omv.lib(), omv.capi
+    descs = []
+    for j in range(n):
+        keep: list = []
+        descs.append((capi.material_descs(sets[j], keep), len(sets[j]), keep))
+    prm = []
+    for j in range(n):
+        pc = br.params.to_c()
+        pc.samples_per_pixel, pc.seed, pc.sample_offset = int(spps[j]), j, 0
+        prm.append(pc)
+    stream = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+
+    def per_call():
+        for j, jb in enumerate(jobs):
+            d, m, _ = descs[j]
+            omv.check(L.omv_scene_set_materials(rs.handle, m, d))
+            omv.check(L.omv_render_device(rs.handle, C.byref(jb.camera), C.byref(prm[j]), C.c_void_p(jb.d_sum_rgb),
+                                          None, C.c_void_p(jb.d_count), stream, None))
+
     chosen = br.autotune(jobs)
     br.render(jobs, graph=True)  # capture
     zero()
@@ -240,6 +261,14 @@ def run_batched(args, dev):
     t_plain = timed(plain)
     ref_sum = [f[0].clone() for f in films]
     ref_cnt = [f[2].clone() for f in films]
+    zero()
+    timed(per_call)  # warm-up
+    zero()
+    t_call = timed(per_call)
+    call_sum = [f[0].clone() for f in films]
+    call_cnt = [f[2].clone() for f in films]
+    keep0: list = []
+    omv.check(L.omv_scene_set_materials(rs.handle, len(sc.materials), capi.material_descs(sc.materials, keep0)))
     zero()
     br.render(jobs, graph=True)  # warm-up replay
     zero()
@@ -252,10 +281,14 @@ def run_batched(args, dev):
     counts_match = all(bool((f[2] == c).all()) for f, c in zip(films, ref_cnt))
     rel = max(float((f[0] - r).abs().max()) / max(1e-30, float(r.abs().max())) for f, r in zip(films, ref_sum))
     match = counts_match and rel <= 5e-6
-    del films, ref_sum, ref_cnt
+    call_counts = all(bool((f[2] == c).all()) for f, c in zip(films, call_cnt))
+    call_rel = max(float((f[0] - r).abs().max()) / max(1e-30, float(r.abs().max())) for f, r in zip(films, call_sum))
+    del films, ref_sum, ref_cnt, call_sum, call_cnt
     torch.cuda.empty_cache()
     return {"jobs": n, "paths": paths, "plain_jobs_per_s": round(n / t_plain, 3),
             "batched_jobs_per_s": round(n / t_batch, 3), "speedup": round(t_plain / t_batch, 3),
+            "per_call_jobs_per_s": round(n / t_call, 3), "speedup_vs_per_call": round(t_call / t_batch, 3),
+            "per_call_films_match": call_counts and call_rel <= 5e-6,
             "plain_mpaths_per_s": round(paths / t_plain / 1e6, 2), "batched_mpaths_per_s": round(paths / t_batch / 1e6, 2),
             "wave_paths": chosen, "shade_block_threads": br.block_threads, "graph": True, "films_match": match,
             "counts_match": counts_match,
