@@ -582,6 +582,24 @@ omv_status omv_brdf_eval_direct(int64_t n, const float* in, float* out);
 omv_status omv_brdf_sample_indirect(int64_t n, const float* in, float* out);
 omv_status omv_om_fresnel(int64_t n, const float* in, float* out);
 
+/* The float library calls of the reference's material and environment
+ * arithmetic as the device evaluates them, correctly rounded: std::sin and
+ * std::cos of the sampling angles (RandomSampler.h:87-103), std::asin and
+ * std::acos of the background lookup (HdrBackground.cpp:61-63), std::pow(x, 5)
+ * and std::pow(x, -2) of the Fresnel and GGX terms (BRDFModel.h:44-80).
+ * `function` is one of OMV_FN_*; n floats in, n floats out (host buffers).
+ * sin / cos take arguments in [0, 8] (the angles 2 pi u), asin / acos in
+ * [-1, 1]. */
+enum {
+    OMV_FN_SIN = 0,
+    OMV_FN_COS = 1,
+    OMV_FN_ASIN = 2,
+    OMV_FN_ACOS = 3,
+    OMV_FN_POW5 = 4,
+    OMV_FN_POW_M2 = 5
+};
+omv_status omv_library_function(int32_t function, int64_t n, const float* in, float* out);
+
 /* BitmapTexture::texture(u, v, fvec4) (BitmapTexture.cpp:73-125) on the device:
  * one width x height RGBA8 image, n (u, v) pairs in, 4 floats each out. */
 omv_status omv_texture_sample(int32_t width, int32_t height, const uint8_t* rgba, int64_t n, const float* uv,

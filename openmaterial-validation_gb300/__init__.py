@@ -124,6 +124,7 @@ def lib():
                                  C.POINTER(C.c_uint32)]
     for n in ("omv_brdf_eval_direct", "omv_brdf_sample_indirect", "omv_om_fresnel"):
         getattr(L, n).argtypes = [C.c_int64, capi.f32p, capi.f32p]
+    L.omv_library_function.argtypes = [C.c_int32, C.c_int64, capi.f32p, capi.f32p]
     L.omv_camera_rays.argtypes = [C.POINTER(capi.Camera), capi.f32p, capi.f32p]
     L.omv_env_radiance.argtypes = [vp, C.c_int64, capi.f32p, capi.f32p]
     L.omv_fc_subject_from_name.argtypes = [C.c_char_p]
@@ -148,7 +149,7 @@ def lib():
               "omv_render_device_static", "omv_batch_set_materials", "omv_render_batch", "omv_batch_autotune",
               "omv_scene_set_materials", "omv_adjoint",
               "omv_trace_rays", "omv_render_ids", "omv_brdf_eval_direct",
-              "omv_brdf_sample_indirect", "omv_om_fresnel", "omv_camera_rays", "omv_env_radiance", "omv_struct_sizes",
+              "omv_brdf_sample_indirect", "omv_om_fresnel", "omv_library_function", "omv_camera_rays", "omv_env_radiance", "omv_struct_sizes",
               "omv_develop", "omv_tonemap", "omv_denoise_median", "omv_rgba8", "omv_save_image",
               "omv_render_fc", "omv_scene_bounds", "omv_lightbox_cameras", "omv_texture_sample"):
         getattr(L, n).restype = st
@@ -607,6 +608,19 @@ def brdf_sample_indirect(x: np.ndarray) -> np.ndarray:
 
 def om_fresnel(x: np.ndarray) -> np.ndarray:
     return _hook("omv_om_fresnel", 7, 3, x)
+
+
+# omv_library_function's OMV_FN_* (include/omv.h)
+FN_SIN, FN_COS, FN_ASIN, FN_ACOS, FN_POW5, FN_POW_M2 = range(6)
+
+
+def library_function(fn: int, x: np.ndarray) -> np.ndarray:
+    """The device's correctly rounded std::sin / cos / asin / acos /
+    pow(x, 5) / pow(x, -2) of float inputs (FN_* selects)."""
+    x = np.ascontiguousarray(x, dtype=np.float32).ravel()
+    out = np.zeros_like(x)
+    check(lib().omv_library_function(fn, len(x), capi.fptr(x), capi.fptr(out)))
+    return out
 
 
 def texture_sample(img: np.ndarray, uv: np.ndarray) -> np.ndarray:

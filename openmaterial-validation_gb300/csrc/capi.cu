@@ -378,8 +378,9 @@ omv_status omv_env_radiance(omv_scene* scene, int64_t n, const float* dirs, floa
     });
 }
 
-static omv_status run_hook(int64_t n, const float* in, float* out, int win, int wout,
-                           void (*fn)(int64_t, const float*, float*, cudaStream_t))
+extern "C++" {  // a template inside the C block
+template <typename Fn>
+static omv_status run_hook(int64_t n, const float* in, float* out, int win, int wout, Fn fn)
 {
     return guarded([&] {
         if (n < 0 || (n > 0 && (!in || !out))) throw omv::ArgError("invalid buffers");
@@ -391,6 +392,7 @@ static omv_status run_hook(int64_t n, const float* in, float* out, int win, int 
         fn(n, di.as<float>(), dout.as<float>(), nullptr);
         OMV_CUDA(cudaMemcpy(out, dout.p, sizeof(float) * wout * n, cudaMemcpyDeviceToHost));
     });
+}
 }
 
 omv_status omv_brdf_eval_direct(int64_t n, const float* in, float* out)
@@ -406,6 +408,14 @@ omv_status omv_brdf_sample_indirect(int64_t n, const float* in, float* out)
 omv_status omv_om_fresnel(int64_t n, const float* in, float* out)
 {
     return run_hook(n, in, out, 7, 3, omv::hook_om_fresnel);
+}
+
+omv_status omv_library_function(int32_t function, int64_t n, const float* in, float* out)
+{
+    if (function < OMV_FN_SIN || function > OMV_FN_POW_M2) return guarded([] { throw omv::ArgError("unknown function"); });
+    return run_hook(n, in, out, 1, 1, [function](int64_t m, const float* a, float* b, cudaStream_t st) {
+        omv::hook_library_function(function, m, a, b, st);
+    });
 }
 
 omv_status omv_texture_sample(int32_t width, int32_t height, const uint8_t* rgba, int64_t n, const float* uv,

@@ -29,7 +29,9 @@
 //   * x^5 and 1/x^2: double-float products; 1/(p + e) by one Newton-Raphson
 //     correction of the rounded reciprocal of p.
 // Everything is plain float arithmetic (the fused multiply-adds are explicit),
-// so the host build (-ffp-contract=off) computes the same bits as the device.
+// so the host build (-ffp-contract=off) computes the same results as the
+// device; only the low-order corrections of asin / acos (a cosine and two
+// quotients that need about 2^-20) use the device's fast approximations.
 #pragma once
 
 #include <cmath>
@@ -207,7 +209,11 @@ OMV_CR_HD FF asin_ff_small(FF t)
     const float y0 = asinf(t.hi);
     const FF s = ff_sin_small(y0);
     const float res = (t.hi - s.hi) + (t.lo - s.lo);  // t.hi - s.hi is exact (Sterbenz)
+#ifdef __CUDA_ARCH__
+    return two_sum(y0, __fdividef(res, cos_rough(y0)));  // two ulp suffice here
+#else
     return two_sum(y0, res / cos_rough(y0));
+#endif
 }
 
 // sqrt of a float as a double-float (the residual a - h^2 is exact by FMA)
@@ -215,7 +221,11 @@ OMV_CR_HD FF sqrt_ff(float a)
 {
     const float h = sqrtf(a);
     if (!(h > 0.0f)) return FF{h, 0.0f};
+#ifdef __CUDA_ARCH__
+    return FF{h, __fdividef(fmaf(-h, h, a), 2.0f * h)};  // the low part needs about 2^-20 only
+#else
     return FF{h, fmaf(-h, h, a) / (2.0f * h)};
+#endif
 }
 
 // The asin of |x| reduced to an argument in [0, 1/2]: |x| itself, or

@@ -839,6 +839,24 @@ __global__ void k_hook_camera(omv_camera cam, const float* jitter, float* rays)
     r[5] = R.z;
 }
 
+// the correctly rounded library functions, one per launch (OMV_FN_*)
+__global__ void k_hook_library(int fn, int64_t n, const float* in, float* out)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float x = in[i];
+    float y = 0.0f, c = 0.0f;
+    switch (fn) {
+    case OMV_FN_SIN: cr::sincos_cr(x, y, c); break;
+    case OMV_FN_COS: cr::sincos_cr(x, c, y); break;
+    case OMV_FN_ASIN: y = cr::asin_cr(x); break;
+    case OMV_FN_ACOS: y = cr::acos_cr(x); break;
+    case OMV_FN_POW5: y = cr::pow5_cr(x); break;
+    default: y = cr::rcp_sq_cr(x); break;
+    }
+    out[i] = y;
+}
+
 inline int hb(int64_t n) { return (int)std::max<int64_t>(1, (n + 255) / 256); }
 
 }  // namespace
@@ -856,6 +874,11 @@ void hook_sample_indirect(int64_t n, const float* in, float* out, cudaStream_t s
 void hook_om_fresnel(int64_t n, const float* in, float* out, cudaStream_t st)
 {
     k_hook_om<<<hb(n), 256, 0, st>>>(n, in, out);
+    OMV_CUDA(cudaGetLastError());
+}
+void hook_library_function(int fn, int64_t n, const float* in, float* out, cudaStream_t st)
+{
+    k_hook_library<<<hb(n), 256, 0, st>>>(fn, n, in, out);
     OMV_CUDA(cudaGetLastError());
 }
 void hook_camera_rays(const omv_camera& cam, const float* jitter, float* rays, cudaStream_t st)

@@ -203,6 +203,7 @@ void save_image(const char* path, const float* rgba, int w, int h);
 void hook_eval_direct(int64_t n, const float* d_in, float* d_out, cudaStream_t st);
 void hook_sample_indirect(int64_t n, const float* d_in, float* d_out, cudaStream_t st);
 void hook_om_fresnel(int64_t n, const float* d_in, float* d_out, cudaStream_t st);
+void hook_library_function(int fn, int64_t n, const float* d_in, float* d_out, cudaStream_t st);
 void hook_camera_rays(const omv_camera& cam, const float* d_jitter, float* d_rays, cudaStream_t st);
 
 }  // namespace omv
