@@ -27,7 +27,11 @@
 //     with sin evaluated in double-float; |t| > 1/2 through
 //     asin(t) = pi/2 - 2 asin(sqrt((1 - t) / 2));
 //   * x^5 and 1/x^2: double-float products; 1/(p + e) by one Newton-Raphson
-//     correction of the rounded reciprocal of p.
+//     correction of the rounded reciprocal of p; both are rational, so where
+//     the double-float result lies near a rounding midpoint (about one input
+//     in 2^20) the side of the midpoint is decided exactly, in double with
+//     error-free products, and exact midpoints (x^5 of odd * 2^j, odd <= 31)
+//     round to even.
 // Everything is plain float arithmetic (the fused multiply-adds are explicit),
 // so the host build (-ffp-contract=off) computes the same results as the
 // device; only the low-order corrections of asin / acos (a cosine and two
@@ -36,6 +40,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 
 #ifdef __CUDACC__
 #define OMV_CR_HD __host__ __device__ __forceinline__
@@ -262,23 +267,70 @@ OMV_CR_HD float acos_cr(float x)
     return v.hi + v.lo;
 }
 
-// correctly rounded x^5 (std::pow(x, 5.0f) of a float)
+// A double-float value h + lo (h = RN(h + lo)) whose exact value is within
+// about 2^-44 |h| of it can round the other way only when h + lo lies near the
+// midpoint between h and its neighbour nb on lo's side: true when
+// ||lo| - gap/2| <= 2^-40 |h| (gap = |nb - h|, exact).
+OMV_CR_HD bool near_midpoint(float h, float lo, float& nb)
+{
+    nb = nextafterf(h, lo > 0.0f ? 3.402823466e+38f : -3.402823466e+38f);
+    const float half = 0.5f * fabsf(nb - h);
+    return lo != 0.0f && fabsf(fabsf(lo) - half) <= 0x1p-40f * fabsf(h);
+}
+
+// the correctly rounded choice between h and nb, given the sign of
+// (exact value - midpoint of h and nb); ties to even
+OMV_CR_HD float round_by_side(float h, float nb, double side)
+{
+    if (side == 0.0) {
+#ifdef __CUDA_ARCH__
+        const uint32_t b = __float_as_uint(h);
+#else
+        uint32_t b;
+        std::memcpy(&b, &h, 4);
+#endif
+        return (b & 1u) ? nb : h;
+    }
+    return ((nb > h) == (side > 0.0)) ? nb : h;
+}
+
+// correctly rounded x^5 (std::pow(x, 5.0f) of a float) for x^5 in the normal
+// range: a double-float product, and near a rounding midpoint (about one
+// input in 2^20) an exact decision: x^5 = p1 + e1 + p2 + e2 exactly in double
+// (x^2 exact, x^4 = d4h + d4l and d4h x, d4l x split by fused multiply-adds)
 OMV_CR_HD float pow5_cr(float x)
 {
     const FF x2 = two_prod(x, x);
     const FF x4 = ff_mul(x2, x2);
     const FF x5 = ff_mul_f(x4, x);
-    return x5.hi;
+    float nb;
+    if (!near_midpoint(x5.hi, x5.lo, nb)) return x5.hi;
+    const double d = (double)x, d2 = d * d;
+    const double d4h = d2 * d2, d4l = fma(d2, d2, -d4h);
+    const double p1 = d4h * d, e1 = fma(d4h, d, -p1);
+    const double p2 = d4l * d, e2 = fma(d4l, d, -p2);
+    const double m = 0.5 * ((double)x5.hi + (double)nb);  // exact
+    return round_by_side(x5.hi, nb, (((p1 - m) + e1) + p2) + e2);  // p1 - m exact (Sterbenz)
 }
 
-// correctly rounded 1 / x^2 (std::pow(x, -2.0f) of a float)
+// correctly rounded 1 / x^2 (std::pow(x, -2.0f) of a float): the rounded
+// reciprocal of x^2 = p.hi + p.lo with one Newton-Raphson correction, and near
+// a rounding midpoint m an exact decision by the sign of 1 - m x^2 (m x^2 is
+// a 73-bit product, split exactly by a fused multiply-add)
 OMV_CR_HD float rcp_sq_cr(float x)
 {
     const FF p = two_prod(x, x);  // x^2 = p.hi + p.lo exactly
     const float q = 1.0f / p.hi;
     if (q == 0.0f || !(q <= 3.402823466e+38f)) return q;  // x = 0 (inf), x^2 overflows (0), NaN
     const float r = fmaf(-q, p.hi, 1.0f);  // exact residual of the rounded reciprocal
-    return q + q * (r - q * p.lo);
+    const float c = q * (r - q * p.lo);
+    const FF v = fast_two_sum(q, c);
+    float nb;
+    if (!near_midpoint(v.hi, v.lo, nb) || !(fabsf(v.hi) >= 0x1p-125f)) return v.hi;
+    const double m = 0.5 * ((double)v.hi + (double)nb);  // exact
+    const double x2 = (double)x * (double)x;                // exact
+    const double mh = m * x2, ml = fma(m, x2, -mh);         // m x^2 = mh + ml exactly
+    return round_by_side(v.hi, nb, -((mh - 1.0) + ml));     // sign of 1/x^2 - m = sign of 1 - m x^2
 }
 
 }  // namespace cr

@@ -8,7 +8,9 @@ The reference value of a float input is the float64 evaluation rounded once to
 float32.  float64 sin, asin, ... are within a few units of 2^-53 relative, so
 that rounding is the correctly rounded float32 except where the float64 value
 lies within a few float64 ulps of a float32 rounding midpoint: those inputs are
-reported as ambiguous and left out of the comparison."""
+reported as ambiguous and left out of the comparison.  x^5 and x^-2 are
+rational, so their ambiguous inputs (and exact midpoints, which round to even)
+are decided exactly with fractions instead."""
 import math
 import os
 import subprocess
@@ -44,9 +46,12 @@ def inputs(fn: int, n: int, seed: int = 0) -> np.ndarray:
                  (np.exp2(rng.uniform(-30, -1, n // 4)) * rng.choice([-1, 1], n // 4)).astype(np.float32),
                  np.array([-1.0, -0.5, 0.0, 0.5, 1.0], np.float32)]
     elif fn == POW5:
-        # (1 - cos) of the Schlick term: [0, 1]; correctly rounded from 2^-20 up
+        # (1 - cos) of the Schlick term: [0, 1]; correctly rounded from 2^-20 up;
+        # odd * 2^j with odd <= 31 make x^5 a rounding midpoint exactly (ties)
+        ties = np.array([o * 2.0 ** j for o in range(1, 32, 2) for j in range(-25, 1)], np.float32)
         parts = [rng.uniform(2.0 ** -20, 1.0, n).astype(np.float32),
-                 np.exp2(rng.uniform(-20, 0, n // 2)).astype(np.float32)]
+                 np.exp2(rng.uniform(-20, 0, n // 2)).astype(np.float32),
+                 ties[(ties >= 2.0 ** -20) & (ties <= 1.0)]]
     else:
         parts = [np.exp2(rng.uniform(-40, 40, n)).astype(np.float32),
                  rng.uniform(0.0, 4.0, n // 2).astype(np.float32)]
@@ -76,7 +81,23 @@ def reference(fn: int, x: np.ndarray):
     nb = np.nextafter(y32, up)
     mid = 0.5 * (y32.astype(np.float64) + nb.astype(np.float64))
     amb = np.abs(y - mid) <= 16.0 * np.spacing(np.abs(y))
+    if fn in (POW5, POW_M2):  # rational: decide those exactly (ties to even)
+        for i in np.flatnonzero(amb):
+            y32[i] = _round_exact(fn, float(x[i]))
+        amb[:] = False
     return y32, amb
+
+
+def _round_exact(fn: int, x: float) -> np.float32:
+    from fractions import Fraction
+    v = Fraction(x) ** 5 if fn == POW5 else 1 / Fraction(x) ** 2
+    a = np.float32(float(v))  # within one float32 step of the answer
+    best = None
+    for c in (np.nextafter(a, np.float32(-np.inf)), a, np.nextafter(a, np.float32(np.inf))):
+        d = abs(Fraction(float(c)) - v)
+        if best is None or d < best[0] or (d == best[0] and int(c.view(np.uint32)) % 2 == 0):
+            best = (d, c)
+    return best[1]
 
 
 HERE = os.path.dirname(os.path.abspath(__file__))

@@ -18,7 +18,7 @@ def test_host_build_is_correctly_rounded(host_cr, fn):
     x = crcheck.inputs(fn, 400_000)
     want, amb = crcheck.reference(fn, x)
     got = host_cr(fn, x)
-    assert amb.sum() <= 2
+    assert amb.sum() <= (0 if fn in (crcheck.POW5, crcheck.POW_M2) else 2)
     bad = (got != want) & ~amb
     assert not bad.any(), (x[bad][:5], got[bad][:5], want[bad][:5])
 

@@ -80,5 +80,5 @@ def test_library_functions_are_correctly_rounded_on_the_device(gpu, fn):
     want, amb = crcheck.reference(fn, x)
     got = gpu.library_function(fn, x)
     bad = (got != want) & ~amb
-    assert amb.sum() <= 4
+    assert amb.sum() <= (0 if fn in (crcheck.POW5, crcheck.POW_M2) else 4)
     assert not bad.any(), (x[bad][:5], got[bad][:5], want[bad][:5])
