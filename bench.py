@@ -696,8 +696,10 @@ def run_ours(args, scene, ws, rank, local):
     torch.cuda.synchronize(dev)
     evs = []
     agg = {k: 0 for k in ("extension_rays", "shadow_rays", "light_rays", "kernel_launches", "nodes_visited",
-                          "triangles_tested", "extend_launches", "stack_overflows")}
-    ext_ms = 0.0
+                          "triangles_tested", "extend_launches", "stack_overflows", "tail_nodes_visited",
+                          "tail_triangles_tested")}
+    ext_ms = tail_ms = 0.0
+    tail_bounce = 0
     for _ in range(args.steps):
         flush.zero_()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -710,6 +712,8 @@ def run_ours(args, scene, ws, rank, local):
         for k in agg:
             agg[k] += getattr(st, k)
         ext_ms += st.extend_ms
+        tail_ms += st.tail_ms
+        tail_bounce = st.tail_bounce
     torch.cuda.synchronize(dev)
     if dist:
         dist.barrier()
@@ -766,7 +770,12 @@ def run_ours(args, scene, ws, rank, local):
                 "mrays_per_s": round(rays / (max_ms / 1e3) / 1e6, 4), "film_counts_ok": cnt_ok,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clock,
                 "gpu_launches": agg["kernel_launches"], "scene_build_ms": round(info["build_ms"], 1),
-                "stack_overflows": agg["stack_overflows"]}
+                "stack_overflows": agg["stack_overflows"],
+                "tail": {"kernel": "k_camera_tail", "from_bounce": tail_bounce,
+                         "ms_per_step": round(tail_ms / args.steps, 4),
+                         "share_of_step": round(tail_ms / max(dev_ms, 1e-9), 4),
+                         "nodes_per_step": agg["tail_nodes_visited"] // args.steps,
+                         "triangles_per_step": agg["tail_triangles_tested"] // args.steps}}
         if ws == 1 and not args.no_lights:
             line["lights"] = run_lights(args, dev, flush)
         if ws == 1 and not args.no_builders:

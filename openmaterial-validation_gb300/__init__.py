@@ -445,7 +445,8 @@ class BDPTRenderer:
         self.last_stats = {"paths": st.paths, "extension_rays": st.extension_rays, "shadow_rays": st.shadow_rays,
                            "light_rays": st.light_rays, "render_ms": st.render_ms,
                            "kernel_launches": st.kernel_launches, "stack_overflows": st.stack_overflows,
-                           "nodes_visited": st.nodes_visited, "triangles_tested": st.triangles_tested}
+                           "nodes_visited": st.nodes_visited, "triangles_tested": st.triangles_tested,
+                           "tail_bounce": st.tail_bounce, "tail_nodes_visited": st.tail_nodes_visited}
         if sums:
             return img, s, q, cnt
         return img

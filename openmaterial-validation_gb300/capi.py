@@ -100,7 +100,8 @@ class Stats(C.Structure):
                 ("nodes_visited", C.c_int64), ("triangles_tested", C.c_int64), ("extend_ms", C.c_double),
                 ("extend_launches", C.c_int64), ("shadow_ms", C.c_double), ("shadow_launches", C.c_int64),
                 ("stack_overflows", C.c_int64), ("shadow_nodes_visited", C.c_int64),
-                ("shadow_triangles_tested", C.c_int64)]
+                ("shadow_triangles_tested", C.c_int64), ("tail_bounce", C.c_int64),
+                ("tail_nodes_visited", C.c_int64), ("tail_triangles_tested", C.c_int64), ("tail_ms", C.c_double)]
 
 
 class Hit(C.Structure):

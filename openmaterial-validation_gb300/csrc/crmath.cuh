@@ -44,8 +44,10 @@
 
 #ifdef __CUDACC__
 #define OMV_CR_HD __host__ __device__ __forceinline__
+#define OMV_CR_RARE static __host__ __device__ __noinline__  // rare paths, out of the callers' registers
 #else
 #define OMV_CR_HD inline
+#define OMV_CR_RARE inline
 #endif
 
 namespace omv {
@@ -267,15 +269,39 @@ OMV_CR_HD float acos_cr(float x)
     return v.hi + v.lo;
 }
 
+OMV_CR_HD uint32_t f2u(float f)
+{
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(f);
+#else
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+#endif
+}
+OMV_CR_HD float u2f(uint32_t u)
+{
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(u);
+#else
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+#endif
+}
+
 // A double-float value h + lo (h = RN(h + lo)) whose exact value is within
 // about 2^-44 |h| of it can round the other way only when h + lo lies near the
-// midpoint between h and its neighbour nb on lo's side: true when
-// ||lo| - gap/2| <= 2^-40 |h| (gap = |nb - h|, exact).
-OMV_CR_HD bool near_midpoint(float h, float lo, float& nb)
+// midpoint between h and its neighbour on lo's side, i.e. |lo| near half that
+// gap: ulp(h) / 2, or ulp(h) / 4 below a power of two.  A few instructions,
+// conservative (true also for |h| < 2^-100, which the callers pass on).
+OMV_CR_HD bool maybe_midpoint(float h, float lo)
 {
-    nb = nextafterf(h, lo > 0.0f ? 3.402823466e+38f : -3.402823466e+38f);
-    const float half = 0.5f * fabsf(nb - h);
-    return lo != 0.0f && fabsf(fabsf(lo) - half) <= 0x1p-40f * fabsf(h);
+    const uint32_t e = f2u(h) & 0x7F800000u;
+    if (e < (27u << 23)) return true;
+    const float u = u2f(e - (23u << 23));  // ulp(h)
+    const float a = fabsf(lo), t = 0x1p-40f * fabsf(h);
+    return fabsf(a - 0.5f * u) <= t || fabsf(a - 0.25f * u) <= t;
 }
 
 // the correctly rounded choice between h and nb, given the sign of
@@ -283,13 +309,7 @@ OMV_CR_HD bool near_midpoint(float h, float lo, float& nb)
 OMV_CR_HD float round_by_side(float h, float nb, double side)
 {
     if (side == 0.0) {
-#ifdef __CUDA_ARCH__
-        const uint32_t b = __float_as_uint(h);
-#else
-        uint32_t b;
-        std::memcpy(&b, &h, 4);
-#endif
-        return (b & 1u) ? nb : h;
+        return (f2u(h) & 1u) ? nb : h;
     }
     return ((nb > h) == (side > 0.0)) ? nb : h;
 }
@@ -298,19 +318,39 @@ OMV_CR_HD float round_by_side(float h, float nb, double side)
 // range: a double-float product, and near a rounding midpoint (about one
 // input in 2^20) an exact decision: x^5 = p1 + e1 + p2 + e2 exactly in double
 // (x^2 exact, x^4 = d4h + d4l and d4h x, d4l x split by fused multiply-adds)
+// the neighbour of h on lo's side
+OMV_CR_HD float side_neighbour(float h, float lo)
+{
+    return nextafterf(h, lo > 0.0f ? 3.402823466e+38f : -3.402823466e+38f);
+}
+
+OMV_CR_RARE float pow5_decide(float x, float h, float lo)
+{
+    const float nb = side_neighbour(h, lo);
+    const double d = (double)x, d2 = d * d;
+    const double d4h = d2 * d2, d4l = fma(d2, d2, -d4h);
+    const double p1 = d4h * d, e1 = fma(d4h, d, -p1);
+    const double p2 = d4l * d, e2 = fma(d4l, d, -p2);
+    const double m = 0.5 * ((double)h + (double)nb);  // exact
+    return round_by_side(h, nb, (((p1 - m) + e1) + p2) + e2);  // p1 - m exact (Sterbenz)
+}
 OMV_CR_HD float pow5_cr(float x)
 {
     const FF x2 = two_prod(x, x);
     const FF x4 = ff_mul(x2, x2);
     const FF x5 = ff_mul_f(x4, x);
-    float nb;
-    if (!near_midpoint(x5.hi, x5.lo, nb)) return x5.hi;
-    const double d = (double)x, d2 = d * d;
-    const double d4h = d2 * d2, d4l = fma(d2, d2, -d4h);
-    const double p1 = d4h * d, e1 = fma(d4h, d, -p1);
-    const double p2 = d4l * d, e2 = fma(d4l, d, -p2);
-    const double m = 0.5 * ((double)x5.hi + (double)nb);  // exact
-    return round_by_side(x5.hi, nb, (((p1 - m) + e1) + p2) + e2);  // p1 - m exact (Sterbenz)
+    if (!maybe_midpoint(x5.hi, x5.lo)) return x5.hi;
+    return pow5_decide(x, x5.hi, x5.lo);
+}
+
+OMV_CR_RARE float rcp_sq_decide(float x, float h, float lo)
+{
+    if (!(fabsf(h) >= 0x1p-125f)) return h;  // subnormal results: not decided
+    const float nb = side_neighbour(h, lo);
+    const double m = 0.5 * ((double)h + (double)nb);  // exact
+    const double x2 = (double)x * (double)x;            // exact
+    const double mh = m * x2, ml = fma(m, x2, -mh);     // m x^2 = mh + ml exactly
+    return round_by_side(h, nb, -((mh - 1.0) + ml));    // sign of 1/x^2 - m = sign of 1 - m x^2
 }
 
 // correctly rounded 1 / x^2 (std::pow(x, -2.0f) of a float): the rounded
@@ -325,12 +365,8 @@ OMV_CR_HD float rcp_sq_cr(float x)
     const float r = fmaf(-q, p.hi, 1.0f);  // exact residual of the rounded reciprocal
     const float c = q * (r - q * p.lo);
     const FF v = fast_two_sum(q, c);
-    float nb;
-    if (!near_midpoint(v.hi, v.lo, nb) || !(fabsf(v.hi) >= 0x1p-125f)) return v.hi;
-    const double m = 0.5 * ((double)v.hi + (double)nb);  // exact
-    const double x2 = (double)x * (double)x;                // exact
-    const double mh = m * x2, ml = fma(m, x2, -mh);         // m x^2 = mh + ml exactly
-    return round_by_side(v.hi, nb, -((mh - 1.0) + ml));     // sign of 1/x^2 - m = sign of 1 - m x^2
+    if (!maybe_midpoint(v.hi, v.lo)) return v.hi;
+    return rcp_sq_decide(x, v.hi, v.lo);
 }
 
 }  // namespace cr

@@ -55,8 +55,13 @@ constexpr int kCtrWork = 192;    // + launch index
 constexpr int kCtrEnv = 448;     // + bounce: MIS environment rays
 enum {
     kStatExt = 0, kStatShadow = 1, kStatLight = 2, kStatNodes = 3, kStatTris = 4, kStatOverflow = 5,
-    kStatShadowNodes = 6, kStatShadowTris = 7
+    kStatShadowNodes = 6, kStatShadowTris = 7, kStatTailNodes = 8, kStatTailTris = 9
 };
+// The camera bounces from this one on run in one launch, each thread taking a
+// path to its end (k_camera_tail): on the 1920x1080x64 benchmark frame about
+// 0.2% of the paths are alive at bounce 5, and one launch pair per bounce
+// costs the latency of that bounce's slowest ray.
+constexpr int kTailFrom = 5;
 
 __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want)
 {
@@ -495,6 +500,115 @@ static __device__ __noinline__ float env_connect(const WaveArgs& A, int b, uint6
 }
 
 // ------------------------------------------------------ camera shade ---
+// Where a camera vertex's connections to the light subpath go: the wavefront
+// queues each for k_shadow; the tail kernel tests it at once.
+struct QueueSink {
+    __device__ __forceinline__ void connect(const WaveArgs& A, int b, int k, V3 lpos, V3 pos, V3 lc)
+    {
+        const uint32_t sl = coalesced_append(&A.R.ctr[kCtrShadow + b]);
+        float4* q = A.R.sq + 3 * (size_t)sl;
+        q[0] = make_float4(lpos.x, lpos.y, lpos.z, __int_as_float(k));
+        q[1] = make_float4(pos.x, pos.y, pos.z, 0.0f);
+        q[2] = make_float4(lc.x, lc.y, lc.z, 0.0f);
+    }
+};
+
+// Camera vertex b of path k, reached by the ray (ra, rb) with hit h: the
+// escape term, the vertex's emission and connections, its throughput and the
+// next ray.  True when the path goes on (next ray: origin so, direction O,
+// tnear); er: the MIS estimator's environment ray (kMis).
+template <bool kMis, typename Sink>
+__device__ __forceinline__ bool camera_vertex(const WaveArgs& A, int b, int k, float4 ra, float4 rb, uint4 h, V3& so,
+                                              V3& O, float& tnear, EnvRay& er, Sink& sink)
+{
+    const DevScene& S = A.S;
+    bool push = false;
+    tnear = ra.w;
+    const V3 in = v3(rb.x, rb.y, rb.z);
+    const bool first = b == 1;  // throughput 1, radiance 0 (not stored yet)
+    const float4 tp4 = first ? make_float4(1.0f, 1.0f, 1.0f, 0.0f) : A.R.tp[k];
+    const V3 tp = v3(tp4.x, tp4.y, tp4.z);
+    if (h.x == kInvalid) {
+        // escape: background x throughput when cp_len <= maxPathLength (:251-258)
+        if (S.env.present && b <= A.max_len) {
+            V3 bg = env_radiance(S.env, in);
+            if (kMis && tp4.w > 0.0f) {  // the sampler's share (power heuristic) against env_connect
+                const float pe = env_pdf(S.env, in);
+                bg = bg * (tp4.w * tp4.w / (tp4.w * tp4.w + pe * pe));
+            }
+            float4 r = first ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : A.R.rad[k];
+            r.x += bg.x * tp.x;
+            r.y += bg.y * tp.y;
+            r.z += bg.z * tp.z;
+            A.R.rad[k] = r;
+        } else if (first) {
+            A.R.rad[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+    } else {
+        if (first) A.R.rad[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const PathCtx c = path_ctx(A, k);
+        const uint32_t pixel = c.pixel, sample = c.sample;
+        const DevMaterial& M = c.mats[__ldg(&S.insts[h.x].material)];
+        const Surf sp = surface_point(S, h.x, h.y, __uint_as_float(h.z), __uint_as_float(h.w), true, &M);
+        const PbrParams P = pbr_params(S, M, sp);
+        const Rng4 u = rng4(c.seed, pixel, sample, (uint32_t)b, kStreamCamera);
+        SampleInfo info;
+        info.kind = -1;
+        const V3 brdf = material_sample(S, M, P, sp, in, true, u, O, kMis ? &info : nullptr);
+        const float ct = fabsf(dot(O, sp.nrm));
+        const V3 tpn = v3(tp.x * brdf.x * ct, tp.y * brdf.y * ct, tp.z * brdf.z * ct);
+        float mis_pdf = 0.0f;  // density of O for the next escape's MIS weight (0: weight 1)
+        if (kMis && M.type == kMatPbr)
+            mis_pdf = env_connect(A, b, c.seed, pixel, sample, pbr_bsdf_in(M, P, sp, in), sp.pos, sp.nrm,
+                                  tp, O, info.kind, tnear, er);
+        if (M.type == kMatPbr && M.emissive_on) {  // Rad += outFactor x emission (:171-173)
+            const V3 e = pbr_emission(S, M, tex_hit(sp));
+            float4 r = A.R.rad[k];
+            r.x += tpn.x * e.x;
+            r.y += tpn.y * e.y;
+            r.z += tpn.z * e.z;
+            A.R.rad[k] = r;
+        }
+        if (S.num_lights > 0) {
+            const uint32_t meta = A.R.lmeta[k];
+            const int lp_len = (int)(meta >> 16);
+            const uint32_t li = meta & 0xFFFFu;
+            const V3 outV = -in;
+            for (int li_v = 0; li_v < lp_len && li_v + b <= A.max_len; ++li_v) {
+                const size_t slot = (size_t)li_v * A.wave_cap + k;
+                const float4 lp = A.R.lv_pos[slot];
+                const V3 lPos = v3(lp.x, lp.y, lp.z);
+                V3 lRad;
+                const V3 LC = normalize(sp.pos - lPos);
+                if (li_v == 0) {
+                    const float4 I = __ldg(S.light_int + li);
+                    const float4 L = __ldg(S.light_pos + li);
+                    const V3 dd = sp.pos - lPos;
+                    const float lsc = light_attenuation(A.atten_mode, A.min_dist, sqrtf(dot(dd, dd)), L.w);
+                    const float f = A.light_scale * lsc;
+                    lRad = v3(I.x * f, I.y * f, I.z * f);
+                } else {
+                    const float4 lr = A.R.lv_rad[slot];
+                    lRad = v3(lr.x, lr.y, lr.z);
+                }
+                const float c = fabsf(dot(LC, sp.nrm));
+                V3 lc = v3(lRad.x * c * tp.x, lRad.y * c * tp.y, lRad.z * c * tp.z);
+                if (intensity(lc) < A.cut) continue;
+                V3 f = material_eval(M, P, sp, LC, outV) * c;
+                lc = v3(f.x * tp.x * lRad.x, f.y * tp.y * lRad.y, f.z * tp.z * lRad.z);
+                if (intensity(lc) < A.cut) continue;
+                sink.connect(A, b, k, lPos, sp.pos, lc);
+            }
+        }
+        A.R.tp[k] = make_float4(tpn.x, tpn.y, tpn.z, mis_pdf);
+        if (b < A.cam_bounces && (tpn.x != 0.0f || tpn.y != 0.0f || tpn.z != 0.0f)) {
+            push = true;
+            so = shifted_origin(sp.pos, O, 1.0f);
+        }
+    }
+    return push;
+}
+
 // BDPTRenderer::computePath for the camera subpath (inv = true), vertex b, plus
 // the escape term and the connections of computePaths (:251-298) at vertex b.
 // kMis: the MIS estimator's environment connections (a separate instantiation,
@@ -520,95 +634,9 @@ __global__ void __launch_bounds__(kShadeThreads, kMis ? 3 : 4) k_camera_shade(Wa
         er.w = v3(0.0f, 0.0f, 1.0f);
         if (i < n) {
             const float4 ra = rq_in[2 * (size_t)i], rb = rq_in[2 * (size_t)i + 1];
-            const uint4 h = A.R.hits[i];
             k = __float_as_int(rb.w);
-            tnear = ra.w;
-            const V3 in = v3(rb.x, rb.y, rb.z);
-            const bool first = b == 1;  // throughput 1, radiance 0 (not stored yet)
-            const float4 tp4 = first ? make_float4(1.0f, 1.0f, 1.0f, 0.0f) : A.R.tp[k];
-            const V3 tp = v3(tp4.x, tp4.y, tp4.z);
-            if (h.x == kInvalid) {
-                // escape: background x throughput when cp_len <= maxPathLength (:251-258)
-                if (S.env.present && b <= A.max_len) {
-                    V3 bg = env_radiance(S.env, in);
-                    if (kMis && tp4.w > 0.0f) {  // the sampler's share (power heuristic) against env_connect
-                        const float pe = env_pdf(S.env, in);
-                        bg = bg * (tp4.w * tp4.w / (tp4.w * tp4.w + pe * pe));
-                    }
-                    float4 r = first ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : A.R.rad[k];
-                    r.x += bg.x * tp.x;
-                    r.y += bg.y * tp.y;
-                    r.z += bg.z * tp.z;
-                    A.R.rad[k] = r;
-                } else if (first) {
-                    A.R.rad[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                }
-            } else {
-                if (first) A.R.rad[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                const PathCtx c = path_ctx(A, k);
-                const uint32_t pixel = c.pixel, sample = c.sample;
-                const DevMaterial& M = c.mats[__ldg(&S.insts[h.x].material)];
-                const Surf sp = surface_point(S, h.x, h.y, __uint_as_float(h.z), __uint_as_float(h.w), true, &M);
-                const PbrParams P = pbr_params(S, M, sp);
-                const Rng4 u = rng4(c.seed, pixel, sample, (uint32_t)b, kStreamCamera);
-                SampleInfo info;
-                info.kind = -1;
-                const V3 brdf = material_sample(S, M, P, sp, in, true, u, O, kMis ? &info : nullptr);
-                const float ct = fabsf(dot(O, sp.nrm));
-                const V3 tpn = v3(tp.x * brdf.x * ct, tp.y * brdf.y * ct, tp.z * brdf.z * ct);
-                float mis_pdf = 0.0f;  // density of O for the next escape's MIS weight (0: weight 1)
-                if (kMis && M.type == kMatPbr)
-                    mis_pdf = env_connect(A, b, c.seed, pixel, sample, pbr_bsdf_in(M, P, sp, in), sp.pos, sp.nrm,
-                                          tp, O, info.kind, tnear, er);
-                if (M.type == kMatPbr && M.emissive_on) {  // Rad += outFactor x emission (:171-173)
-                    const V3 e = pbr_emission(S, M, tex_hit(sp));
-                    float4 r = A.R.rad[k];
-                    r.x += tpn.x * e.x;
-                    r.y += tpn.y * e.y;
-                    r.z += tpn.z * e.z;
-                    A.R.rad[k] = r;
-                }
-                if (S.num_lights > 0) {
-                    const uint32_t meta = A.R.lmeta[k];
-                    const int lp_len = (int)(meta >> 16);
-                    const uint32_t li = meta & 0xFFFFu;
-                    const V3 outV = -in;
-                    for (int li_v = 0; li_v < lp_len && li_v + b <= A.max_len; ++li_v) {
-                        const size_t slot = (size_t)li_v * A.wave_cap + k;
-                        const float4 lp = A.R.lv_pos[slot];
-                        const V3 lPos = v3(lp.x, lp.y, lp.z);
-                        V3 lRad;
-                        const V3 LC = normalize(sp.pos - lPos);
-                        if (li_v == 0) {
-                            const float4 I = __ldg(S.light_int + li);
-                            const float4 L = __ldg(S.light_pos + li);
-                            const V3 dd = sp.pos - lPos;
-                            const float lsc = light_attenuation(A.atten_mode, A.min_dist, sqrtf(dot(dd, dd)), L.w);
-                            const float f = A.light_scale * lsc;
-                            lRad = v3(I.x * f, I.y * f, I.z * f);
-                        } else {
-                            const float4 lr = A.R.lv_rad[slot];
-                            lRad = v3(lr.x, lr.y, lr.z);
-                        }
-                        const float c = fabsf(dot(LC, sp.nrm));
-                        V3 lc = v3(lRad.x * c * tp.x, lRad.y * c * tp.y, lRad.z * c * tp.z);
-                        if (intensity(lc) < A.cut) continue;
-                        V3 f = material_eval(M, P, sp, LC, outV) * c;
-                        lc = v3(f.x * tp.x * lRad.x, f.y * tp.y * lRad.y, f.z * tp.z * lRad.z);
-                        if (intensity(lc) < A.cut) continue;
-                        const uint32_t sl = coalesced_append(&A.R.ctr[kCtrShadow + b]);
-                        float4* q = A.R.sq + 3 * (size_t)sl;
-                        q[0] = make_float4(lPos.x, lPos.y, lPos.z, __int_as_float(k));
-                        q[1] = make_float4(sp.pos.x, sp.pos.y, sp.pos.z, 0.0f);
-                        q[2] = make_float4(lc.x, lc.y, lc.z, 0.0f);
-                    }
-                }
-                A.R.tp[k] = make_float4(tpn.x, tpn.y, tpn.z, mis_pdf);
-                if (b < A.cam_bounces && (tpn.x != 0.0f || tpn.y != 0.0f || tpn.z != 0.0f)) {
-                    push = true;
-                    so = shifted_origin(sp.pos, O, 1.0f);
-                }
-            }
+            QueueSink qs;
+            push = camera_vertex<kMis>(A, b, k, ra, rb, A.R.hits[i], so, O, tnear, er, qs);
         }
         const uint32_t slot = block_append_binned(&A.R.ctr[kCtrCam + b + 1], push, direction_bin(O), bins);
         if (push) {
@@ -628,15 +656,66 @@ __global__ void __launch_bounds__(kShadeThreads, kMis ? 3 : 4) k_camera_shade(Wa
 }
 
 // ------------------------------------------------------------ shadow ---
-// kEnv = false: BDPTRenderer::isConnected (BDPTRenderer.cpp:208-235) for the
-// vertex connections (records: end points A, B and the contribution); without
-// alpha-masked materials the closest-hit query stops at a hit well short of B,
-// which already decides "not connected".
-// kEnv = true: the MIS estimator's environment rays (records: shifted origin,
-// direction and tnear, contribution), which reach the environment when a
-// sampled ray in that direction would escape: no hit at all.  Without
-// alpha-masked materials that is an any-hit query; with them sceneIntersect's
-// closest hit and retries decide, as in k_extend (`masked` != 0).
+// BDPTRenderer::isConnected (BDPTRenderer.cpp:208-235): whether vertex A sees
+// vertex B.  Without alpha-masked materials the closest-hit query stops at a
+// hit well short of B, which already decides "not connected".
+template <bool kMasked>
+__device__ __forceinline__ bool is_connected(const DevScene& S, const uint32_t* items, V3 A, V3 B, TraceStack& st,
+                                             TraceCounters& tc, uint32_t root)
+{
+    bool connected = true;
+    V3 dir = B - A;
+    const float len = sqrtf(dot(dir, dir));
+    float maxsz = max_abs(A, 1.0f);
+    float safeD = 2.0f * kEpsAcc * kEps * maxsz;
+    if (!(len <= safeD)) {
+        dir = v3(dir.x / len, dir.y / len, dir.z / len);
+        float tnear = safeD;
+        const float tfar = len + (0.1f * len > safeD ? 0.1f * len : safeD);
+        const float sb = 10.0f * kEps * max_abs(B, 1.0f);
+        RayHit h;
+        bool hit;
+        if (kMasked) {
+            hit = scene_intersect(S, items, A, dir, tnear, tfar, h, st, tc, root);
+        } else {
+            // any hit this far short of B is farther than sb from it (the
+            // margin is ~800 ulps of the coordinates, far above the error of
+            // the hit's surface position), so it decides: not connected,
+            // whichever hit is the closest.  Hits near B get the exact test.
+            const float margin = 1.0e-4f * fmaxf(maxsz, max_abs(B, 1.0f)) + 2.0f * sb;
+            hit = trace_closest_or_below(S, items, A, dir, tnear, tfar, len - margin, h, st, tc, root);
+            if (hit && h.t < len - margin) {
+                hit = false;
+                connected = false;
+            }
+        }
+        if (hit) {
+            const Surf sp = surface_point(S, h.inst, h.prim, h.u, h.v, false);
+            const V3 dd = sp.pos - B;
+            const float sd = dot(dd, dd);
+            connected = sd <= sb * sb;
+        }
+    }
+    return connected;
+}
+
+// whether the environment ray (shifted origin so, direction w, the path's
+// tnear) escapes: no hit at all
+template <bool kMasked>
+__device__ __forceinline__ bool env_escapes(const DevScene& S, const uint32_t* items, V3 so, V3 w, float tnear,
+                                            TraceStack& st, TraceCounters& tc, uint32_t root)
+{
+    RayHit h;
+    return kMasked ? !scene_intersect(S, items, so, w, tnear, kFltMax, h, st, tc, root)
+                   : !trace_any(S, items, so, w, tnear, kFltMax, st, tc, root);
+}
+
+// kEnv = false: the vertex connections (records: end points A, B and the
+// contribution).  kEnv = true: the MIS estimator's environment rays (records:
+// shifted origin, direction and tnear, contribution), which reach the
+// environment when a sampled ray in that direction would escape: no hit at
+// all.  Without alpha-masked materials that is an any-hit query; with them
+// sceneIntersect's closest hit and retries decide, as in k_extend.
 template <bool kEnv, bool kMasked>
 __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevScene S, const uint32_t* items, const float4* sq,
                                                           const uint32_t* count, uint32_t* work, float4* rad,
@@ -662,46 +741,8 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevSc
         const V3 A = v3(q0.x, q0.y, q0.z), B = v3(q1.x, q1.y, q1.z);
         const int k = __float_as_int(q0.w);
         const uint32_t root = path_root(jobs, path_job, k);
-        bool connected = true;
-        if (kEnv) {
-            float tn = q1.w;
-            RayHit h;
-            connected = kMasked ? !scene_intersect(S, items, A, B, tn, kFltMax, h, st, tc, root)
-                                : !trace_any(S, items, A, B, tn, kFltMax, st, tc, root);
-        } else {
-            V3 dir = B - A;
-            const float len = sqrtf(dot(dir, dir));
-            float maxsz = max_abs(A, 1.0f);
-            float safeD = 2.0f * kEpsAcc * kEps * maxsz;
-            if (!(len <= safeD)) {
-                dir = v3(dir.x / len, dir.y / len, dir.z / len);
-                float tnear = safeD;
-                const float tfar = len + (0.1f * len > safeD ? 0.1f * len : safeD);
-                const float sb = 10.0f * kEps * max_abs(B, 1.0f);
-                RayHit h;
-                bool hit;
-                if (kMasked) {
-                    hit = scene_intersect(S, items, A, dir, tnear, tfar, h, st, tc, root);
-                } else {
-                    // any hit this far short of B is farther than sb from it (the
-                    // margin is ~800 ulps of the coordinates, far above the error of
-                    // the hit's surface position), so it decides: not connected,
-                    // whichever hit is the closest.  Hits near B get the exact test.
-                    const float margin = 1.0e-4f * fmaxf(maxsz, max_abs(B, 1.0f)) + 2.0f * sb;
-                    hit = trace_closest_or_below(S, items, A, dir, tnear, tfar, len - margin, h, st, tc, root);
-                    if (hit && h.t < len - margin) {
-                        hit = false;
-                        connected = false;
-                    }
-                }
-                if (hit) {
-                    const Surf sp = surface_point(S, h.inst, h.prim, h.u, h.v, false);
-                    const V3 dd = sp.pos - B;
-                    const float sd = dot(dd, dd);
-                    connected = sd <= sb * sb;
-                }
-            }
-        }
+        const bool connected = kEnv ? env_escapes<kMasked>(S, items, A, B, q1.w, st, tc, root)
+                                    : is_connected<kMasked>(S, items, A, B, st, tc, root);
         if (connected) {
             atomicAdd(&rad[k].x, q2.x);
             atomicAdd(&rad[k].y, q2.y);
@@ -720,6 +761,106 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevSc
         atomicAdd(&stats[kStatShadowNodes], (unsigned long long)nodes);
         atomicAdd(&stats[kStatShadowTris], (unsigned long long)tris);
         if (ov) atomicAdd(&stats[kStatOverflow], 1ull);
+    }
+}
+
+// ------------------------------------------------------- camera tail ---
+// A camera vertex's connections tested at once (the tail kernel's sink):
+// the path's radiance is this thread's alone while the tail runs.
+template <bool kMasked>
+struct TestSink {
+    const uint32_t* items;
+    TraceStack* st;
+    TraceCounters* tc;
+    uint32_t root;
+    uint32_t* tests;
+    __device__ __forceinline__ void connect(const WaveArgs& A, int b, int k, V3 lpos, V3 pos, V3 lc)
+    {
+        ++*tests;
+        if (is_connected<kMasked>(A.S, items, lpos, pos, *st, *tc, root)) {
+            float4 r = A.R.rad[k];
+            r.x += lc.x;
+            r.y += lc.y;
+            r.z += lc.z;
+            A.R.rad[k] = r;
+        }
+    }
+};
+
+// Camera bounces b0 .. camera bounces in one launch: each thread takes a path
+// alive at bounce b0 (queue rq_in) and runs it to its end: extension ray,
+// vertex (camera_vertex, as k_camera_shade), connections and MIS environment
+// ray tested at once, the next ray kept in registers.  The additions to the
+// path's radiance come in the wavefront's order (escape / emission, then
+// connections, then the environment ray, bounce by bounce).
+template <bool kMis, bool kMasked>
+__global__ void __launch_bounds__(kTraceThreads, 4) k_camera_tail(WaveArgs A, int b0, const float4* rq_in, uint32_t* work,
+                                                                  const DevJob* jobs)
+{
+    __shared__ uint2 sstack[kStackShared * kTraceThreads];
+    TraceStack st;
+    st.sh = sstack + threadIdx.x;
+    st.stride = kTraceThreads;
+    st.overflow = 0;
+    TraceCounters tc{0u, 0u};
+    uint32_t rays = 0, tests = 0;
+    const DevScene& S = A.S;
+    const uint32_t n = A.R.ctr[kCtrCam + b0];
+    const int lane = threadIdx.x & 31;
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(work, 32u);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= n) break;
+        const uint32_t i = base + lane;
+        if (i < n) {
+            float4 ra = rq_in[2 * (size_t)i], rb = rq_in[2 * (size_t)i + 1];
+            const int k = __float_as_int(rb.w);
+            const uint32_t root = path_root(jobs, A.path_job, k);
+            TestSink<kMasked> sink{A.items, &st, &tc, root, &tests};
+            for (int b = b0; b <= A.cam_bounces; ++b) {
+                float tn = ra.w;
+                RayHit hh;
+                ++rays;
+                uint4 h = make_uint4(kInvalid, kInvalid, 0u, 0u);
+                if (scene_intersect(S, A.items, v3(ra.x, ra.y, ra.z), v3(rb.x, rb.y, rb.z), tn, kFltMax, hh, st, tc, root))
+                    h = make_uint4(hh.inst, hh.prim, __float_as_uint(hh.u), __float_as_uint(hh.v));
+                ra.w = tn;
+                V3 so = v3(0.0f, 0.0f, 0.0f), O = v3(0.0f, 0.0f, 1.0f);
+                float tnear = 0.0f;
+                EnvRay er;
+                er.push = false;
+                const bool more = camera_vertex<kMis>(A, b, k, ra, rb, h, so, O, tnear, er, sink);
+                if (kMis && er.push) {
+                    ++tests;
+                    if (env_escapes<kMasked>(S, A.items, er.so, er.w, er.tnear, st, tc, root)) {
+                        float4 r = A.R.rad[k];
+                        r.x += er.c.x;
+                        r.y += er.c.y;
+                        r.z += er.c.z;
+                        A.R.rad[k] = r;
+                    }
+                }
+                if (!more) break;
+                ra = make_float4(so.x, so.y, so.z, tnear);
+                rb = make_float4(O.x, O.y, O.z, __int_as_float(k));
+            }
+        }
+    }
+    uint32_t nodes = tc.nodes, tris = tc.tris;
+    for (int o = 16; o; o >>= 1) {
+        nodes += __shfl_xor_sync(0xFFFFFFFFu, nodes, o);
+        tris += __shfl_xor_sync(0xFFFFFFFFu, tris, o);
+        rays += __shfl_xor_sync(0xFFFFFFFFu, rays, o);
+        tests += __shfl_xor_sync(0xFFFFFFFFu, tests, o);
+    }
+    const bool ov = __any_sync(0xFFFFFFFFu, st.overflow);
+    if (lane == 0) {
+        atomicAdd(&A.R.stats[kStatExt], (unsigned long long)rays);
+        atomicAdd(&A.R.stats[kStatShadow], (unsigned long long)tests);
+        atomicAdd(&A.R.stats[kStatTailNodes], (unsigned long long)nodes);
+        atomicAdd(&A.R.stats[kStatTailTris], (unsigned long long)tris);
+        if (ov) atomicAdd(&A.R.stats[kStatOverflow], 1ull);
     }
 }
 
@@ -1096,12 +1237,15 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
     OMV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, mis ? k_camera_shade<true> : k_camera_shade<false>,
                                                            sth, 0));
     const int trace_grid = std::max(1, occ_t) * s.num_sms;
+    int occ_tail = 0;
+    OMV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_tail, k_camera_tail<false, false>, kTraceThreads, 0));
+    const int tail_grid = std::max(1, occ_tail) * s.num_sms;
     // a batch over a group of scenes: every ray starts at its own scene's top-level tree
     const DevJob* gjobs = batch && s.parts.size() > 1 ? batch->d_jobs : nullptr;
     const int shade_grid = std::max(1, occ_s) * s.num_sms;
     int64_t launches = 0;
     // optional per-launch events around the closest-hit kernels
-    std::vector<cudaEvent_t> ext_ev, sh_ev;
+    std::vector<cudaEvent_t> ext_ev, sh_ev, tail_ev;
     const bool time_kernels = events && p.time_kernels;
     auto timed = [&](std::vector<cudaEvent_t>& pool) -> cudaEvent_t {
         cudaEvent_t e;
@@ -1161,6 +1305,18 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
                 const NvtxRange bounce_range(bounce_name(b));
                 float4* in = R.rq[(b + 1) % 2];
                 float4* out = R.rq[b % 2];
+                if (b >= kTailFrom) {  // the remaining bounces in one launch
+                    if (time_kernels) timed(tail_ev);
+                    if (mis)
+                        masked ? k_camera_tail<true, true><<<tail_grid, kTraceThreads, 0, st>>>(A, b, in, R.ctr + kCtrWork + work++, gjobs)
+                               : k_camera_tail<true, false><<<tail_grid, kTraceThreads, 0, st>>>(A, b, in, R.ctr + kCtrWork + work++, gjobs);
+                    else
+                        masked ? k_camera_tail<false, true><<<tail_grid, kTraceThreads, 0, st>>>(A, b, in, R.ctr + kCtrWork + work++, gjobs)
+                               : k_camera_tail<false, false><<<tail_grid, kTraceThreads, 0, st>>>(A, b, in, R.ctr + kCtrWork + work++, gjobs);
+                    if (time_kernels) timed(tail_ev);
+                    ++launches;
+                    break;
+                }
                 if (time_kernels) timed(ext_ev);
                 k_extend<<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, in, R.hits, R.ctr + kCtrCam + b,
                                                                R.ctr + kCtrWork + work++, R.stats, kStatExt, gjobs,
@@ -1231,6 +1387,9 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
         stats->stack_overflows = (int64_t)h[kStatOverflow];
         stats->shadow_nodes_visited = (int64_t)h[kStatShadowNodes];
         stats->shadow_triangles_tested = (int64_t)h[kStatShadowTris];
+        stats->tail_nodes_visited = (int64_t)h[kStatTailNodes];
+        stats->tail_triangles_tested = (int64_t)h[kStatTailTris];
+        stats->tail_bounce = p.camera_bounces >= kTailFrom ? kTailFrom : 0;
         auto sum_pairs = [](std::vector<cudaEvent_t>& ev) {
             double t = 0.0;
             for (size_t i = 0; i + 1 < ev.size(); i += 2) {
@@ -1244,11 +1403,13 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
         stats->extend_launches = (int64_t)ext_ev.size() / 2;
         stats->shadow_ms = sum_pairs(sh_ev);
         stats->shadow_launches = (int64_t)sh_ev.size() / 2;
-    } else if (!ext_ev.empty() || !sh_ev.empty()) {
+        stats->tail_ms = sum_pairs(tail_ev);
+    } else if (!ext_ev.empty() || !sh_ev.empty() || !tail_ev.empty()) {
         OMV_CUDA(cudaStreamSynchronize(st));
     }
     for (auto e : ext_ev) cudaEventDestroy(e);
     for (auto e : sh_ev) cudaEventDestroy(e);
+    for (auto e : tail_ev) cudaEventDestroy(e);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
 }
@@ -1543,6 +1704,8 @@ void load_wave_kernels()
     OMV_CUDA(cudaFuncGetAttributes(&a, k_camera_shade<false>));
     OMV_CUDA(cudaFuncGetAttributes(&a, k_shadow<false, false>));
     OMV_CUDA(cudaFuncGetAttributes(&a, k_shadow<false, true>));
+    OMV_CUDA(cudaFuncGetAttributes(&a, k_camera_tail<false, false>));
+    OMV_CUDA(cudaFuncGetAttributes(&a, k_camera_tail<false, true>));
     OMV_CUDA(cudaFuncGetAttributes(&a, k_film));
 }
 

@@ -96,3 +96,29 @@ def test_adjoint_rejects_textured_materials(gpu, textured):
     st = gpu.lib().omv_adjoint(rs.handle, C.byref(cam), C.byref(p), C.c_void_p(a.data_ptr()),
                                C.c_void_p(g.data_ptr()), None)
     assert st == 1 and b"untextured" in gpu.lib().omv_last_error()
+
+
+def test_textured_scene_deep_paths_statistically_match_oracle(gpu, oracle, scenes):
+    """Seven camera bounces on the alpha-masked, lit, textured scene: the last
+    bounces run in the tail kernel (one thread per path to its end, masked
+    hits retried, connections tested at once) and the image still matches
+    the oracle's."""
+    import dataclasses
+
+    sc = scenes.scene_textured(32, 32, 1)
+    sc = dataclasses.replace(sc, render=dataclasses.replace(sc.render, camera_bounces=7, light_bounces=6,
+                                                            max_path_length=9))
+    osc = oracle.OracleScene(sc)
+    n_cpu = 4096
+    film, sumsq, _ = osc.render(params=_params(oracle, sc, n_cpu), mode=1, threads=os.cpu_count() or 8, seed=6,
+                                variance=True)
+    ref = film[..., :3].astype(np.float64)
+    var_ref = np.maximum(sumsq / n_cpu - ref ** 2, 0.0)
+    n = 8192
+    _, s, q, cnt, st = _render(gpu, sc, n, seed=3)
+    assert st["tail_bounce"] > 0 and st["tail_nodes_visited"] > 0
+    mean = s / n
+    var = np.maximum(q / n - mean ** 2, 0.0)
+    frac3, glob = _zstats(mean, n, var, ref, n_cpu, var_ref)
+    assert frac3 < 0.01, frac3
+    assert abs(glob) < 4, glob
