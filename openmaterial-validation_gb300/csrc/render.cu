@@ -60,7 +60,10 @@ enum {
 // The camera bounces from this one on run in one launch, each thread taking a
 // path to its end (k_camera_tail): on the 1920x1080x64 benchmark frame about
 // 0.2% of the paths are alive at bounce 5, and one launch pair per bounce
-// costs the latency of that bounce's slowest ray.
+// costs the latency of that bounce's slowest ray.  Measured per frame: 38.54
+// ms from bounce 5, 38.97 without the tail kernel, 38.67 from bounce 6, 39.13
+// from bounce 4 and 43.4 from bounce 3 (one path per thread is slower than
+// the wavefront while many paths are alive).
 constexpr int kTailFrom = 5;
 
 __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want)
