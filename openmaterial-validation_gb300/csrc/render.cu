@@ -392,12 +392,56 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_extend(DevSc
 }
 
 // ------------------------------------------------------- light shade ---
-// BDPTRenderer::computePath for the light subpath (inv = false), vertex b
+// BDPTRenderer::computePath for the light subpath (inv = false), vertex b of
+// path k reached by the ray (ra, rb) with hit h: the vertex's position and
+// radiance for the connections, its throughput and the next ray.  True when
+// the path goes on (next ray: origin so, direction O, tnear).
+__device__ __forceinline__ bool light_vertex(const WaveArgs& A, int b, int k, float4 ra, float4 rb, uint4 h, V3& so,
+                                             V3& O, float& tnear)
+{
+    const DevScene& S = A.S;
+    bool push = false;
+    tnear = ra.w;
+    if (h.x == kInvalid) return false;
+    const PathCtx c = path_ctx(A, k);
+    const uint32_t pixel = c.pixel, sample = c.sample;
+    const DevMaterial& M = c.mats[__ldg(&S.insts[h.x].material)];
+    const Surf sp = surface_point(S, h.x, h.y, __uint_as_float(h.z), __uint_as_float(h.w), true, &M);
+    const V3 in = v3(rb.x, rb.y, rb.z);
+    const Rng4 u = rng4(c.seed, pixel, sample, kDimLightBounce + (uint32_t)b, kStreamLight);
+    const V3 brdf = material_sample(S, M, pbr_params(S, M, sp), sp, in, false, u, O);
+    const float ct = fabsf(dot(in, sp.nrm));
+    const float4 tp0 = A.R.ltp[k];
+    float4 lr = A.R.lrad[k];
+    const V3 tp = v3(tp0.x * brdf.x * ct, tp0.y * brdf.y * ct, tp0.z * brdf.z * ct);
+    const uint32_t meta = A.R.lmeta[k];
+    const uint32_t li = meta & 0xFFFFu;
+    if (b == 1) {
+        const float4 lp = __ldg(S.light_pos + li);
+        const V3 d = sp.pos - v3(lp.x, lp.y, lp.z);
+        lr.w = light_attenuation(A.atten_mode, A.min_dist, sqrtf(dot(d, d)), lp.w);
+        A.R.lrad[k] = lr;
+    }
+    const V3 orad = v3(tp.x * lr.x * lr.w, tp.y * lr.y * lr.w, tp.z * lr.z * lr.w);
+    if (!(intensity(orad) < A.cut)) {
+        const size_t slot = (size_t)b * A.wave_cap + k;
+        A.R.lv_pos[slot] = make_float4(sp.pos.x, sp.pos.y, sp.pos.z, 0.0f);
+        A.R.lv_rad[slot] = make_float4(orad.x, orad.y, orad.z, 0.0f);
+        A.R.lmeta[k] = li | ((uint32_t)(b + 1) << 16);
+        A.R.ltp[k] = make_float4(tp.x, tp.y, tp.z, 0.0f);
+        if (b < A.light_bounces && (tp.x != 0.0f || tp.y != 0.0f || tp.z != 0.0f)) {
+            push = true;
+            so = shifted_origin(sp.pos, O, 1.0f);
+        }
+    }
+    return push;
+}
+
+// k_light_shade: light_vertex for every ray of the bounce-b queue
 __global__ void __launch_bounds__(kShadeThreads, 4) k_light_shade(WaveArgs A, int b, const float4* rq_in,
                                                                 float4* rq_out)
 {
     const uint32_t n = A.R.ctr[kCtrLight + b];
-    const DevScene& S = A.S;
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
         const uint32_t i = i0 + threadIdx.x;
         bool push = false;
@@ -406,42 +450,8 @@ __global__ void __launch_bounds__(kShadeThreads, 4) k_light_shade(WaveArgs A, in
         int k = 0;
         if (i < n) {
             const float4 ra = rq_in[2 * (size_t)i], rb = rq_in[2 * (size_t)i + 1];
-            const uint4 h = A.R.hits[i];
             k = __float_as_int(rb.w);
-            tnear = ra.w;
-            if (h.x != kInvalid) {
-                const PathCtx c = path_ctx(A, k);
-                const uint32_t pixel = c.pixel, sample = c.sample;
-                const DevMaterial& M = c.mats[__ldg(&S.insts[h.x].material)];
-                const Surf sp = surface_point(S, h.x, h.y, __uint_as_float(h.z), __uint_as_float(h.w), true, &M);
-                const V3 in = v3(rb.x, rb.y, rb.z);
-                const Rng4 u = rng4(c.seed, pixel, sample, kDimLightBounce + (uint32_t)b, kStreamLight);
-                const V3 brdf = material_sample(S, M, pbr_params(S, M, sp), sp, in, false, u, O);
-                const float ct = fabsf(dot(in, sp.nrm));
-                const float4 tp0 = A.R.ltp[k];
-                float4 lr = A.R.lrad[k];
-                const V3 tp = v3(tp0.x * brdf.x * ct, tp0.y * brdf.y * ct, tp0.z * brdf.z * ct);
-                const uint32_t meta = A.R.lmeta[k];
-                const uint32_t li = meta & 0xFFFFu;
-                if (b == 1) {
-                    const float4 lp = __ldg(S.light_pos + li);
-                    const V3 d = sp.pos - v3(lp.x, lp.y, lp.z);
-                    lr.w = light_attenuation(A.atten_mode, A.min_dist, sqrtf(dot(d, d)), lp.w);
-                    A.R.lrad[k] = lr;
-                }
-                const V3 orad = v3(tp.x * lr.x * lr.w, tp.y * lr.y * lr.w, tp.z * lr.z * lr.w);
-                if (!(intensity(orad) < A.cut)) {
-                    const size_t slot = (size_t)b * A.wave_cap + k;
-                    A.R.lv_pos[slot] = make_float4(sp.pos.x, sp.pos.y, sp.pos.z, 0.0f);
-                    A.R.lv_rad[slot] = make_float4(orad.x, orad.y, orad.z, 0.0f);
-                    A.R.lmeta[k] = li | ((uint32_t)(b + 1) << 16);
-                    A.R.ltp[k] = make_float4(tp.x, tp.y, tp.z, 0.0f);
-                    if (b < A.light_bounces && (tp.x != 0.0f || tp.y != 0.0f || tp.z != 0.0f)) {
-                        push = true;
-                        so = shifted_origin(sp.pos, O, 1.0f);
-                    }
-                }
-            }
+            push = light_vertex(A, b, k, ra, rb, A.R.hits[i], so, O, tnear);
         }
         const uint32_t slot = warp_append(&A.R.ctr[kCtrLight + b + 1], push);
         if (push) {
@@ -861,6 +871,62 @@ __global__ void __launch_bounds__(kTraceThreads, 4) k_camera_tail(WaveArgs A, in
     if (lane == 0) {
         atomicAdd(&A.R.stats[kStatExt], (unsigned long long)rays);
         atomicAdd(&A.R.stats[kStatShadow], (unsigned long long)tests);
+        atomicAdd(&A.R.stats[kStatTailNodes], (unsigned long long)nodes);
+        atomicAdd(&A.R.stats[kStatTailTris], (unsigned long long)tris);
+        if (ov) atomicAdd(&A.R.stats[kStatOverflow], 1ull);
+    }
+}
+
+// Light bounces b0 .. light bounces in one launch, like k_camera_tail: each
+// thread takes a light path alive at bounce b0 to its end.
+__global__ void __launch_bounds__(kTraceThreads, 4) k_light_tail(WaveArgs A, int b0, const float4* rq_in, uint32_t* work,
+                                                                 const DevJob* jobs)
+{
+    __shared__ uint2 sstack[kStackShared * kTraceThreads];
+    TraceStack st;
+    st.sh = sstack + threadIdx.x;
+    st.stride = kTraceThreads;
+    st.overflow = 0;
+    TraceCounters tc{0u, 0u};
+    uint32_t rays = 0;
+    const DevScene& S = A.S;
+    const uint32_t n = A.R.ctr[kCtrLight + b0];
+    const int lane = threadIdx.x & 31;
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(work, 32u);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= n) break;
+        const uint32_t i = base + lane;
+        if (i < n) {
+            float4 ra = rq_in[2 * (size_t)i], rb = rq_in[2 * (size_t)i + 1];
+            const int k = __float_as_int(rb.w);
+            const uint32_t root = path_root(jobs, A.path_job, k);
+            for (int b = b0; b <= A.light_bounces; ++b) {
+                float tn = ra.w;
+                RayHit hh;
+                ++rays;
+                uint4 h = make_uint4(kInvalid, kInvalid, 0u, 0u);
+                if (scene_intersect(S, A.items, v3(ra.x, ra.y, ra.z), v3(rb.x, rb.y, rb.z), tn, kFltMax, hh, st, tc, root))
+                    h = make_uint4(hh.inst, hh.prim, __float_as_uint(hh.u), __float_as_uint(hh.v));
+                ra.w = tn;
+                V3 so = v3(0.0f, 0.0f, 0.0f), O = v3(0.0f, 0.0f, 1.0f);
+                float tnear = 0.0f;
+                if (!light_vertex(A, b, k, ra, rb, h, so, O, tnear)) break;
+                ra = make_float4(so.x, so.y, so.z, tnear);
+                rb = make_float4(O.x, O.y, O.z, __int_as_float(k));
+            }
+        }
+    }
+    uint32_t nodes = tc.nodes, tris = tc.tris;
+    for (int o = 16; o; o >>= 1) {
+        nodes += __shfl_xor_sync(0xFFFFFFFFu, nodes, o);
+        tris += __shfl_xor_sync(0xFFFFFFFFu, tris, o);
+        rays += __shfl_xor_sync(0xFFFFFFFFu, rays, o);
+    }
+    const bool ov = __any_sync(0xFFFFFFFFu, st.overflow);
+    if (lane == 0) {
+        atomicAdd(&A.R.stats[kStatLight], (unsigned long long)rays);
         atomicAdd(&A.R.stats[kStatTailNodes], (unsigned long long)nodes);
         atomicAdd(&A.R.stats[kStatTailTris], (unsigned long long)tris);
         if (ov) atomicAdd(&A.R.stats[kStatOverflow], 1ull);
@@ -1291,6 +1357,13 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
                 float4* in = R.rq[1];
                 float4* out = R.rq[0];
                 if (b % 2 == 0) std::swap(in, out);
+                if (b >= kTailFrom) {  // the remaining bounces in one launch
+                    if (time_kernels) timed(tail_ev);
+                    k_light_tail<<<tail_grid, kTraceThreads, 0, st>>>(A, b, in, R.ctr + kCtrWork + work++, gjobs);
+                    if (time_kernels) timed(tail_ev);
+                    ++launches;
+                    break;
+                }
                 if (time_kernels) timed(ext_ev);
                 k_extend<<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, in, R.hits,
                                                                R.ctr + kCtrLight + b, R.ctr + kCtrWork + work++,
@@ -1392,7 +1465,7 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
         stats->shadow_triangles_tested = (int64_t)h[kStatShadowTris];
         stats->tail_nodes_visited = (int64_t)h[kStatTailNodes];
         stats->tail_triangles_tested = (int64_t)h[kStatTailTris];
-        stats->tail_bounce = p.camera_bounces >= kTailFrom ? kTailFrom : 0;
+        stats->tail_bounce = std::max(p.camera_bounces, lights ? p.light_bounces : 0) >= kTailFrom ? kTailFrom : 0;
         auto sum_pairs = [](std::vector<cudaEvent_t>& ev) {
             double t = 0.0;
             for (size_t i = 0; i + 1 < ev.size(); i += 2) {
@@ -1709,6 +1782,7 @@ void load_wave_kernels()
     OMV_CUDA(cudaFuncGetAttributes(&a, k_shadow<false, true>));
     OMV_CUDA(cudaFuncGetAttributes(&a, k_camera_tail<false, false>));
     OMV_CUDA(cudaFuncGetAttributes(&a, k_camera_tail<false, true>));
+    OMV_CUDA(cudaFuncGetAttributes(&a, k_light_tail));
     OMV_CUDA(cudaFuncGetAttributes(&a, k_film));
 }
 

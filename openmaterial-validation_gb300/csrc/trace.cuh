@@ -137,9 +137,22 @@ __device__ __forceinline__ bool tri_hit(const Shear& w, V3 o, float4 p0, float4 
     return true;
 }
 
-// reciprocal for box tests only: zero components become +-1e-20 so that no
-// 0 * inf NaN can appear (the triangle test uses the true direction)
-__device__ __forceinline__ float box_rcp(float d) { return 1.0f / (fabsf(d) < 1e-20f ? copysignf(1e-20f, d) : d); }
+// Reciprocal for box tests only (the triangle test uses the true direction):
+// zero components become +-1e-20 so that no 0 * inf NaN can appear.  The fast
+// reciprocal (__fdividef: within 2 ulp for divisors up to 2^126, so the
+// component is quartered first and the result quartered after, exactly while
+// the result is a normal float) scales the slab distances of its axis by at
+// most 1 +- 2^-22; with the roundings of the distance itself (about 2^-22
+// more) that stays inside the box test's relative margins (1 -+ 2^-21), so
+// the test remains conservative for direction components up to 2^126 in
+// magnitude (beyond, the subnormal result adds up to 2^-22 more).  38.17
+// instead of 38.55 ms per benchmark frame against the correctly rounded
+// division (PTX rcp.approx.f32, subnormal results included: 38.40).
+__device__ __forceinline__ float box_rcp(float d)
+{
+    const float x = fabsf(d) < 1e-20f ? copysignf(1e-20f, d) : d;
+    return __fdividef(1.0f, 0.25f * x) * 0.25f;
+}
 
 // world -> object space, 3x4 row-major inverse, fixed order
 __device__ __forceinline__ void to_object(const float* m, V3 o, V3 d, V3& ro, V3& rd)
