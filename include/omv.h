@@ -278,8 +278,9 @@ typedef struct omv_stats {
                                   entries; 0 unless a tree is degenerate */
     int64_t shadow_nodes_visited;     /* nodes fetched by the shadow-ray kernel */
     int64_t shadow_triangles_tested;  /* triangle records fetched by the shadow-ray kernel */
-    int64_t tail_bounce;              /* first camera bounce run by the tail kernel, which takes
-                                         each path still alive there to its end (0: none) */
+    int64_t tail_bounce;              /* the camera bounce from which the tail kernel took each
+                                         path still alive to its end, once few enough were left
+                                         (the latest over the frame's waves; 0: none) */
     int64_t tail_nodes_visited;       /* nodes fetched by the tail kernel (its extension,
                                          connection and environment rays) */
     int64_t tail_triangles_tested;    /* triangle records fetched by the tail kernel */

@@ -55,16 +55,28 @@ constexpr int kCtrWork = 192;    // + launch index
 constexpr int kCtrEnv = 448;     // + bounce: MIS environment rays
 enum {
     kStatExt = 0, kStatShadow = 1, kStatLight = 2, kStatNodes = 3, kStatTris = 4, kStatOverflow = 5,
-    kStatShadowNodes = 6, kStatShadowTris = 7, kStatTailNodes = 8, kStatTailTris = 9
+    kStatShadowNodes = 6, kStatShadowTris = 7, kStatTailNodes = 8, kStatTailTris = 9, kStatTailCam = 10
 };
-// The camera bounces from this one on run in one launch, each thread taking a
-// path to its end (k_camera_tail): on the 1920x1080x64 benchmark frame about
-// 0.2% of the paths are alive at bounce 5, and one launch pair per bounce
-// costs the latency of that bounce's slowest ray.  Measured per frame: 38.54
-// ms from bounce 5, 38.97 without the tail kernel, 38.67 from bounce 6, 39.13
-// from bounce 4 and 43.4 from bounce 3 (one path per thread is slower than
-// the wavefront while many paths are alive).
-constexpr int kTailFrom = 5;
+// Tail kernel (k_camera_tail): once at most kTailPaths camera paths
+// are alive at a bounce (from bounce kTailMin on), one launch takes each of
+// them to its end, one thread per path, instead of a launch pair (or three)
+// per remaining bounce, each of which costs the latency of its slowest ray.
+// The decision is made on the device from the bounce's queue count, so the
+// host launches the tail kernel before every bounce from kTailMin on; it returns
+// at once while more paths are alive, and after it has run, the queue count
+// it leaves at zero makes the bounce's wavefront kernels return at once.
+// Only for scenes without point lights: with vertex connections, one thread
+// testing a path's connections one after another loses to the wavefront's
+// shadow-ray kernel (measured: the 256x256x16 C1 frame 1.72 instead of 1.30
+// ms, the 1920x1080x64 one 48.4 instead of 47.1, the 256-job sweep one job
+// per call 94.5 instead of 103.1 jobs/s), and so did the light subpaths'
+// analogue.  On the benchmark frame: 38.40 instead of 38.67 ms (at most 2^17
+// paths: the same; 2^19 or 2^20, which start the tail at bounce 4: 39.0).
+constexpr int kTailMin = 3;
+constexpr uint32_t kTailPaths = 1u << 18;
+// counter slots of the tail kernel (beyond the per-bounce ranges)
+constexpr int kCtrTailWorkCam = 510;
+constexpr int kCtrTailDone = 511;
 
 __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want)
 {
@@ -635,7 +647,6 @@ __global__ void __launch_bounds__(kShadeThreads, kMis ? 3 : 4) k_camera_shade(Wa
 {
     __shared__ BinScratch bins;
     const uint32_t n = A.R.ctr[kCtrCam + b];
-    const DevScene& S = A.S;
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
         const uint32_t i = i0 + threadIdx.x;
         bool push = false;
@@ -778,6 +789,22 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevSc
 }
 
 // ------------------------------------------------------- camera tail ---
+// End of a tail kernel that ran: the last block to finish (every block has
+// read the queue count by then) sets the count to zero, so that the bounce's
+// wavefront kernels find nothing to do, and records the bounce.
+__device__ __forceinline__ void tail_finish(const WaveArgs& A, uint32_t* count, int stat, int b0)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&A.R.ctr[kCtrTailDone], 1u) == gridDim.x - 1u) {
+            *count = 0u;
+            A.R.ctr[kCtrTailDone] = 0u;
+            atomicMax(&A.R.stats[stat], (unsigned long long)b0);
+        }
+    }
+}
+
 // A camera vertex's connections tested at once (the tail kernel's sink):
 // the path's radiance is this thread's alone while the tail runs.
 template <bool kMasked>
@@ -819,6 +846,7 @@ __global__ void __launch_bounds__(kTraceThreads, 4) k_camera_tail(WaveArgs A, in
     uint32_t rays = 0, tests = 0;
     const DevScene& S = A.S;
     const uint32_t n = A.R.ctr[kCtrCam + b0];
+    if (n == 0u || n > kTailPaths) return;  // the same decision in every block
     const int lane = threadIdx.x & 31;
     while (true) {
         uint32_t base = 0;
@@ -875,62 +903,7 @@ __global__ void __launch_bounds__(kTraceThreads, 4) k_camera_tail(WaveArgs A, in
         atomicAdd(&A.R.stats[kStatTailTris], (unsigned long long)tris);
         if (ov) atomicAdd(&A.R.stats[kStatOverflow], 1ull);
     }
-}
-
-// Light bounces b0 .. light bounces in one launch, like k_camera_tail: each
-// thread takes a light path alive at bounce b0 to its end.
-__global__ void __launch_bounds__(kTraceThreads, 4) k_light_tail(WaveArgs A, int b0, const float4* rq_in, uint32_t* work,
-                                                                 const DevJob* jobs)
-{
-    __shared__ uint2 sstack[kStackShared * kTraceThreads];
-    TraceStack st;
-    st.sh = sstack + threadIdx.x;
-    st.stride = kTraceThreads;
-    st.overflow = 0;
-    TraceCounters tc{0u, 0u};
-    uint32_t rays = 0;
-    const DevScene& S = A.S;
-    const uint32_t n = A.R.ctr[kCtrLight + b0];
-    const int lane = threadIdx.x & 31;
-    while (true) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(work, 32u);
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if (base >= n) break;
-        const uint32_t i = base + lane;
-        if (i < n) {
-            float4 ra = rq_in[2 * (size_t)i], rb = rq_in[2 * (size_t)i + 1];
-            const int k = __float_as_int(rb.w);
-            const uint32_t root = path_root(jobs, A.path_job, k);
-            for (int b = b0; b <= A.light_bounces; ++b) {
-                float tn = ra.w;
-                RayHit hh;
-                ++rays;
-                uint4 h = make_uint4(kInvalid, kInvalid, 0u, 0u);
-                if (scene_intersect(S, A.items, v3(ra.x, ra.y, ra.z), v3(rb.x, rb.y, rb.z), tn, kFltMax, hh, st, tc, root))
-                    h = make_uint4(hh.inst, hh.prim, __float_as_uint(hh.u), __float_as_uint(hh.v));
-                ra.w = tn;
-                V3 so = v3(0.0f, 0.0f, 0.0f), O = v3(0.0f, 0.0f, 1.0f);
-                float tnear = 0.0f;
-                if (!light_vertex(A, b, k, ra, rb, h, so, O, tnear)) break;
-                ra = make_float4(so.x, so.y, so.z, tnear);
-                rb = make_float4(O.x, O.y, O.z, __int_as_float(k));
-            }
-        }
-    }
-    uint32_t nodes = tc.nodes, tris = tc.tris;
-    for (int o = 16; o; o >>= 1) {
-        nodes += __shfl_xor_sync(0xFFFFFFFFu, nodes, o);
-        tris += __shfl_xor_sync(0xFFFFFFFFu, tris, o);
-        rays += __shfl_xor_sync(0xFFFFFFFFu, rays, o);
-    }
-    const bool ov = __any_sync(0xFFFFFFFFu, st.overflow);
-    if (lane == 0) {
-        atomicAdd(&A.R.stats[kStatLight], (unsigned long long)rays);
-        atomicAdd(&A.R.stats[kStatTailNodes], (unsigned long long)nodes);
-        atomicAdd(&A.R.stats[kStatTailTris], (unsigned long long)tris);
-        if (ov) atomicAdd(&A.R.stats[kStatOverflow], 1ull);
-    }
+    tail_finish(A, &A.R.ctr[kCtrCam + b0], kStatTailCam, b0);
 }
 
 // -------------------------------------------------------------- film ---
@@ -1357,13 +1330,6 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
                 float4* in = R.rq[1];
                 float4* out = R.rq[0];
                 if (b % 2 == 0) std::swap(in, out);
-                if (b >= kTailFrom) {  // the remaining bounces in one launch
-                    if (time_kernels) timed(tail_ev);
-                    k_light_tail<<<tail_grid, kTraceThreads, 0, st>>>(A, b, in, R.ctr + kCtrWork + work++, gjobs);
-                    if (time_kernels) timed(tail_ev);
-                    ++launches;
-                    break;
-                }
                 if (time_kernels) timed(ext_ev);
                 k_extend<<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, in, R.hits,
                                                                R.ctr + kCtrLight + b, R.ctr + kCtrWork + work++,
@@ -1381,17 +1347,17 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
                 const NvtxRange bounce_range(bounce_name(b));
                 float4* in = R.rq[(b + 1) % 2];
                 float4* out = R.rq[b % 2];
-                if (b >= kTailFrom) {  // the remaining bounces in one launch
+                if (!lights && b >= kTailMin) {  // the remaining bounces in one launch, once few paths are alive
+                    uint32_t* tw = R.ctr + kCtrTailWorkCam;
                     if (time_kernels) timed(tail_ev);
                     if (mis)
-                        masked ? k_camera_tail<true, true><<<tail_grid, kTraceThreads, 0, st>>>(A, b, in, R.ctr + kCtrWork + work++, gjobs)
-                               : k_camera_tail<true, false><<<tail_grid, kTraceThreads, 0, st>>>(A, b, in, R.ctr + kCtrWork + work++, gjobs);
+                        masked ? k_camera_tail<true, true><<<tail_grid, kTraceThreads, 0, st>>>(A, b, in, tw, gjobs)
+                               : k_camera_tail<true, false><<<tail_grid, kTraceThreads, 0, st>>>(A, b, in, tw, gjobs);
                     else
-                        masked ? k_camera_tail<false, true><<<tail_grid, kTraceThreads, 0, st>>>(A, b, in, R.ctr + kCtrWork + work++, gjobs)
-                               : k_camera_tail<false, false><<<tail_grid, kTraceThreads, 0, st>>>(A, b, in, R.ctr + kCtrWork + work++, gjobs);
+                        masked ? k_camera_tail<false, true><<<tail_grid, kTraceThreads, 0, st>>>(A, b, in, tw, gjobs)
+                               : k_camera_tail<false, false><<<tail_grid, kTraceThreads, 0, st>>>(A, b, in, tw, gjobs);
                     if (time_kernels) timed(tail_ev);
                     ++launches;
-                    break;
                 }
                 if (time_kernels) timed(ext_ev);
                 k_extend<<<trace_grid, kTraceThreads, 0, st>>>(s.dev, s.tlas_items, in, R.hits, R.ctr + kCtrCam + b,
@@ -1465,7 +1431,7 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
         stats->shadow_triangles_tested = (int64_t)h[kStatShadowTris];
         stats->tail_nodes_visited = (int64_t)h[kStatTailNodes];
         stats->tail_triangles_tested = (int64_t)h[kStatTailTris];
-        stats->tail_bounce = std::max(p.camera_bounces, lights ? p.light_bounces : 0) >= kTailFrom ? kTailFrom : 0;
+        stats->tail_bounce = (int64_t)h[kStatTailCam];
         auto sum_pairs = [](std::vector<cudaEvent_t>& ev) {
             double t = 0.0;
             for (size_t i = 0; i + 1 < ev.size(); i += 2) {
@@ -1782,7 +1748,6 @@ void load_wave_kernels()
     OMV_CUDA(cudaFuncGetAttributes(&a, k_shadow<false, true>));
     OMV_CUDA(cudaFuncGetAttributes(&a, k_camera_tail<false, false>));
     OMV_CUDA(cudaFuncGetAttributes(&a, k_camera_tail<false, true>));
-    OMV_CUDA(cudaFuncGetAttributes(&a, k_light_tail));
     OMV_CUDA(cudaFuncGetAttributes(&a, k_film));
 }
 
