@@ -56,6 +56,7 @@ struct alignas(16) DevInstance {
     uint32_t vert_base;
     uint32_t valid;
     uint32_t uv_mask;  // the mesh's coordinate sets: bit 0 TEXCOORD_0, bit 1 TEXCOORD_1
+    float4 olo, ohi;   // object-space bounds of the mesh's vertices (w unused)
 };
 
 enum : int32_t { kMatPbr = 0, kMatOm = 1, kMatMissing = 2 };

@@ -576,6 +576,14 @@ SceneHost* scene_create(const omv_scene_desc& d, int device, const std::vector<i
         I.face_base = valid ? face_base[id.mesh] : 0u;
         I.vert_base = valid ? vert_base[id.mesh] : 0u;
         I.uv_mask = valid ? mesh_uv_mask[id.mesh] : 0u;
+        if (valid) {
+            const MeshGeom& g = geo[id.mesh];
+            I.olo = make_float4(g.lo[0], g.lo[1], g.lo[2], 0.0f);
+            I.ohi = make_float4(g.hi[0], g.hi[1], g.hi[2], 0.0f);
+        } else {  // never entered: invalid instances are not in the top-level tree
+            I.olo = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            I.ohi = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
         igeo[i].valid = valid;
         igeo[i].mesh = valid ? id.mesh : -1;
         igeo[i].part = inst_part ? (*inst_part)[i] : 0;

@@ -154,6 +154,19 @@ __device__ __forceinline__ float box_rcp(float d)
     return __fdividef(1.0f, 0.25f * x) * 0.25f;
 }
 
+// Whether the ray (origin o, box reciprocal rid) meets the box [lo, hi] within
+// [tnear, tfar]: slab distances with the node test's relative margins, so
+// conservative in the same way.
+__device__ __forceinline__ bool object_box_hit(float4 lo, float4 hi, V3 o, V3 rid, float tnear, float tfar)
+{
+    const float ax = (lo.x - o.x) * rid.x, bx = (hi.x - o.x) * rid.x;
+    const float ay = (lo.y - o.y) * rid.y, by = (hi.y - o.y) * rid.y;
+    const float az = (lo.z - o.z) * rid.z, bz = (hi.z - o.z) * rid.z;
+    const float tin = fmaxf(fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fminf(az, bz)) * 0.99999952f, tnear);
+    const float tout = fminf(fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fmaxf(az, bz)) * 1.00000048f, tfar);
+    return tin <= tout;
+}
+
 // world -> object space, 3x4 row-major inverse, fixed order
 __device__ __forceinline__ void to_object(const float* m, V3 o, V3 d, V3& ro, V3& rd)
 {
@@ -267,11 +280,14 @@ __device__ __forceinline__ bool trace_step(const DevScene& S, const uint32_t* __
         for (int k = 0; k < 12; ++k) m[k] = __ldg(&I->inv[k]);
         V3 rd;
         to_object(m, T.o, T.d, T.ro, rd);
-        if (!shear_setup(rd, T.rs)) {
+        const V3 rid = v3(box_rcp(rd.x), box_rcp(rd.y), box_rcp(rd.z));
+        // the object's own bounds first: most rays that cross an instance's
+        // world box (the box of a rotated object) miss the object's box
+        if (!object_box_hit(__ldg(&I->olo), __ldg(&I->ohi), T.ro, rid, T.tnear, T.best_t) || !shear_setup(rd, T.rs)) {
             T.ro = T.o;
             return true;
         }
-        T.rid = v3(box_rcp(rd.x), box_rcp(rd.y), box_rcp(rd.z));
+        T.rid = rid;
         T.in_blas = true;
         T.blas_base = st.sp;
         T.cur_inst = ii;
