@@ -113,16 +113,6 @@ __device__ __forceinline__ uint32_t coalesced_append(uint32_t* counter)
     return g.shfl(base, 0) + (uint32_t)g.thread_rank();
 }
 
-// The next 32 rays of a persistent trace kernel's queue (n rays): the
-// counter is read before it is incremented, so that once the queue is drained
-// the warps leave without one more atomic each on the same word (thousands of
-// them would queue behind one another at the end of every launch).
-__device__ __forceinline__ uint32_t take_rays(uint32_t* work, uint32_t n)
-{
-    if (__ldcg(work) >= n) return n;
-    return atomicAdd(work, 32u);
-}
-
 // Direction bin of a ray: the cube face its direction points to (dominant
 // axis and sign) and the quadrant on that face, 24 bins.
 constexpr int kDirBins = 24;
@@ -380,7 +370,7 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_extend(DevSc
     const int lane = threadIdx.x & 31;
     while (true) {
         uint32_t base = 0;
-        if (lane == 0) base = take_rays(work, n);
+        if (lane == 0) base = atomicAdd(work, 32u);
         base = __shfl_sync(0xFFFFFFFFu, base, 0);
         if (base >= n) break;
         const uint32_t i = base + lane;
@@ -766,7 +756,7 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevSc
     const int lane = threadIdx.x & 31;
     while (true) {
         uint32_t base = 0;
-        if (lane == 0) base = take_rays(work, n);
+        if (lane == 0) base = atomicAdd(work, 32u);
         base = __shfl_sync(0xFFFFFFFFu, base, 0);
         if (base >= n) break;
         const uint32_t i = base + lane;
@@ -860,7 +850,7 @@ __global__ void __launch_bounds__(kTraceThreads, 4) k_camera_tail(WaveArgs A, in
     const int lane = threadIdx.x & 31;
     while (true) {
         uint32_t base = 0;
-        if (lane == 0) base = take_rays(work, n);
+        if (lane == 0) base = atomicAdd(work, 32u);
         base = __shfl_sync(0xFFFFFFFFu, base, 0);
         if (base >= n) break;
         const uint32_t i = base + lane;
