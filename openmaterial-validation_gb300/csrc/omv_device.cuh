@@ -489,14 +489,17 @@ __device__ __forceinline__ V3 env_radiance(const DevEnv& e, V3 dir)
     float u = xang / (2.0f * kPi);
     float v = 1.0f - yang / kPi;
     const int W = e.width, H = e.height;
-    u -= floorf(u - 0.5f / (float)W);
-    v -= floorf(v - 0.5f / (float)H);
-    u *= (float)W;
-    v *= (float)H;
+    u -= floorf(u - e.half_u);
+    v -= floorf(v - e.half_v);
+    u *= e.fwidth;
+    v *= e.fheight;
     int iu = (int)u, iv = (int)v;
     float kui = u - (float)iu, kvi = v - (float)iv;
     float ku = 1.0f - kui, kv = 1.0f - kvi;
-    int l = iu % W, r = (iu + 1) % W, b = iv % H, t = (iv + 1) % H;
+    // u is in [0, 1] here (an angle over 2 pi), so iu is in [0, W]: the
+    // reference's iu % W and (iu + 1) % W by one conditional subtraction
+    const int l = iu >= W ? iu - W : iu, r = iu + 1 >= W ? iu + 1 - W : iu + 1;
+    const int b = iv >= H ? iv - H : iv, t = iv + 1 >= H ? iv + 1 - H : iv + 1;
     float4 c0 = __ldg(e.rgb + b * W + l), c1 = __ldg(e.rgb + b * W + r);
     float4 c2 = __ldg(e.rgb + t * W + l), c3 = __ldg(e.rgb + t * W + r);
     float w0 = ku * kv, w1 = kui * kv, w2 = ku * kvi, w3 = kui * kvi;
@@ -525,8 +528,8 @@ __device__ __forceinline__ float env_pdf(const DevEnv& e, V3 dir)
     if (e.smp.cells <= 0) return 0.0f;
     float u, v;
     env_uv(e, dir, u, v);
-    const int i = min(max((int)(u * (float)e.width), 0), e.width - 1);
-    const int j = min(max((int)(v * (float)e.height), 0), e.height - 1);
+    const int i = min(max((int)(u * e.fwidth), 0), e.width - 1);
+    const int j = min(max((int)(v * e.fheight), 0), e.height - 1);
     return __ldg(e.smp.pdf + (size_t)j * e.width + i);
 }
 

@@ -119,6 +119,8 @@ struct DevEnvSampler {
 struct DevEnv {
     const float4* rgb;
     int32_t width, height;
+    float fwidth, fheight;     // (float)width, (float)height
+    float half_u, half_v;      // 0.5f / (float)width, 0.5f / (float)height
     float rot[9];
     float scale;
     int32_t present;

@@ -703,6 +703,10 @@ SceneHost* scene_create(const omv_scene_desc& d, int device, const std::vector<i
         D.env.rgb = s->upload(tex);
         D.env.width = h.width;
         D.env.height = h.height;
+        D.env.fwidth = (float)h.width;
+        D.env.fheight = (float)h.height;
+        D.env.half_u = 0.5f / D.env.fwidth;  // the lookup's 0.5f / (float)W, rounded alike
+        D.env.half_v = 0.5f / D.env.fheight;
         for (int r = 0; r < 3; ++r)
             for (int c = 0; c < 3; ++c) D.env.rot[3 * r + c] = h.rotation[r][c];
         D.env.scale = h.scale;
