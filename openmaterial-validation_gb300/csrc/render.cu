@@ -168,6 +168,32 @@ __device__ __forceinline__ uint32_t block_append_binned(uint32_t* counter, bool 
     return slot;
 }
 
+// Division of 32-bit unsigned integers by a divisor fixed for a frame, by one
+// multiply-high, a subtraction and two shifts (Granlund & Montgomery,
+// "Division by invariant integers using multiplication", PLDI 1994, 4.1):
+// exact for every numerator and every divisor >= 1, where the hardware has
+// no integer divide.
+struct FastDiv {
+    uint32_t d, m;
+    int s1, s2;
+};
+inline FastDiv make_fastdiv(uint32_t d)
+{
+    int l = 0;
+    while (l < 32 && (1ull << l) < d) ++l;
+    FastDiv f;
+    f.d = d;
+    f.m = (uint32_t)(((((1ull << l) - d) << 32) / d) + 1);
+    f.s1 = l < 1 ? l : 1;
+    f.s2 = l > 1 ? l - 1 : 0;
+    return f;
+}
+__device__ __forceinline__ uint32_t fast_div(const FastDiv& f, uint32_t n)
+{
+    const uint32_t t1 = __umulhi(f.m, n);
+    return (t1 + ((n - t1) >> f.s1)) >> f.s2;
+}
+
 struct WaveArgs {
     DevScene S;
     const uint32_t* items;
@@ -188,6 +214,7 @@ struct WaveArgs {
     int32_t cam_bounces, light_bounces, max_len;
     int32_t atten_mode;
     float light_scale, min_dist, cut;
+    FastDiv spp_div, width_div;  // by spp and by cam.width (one frame)
     RenderScratch R;
 };
 
@@ -198,8 +225,9 @@ struct WaveArgs {
 __device__ __forceinline__ void path_ids(const WaveArgs& A, int k, uint32_t& pixel, uint32_t& sample)
 {
     const uint32_t t = A.base_r + (uint32_t)k;  // < spp + 2^31
-    pixel = A.base_q + t / (uint32_t)A.spp;
-    sample = (uint32_t)A.sample_offset + t % (uint32_t)A.spp;
+    const uint32_t q = fast_div(A.spp_div, t);
+    pixel = A.base_q + q;
+    sample = (uint32_t)A.sample_offset + (t - q * (uint32_t)A.spp);
 }
 
 // What a path needs to know about its job: pixel and sample within the job,
@@ -257,7 +285,8 @@ __global__ void __launch_bounds__(kShadeThreads) k_camera_gen(WaveArgs A)
         sample = c.sample;
         const omv_camera& cam = A.num_jobs ? A.jobs[A.path_job[k]].cam : A.cam;
         Rng4 r = rng4(c.seed, pixel, sample, 0u, kStreamCamera);
-        camera_ray(cam, (int)(pixel % (uint32_t)cam.width), (int)(pixel / (uint32_t)cam.width), r.u[0], r.u[1], O, R);
+        const uint32_t row = A.num_jobs ? pixel / (uint32_t)cam.width : fast_div(A.width_div, pixel);
+        camera_ray(cam, (int)(pixel - row * (uint32_t)cam.width), (int)row, r.u[0], r.u[1], O, R);
         // throughput starts at 1 and radiance at 0: the first camera shade uses
         // the constants and writes both, so only a frame without camera
         // bounces needs the radiance cleared here
@@ -946,7 +975,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_film(WaveArgs A, int group, d
     const int j = threadIdx.x & (group - 1);
     const int64_t spp = A.spp;
     const int64_t g_begin = A.wave_base, g_end = A.wave_base + A.wave_n;
-    const int64_t p = (int64_t)A.base_q + t / group;
+    const int64_t p = (int64_t)A.base_q + (t >> (__ffs(group) - 1));  // group is a power of two
     const bool live = p <= (int64_t)A.last_pixel;
     // the pixel's paths, film and index in it (batch: p is a pixel of the
     // concatenated job films)
@@ -1258,6 +1287,8 @@ void run_waves(SceneHost& s, RenderScratch& R, const FramePlan& P, const omv_cam
     A.wave_cap = (int32_t)cap;
     A.npix = (int32_t)npix;
     A.spp = p.samples_per_pixel;
+    A.spp_div = make_fastdiv((uint32_t)std::max(1, p.samples_per_pixel));  // used by single frames only
+    A.width_div = make_fastdiv((uint32_t)std::max(1, cam.width));
     A.sample_offset = p.sample_offset;
     A.cam_bounces = p.camera_bounces;
     A.light_bounces = p.light_bounces;
