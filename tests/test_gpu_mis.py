@@ -190,3 +190,28 @@ def test_mis_rejected_where_unsupported(gpu, scenes):
     assert b"reference estimator" in L.omv_last_error()
     p.estimator = 7
     assert L.omv_render(rs.handle, C.byref(cam), C.byref(p), None, None, None, None, None) == 1
+
+
+def test_mis_in_the_tail_kernel_matches_the_reference_estimator(gpu, scenes):
+    """Frames of at most 2^18 paths: from bounce 3 on the tail kernel runs
+    the MIS estimator's vertices and environment rays (one thread per path),
+    and the image still converges to the reference estimator's."""
+    sc = scenes.scene_c2(40, 24, 1, tri_scale=0.02, suns=False, sky_size=(256, 128))
+    rs = gpu.RenderScene(sc)
+    r = gpu.BDPTRenderer()
+    r.set_scene(rs)
+    cam = gpu.PinholeCamera.from_spec(sc.camera)
+    n, chunk = 8192, 256
+    s = q = 0.0
+    for off in range(0, n, chunk):
+        r.set_parameters(gpu.RendererParameters.for_scene(sc, samplesPerPixel=chunk, seed=11, sample_offset=off,
+                                                          accumulate_variance=True, estimator=gpu.ESTIMATOR_MIS))
+        _, s1, q1, _ = r.render(cam, sums=True)
+        assert r.last_stats["tail_bounce"] == 3
+        s, q = s + s1, q + q1
+    m_mis = s / n
+    v_mis = np.maximum(q / n - m_mis ** 2, 0.0)
+    m_ref, v_ref = _render(gpu, sc, n, 12, gpu.ESTIMATOR_REFERENCE)
+    frac3, glob = _zstats(m_mis, n, v_mis, m_ref, n, v_ref)
+    assert frac3 < 0.01, frac3
+    assert abs(glob) < 4, glob
