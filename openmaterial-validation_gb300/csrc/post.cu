@@ -72,15 +72,15 @@ __global__ void k_develop(const double* __restrict__ sum, const uint32_t* __rest
     const int64_t n = (int64_t)w * h;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const double c = (double)count[i];
-        const double s = c < 0.5 ? 1.0 : 1.0 / c;
+        const double s = c < 0.5 ? 1.0 : __drcp_rn(c);  // 1.0 / c, the same correctly rounded bits
         const float4 lin = make_float4((float)(sum[3 * i] * s), (float)(sum[3 * i + 1] * s),
                                        (float)(sum[3 * i + 2] * s), 1.0f);
         if (linear) linear[i] = lin;
         if (!toned && !rgba8) continue;
         const float4 t = gamma_correct(lin, A, gamma);
         if (toned) toned[i] = t;
-        if (rgba8) {
-            const int64_t y = i / w, x = i - y * w;
+        if (rgba8) {  // i < 2^31: a 32-bit division for the row
+            const int64_t y = (int64_t)((uint32_t)i / (uint32_t)w), x = i - y * w;
             rgba8[flip ? (h - 1 - y) * (int64_t)w + x : i] = to_u8x4(t);
         }
     }
@@ -96,7 +96,7 @@ __global__ void k_rgba8(const float4* __restrict__ in, uchar4* __restrict__ out,
 {
     const int64_t n = (int64_t)w * h;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t y = i / w, x = i - y * w;
+        const int64_t y = (int64_t)((uint32_t)i / (uint32_t)w), x = i - y * w;  // i < 2^31
         out[flip ? (h - 1 - y) * (int64_t)w + x : i] = to_u8x4(in[i]);
     }
 }
