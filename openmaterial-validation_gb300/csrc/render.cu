@@ -321,10 +321,10 @@ __global__ void __launch_bounds__(kShadeThreads) k_light_gen(WaveArgs A)
             lmax = J.light_max;
         }
         const float* cdf = S.light_cdf + lbase;
-        // DistanceRandom::getValue (DistanceRandom.h:98-115)
-        const float d = rng4(c.seed, pixel, sample, 0u, kStreamLight).u[0] * lmax;
+        // DistanceRandom::getValue (DistanceRandom.h:98-115); one light: no draw
         int li = 0;
         if (N > 1) {
+            const float d = rng4(c.seed, pixel, sample, 0u, kStreamLight).u[0] * lmax;
             if (d <= cdf[0])
                 li = 0;
             else if (d >= cdf[N - 2])
@@ -353,14 +353,11 @@ __global__ void __launch_bounds__(kShadeThreads) k_light_gen(WaveArgs A)
         }
         R = v * (1.0f / sqrtf(sl));
         const float4 lp = __ldg(S.light_pos + li);
-        const float4 I = __ldg(S.light_int + li);
         O = v3(lp.x, lp.y, lp.z);
-        const V3 rad = v3(I.x * A.light_scale, I.y * A.light_scale, I.z * A.light_scale);
-        A.R.ltp[k] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-        A.R.lrad[k] = make_float4(rad.x, rad.y, rad.z, 1.0f);
+        // the light vertex itself is the light's position and intensity: the
+        // connections and the first light vertex read them from the light, so
+        // only the light index (and the subpath length 1) is stored here
         A.R.lmeta[k] = (uint32_t)li | (1u << 16);
-        A.R.lv_pos[k] = make_float4(O.x, O.y, O.z, 0.0f);
-        A.R.lv_rad[k] = make_float4(rad.x, rad.y, rad.z, 0.0f);
     }
     // with light bounces every path emits a light ray: queue slot = path index
     const bool push = ok && A.light_bounces >= 1;
@@ -452,17 +449,22 @@ __device__ __forceinline__ bool light_vertex(const WaveArgs& A, int b, int k, fl
     const Rng4 u = rng4(c.seed, pixel, sample, kDimLightBounce + (uint32_t)b, kStreamLight);
     const V3 brdf = material_sample(S, M, pbr_params(S, M, sp), sp, in, false, u, O);
     const float ct = fabsf(dot(in, sp.nrm));
-    const float4 tp0 = A.R.ltp[k];
-    float4 lr = A.R.lrad[k];
-    const V3 tp = v3(tp0.x * brdf.x * ct, tp0.y * brdf.y * ct, tp0.z * brdf.z * ct);
     const uint32_t meta = A.R.lmeta[k];
     const uint32_t li = meta & 0xFFFFu;
-    if (b == 1) {
+    float4 tp0, lr;
+    if (b == 1) {  // throughput 1; the light's radiance and the attenuation to this vertex
+        tp0 = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        const float4 I = __ldg(S.light_int + li);
         const float4 lp = __ldg(S.light_pos + li);
         const V3 d = sp.pos - v3(lp.x, lp.y, lp.z);
-        lr.w = light_attenuation(A.atten_mode, A.min_dist, sqrtf(dot(d, d)), lp.w);
+        lr = make_float4(I.x * A.light_scale, I.y * A.light_scale, I.z * A.light_scale,
+                         light_attenuation(A.atten_mode, A.min_dist, sqrtf(dot(d, d)), lp.w));
         A.R.lrad[k] = lr;
+    } else {
+        tp0 = A.R.ltp[k];
+        lr = A.R.lrad[k];
     }
+    const V3 tp = v3(tp0.x * brdf.x * ct, tp0.y * brdf.y * ct, tp0.z * brdf.z * ct);
     const V3 orad = v3(tp.x * lr.x * lr.w, tp.y * lr.y * lr.w, tp.z * lr.z * lr.w);
     if (!(intensity(orad) < A.cut)) {
         const size_t slot = (size_t)b * A.wave_cap + k;
@@ -490,9 +492,12 @@ __global__ void __launch_bounds__(kShadeThreads, 4) k_light_shade(WaveArgs A, in
         float tnear = 0.0f;
         int k = 0;
         if (i < n) {
-            const float4 ra = rq_in[2 * (size_t)i], rb = rq_in[2 * (size_t)i + 1];
-            k = __float_as_int(rb.w);
-            push = light_vertex(A, b, k, ra, rb, A.R.hits[i], so, O, tnear);
+            const uint4 h = A.R.hits[i];
+            if (h.x != kInvalid) {  // most light rays leave the scene: their ray is not read
+                const float4 ra = rq_in[2 * (size_t)i], rb = rq_in[2 * (size_t)i + 1];
+                k = __float_as_int(rb.w);
+                push = light_vertex(A, b, k, ra, rb, h, so, O, tnear);
+            }
         }
         const uint32_t slot = warp_append(&A.R.ctr[kCtrLight + b + 1], push);
         if (push) {
@@ -630,7 +635,7 @@ __device__ __forceinline__ bool camera_vertex(const WaveArgs& A, int b, int k, f
             const V3 outV = -in;
             for (int li_v = 0; li_v < lp_len && li_v + b <= A.max_len; ++li_v) {
                 const size_t slot = (size_t)li_v * A.wave_cap + k;
-                const float4 lp = A.R.lv_pos[slot];
+                const float4 lp = li_v == 0 ? __ldg(S.light_pos + li) : A.R.lv_pos[slot];  // vertex 0: the light
                 const V3 lPos = v3(lp.x, lp.y, lp.z);
                 V3 lRad;
                 const V3 LC = normalize(sp.pos - lPos);
