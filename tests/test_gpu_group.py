@@ -118,3 +118,33 @@ def test_group_rejects_mixed_lighting_and_bad_parts(gpu, scenes):
          torch.zeros((cam.height, cam.width), dtype=torch.int32, device="cuda"))
     with pytest.raises(gpu.OmvError, match="part"):
         br.render([br.job(cam, 4, f, part=2)])
+
+
+def test_unlit_group_batch_in_the_tail_kernel_matches_each_scene_alone(gpu, scenes):
+    """Two scenes under one sky (no point light) as a group batch small enough
+    (at most 2^18 paths) that from bounce 3 on the tail kernel runs each path
+    to its end with its job's scene, camera and materials: every job still
+    reproduces its scene rendered alone (to FP32 summation order)."""
+    import dataclasses
+
+    torch = pytest.importorskip("torch")
+    a = scenes.scene_c2(24, 16, 1, seed=1, tri_scale=0.01, suns=False, sky_size=(128, 64))
+    b = dataclasses.replace(scenes.scene_c2(24, 16, 1, seed=2, tri_scale=0.01, suns=False, sky_size=(128, 64)),
+                            hdri=a.hdri)
+    parts = [a, b]
+    group = gpu.RenderScene.group(parts)
+    br = gpu.BatchRenderer(group, gpu.RendererParameters.for_scene(a))
+    jobs, films, want = [], [], []
+    for p, sc in enumerate(parts):
+        spp, seed = 64, 90 + p
+        _, cam, _, s, c = _alone(gpu, torch, sc, spp, seed)
+        want.append((s, c))
+        f = (torch.zeros_like(s), None, torch.zeros_like(c))
+        films.append(f)
+        jobs.append(br.job(cam, spp, f, seed=seed, part=p))
+    st = br.render(jobs, stats=True)
+    torch.cuda.synchronize()
+    assert st.tail_bounce == 3 and st.tail_nodes_visited > 0
+    for (s, c), f in zip(want, films):
+        assert torch.equal(c, f[2])
+        assert float((s - f[0]).abs().max()) <= 1e-5 * float(s.abs().max())
