@@ -189,7 +189,11 @@ struct CamVert {
     LocalGrad gG;  // d G / d params (through the connection evaluations)
 };
 
-__global__ void __launch_bounds__(kAdjThreads) k_adjoint(AdjArgs A)
+// 4 resident blocks of 128 (128 registers, some spilled): 0.109 s per
+// gradient of the 512x512x32 adjoint benchmark and 0.497 s per inverse-fit
+// step, against 0.111 / 0.509 at the natural 168 registers (3 blocks) and
+// 0.115 / 0.531 at 246 registers (2 blocks, no spills)
+__global__ void __launch_bounds__(kAdjThreads, 4) k_adjoint(AdjArgs A)
 {
     __shared__ uint2 sstack[kStackShared * kAdjThreads];
     __shared__ float sgrad[kAdjMaxMaterials * kSlots];
