@@ -46,14 +46,14 @@ def _peaks():
         return HBM_FALLBACK_GBS, "fallback"
 
 
-def frame_config(scene, parallelism: str) -> dict:
-    """The workload keys both arms report (the same scene on both sides)."""
+def frame_config(scene) -> dict:
+    """The workload keys both arms report, identical on both sides (the same
+    scene and frame); how each arm runs it is its line's `parallelism`."""
     workload = WORKLOAD if scene.name != "c1" else "plain BDPT, point-light scene (C1 geometry and light)"
     return {"workload": workload, "width": scene.camera.width, "height": scene.camera.height,
             "spp": scene.render.samples_per_pixel, "max_path_length": scene.render.max_path_length,
             "triangles": scene.num_triangles, "instances": len(scene.instances),
-            "l2": "flushed by a 256 MiB write between timed frames", "parallelism": parallelism,
-            "film": "FP64 sums"}
+            "l2": "flushed by a 256 MiB write between timed frames (GPU arm)", "film": "FP64 sums"}
 
 
 class Clocks:
@@ -174,7 +174,7 @@ def run_reference(args, scene, rank):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * statistics.mean(secs), 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "impl": "reference",
-            "config": frame_config(scene, f"{cores} host threads"),
+            "config": frame_config(scene), "parallelism": f"{cores} host threads",
             "mrays_per_s": round(statistics.mean(rvals), 4),
             "cpu_baseline": {"value": round(value, 4), "unit": "Mpaths/s", "cores": cores, "kind": "port",
                              "sample": sample},
@@ -766,7 +766,7 @@ def run_ours(args, scene, ws, rank, local):
         line = {"metric": METRIC, "value": round(value, 4), "unit": "Mpaths/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": round(max_ms / args.steps, 3), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": frame_config(scene, f"replicas x{ws} (disjoint sample ranges)"),
+                "config": frame_config(scene), "parallelism": f"replicas x{ws} (disjoint sample ranges)",
                 "mrays_per_s": round(rays / (max_ms / 1e3) / 1e6, 4), "film_counts_ok": cnt_ok,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clock,
                 "gpu_launches": agg["kernel_launches"], "scene_build_ms": round(info["build_ms"], 1),
