@@ -68,3 +68,21 @@ def test_reference_arm_works_on_rank_zero_only(monkeypatch, capsys):
     monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--gpus", "2"])
     assert bench.main() is None
     assert capsys.readouterr().out == ""
+
+
+def test_both_arms_report_the_same_workload_config():
+    """The GPU arm and the reference arm describe their workload with the
+    same keys and values (one function builds both); how each runs it is the
+    line's separate `parallelism` key."""
+    sys.path.insert(0, ROOT)
+    import importlib
+
+    import bench
+
+    S = importlib.import_module("openmaterial-validation_gb300.scenes")
+    sc = S.scene_c2(48, 27, 4, tri_scale=0.01, suns=False, sky_size=(64, 32))
+    a, b = bench.frame_config(sc), bench.frame_config(sc)
+    assert a == b
+    assert {"workload", "width", "height", "spp", "max_path_length", "triangles", "instances"} <= set(a)
+    assert "parallelism" not in a
+    assert (a["width"], a["height"], a["spp"]) == (48, 27, 4)
