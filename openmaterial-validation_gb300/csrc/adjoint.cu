@@ -244,15 +244,7 @@ __global__ void __launch_bounds__(kAdjThreads, 4) k_adjoint(AdjArgs A)
                     li = (lo + hi) / 2;
                 }
             }
-            V3 v = v3(1.0f, 0.0f, 0.0f);
-            float sl = 1.0f;
-            for (uint32_t t = 0; t < 64; ++t) {
-                Rng4 r = rng4(A.seed, pixel, sample, 1u + t, kStreamLight);
-                v = v3(r.u[0], r.u[1], r.u[2]);
-                sl = dot(v, v);
-                if (!(sl > 1.0f || sl < kEps)) break;
-            }
-            V3 R = v * (1.0f / sqrtf(sl));
+            V3 R = light_direction(A.seed, pixel, sample);  // as k_light_gen
             const float4 lp = __ldg(S.light_pos + li);
             const float4 I = __ldg(S.light_int + li);
             l0pos = v3(lp.x, lp.y, lp.z);

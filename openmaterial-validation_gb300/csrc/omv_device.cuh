@@ -153,6 +153,23 @@ __device__ __forceinline__ Rng4 rng4(uint64_t seed, uint32_t pixel, uint32_t sam
 enum : uint32_t { kStreamCamera = 0u, kStreamLight = 1u };
 constexpr uint32_t kDimLightBounce = 1024u;
 
+// The direction of a light path's first ray.  RandomSampler::uniformSphere
+// (RandomSampler.h:75-84) draws v uniformly in [0,1)^3 until eps <= |v|^2 <= 1
+// and returns v / |v|: a direction uniform over the positive octant of the unit
+// sphere (the ball is invariant under rotations).  Drawn here without the
+// rejection loop, in which a warp waits for its slowest lane's draws: z
+// uniform in [0, 1) (on a sphere, slices of equal height have equal areas) and
+// the azimuth uniform in [0, pi/2).
+__device__ __forceinline__ V3 light_direction(uint64_t seed, uint32_t pixel, uint32_t sample)
+{
+    const Rng4 r = rng4(seed, pixel, sample, 1u, kStreamLight);
+    const float z = r.u[0];
+    const float rxy = sqrtf(fmaxf(0.0f, 1.0f - z * z));
+    float s, c;
+    sincosf(0.5f * kPi * r.u[1], &s, &c);
+    return v3(rxy * c, rxy * s, z);
+}
+
 // ------------------------------------------------------ camera / ray ---
 
 // PinholeCamera::getRay (PinholeCamera.cpp:80-95), exact float order

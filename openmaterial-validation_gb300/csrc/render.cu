@@ -342,16 +342,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_light_gen(WaveArgs A)
             }
         }
         li += lbase;
-        // RandomSampler::uniformSphere: rejection in the [0,1)^3 cube
-        V3 v = v3(1.0f, 0.0f, 0.0f);
-        float sl = 1.0f;
-        for (uint32_t t = 0; t < 64; ++t) {
-            Rng4 r = rng4(c.seed, pixel, sample, 1u + t, kStreamLight);
-            v = v3(r.u[0], r.u[1], r.u[2]);
-            sl = dot(v, v);
-            if (!(sl > 1.0f || sl < kEps)) break;
-        }
-        R = v * (1.0f / sqrtf(sl));
+        R = light_direction(c.seed, pixel, sample);  // RandomSampler::uniformSphere
         const float4 lp = __ldg(S.light_pos + li);
         O = v3(lp.x, lp.y, lp.z);
         // the light vertex itself is the light's position and intensity: the
